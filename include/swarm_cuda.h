@@ -1,0 +1,192 @@
+/*
+ * swarm_cuda.h -- C ABI of the GB300-native SWARM crowd step (libswarm_gb300.so).
+ *
+ * One handle = one simulation on one GPU: the agent state, the neighbour grid, the venue and a CUDA stream.
+ * Every entry point returns SWARM_OK (0) or a negative status; swarm_last_error() gives the message.
+ * No C++ exception, no torch type and no CUDA type crosses this boundary (streams are passed as void*).
+ *
+ * Reference interface replaced (DedovSergei/swarm-crowd-simulation, paths within that project):
+ *   class swarm::CrowdSim        include/swarm/crowd_sim.hpp:53-194  (GPU step / state API, OpenGL compute)
+ *   class swarm::CpuCrowdSim     include/swarm/cpu_crowd_sim.hpp:30-169 (its CPU mirror)
+ * Each declaration below names the member it stands in for.
+ *
+ * State format: the reference's GpuBoid (include/swarm/gpu_types.hpp:17-20), 8 floats per agent:
+ *   position.xyz, position.w (1 = active, 0 = evacuated / parked), velocity.xyz, velocity.w (speed).
+ * Agent ids are the indices into that array (the reference's boidID).
+ */
+#ifndef SWARM_CUDA_H
+#define SWARM_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+enum {
+    SWARM_OK = 0,
+    SWARM_E_INVALID = -1,  /* bad argument (std::invalid_argument in the reference) */
+    SWARM_E_CUDA = -2,     /* a CUDA call failed */
+    SWARM_E_OOM = -3,      /* device allocation failed */
+    SWARM_E_TIMEOUT = -4,  /* a bounded device-side wait gave up (the kernel returned instead of hanging) */
+    SWARM_E_STATE = -5     /* call out of order (e.g. step before a state was uploaded) */
+};
+
+/* ---- venue kinds ---- */
+enum {
+    /* The reference's baked terrace (venue "terrace"): stadium.sdf (130^3 float32, [x][y][z] z fastest), the analytic
+     * pitch fence and the egress router, model units, uniform body radius (include/swarm/sim_params.hpp). */
+    SWARM_VENUE_STADIUM = 0,
+    /* A plan venue on grids, SI units, per-agent radius and desired speed: a horizontal wall SDF, a geodesic
+     * distance-to-exit field whose negative normalised gradient is the walking direction, an optional floor
+     * heightfield and stair speed factors. The synthetic halls and the seated bowl are built as these. */
+    SWARM_VENUE_GRID = 1
+};
+
+/* Every model constant of the step (the reference's include/swarm/sim_params.hpp, including its folded constant
+ * expressions). swarm_params_reference() fills the reference's values (model units, K = 32);
+ * swarm_params_si() the SI preset of the grid venues (dt 0.05 s, K = 8, per-agent radius and v0). */
+typedef struct SwarmParams {
+    /* step */
+    float dt;                     /* DT */
+    int32_t proj_iterations;      /* PROJ_ITERATIONS: Jacobi sweeps per step, the last one in the final pass */
+    int32_t perc_ring;            /* PERC_RING: cells searched to each side in the predict pass */
+    int32_t uniform_body;         /* 1: every agent is BODY_RADIUS / V_MAX (stadium); 0: per-agent radius and v0 */
+    /* body model */
+    float body_radius;            /* BODY_RADIUS (uniform body; the default radius otherwise) */
+    float body_diam, body_diam2;  /* BODY_DIAM, BODY_DIAM * BODY_DIAM (folded) */
+    float r_sep, r_sep2;          /* R_SEP, R_SEP * R_SEP (uniform body) */
+    float sep_margin;             /* per-agent body: the separation support of a pair is r_i + r_j + sep_margin */
+    float k_sep;                  /* K_SEP */
+    float r_perc2;                /* R_PERC * R_PERC */
+    float v_max;                  /* V_MAX: the free speed (uniform body) and the |v_xy| clamp */
+    float headway_rate;           /* 1 / T_HEADWAY */
+    float relax_step;             /* exp(-DT / TAU_RELAX) */
+    float tau_relax;              /* TAU_RELAX */
+    float gravity_dt;             /* GRAVITY * DT */
+    float proj_relax, proj_max_shift;   /* PROJ_RELAX, PROJ_MAX_SHIFT */
+    float safe_eps;               /* SAFE_NORMALIZE_EPS */
+    float stacked_xy2;            /* SEP_STACKED_XY2 */
+    float hash_to_radians;        /* 2 pi / 2^32 */
+    float goal_deadzone;          /* GOAL_DEADZONE */
+    /* obstacle avoidance */
+    float torso_height, obstacle_range, w_obs, obstacle_gain, obstacle_min_normal, obstacle_grad_h, obstacle_grad_scale;
+    /* static contacts */
+    int32_t feeler_count, wall_root_steps, wall_recast_steps, wall_passes;
+    int32_t floor_search_cells, sweep_bisections, fence_ccd_bisections, pad0;
+    float feeler_reach, plane_probe_reach, wall_recast_tol, wall_max_nz, centre_grad_min, floor_settle_reach;
+    float feeler_dir[16][2], feeler_off[16][2], probe_off[16][2];
+    /* step-up limit */
+    float max_step_up, step_up_tol, step_up_floor_reach, step_up_sample;
+    int32_t step_up_bisections, step_up_max_samples, step_up_slide_tries, pad1;
+    float step_up_slide[3][2];
+    /* analytic pitch fence (stadium) */
+    float fence_center[2], fence_half_mid[2], fence_half_thk_coll;
+    /* egress router (stadium) */
+    float avenue_half, walkway_min, walkway_max, walkway_centre, aisle_max, aisle_centre;
+    float avenue_target_depth, pitch_recovery_depth;
+    float park_coord;             /* PARK_COORD */
+    /* metrics (fixed-point cloud-in-cell density; include/swarm/metrics.hpp) */
+    float metric_cells_per_unit;  /* metric cells per length unit */
+    float metric_speed_scale;     /* m/s per speed unit */
+    float pad2[6];
+} SwarmParams;
+
+/* The venue: the neighbour grid, the exit test, and the static fields of its kind. Host pointers; swarm_create
+ * copies them to the device. */
+typedef struct SwarmVenue {
+    int32_t kind;                 /* SWARM_VENUE_* */
+    int32_t grid_res_x, grid_res_y;   /* neighbour (hash) grid cells per axis */
+    int32_t n_exits;              /* exits listed in exit_boxes (grid venues; metrics) */
+    float domain_min_x, domain_min_y, domain_span_x, domain_span_y;   /* the hash grid's extent */
+    /* exit test: an agent is parked (evacuated) when it leaves [exit_lo, exit_hi] below exit_max_z, or the domain.
+     * Stadium: max(|x|, |y|) > exit_hi_x (EXIT_DEPTH) below exit_max_z (EXIT_MAX_Z). */
+    float exit_lo_x, exit_lo_y, exit_hi_x, exit_hi_y, exit_max_z;
+    /* stadium: the baked volume */
+    const float* sdf;             /* sdf_res^3 floats */
+    int32_t sdf_res;
+    float sdf_origin[3];          /* SDF_ORIGIN: world position of sample index 1 */
+    float sdf_spacing;            /* SDF_SPACING */
+    /* grid venues: node (i, j) of every field sits at origin + (i, j) * h; arrays x fastest */
+    const float* wall_sdf;        /* horizontal signed distance to the walls (< 0 inside a wall) */
+    int32_t wall_nx, wall_ny;
+    float wall_origin_x, wall_origin_y, wall_h;
+    const float* nav_dist;        /* geodesic distance to the nearest exit (walls: a large value) */
+    int32_t nav_nx, nav_ny;
+    float nav_origin_x, nav_origin_y, nav_h;
+    const float* floor_height;    /* optional (NULL: a flat floor at z = 0), on the wall grid */
+    const float* speed_factor;    /* optional (NULL: 1), on the wall grid: the desired-speed factor (stairs) */
+    const float* exit_boxes;      /* n_exits x (lo_x, lo_y, hi_x, hi_y): the metric's exit attribution */
+    /* metrics: the 1 m floor grid, metric_res^2 cells centred on metric_center */
+    int32_t metric_res;
+    float metric_center_x, metric_center_y;
+} SwarmVenue;
+
+typedef struct SwarmSim* SwarmHandle;
+
+/* Per-stage device time of the last timed step, milliseconds (CpuCrowdSim::StageTimesMs,
+ * include/swarm/cpu_crowd_sim.hpp:76; CrowdSim::readTimings, src/crowd_sim.cpp:449-478). */
+typedef struct SwarmStageTimes {
+    float hash, sort, cells, predict, project, final_pass, total;
+} SwarmStageTimes;
+
+/* ---- parameters ---- */
+/* sim_params.hpp's values, folded as the reference folds them (include/swarm/sim_params.hpp:28-54, 499-512). */
+int swarm_params_reference(SwarmParams* out);
+/* The SI preset of the grid venues: dt 0.05 s, K = 8 sweeps, tau 0.5 s, per-agent radius and v0. */
+int swarm_params_si(SwarmParams* out);
+
+/* ---- lifecycle ----
+ * swarm_create: CrowdSim(shaderDir, numBoids, venue) (src/crowd_sim.cpp:96-202) / CpuCrowdSim(venue, sdf)
+ *   (src/cpu_crowd_sim.cpp:918-927). n_capacity: the agent buffer size (no power-of-two rule: the key sort has none). */
+int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capacity, SwarmHandle* out);
+int swarm_destroy(SwarmHandle h);
+/* Optional: run on the caller's stream (a cudaStream_t) instead of the handle's own. */
+int swarm_set_stream(SwarmHandle h, void* cuda_stream);
+int swarm_last_error(SwarmHandle h, char* buf, int len);
+
+/* ---- state I/O ----
+ * swarm_upload_state: CrowdSim::upload (src/crowd_sim.cpp:285-309) / CpuCrowdSim::setState. boids: n x 8 floats
+ *   (GpuBoid). Sets the active agent count to n (<= capacity). Host memory. */
+int swarm_upload_state(SwarmHandle h, const float* boids, int n);
+/* The latest state, n x 8 floats (CpuCrowdSim::state(); CrowdSim::currentStateBuffer readback). */
+int swarm_download_state(SwarmHandle h, float* boids, int n);
+/* Per-agent radius and desired speed (grid venues): n floats each. Default: body_radius and v_max. */
+int swarm_set_agent_params(SwarmHandle h, const float* radius, const float* v0, int n);
+/* Device-resident variants: pointers to device memory on the handle's device, same layouts. */
+int swarm_upload_state_device(SwarmHandle h, const float* d_boids, int n);
+int swarm_download_state_device(SwarmHandle h, float* d_boids, int n);
+
+/* ---- stepping ----
+ * swarm_step: `steps` x CrowdSim::step (src/crowd_sim.cpp:316-412) = hash, key sort, cell ranges + gather,
+ *   predict, K - 1 Jacobi sweeps, final pass; asynchronous on the handle's stream. */
+int swarm_step(SwarmHandle h, int steps);
+/* CpuCrowdSim::setProjectionIterations / CrowdSim::setProjectionIterations (src/crowd_sim.cpp:480-483). */
+int swarm_set_iterations(SwarmHandle h, int k);
+/* CpuCrowdSim::setDriveTable (include/swarm/cpu_crowd_sim.hpp:114): e_goal of agent i is dirs[2i..2i+1];
+ * NULL restores the venue's router / navigation field. */
+int swarm_set_drive_table(SwarmHandle h, const float* dirs, int n);
+/* Captures one step in a CUDA graph and replays it (1) or launches kernel by kernel (0, the default). */
+int swarm_set_graph(SwarmHandle h, int enabled);
+int swarm_synchronize(SwarmHandle h);
+
+/* ---- inspection (the reference's parity tests read these) ----
+ * swarm_get_grid: CpuCrowdSim::grid() -- the last step's sorted (gridID, boidID) pairs, n each. */
+int swarm_get_grid(SwarmHandle h, uint32_t* grid_id, uint32_t* boid_id, int n);
+/* CpuCrowdSim::cells(): (startIndex, agentCount) per cell, 2 x n_cells; returns the cell count if the buffer is NULL. */
+int swarm_get_cells(SwarmHandle h, uint32_t* start_count, int n_cells);
+/* CpuCrowdSim::contacts(): the ContactBits per agent of the last step. */
+int swarm_get_contacts(SwarmHandle h, uint8_t* bits, int n);
+/* Times every stage of the following steps with CUDA events (0: off, the default). */
+int swarm_set_timing(SwarmHandle h, int enabled);
+int swarm_stage_times(SwarmHandle h, SwarmStageTimes* out);
+/* Kernel launches the last swarm_step issued (evidence for benchmarks). */
+int swarm_launch_count(SwarmHandle h, int64_t* out);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif /* SWARM_CUDA_H */

@@ -1,0 +1,78 @@
+"""ctypes mirror of the C ABI in include/swarm_cuda.h (the structs and status codes).
+
+The structs are the data format of the library's boundary: the CUDA library, the C++ host class and the test-only
+oracle all take them. Field order and types must match the header exactly (tests/test_abi.py checks the sizes).
+"""
+import ctypes as C
+
+SWARM_OK = 0
+SWARM_E_INVALID = -1
+SWARM_E_CUDA = -2
+SWARM_E_OOM = -3
+SWARM_E_TIMEOUT = -4
+SWARM_E_STATE = -5
+
+SWARM_VENUE_STADIUM = 0
+SWARM_VENUE_GRID = 1
+
+INACTIVE_CELL = 0xFFFFFFFF
+
+# ContactBits (reference include/swarm/cpu_crowd_sim.hpp:52-61)
+CONTACT_EXIT, CONTACT_FENCE_CCD, CONTACT_FENCE, CONTACT_FLOOR = 1, 2, 4, 8
+CONTACT_WALL, CONTACT_AGENT, CONTACT_SWEEP, CONTACT_STEP_UP = 16, 32, 64, 128
+
+_f = C.c_float
+_i = C.c_int32
+
+
+class SwarmParams(C.Structure):
+    _fields_ = [
+        ("dt", _f), ("proj_iterations", _i), ("perc_ring", _i), ("uniform_body", _i),
+        ("body_radius", _f), ("body_diam", _f), ("body_diam2", _f), ("r_sep", _f), ("r_sep2", _f),
+        ("sep_margin", _f), ("k_sep", _f), ("r_perc2", _f), ("v_max", _f), ("headway_rate", _f),
+        ("relax_step", _f), ("tau_relax", _f), ("gravity_dt", _f), ("proj_relax", _f), ("proj_max_shift", _f),
+        ("safe_eps", _f), ("stacked_xy2", _f), ("hash_to_radians", _f), ("goal_deadzone", _f),
+        ("torso_height", _f), ("obstacle_range", _f), ("w_obs", _f), ("obstacle_gain", _f),
+        ("obstacle_min_normal", _f), ("obstacle_grad_h", _f), ("obstacle_grad_scale", _f),
+        ("feeler_count", _i), ("wall_root_steps", _i), ("wall_recast_steps", _i), ("wall_passes", _i),
+        ("floor_search_cells", _i), ("sweep_bisections", _i), ("fence_ccd_bisections", _i), ("pad0", _i),
+        ("feeler_reach", _f), ("plane_probe_reach", _f), ("wall_recast_tol", _f), ("wall_max_nz", _f),
+        ("centre_grad_min", _f), ("floor_settle_reach", _f),
+        ("feeler_dir", (_f * 2) * 16), ("feeler_off", (_f * 2) * 16), ("probe_off", (_f * 2) * 16),
+        ("max_step_up", _f), ("step_up_tol", _f), ("step_up_floor_reach", _f), ("step_up_sample", _f),
+        ("step_up_bisections", _i), ("step_up_max_samples", _i), ("step_up_slide_tries", _i), ("pad1", _i),
+        ("step_up_slide", (_f * 2) * 3),
+        ("fence_center", _f * 2), ("fence_half_mid", _f * 2), ("fence_half_thk_coll", _f),
+        ("avenue_half", _f), ("walkway_min", _f), ("walkway_max", _f), ("walkway_centre", _f),
+        ("aisle_max", _f), ("aisle_centre", _f), ("avenue_target_depth", _f), ("pitch_recovery_depth", _f),
+        ("park_coord", _f),
+        ("metric_cells_per_unit", _f), ("metric_speed_scale", _f), ("pad2", _f * 6),
+    ]
+
+
+class SwarmVenue(C.Structure):
+    _fields_ = [
+        ("kind", _i), ("grid_res_x", _i), ("grid_res_y", _i), ("n_exits", _i),
+        ("domain_min_x", _f), ("domain_min_y", _f), ("domain_span_x", _f), ("domain_span_y", _f),
+        ("exit_lo_x", _f), ("exit_lo_y", _f), ("exit_hi_x", _f), ("exit_hi_y", _f), ("exit_max_z", _f),
+        ("sdf", C.POINTER(_f)), ("sdf_res", _i), ("sdf_origin", _f * 3), ("sdf_spacing", _f),
+        ("wall_sdf", C.POINTER(_f)), ("wall_nx", _i), ("wall_ny", _i),
+        ("wall_origin_x", _f), ("wall_origin_y", _f), ("wall_h", _f),
+        ("nav_dist", C.POINTER(_f)), ("nav_nx", _i), ("nav_ny", _i),
+        ("nav_origin_x", _f), ("nav_origin_y", _f), ("nav_h", _f),
+        ("floor_height", C.POINTER(_f)), ("speed_factor", C.POINTER(_f)), ("exit_boxes", C.POINTER(_f)),
+        ("metric_res", _i), ("metric_center_x", _f), ("metric_center_y", _f),
+    ]
+
+
+class SwarmStageTimes(C.Structure):
+    _fields_ = [("hash", _f), ("sort", _f), ("cells", _f), ("predict", _f), ("project", _f),
+                ("final_pass", _f), ("total", _f)]
+
+
+def fptr(a):
+    """A float* into a C-contiguous float32 numpy array (None for None)."""
+    if a is None:
+        return None
+    assert a.dtype.name == "float32" and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.POINTER(_f))
