@@ -185,6 +185,37 @@ int swarm_stage_times(SwarmHandle h, SwarmStageTimes* out);
 /* Kernel launches the last swarm_step issued (evidence for benchmarks). */
 int swarm_launch_count(SwarmHandle h, int64_t* out);
 
+/* ---- synthetic venues and spawns (host code; inputs of the step, built once) ----
+ * A rectangular hall centred on the origin: interior size_x x size_y metres, walls of wall_thickness around it with
+ * door gaps, the exit line exit_depth beyond the walls' outer faces (agents past it are evacuated), a margin of open
+ * ground around that. The walls' horizontal SDF is exact (boxes); the navigation field is the first-order fast-marching
+ * geodesic distance, through the free nodes, to the free nodes beyond the exit line. */
+typedef struct SwarmHallSpec {
+    float size_x, size_y;         /* interior, metres */
+    float wall_thickness;         /* metres */
+    float exit_depth;             /* exit line beyond the walls' outer faces */
+    float margin;                 /* open ground beyond the exit line */
+    float wall_h, nav_h, cell;    /* wall SDF spacing (0.05), nav spacing (0.1), hash cell (0.5) */
+    int32_t n_doors;              /* <= 8 */
+    int32_t door_wall[8];         /* 0: the -x wall, 1: +x, 2: -y, 3: +y */
+    float door_center[8];         /* along the wall, from the wall's midpoint */
+    float door_width[8];
+} SwarmHallSpec;
+
+/* Fills every scalar of *venue (grid sizes, origins, domain, exit test) and leaves its array pointers NULL; the
+ * array sizes are wall_nx * wall_ny and nav_nx * nav_ny floats, and 4 * n_exits for the exit boxes. */
+int swarm_hall_layout(const SwarmHallSpec* spec, SwarmVenue* venue);
+/* Fills the arrays of a layout made by swarm_hall_layout (caller-allocated). */
+int swarm_hall_fields(const SwarmHallSpec* spec, const SwarmVenue* venue, float* wall_sdf, float* nav_dist, float* exit_boxes);
+
+/* A jittered lattice of nx x ny agents (row-major, the first n of them) at `spacing`, centred on (cx, cy), resting on
+ * the floor (z = radius), at rest. Jitter U(-jitter, jitter) per axis, radius U[r_lo, r_hi], desired speed
+ * N(v_mean, v_sd) clipped to [v_lo, v_hi]; seeded, identical on every platform (splitmix64 + Box-Muller in double).
+ * boids: n x 8 floats (GpuBoid), radius and v0: n floats each. */
+int swarm_spawn_lattice(int nx, int ny, int n, float spacing, float cx, float cy, float jitter, uint64_t seed,
+                        float r_lo, float r_hi, float v_mean, float v_sd, float v_lo, float v_hi,
+                        float* boids, float* radius, float* v0);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif

@@ -1,0 +1,214 @@
+"""ORACLE -- test infrastructure only: ctypes wrapper of liboracle.so (the CPU restatement, swarm_oracle.cpp) and of
+_ref/libswarm_ref.so (the unmodified reference CPU step, built in this container only; see Makefile).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this module, as the checker.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libswarm_ref.so")
+_o = None
+_r = None
+
+
+def build(ref=False):
+    """make -C oracle (and the reference's own CPU step when ref and the reference tree exists)."""
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    if ref and os.path.isdir(os.environ.get("REF_DIR", "/root/reference")):
+        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref"], check=True)
+
+
+def lib():
+    global _o
+    if _o is None:
+        if not os.path.exists(ORACLE_SO):
+            build()
+        L = C.CDLL(ORACLE_SO)
+        V = C.c_void_p
+        L.oracle_create.restype = V
+        L.oracle_create.argtypes = [V, V, C.c_int]
+        L.oracle_last_error.restype = C.c_char_p
+        for name in ["oracle_destroy", "oracle_set_state", "oracle_set_agent_params", "oracle_set_iterations",
+                     "oracle_set_threads", "oracle_set_drive_table", "oracle_step", "oracle_get_state",
+                     "oracle_get_grid", "oracle_get_cells", "oracle_get_contacts"]:
+            getattr(L, name).restype = C.c_int
+        L.oracle_destroy.argtypes = [V]
+        L.oracle_set_state.argtypes = [V, V, C.c_int]
+        L.oracle_set_agent_params.argtypes = [V, V, V, C.c_int]
+        L.oracle_set_iterations.argtypes = [V, C.c_int]
+        L.oracle_set_threads.argtypes = [V, C.c_int]
+        L.oracle_set_drive_table.argtypes = [V, V, C.c_int]
+        L.oracle_step.argtypes = [V, C.c_int]
+        L.oracle_get_state.argtypes = [V, V]
+        L.oracle_get_grid.argtypes = [V, V, V]
+        L.oracle_get_cells.argtypes = [V, V, C.c_int]
+        L.oracle_get_contacts.argtypes = [V, V]
+        _o = L
+    return _o
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class OracleSim:
+    """The CPU restatement, with CpuCrowdSim's API (same method names as swarm_gb300.CrowdSim)."""
+
+    def __init__(self, params, venue_struct, threads=0):
+        self._h = lib().oracle_create(C.byref(params), C.byref(venue_struct), threads)
+        if not self._h:
+            raise RuntimeError("oracle_create: " + lib().oracle_last_error().decode())
+        self.ncells = venue_struct.grid_res_x * venue_struct.grid_res_y
+        self.n = 0
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().oracle_destroy(self._h)
+            self._h = None
+
+    def set_state(self, boids):
+        b = np.ascontiguousarray(boids, dtype=np.float32).reshape(-1, 8)
+        assert lib().oracle_set_state(self._h, _p(b), b.shape[0]) == 0
+        self.n = b.shape[0]
+
+    def set_agent_params(self, radius, v0):
+        r = np.ascontiguousarray(radius, dtype=np.float32)
+        v = np.ascontiguousarray(v0, dtype=np.float32)
+        assert lib().oracle_set_agent_params(self._h, _p(r), _p(v), r.shape[0]) == 0
+
+    def set_projection_iterations(self, k):
+        if lib().oracle_set_iterations(self._h, int(k)) != 0:
+            raise ValueError(lib().oracle_last_error().decode())
+
+    def set_threads(self, t):
+        return lib().oracle_set_threads(self._h, int(t))
+
+    def set_drive_table(self, dirs):
+        if dirs is None:
+            lib().oracle_set_drive_table(self._h, None, 0)
+            return
+        d = np.ascontiguousarray(dirs, dtype=np.float32).reshape(-1, 2)
+        lib().oracle_set_drive_table(self._h, _p(d), d.shape[0])
+
+    def step(self, steps=1):
+        assert lib().oracle_step(self._h, int(steps)) == 0, lib().oracle_last_error().decode()
+
+    def state(self):
+        out = np.empty((self.n, 8), np.float32)
+        lib().oracle_get_state(self._h, _p(out))
+        return out
+
+    def grid(self):
+        g = np.empty(self.n, np.uint32)
+        b = np.empty(self.n, np.uint32)
+        lib().oracle_get_grid(self._h, _p(g), _p(b))
+        return g, b
+
+    def cells(self):
+        out = np.empty((self.ncells, 2), np.uint32)
+        lib().oracle_get_cells(self._h, _p(out), self.ncells)
+        return out
+
+    def contacts(self):
+        out = np.empty(self.n, np.uint8)
+        lib().oracle_get_contacts(self._h, _p(out))
+        return out
+
+
+# ---- the unmodified reference (this container only) ----
+def ref_available():
+    return os.path.exists(REF_SO)
+
+
+def ref_lib():
+    global _r
+    if _r is None:
+        L = C.CDLL(REF_SO)
+        V = C.c_void_p
+        L.ref_create.restype = V
+        L.ref_create.argtypes = [C.c_char_p, C.c_int, C.c_int]
+        L.ref_last_error.restype = C.c_char_p
+        L.ref_set_state.argtypes = [V, V, C.c_int]
+        L.ref_step.argtypes = [V, C.c_int]
+        L.ref_get_state.argtypes = [V, V]
+        L.ref_get_grid.argtypes = [V, V, V]
+        L.ref_get_cells.argtypes = [V, V, C.c_int]
+        L.ref_get_contacts.argtypes = [V, V]
+        L.ref_set_iterations.argtypes = [V, C.c_int]
+        L.ref_destroy.argtypes = [V]
+        L.ref_spawn_terrace.argtypes = [C.c_int, C.c_uint, V]
+        L.ref_spawn_seated.argtypes = [C.c_char_p, C.c_int, C.c_double, C.c_uint, V]
+        L.ref_load_sdf.argtypes = [C.c_char_p]
+        L.ref_timings.argtypes = [V, V]
+        _r = L
+    return _r
+
+
+class RefSim:
+    """swarm::CpuCrowdSim itself (counting sort), on venue 'terrace' | 'S' | 'M' | 'L'."""
+
+    def __init__(self, venue="terrace", threads=0):
+        self._h = ref_lib().ref_create(venue.encode(), 0, threads)
+        if not self._h:
+            raise RuntimeError(ref_lib().ref_last_error().decode())
+        self.n = 0
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            ref_lib().ref_destroy(self._h)
+
+    def set_state(self, boids):
+        b = np.ascontiguousarray(boids, dtype=np.float32).reshape(-1, 8)
+        assert ref_lib().ref_set_state(self._h, _p(b), b.shape[0]) == 0
+        self.n = b.shape[0]
+
+    def set_projection_iterations(self, k):
+        assert ref_lib().ref_set_iterations(self._h, int(k)) == 0
+
+    def step(self, steps=1):
+        assert ref_lib().ref_step(self._h, int(steps)) == 0
+
+    def state(self):
+        out = np.empty((self.n, 8), np.float32)
+        ref_lib().ref_get_state(self._h, _p(out))
+        return out
+
+    def grid(self):
+        g = np.empty(self.n, np.uint32)
+        b = np.empty(self.n, np.uint32)
+        ref_lib().ref_get_grid(self._h, _p(g), _p(b))
+        return g, b
+
+    def cells(self, ncells=1600):
+        out = np.empty((ncells, 2), np.uint32)
+        ref_lib().ref_get_cells(self._h, _p(out), ncells)
+        return out
+
+    def contacts(self):
+        out = np.empty(self.n, np.uint8)
+        ref_lib().ref_get_contacts(self._h, _p(out))
+        return out
+
+
+def ref_load_sdf(path):
+    return ref_lib().ref_load_sdf(path.encode()) == 0
+
+
+def ref_spawn_terrace(n, seed=1337):
+    out = np.empty((n, 8), np.float32)
+    assert ref_lib().ref_spawn_terrace(n, seed, _p(out)) == 0
+    return out
+
+
+def state_hash(state):
+    """FNV-1a 64 of the raw state bytes (the reference's golden::stateHash, tools/golden_state.hpp:121-126)."""
+    h = 0xcbf29ce484222325
+    for byte in np.ascontiguousarray(state, dtype=np.float32).tobytes():
+        h ^= byte
+        h = (h * 0x100000001b3) & 0xFFFFFFFFFFFFFFFF
+    return h

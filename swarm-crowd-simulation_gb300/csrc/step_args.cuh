@@ -1,0 +1,71 @@
+// The arguments every kernel of the step takes (by value: kernel parameter space, so that handles with different
+// venues and constants coexist in one process).
+#pragma once
+
+#include <cstdint>
+
+#include "../../include/swarm_cuda.h"
+
+namespace swarm_gpu {
+
+constexpr uint32_t INACTIVE_CELL = 0xFFFFFFFFu;
+constexpr float PLANE_WALL = 1.0f, PLANE_GROUNDED = 2.0f;
+constexpr float WALL_NONE = 1e9f;
+// ContactBits (reference include/swarm/cpu_crowd_sim.hpp:52-61)
+enum : uint8_t { C_EXIT = 1, C_FENCE_CCD = 2, C_FENCE = 4, C_FLOOR = 8, C_WALL = 16, C_AGENT = 32, C_SWEEP = 64, C_STEP_UP = 128 };
+
+// Device-side error flags (bit set by a kernel, read by the host after the step)
+enum : int { ERR_TIMEOUT = 1, ERR_BOUNDS = 2 };
+
+struct VenueArgs {
+    int32_t kind;
+    int32_t resX, resY, ncells;
+    float dminX, dminY, dspanX, dspanY, dmaxX, dmaxY;
+    float exloX, exloY, exhiX, exhiY, exMaxZ;
+    // stadium
+    const float* sdf;
+    int32_t sdfRes;
+    float sdfMinX, sdfMinY, sdfMinZ, sdfSpacing, sdfInv;
+    // grid
+    const float* wall;
+    int32_t wnx, wny;
+    float wox, woy, winv;
+    const float* nav;
+    int32_t nnx, nny;
+    float nox, noy, ninv;
+    const float* floorH;
+    const float* speedF;
+};
+
+struct StepArgs {
+    SwarmParams P;
+    VenueArgs V;
+    int32_t n;              // agents in the state
+    int32_t projectInFinal; // K > 0
+    // agent order: the GpuBoid state (position, velocity interleaved: 2 float4 per agent); ping-pong by step
+    float4* stateIn;
+    float4* stateOut;
+    const float2* aparam;   // (radius, v0) per agent
+    const float2* drive;    // forced e_goal per agent, or null
+    uint8_t* contacts;      // ContactBits per agent (the last step's)
+    // sort
+    uint32_t* key;          // cell of each agent (INACTIVE_CELL: evacuated)
+    uint32_t* rank;         // arrival order of each agent in its cell's counter
+    uint32_t* count;        // agents per cell; ncells + 1 buckets (the last: inactive)
+    uint32_t* start;        // exclusive scan of count
+    uint2* cells;           // (startIndex, agentCount) per cell, CpuCrowdSim::cells()
+    uint32_t* sidTmp;       // agent ids in scatter order (any order within a cell)
+    uint32_t* sid;          // agent ids in slot order (ascending within a cell)
+    uint32_t* skey;         // cell of each slot
+    // slot order
+    float4* pos0;           // start-of-step position (w: 1 active)
+    float4* vel0;           // start-of-step velocity
+    float2* prm;            // (radius, v0)
+    float4* proj[2];        // projection state: xyz, w = displacement so far (>= 0) or -1 (parked this step)
+    float4* vel1;           // predicted velocity
+    float4* plane;          // wall plane (n.xy, offset) and flags
+    uint8_t* ctc;           // the predict pass's contact bits
+    int* err;
+};
+
+}  // namespace swarm_gpu

@@ -1,0 +1,378 @@
+// The kernels of one crowd step (DedovSergei/swarm-crowd-simulation CrowdSim::step, src/crowd_sim.cpp:316-412;
+// its CPU port CpuCrowdSim::step, src/cpu_crowd_sim.cpp:967-1088):
+//
+//   k_hash        per agent: cell key (calc_grid.comp / CpuCrowdSim::hash :983-993) and its arrival rank in the cell's
+//                 counter (warp-aggregated atomics: one atomic per distinct cell per warp)
+//   k_scan        exclusive scan of the per-cell counts -> run starts; the cell table (start, count); counts cleared
+//   k_scatter     agent -> a slot in its cell's run (arrival order)
+//   k_rank_gather per slot: the agent's rank by id among its cell's agents -> the final slot (the key order over
+//                 unique (cell, id) keys = the reference's stable counting sort, CpuCrowdSim::sortCounting :997-1006);
+//                 gathers the start-of-step state into slot order (reorder.comp)
+//   k_predict     physics.comp PHYSICS_PASS 1 (cpu_crowd_sim.cpp:655-777)
+//   k_project     one Jacobi sweep, PHYSICS_PASS 2 (cpu_crowd_sim.cpp:781-831), K - 1 launches
+//   k_final       the last sweep, the final static contacts, the step-up limit, scatter to agent order (PHYSICS_PASS 3,
+//                 cpu_crowd_sim.cpp:835-866)
+//
+// The inactive agents (evacuated) sort after every cell; they keep their scatter order in the tail, which no pass
+// reads by position (the final pass copies each one's state by id). swarm_get_grid orders the tail by id on readout.
+#include "step_kernels.cuh"
+
+#include <type_traits>
+
+#include "device_math.cuh"
+#include "venue_grid.cuh"
+#include "venue_stadium.cuh"
+
+namespace swarm_gpu {
+
+__device__ __forceinline__ uint32_t cellID(const VenueArgs& V, float4 p) {
+    const int x = sclamp(int((p.x - V.dminX) / V.dspanX * float(V.resX)), 0, V.resX - 1);
+    const int y = sclamp(int((p.y - V.dminY) / V.dspanY * float(V.resY)), 0, V.resY - 1);
+    return uint32_t(x + y * V.resX);
+}
+
+__global__ void k_hash(StepArgs A) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.n) return;
+    float4 p = A.stateIn[2 * i];
+    if (isnan(p.x)) { p = make_float4(0.0f, 0.0f, 0.0f, 1.0f); A.stateIn[2 * i] = p; }
+    const uint32_t key = p.w == 0.0f ? INACTIVE_CELL : cellID(A.V, p);
+    const uint32_t bucket = key == INACTIVE_CELL ? uint32_t(A.V.ncells) : key;
+    const unsigned lane = threadIdx.x & 31u;
+    const int warpBase = i - int(lane);
+    const unsigned valid = A.n - warpBase >= 32 ? 0xffffffffu : ((1u << (A.n - warpBase)) - 1u);
+    const unsigned peers = __match_any_sync(valid, bucket);
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (int(lane) == leader) base = atomicAdd(A.count + bucket, uint32_t(__popc(peers)));
+    base = __shfl_sync(peers, base, leader);
+    A.key[i] = key;
+    A.rank[i] = base + uint32_t(__popc(peers & ((1u << lane) - 1u)));
+}
+
+// One block of SCAN_THREADS: each thread scans a contiguous chunk; a block-wide scan of the chunk sums links them.
+constexpr int SCAN_THREADS = 1024;
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan(StepArgs A) {
+    __shared__ uint32_t warpSums[32];
+    const int nb = A.V.ncells + 1;
+    const int chunk = (nb + SCAN_THREADS - 1) / SCAN_THREADS;
+    const int t = threadIdx.x;
+    const int b0 = t * chunk, b1 = min(b0 + chunk, nb);
+    uint32_t sum = 0;
+    for (int b = b0; b < b1; ++b) sum += A.count[b];
+    // block exclusive scan of the chunk sums
+    const unsigned lane = t & 31, warp = t >> 5;
+    uint32_t inc = sum;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (int(lane) >= o) inc += v;
+    }
+    if (lane == 31) warpSums[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = warpSums[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t v = __shfl_up_sync(0xffffffffu, w, o);
+            if (int(lane) >= o) w += v;
+        }
+        warpSums[lane] = w;   // inclusive
+    }
+    __syncthreads();
+    uint32_t run = inc - sum + (warp > 0 ? warpSums[warp - 1] : 0u);
+    for (int b = b0; b < b1; ++b) {
+        const uint32_t c = A.count[b];
+        A.start[b] = run;
+        if (b < A.V.ncells) A.cells[b] = c ? make_uint2(run, c) : make_uint2(0u, 0u);
+        A.count[b] = 0u;   // ready for the next step's hash
+        run += c;
+    }
+}
+
+__global__ void k_scatter(StepArgs A) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.n) return;
+    const uint32_t key = A.key[i];
+    const uint32_t bucket = key == INACTIVE_CELL ? uint32_t(A.V.ncells) : key;
+    const uint32_t slot = A.start[bucket] + A.rank[i];
+    if (slot >= uint32_t(A.n)) { atomicOr(A.err, ERR_BOUNDS); return; }   // counts out of step with the keys
+    A.sidTmp[slot] = uint32_t(i);
+}
+
+template <bool kPerAgent>
+__global__ void k_rank_gather(StepArgs A) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= A.n) return;
+    const int nActive = int(A.start[A.V.ncells]);
+    const uint32_t me = A.sidTmp[s];
+    if (me >= uint32_t(A.n)) { atomicOr(A.err, ERR_BOUNDS); return; }
+    if (s >= nActive) { A.sid[s] = me; A.skey[s] = INACTIVE_CELL; return; }
+    const uint32_t c = A.key[me];
+    const uint2 cs = A.cells[c];
+    uint32_t r = 0;
+    for (uint32_t j = cs.x; j < cs.x + cs.y; ++j) r += A.sidTmp[j] < me ? 1u : 0u;
+    const uint32_t t = cs.x + r;
+    A.sid[t] = me;
+    A.skey[t] = c;
+    A.pos0[t] = A.stateIn[2 * size_t(me)];
+    A.vel0[t] = A.stateIn[2 * size_t(me) + 1];
+    if (kPerAgent) A.prm[t] = A.aparam[me];
+}
+
+// ---- the physics passes ----
+template <class Venue>
+struct Body {
+    static constexpr bool kUniform = std::is_same<Venue, Stadium>::value;
+};
+
+template <class Venue>
+__device__ __forceinline__ f2 goalOf(const StepArgs& A, const Venue& ven, f3 p, uint32_t id) {
+    if (A.drive) { const float2 d = A.drive[id]; return f2{d.x, d.y}; }
+    return ven.goal(p);
+}
+
+__device__ __forceinline__ f2 separationForce(const SwarmParams& P, f3 offset, uint32_t self, uint32_t other, float rsep, float rsep2) {
+    const float d2 = dot(offset, offset);
+    if (d2 >= rsep2) return f2{0.0f, 0.0f};
+    const float w = 1.0f - sqrtf(d2) / rsep;
+    const float magnitude = P.k_sep * w * w;
+    const float dxy2 = dot(xy(offset), xy(offset));
+    if (dxy2 <= P.stacked_xy2) return magnitude * pairDirection(self, other, P.hash_to_radians);
+    return magnitude * xy(offset) * (1.0f / sqrtf(dxy2));
+}
+
+template <class Venue>
+__global__ void __launch_bounds__(128) k_predict(StepArgs A) {
+    constexpr bool kUniform = Body<Venue>::kUniform;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= A.n) return;
+    const int nActive = int(A.start[A.V.ncells]);
+    if (s >= nActive) return;
+    const SwarmParams& P = A.P;
+    const Venue ven{A.P, A.V};
+    const uint32_t self = A.sid[s], cid = A.skey[s];
+    uint32_t contact = 0;
+    const float4 p = A.pos0[s], v = A.vel0[s];
+    if (ven.exits(p)) {
+        A.proj[0][s] = make_float4(P.park_coord, P.park_coord, P.park_coord, -1.0f);
+        A.vel1[s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        A.ctc[s] = C_EXIT;
+        return;
+    }
+    const f2 eGoal = goalOf(A, ven, xyz(p), self);
+    const float ri = kUniform ? P.body_radius : A.prm[s].x;
+    const int resX = A.V.resX, resY = A.V.resY;
+    const int cx = int(cid % uint32_t(resX)), cy = int(cid / uint32_t(resX));
+    f2 sep{0.0f, 0.0f};
+    float sAhead = 1e9f;
+    const int R = P.perc_ring;
+    for (int y = -R; y <= R; y++) {
+        const int ny = cy + y;
+        if (ny < 0 || ny >= resY) continue;
+        for (int x = -R; x <= R; x++) {
+            const int nx = cx + x;
+            if (nx < 0 || nx >= resX) continue;
+            const uint2 cell = __ldg(reinterpret_cast<const uint2*>(A.cells) + (nx + ny * resX));
+            for (uint32_t k = cell.x; k < cell.x + cell.y; k++) {
+                if (int(k) == s) continue;
+                const float4 op = A.pos0[k];
+                const f3 offset = xyz(p) - xyz(op);
+                const float dxy2 = dot(xy(offset), xy(offset));
+                if (dxy2 < P.r_perc2) {
+                    const uint32_t other = A.sid[k];
+                    float dc, rs, rs2;
+                    if (kUniform) { dc = P.body_diam; rs = P.r_sep; rs2 = P.r_sep2; }
+                    else { dc = ri + A.prm[k].x; rs = dc + P.sep_margin; rs2 = rs * rs; }
+                    sep = sep + separationForce(P, offset, self, other, rs, rs2);
+                    const float ahead = -dot(xy(offset), eGoal);
+                    const float lateral = fabsf(offset.x * eGoal.y - offset.y * eGoal.x);
+                    const float dxy = sqrtf(dxy2);
+                    const float key = kUniform ? dxy : dxy - dc;
+                    if (ahead > 0.0f && lateral < dc && key < sAhead) {
+                        const f2 eOther = goalOf(A, ven, xyz(op), other);
+                        const float aheadOther = dot(xy(offset), eOther);
+                        const bool mutual = aheadOther > 0.0f && fabsf(offset.x * eOther.y - offset.y * eOther.x) < dc;
+                        if (!mutual || ahead > aheadOther || (ahead == aheadOther && self > other)) sAhead = key;
+                    }
+                }
+            }
+        }
+    }
+    float vDes;
+    if (kUniform) {
+        vDes = sclamp((sAhead - P.body_diam) * P.headway_rate, 0.0f, P.v_max) * length(eGoal);
+    } else {
+        const float vFree = A.prm[s].y * ven.speedFactor(xyz(p));
+        vDes = sclamp(sAhead * P.headway_rate, 0.0f, vFree) * length(eGoal);
+    }
+    const f2 eDir = safeNormalize(eGoal + sep, P.safe_eps);
+
+    // obstacle avoidance at torso height
+    f2 aObs{0.0f, 0.0f};
+    const f3 torso{p.x + 0.0f, p.y + 0.0f, p.z + P.torso_height};
+    bool onFence = false;
+    const float dTorso = ven.sceneDist(torso, onFence);
+    if (dTorso < P.obstacle_range) {
+        const f2 norm = ven.sceneNormal(torso, onFence);
+        if (length(norm) > P.obstacle_min_normal)
+            aObs = safeNormalize(norm, P.safe_eps) * (P.obstacle_range - dTorso) * P.w_obs * P.obstacle_gain;
+    }
+
+    // kinematics
+    const f2 vEq = eDir * vDes + aObs * P.tau_relax;
+    f3 nv = xyz(v);
+    setXY(nv, vEq + (xy(nv) - vEq) * P.relax_step);
+    const float along = dot(xy(nv), eGoal);
+    if (along > vDes) setXY(nv, xy(nv) - eGoal * (along - vDes));
+    nv.z -= P.gravity_dt;
+    nv.z = smin(nv.z, 0.0f);
+    if (length(xy(nv)) > P.v_max) setXY(nv, safeNormalize(xy(nv), P.safe_eps) * P.v_max);
+    f3 np = xyz(p) + nv * P.dt;
+
+    f3 wall;
+    const bool grounded = ven.resolveStatic(xyz(p), np, nv, false, wall, contact, ri);
+    if (wall.x == 0.0f && wall.y == 0.0f) wall = ven.wallPlaneProbe(np, ri);
+    A.proj[0][s] = make_float4(np.x, np.y, np.z, 0.0f);
+    A.vel1[s] = make_float4(nv.x, nv.y, nv.z, 0.0f);
+    const f2 wn{wall.x, wall.y};
+    A.plane[s] = make_float4(wn.x, wn.y, dot(xy(np), wn) - wall.z,
+                             (nonzero(wn) ? PLANE_WALL : 0.0f) + (grounded ? PLANE_GROUNDED : 0.0f));
+    A.ctc[s] = uint8_t(contact);
+}
+
+// One Jacobi sweep for slot s reading `in` (cpu_crowd_sim.cpp:781-822 projectSlot); w of the result: displacement
+template <class Venue>
+__device__ __forceinline__ float4 projectSlot(const StepArgs& A, const Venue& ven, const float4* __restrict__ in, int s) {
+    constexpr bool kUniform = Body<Venue>::kUniform;
+    const SwarmParams& P = A.P;
+    const float4 b = in[s];
+    if (b.w < 0.0f) return b;   // parked this step
+    const uint32_t cid = A.skey[s];
+    const int resX = A.V.resX, resY = A.V.resY;
+    const int cx = int(cid % uint32_t(resX)), cy = int(cid / uint32_t(resX));
+    const float ri = kUniform ? P.body_radius : A.prm[s].x;
+    f2 corr{0.0f, 0.0f};
+    int nContacts = 0;
+    for (int y = -1; y <= 1; y++) {
+        const int ny = cy + y;
+        if (ny < 0 || ny >= resY) continue;
+        for (int x = -1; x <= 1; x++) {
+            const int nx = cx + x;
+            if (nx < 0 || nx >= resX) continue;
+            const uint2 cell = __ldg(reinterpret_cast<const uint2*>(A.cells) + (nx + ny * resX));
+            for (uint32_t k = cell.x; k < cell.x + cell.y; k++) {
+                if (int(k) == s) continue;
+                const float4 op = in[k];
+                const f3 offset = xyz(b) - xyz(op);
+                float dc, dc2;
+                if (kUniform) { dc = P.body_diam; dc2 = P.body_diam2; }
+                else { dc = ri + A.prm[k].x; dc2 = dc * dc; }
+                const float dxy2 = dot(xy(offset), xy(offset));
+                if (op.w >= 0.0f && fabsf(offset.z) < dc && dxy2 < dc2) {
+                    const float dxy = sqrtf(dxy2);
+                    const float shift = 0.5f * (dc - dxy);
+                    f2 c;
+                    if (dxy2 <= P.stacked_xy2) c = shift * pairDirection(A.sid[s], A.sid[k], P.hash_to_radians);
+                    else c = shift * (xy(offset) / dxy);
+                    corr = corr + c;
+                    ++nContacts;
+                }
+            }
+        }
+    }
+    corr = corr * (P.proj_relax / float(smax(nContacts, 1)));
+    const float len = length(corr);
+    if (len > P.proj_max_shift) corr = corr * (P.proj_max_shift / len);
+    f3 q = xyz(b);
+    setXY(q, xy(q) + corr);
+    ven.fenceProject(q);
+    const float4 plane = A.plane[s];
+    if (plane.w == PLANE_WALL || plane.w == PLANE_WALL + PLANE_GROUNDED) {   // fmod(w, 2) == PLANE_WALL, w in {0, 1, 2, 3}
+        const float sd = plane.z - dot(xy(q), f2{plane.x, plane.y});
+        if (sd > 0.0f) setXY(q, xy(q) + f2{plane.x, plane.y} * sd);
+    }
+    const f2 d = xy(q) - xy(b);
+    return make_float4(q.x, q.y, b.z, b.w + length(d));
+}
+
+template <class Venue>
+__global__ void __launch_bounds__(128) k_project(StepArgs A, int inBuf) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= A.n) return;
+    if (s >= int(A.start[A.V.ncells])) return;
+    const Venue ven{A.P, A.V};
+    A.proj[inBuf ^ 1][s] = projectSlot(A, ven, A.proj[inBuf], s);
+}
+
+template <class Venue>
+__global__ void __launch_bounds__(128) k_final(StepArgs A, int inBuf) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= A.n) return;
+    const uint32_t self = A.sid[s];
+    if (s >= int(A.start[A.V.ncells])) {   // evacuated before this step: carried over
+        A.stateOut[2 * size_t(self)] = A.stateIn[2 * size_t(self)];
+        A.stateOut[2 * size_t(self) + 1] = A.stateIn[2 * size_t(self) + 1];
+        A.contacts[self] = 0;
+        return;
+    }
+    const SwarmParams& P = A.P;
+    const Venue ven{A.P, A.V};
+    const float4 b = A.projectInFinal ? projectSlot(A, ven, A.proj[inBuf], s) : A.proj[inBuf][s];
+    if (b.w < 0.0f) {   // parked this step
+        A.stateOut[2 * size_t(self)] = make_float4(P.park_coord, P.park_coord, P.park_coord, 0.0f);
+        A.stateOut[2 * size_t(self) + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        A.contacts[self] = A.ctc[s];
+        return;
+    }
+    constexpr bool kUniform = Body<Venue>::kUniform;
+    const float ri = kUniform ? P.body_radius : A.prm[s].x;
+    f3 np = xyz(b);
+    f3 nv = xyz(A.vel1[s]);
+    const f3 pOld = xyz(A.pos0[s]);
+    uint32_t contact = A.ctc[s];
+    if (b.w > 0.0f) {   // the projection moved it: the final static contacts
+        contact |= C_AGENT;
+        f3 wall;
+        ven.resolveStatic(pOld, np, nv, A.plane[s].w >= PLANE_GROUNDED, wall, contact, ri);
+    }
+    if (ven.limitStepUp(pOld, np, nv, ri)) contact |= C_STEP_UP;
+    A.stateOut[2 * size_t(self)] = make_float4(np.x, np.y, np.z, 1.0f);
+    A.stateOut[2 * size_t(self) + 1] = make_float4(nv.x, nv.y, nv.z, length(nv));
+    A.contacts[self] = uint8_t(contact);
+}
+
+// ---- host launchers ----
+namespace {
+inline int blocks(int n, int t) { return (n + t - 1) / t; }
+}
+
+void launch_sort(const StepArgs& A, cudaStream_t st, int64_t* launches) {
+    const int n = A.n;
+    k_hash<<<blocks(n, 256), 256, 0, st>>>(A);
+    k_scan<<<1, SCAN_THREADS, 0, st>>>(A);
+    k_scatter<<<blocks(n, 256), 256, 0, st>>>(A);
+    if (A.P.uniform_body) k_rank_gather<false><<<blocks(n, 256), 256, 0, st>>>(A);
+    else k_rank_gather<true><<<blocks(n, 256), 256, 0, st>>>(A);
+    *launches += 4;
+}
+
+template <class Venue>
+static void physicsImpl(const StepArgs& A, cudaStream_t st, int64_t* launches, cudaEvent_t* ev) {
+    const int n = A.n, K = A.P.proj_iterations;
+    k_predict<Venue><<<blocks(n, 128), 128, 0, st>>>(A);
+    if (ev) cudaEventRecord(ev[0], st);
+    int in = 0;
+    for (int it = 1; it < K; ++it) {
+        k_project<Venue><<<blocks(n, 128), 128, 0, st>>>(A, in);
+        in ^= 1;
+    }
+    if (ev) cudaEventRecord(ev[1], st);
+    k_final<Venue><<<blocks(n, 128), 128, 0, st>>>(A, in);
+    *launches += 2 + (K > 1 ? K - 1 : 0);
+}
+
+void launch_physics(const StepArgs& A, cudaStream_t st, int64_t* launches, cudaEvent_t* ev) {
+    if (A.V.kind == SWARM_VENUE_STADIUM) physicsImpl<Stadium>(A, st, launches, ev);
+    else physicsImpl<GridVenue>(A, st, launches, ev);
+}
+
+}  // namespace swarm_gpu

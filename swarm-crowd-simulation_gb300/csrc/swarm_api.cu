@@ -1,0 +1,376 @@
+// The C ABI of include/swarm_cuda.h: one handle = one simulation on the current CUDA device.
+//
+// Stands in for the reference's CrowdSim (DedovSergei/swarm-crowd-simulation include/swarm/crowd_sim.hpp:53-194,
+// src/crowd_sim.cpp) and mirrors its CPU port CpuCrowdSim (include/swarm/cpu_crowd_sim.hpp:30-169): upload writes the
+// state, step runs hash -> key sort -> cell ranges + gather -> predict -> K - 1 sweeps -> final and swaps the state
+// halves, the inspection calls return the last step's sorted pairs, cell table and contact bits.
+// No exception crosses the boundary: every entry returns a status, swarm_last_error the message.
+
+#include "../../include/swarm_cuda.h"
+#include "step_kernels.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+using swarm_gpu::StepArgs;
+
+struct SwarmSim {
+    SwarmParams P{};
+    SwarmVenue V{};
+    int device = 0;
+    int capacity = 0;
+    int n = 0;
+    int readIdx = 0;
+    bool hasState = false;
+    cudaStream_t ownStream = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    // device buffers
+    float4* state[2] = {nullptr, nullptr};
+    float2* aparam = nullptr;
+    float2* drive = nullptr;
+    bool driveOn = false;
+    uint8_t* contacts = nullptr;
+    uint32_t *key = nullptr, *rank = nullptr, *count = nullptr, *start = nullptr, *sidTmp = nullptr, *sid = nullptr, *skey = nullptr;
+    uint2* cells = nullptr;
+    float4 *pos0 = nullptr, *vel0 = nullptr, *proj0 = nullptr, *proj1 = nullptr, *vel1 = nullptr, *plane = nullptr;
+    float2* prm = nullptr;
+    uint8_t* ctc = nullptr;
+    int* errFlag = nullptr;
+    float *dSdf = nullptr, *dWall = nullptr, *dNav = nullptr, *dFloor = nullptr, *dSpeed = nullptr;
+    int ncells = 0;
+    // execution
+    bool useGraph = false;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    bool timing = false;
+    cudaEvent_t ev[6] = {};
+    SwarmStageTimes times{};
+    int64_t launches = 0;
+    std::vector<void*> allocs;
+
+    StepArgs args(int in) const;
+    int fail(int code, const std::string& msg) { err = msg; return code; }
+    void dropGraphs() {
+        for (auto& g : graph) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    }
+    int enqueueStep(int in, cudaEvent_t* evs);
+    ~SwarmSim();
+};
+
+namespace {
+
+bool cudaOk(SwarmSim* h, cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return true;
+    h->err = std::string(what) + ": " + cudaGetErrorString(e);
+    return false;
+}
+
+template <class T>
+bool devAlloc(SwarmSim* h, T** p, size_t count) {
+    void* q = nullptr;
+    if (cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T)) != cudaSuccess) return false;
+    h->allocs.push_back(q);
+    *p = static_cast<T*>(q);
+    return true;
+}
+
+}  // namespace
+
+SwarmSim::~SwarmSim() {
+    dropGraphs();
+    for (auto& e : ev) if (e) cudaEventDestroy(e);
+    for (void* p : allocs) cudaFree(p);
+    if (ownStream) cudaStreamDestroy(ownStream);
+}
+
+StepArgs SwarmSim::args(int in) const {
+    StepArgs A{};
+    A.P = P;
+    auto& v = A.V;
+    v.kind = V.kind;
+    v.resX = V.grid_res_x; v.resY = V.grid_res_y; v.ncells = ncells;
+    v.dminX = V.domain_min_x; v.dminY = V.domain_min_y; v.dspanX = V.domain_span_x; v.dspanY = V.domain_span_y;
+    v.dmaxX = V.domain_min_x + V.domain_span_x; v.dmaxY = V.domain_min_y + V.domain_span_y;
+    v.exloX = V.exit_lo_x; v.exloY = V.exit_lo_y; v.exhiX = V.exit_hi_x; v.exhiY = V.exit_hi_y; v.exMaxZ = V.exit_max_z;
+    v.sdf = dSdf; v.sdfRes = V.sdf_res;
+    v.sdfMinX = V.sdf_origin[0]; v.sdfMinY = V.sdf_origin[1]; v.sdfMinZ = V.sdf_origin[2];
+    v.sdfSpacing = V.sdf_spacing; v.sdfInv = V.sdf_spacing > 0.0f ? 1.0f / V.sdf_spacing : 0.0f;
+    v.wall = dWall; v.wnx = V.wall_nx; v.wny = V.wall_ny; v.wox = V.wall_origin_x; v.woy = V.wall_origin_y;
+    v.winv = V.wall_h > 0.0f ? 1.0f / V.wall_h : 0.0f;
+    v.nav = dNav; v.nnx = V.nav_nx; v.nny = V.nav_ny; v.nox = V.nav_origin_x; v.noy = V.nav_origin_y;
+    v.ninv = V.nav_h > 0.0f ? 1.0f / V.nav_h : 0.0f;
+    v.floorH = dFloor; v.speedF = dSpeed;
+    A.n = n;
+    A.projectInFinal = P.proj_iterations > 0 ? 1 : 0;
+    A.stateIn = state[in];
+    A.stateOut = state[in ^ 1];
+    A.aparam = aparam;
+    A.drive = driveOn ? drive : nullptr;
+    A.contacts = contacts;
+    A.key = key; A.rank = rank; A.count = count; A.start = start; A.cells = cells;
+    A.sidTmp = sidTmp; A.sid = sid; A.skey = skey;
+    A.pos0 = pos0; A.vel0 = vel0; A.prm = prm; A.proj[0] = proj0; A.proj[1] = proj1;
+    A.vel1 = vel1; A.plane = plane; A.ctc = ctc; A.err = errFlag;
+    return A;
+}
+
+int SwarmSim::enqueueStep(int in, cudaEvent_t* evs) {
+    const StepArgs A = args(in);
+    if (evs) cudaEventRecord(evs[0], stream);
+    swarm_gpu::launch_sort(A, stream, &launches);
+    if (evs) cudaEventRecord(evs[1], stream);
+    swarm_gpu::launch_physics(A, stream, &launches, evs ? evs + 2 : nullptr);
+    if (evs) cudaEventRecord(evs[4], stream);
+    return cudaOk(this, cudaGetLastError(), "kernel launch") ? SWARM_OK : SWARM_E_CUDA;
+}
+
+extern "C" {
+
+int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capacity, SwarmHandle* out) {
+    if (!params || !venue || !out || n_capacity <= 0) return SWARM_E_INVALID;
+    *out = nullptr;
+    SwarmSim* h = new (std::nothrow) SwarmSim();
+    if (!h) return SWARM_E_OOM;
+    h->P = *params;
+    h->V = *venue;
+    h->capacity = n_capacity;
+    const SwarmVenue& V = *venue;
+    auto bad = [&](const char* m) { delete h; (void)m; return SWARM_E_INVALID; };
+    if (V.kind != SWARM_VENUE_STADIUM && V.kind != SWARM_VENUE_GRID) return bad("venue kind");
+    if (V.grid_res_x <= 0 || V.grid_res_y <= 0 || !(V.domain_span_x > 0.0f) || !(V.domain_span_y > 0.0f)) return bad("grid");
+    if (params->proj_iterations < 0 || params->perc_ring < 1) return bad("params");
+    if (V.kind == SWARM_VENUE_STADIUM && (!V.sdf || V.sdf_res < 2 || !(V.sdf_spacing > 0.0f))) return bad("sdf");
+    if (V.kind == SWARM_VENUE_GRID && (!V.wall_sdf || !V.nav_dist || V.wall_nx < 2 || V.wall_ny < 2 || V.nav_nx < 2 || V.nav_ny < 2 ||
+                                       !(V.wall_h > 0.0f) || !(V.nav_h > 0.0f)))
+        return bad("grid fields");
+    const double cells = double(V.grid_res_x) * double(V.grid_res_y);
+    if (cells > 2.0e9) return bad("too many cells");
+    h->ncells = int(cells);
+    cudaGetDevice(&h->device);
+    if (!cudaOk(h, cudaStreamCreateWithFlags(&h->ownStream, cudaStreamNonBlocking), "stream")) { delete h; return SWARM_E_CUDA; }
+    h->stream = h->ownStream;
+    const size_t N = size_t(n_capacity);
+    bool ok = devAlloc(h, &h->state[0], 2 * N) && devAlloc(h, &h->state[1], 2 * N) && devAlloc(h, &h->aparam, N) &&
+              devAlloc(h, &h->drive, N) && devAlloc(h, &h->contacts, N) && devAlloc(h, &h->key, N) && devAlloc(h, &h->rank, N) &&
+              devAlloc(h, &h->count, size_t(h->ncells) + 1) && devAlloc(h, &h->start, size_t(h->ncells) + 1) &&
+              devAlloc(h, &h->cells, size_t(h->ncells)) && devAlloc(h, &h->sidTmp, N) && devAlloc(h, &h->sid, N) &&
+              devAlloc(h, &h->skey, N) && devAlloc(h, &h->pos0, N) && devAlloc(h, &h->vel0, N) && devAlloc(h, &h->proj0, N) &&
+              devAlloc(h, &h->proj1, N) && devAlloc(h, &h->vel1, N) && devAlloc(h, &h->plane, N) && devAlloc(h, &h->prm, N) &&
+              devAlloc(h, &h->ctc, N) && devAlloc(h, &h->errFlag, 1);
+    if (ok && V.kind == SWARM_VENUE_STADIUM) {
+        const size_t nv = size_t(V.sdf_res) * size_t(V.sdf_res) * size_t(V.sdf_res);
+        ok = devAlloc(h, &h->dSdf, nv) && cudaMemcpy(h->dSdf, V.sdf, nv * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
+    }
+    if (ok && V.kind == SWARM_VENUE_GRID) {
+        const size_t nw = size_t(V.wall_nx) * size_t(V.wall_ny), nn = size_t(V.nav_nx) * size_t(V.nav_ny);
+        ok = devAlloc(h, &h->dWall, nw) && cudaMemcpy(h->dWall, V.wall_sdf, nw * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
+             devAlloc(h, &h->dNav, nn) && cudaMemcpy(h->dNav, V.nav_dist, nn * 4, cudaMemcpyHostToDevice) == cudaSuccess;
+        if (ok && V.floor_height)
+            ok = devAlloc(h, &h->dFloor, nw) && cudaMemcpy(h->dFloor, V.floor_height, nw * 4, cudaMemcpyHostToDevice) == cudaSuccess;
+        if (ok && V.speed_factor)
+            ok = devAlloc(h, &h->dSpeed, nw) && cudaMemcpy(h->dSpeed, V.speed_factor, nw * 4, cudaMemcpyHostToDevice) == cudaSuccess;
+    }
+    // host pointers of the venue are not kept
+    h->V.sdf = nullptr; h->V.wall_sdf = nullptr; h->V.nav_dist = nullptr; h->V.floor_height = nullptr;
+    h->V.speed_factor = nullptr; h->V.exit_boxes = nullptr;
+    if (!ok) { delete h; return SWARM_E_OOM; }
+    if (cudaMemset(h->count, 0, (size_t(h->ncells) + 1) * 4) != cudaSuccess || cudaMemset(h->errFlag, 0, 4) != cudaSuccess ||
+        cudaMemset(h->contacts, 0, N) != cudaSuccess) {
+        delete h;
+        return SWARM_E_CUDA;
+    }
+    // default per-agent parameters: the uniform body
+    std::vector<float2> ap(N, make_float2(params->body_radius, params->v_max));
+    cudaMemcpy(h->aparam, ap.data(), N * sizeof(float2), cudaMemcpyHostToDevice);
+    for (auto& e : h->ev) cudaEventCreate(&e);
+    *out = h;
+    return SWARM_OK;
+}
+
+int swarm_destroy(SwarmHandle h) {
+    if (!h) return SWARM_E_INVALID;
+    cudaStreamSynchronize(h->stream);
+    delete h;
+    return SWARM_OK;
+}
+
+int swarm_set_stream(SwarmHandle h, void* s) {
+    if (!h) return SWARM_E_INVALID;
+    h->dropGraphs();
+    h->stream = s ? static_cast<cudaStream_t>(s) : h->ownStream;
+    return SWARM_OK;
+}
+
+int swarm_last_error(SwarmHandle h, char* buf, int len) {
+    if (!h || !buf || len <= 0) return SWARM_E_INVALID;
+    std::snprintf(buf, size_t(len), "%s", h->err.c_str());
+    return SWARM_OK;
+}
+
+static int uploadImpl(SwarmHandle h, const float* boids, int n, cudaMemcpyKind kind) {
+    if (!h || !boids) return SWARM_E_INVALID;
+    if (n <= 0 || n > h->capacity) return h->fail(SWARM_E_INVALID, "agent count " + std::to_string(n) + " outside 1.." + std::to_string(h->capacity));
+    if (n != h->n) h->dropGraphs();
+    h->n = n;
+    h->readIdx = 0;
+    const size_t bytes = size_t(n) * 32;
+    // both halves, as CrowdSim::upload / CpuCrowdSim::setState
+    if (!cudaOk(h, cudaMemcpyAsync(h->state[0], boids, bytes, kind, h->stream), "upload") ||
+        !cudaOk(h, cudaMemcpyAsync(h->state[1], boids, bytes, kind, h->stream), "upload"))
+        return SWARM_E_CUDA;
+    h->hasState = true;
+    return SWARM_OK;
+}
+
+int swarm_upload_state(SwarmHandle h, const float* boids, int n) { return uploadImpl(h, boids, n, cudaMemcpyHostToDevice); }
+int swarm_upload_state_device(SwarmHandle h, const float* d, int n) { return uploadImpl(h, d, n, cudaMemcpyDeviceToDevice); }
+
+static int downloadImpl(SwarmHandle h, float* boids, int n, cudaMemcpyKind kind) {
+    if (!h || !boids) return SWARM_E_INVALID;
+    if (!h->hasState) return h->fail(SWARM_E_STATE, "no state uploaded");
+    if (n != h->n) return h->fail(SWARM_E_INVALID, "download size " + std::to_string(n) + " != state size " + std::to_string(h->n));
+    if (!cudaOk(h, cudaMemcpyAsync(boids, h->state[h->readIdx], size_t(n) * 32, kind, h->stream), "download")) return SWARM_E_CUDA;
+    if (kind == cudaMemcpyDeviceToHost && !cudaOk(h, cudaStreamSynchronize(h->stream), "download sync")) return SWARM_E_CUDA;
+    return SWARM_OK;
+}
+
+int swarm_download_state(SwarmHandle h, float* boids, int n) { return downloadImpl(h, boids, n, cudaMemcpyDeviceToHost); }
+int swarm_download_state_device(SwarmHandle h, float* d, int n) { return downloadImpl(h, d, n, cudaMemcpyDeviceToDevice); }
+
+int swarm_set_agent_params(SwarmHandle h, const float* radius, const float* v0, int n) {
+    if (!h || !radius || !v0 || n <= 0 || n > h->capacity) return SWARM_E_INVALID;
+    std::vector<float2> ap(static_cast<size_t>(n));
+    for (int i = 0; i < n; ++i) ap[size_t(i)] = make_float2(radius[i], v0[i]);
+    if (!cudaOk(h, cudaMemcpyAsync(h->aparam, ap.data(), size_t(n) * sizeof(float2), cudaMemcpyHostToDevice, h->stream), "params"))
+        return SWARM_E_CUDA;
+    return cudaOk(h, cudaStreamSynchronize(h->stream), "params") ? SWARM_OK : SWARM_E_CUDA;
+}
+
+int swarm_set_iterations(SwarmHandle h, int k) {
+    if (!h) return SWARM_E_INVALID;
+    if (k < 0) return h->fail(SWARM_E_INVALID, "iterations must be >= 0");
+    h->P.proj_iterations = k;
+    h->dropGraphs();
+    return SWARM_OK;
+}
+
+int swarm_set_drive_table(SwarmHandle h, const float* dirs, int n) {
+    if (!h) return SWARM_E_INVALID;
+    h->dropGraphs();
+    if (!dirs) { h->driveOn = false; return SWARM_OK; }
+    if (n != h->n) return h->fail(SWARM_E_INVALID, "the drive table must have one entry per agent");
+    if (!cudaOk(h, cudaMemcpyAsync(h->drive, dirs, size_t(n) * sizeof(float2), cudaMemcpyHostToDevice, h->stream), "drive"))
+        return SWARM_E_CUDA;
+    h->driveOn = true;
+    return cudaOk(h, cudaStreamSynchronize(h->stream), "drive") ? SWARM_OK : SWARM_E_CUDA;
+}
+
+int swarm_set_graph(SwarmHandle h, int enabled) {
+    if (!h) return SWARM_E_INVALID;
+    h->useGraph = enabled != 0;
+    if (!h->useGraph) h->dropGraphs();
+    return SWARM_OK;
+}
+
+int swarm_set_timing(SwarmHandle h, int enabled) {
+    if (!h) return SWARM_E_INVALID;
+    h->timing = enabled != 0;
+    return SWARM_OK;
+}
+
+int swarm_step(SwarmHandle h, int steps) {
+    if (!h) return SWARM_E_INVALID;
+    if (!h->hasState) return h->fail(SWARM_E_STATE, "no state (upload one first)");
+    if (steps < 0) return h->fail(SWARM_E_INVALID, "steps must be >= 0");
+    h->launches = 0;
+    for (int s = 0; s < steps; ++s) {
+        const int in = h->readIdx;
+        const bool timeThis = h->timing && s == steps - 1;
+        if (h->useGraph && !timeThis) {
+            if (!h->graph[in]) {
+                cudaGraph_t g = nullptr;
+                if (!cudaOk(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "capture")) return SWARM_E_CUDA;
+                int64_t saved = h->launches;
+                const int rc = h->enqueueStep(in, nullptr);
+                h->launches = saved;
+                if (!cudaOk(h, cudaStreamEndCapture(h->stream, &g), "capture end") || rc != SWARM_OK) return SWARM_E_CUDA;
+                const bool inst = cudaOk(h, cudaGraphInstantiate(&h->graph[in], g, 0), "graph instantiate");
+                cudaGraphDestroy(g);
+                if (!inst) return SWARM_E_CUDA;
+            }
+            if (!cudaOk(h, cudaGraphLaunch(h->graph[in], h->stream), "graph launch")) return SWARM_E_CUDA;
+            h->launches += 6 + std::max(h->P.proj_iterations - 1, 0);
+        } else {
+            const int rc = h->enqueueStep(in, timeThis ? h->ev : nullptr);
+            if (rc != SWARM_OK) return rc;
+        }
+        if (timeThis) {
+            if (!cudaOk(h, cudaEventSynchronize(h->ev[4]), "timing")) return SWARM_E_CUDA;
+            float sort = 0, pred = 0, proj = 0, fin = 0;
+            cudaEventElapsedTime(&sort, h->ev[0], h->ev[1]);
+            cudaEventElapsedTime(&pred, h->ev[1], h->ev[2]);
+            cudaEventElapsedTime(&proj, h->ev[2], h->ev[3]);
+            cudaEventElapsedTime(&fin, h->ev[3], h->ev[4]);
+            h->times = SwarmStageTimes{0.0f, sort, 0.0f, pred, proj, fin, sort + pred + proj + fin};
+        }
+        h->readIdx ^= 1;
+    }
+    return SWARM_OK;
+}
+
+int swarm_synchronize(SwarmHandle h) {
+    if (!h) return SWARM_E_INVALID;
+    if (!cudaOk(h, cudaStreamSynchronize(h->stream), "synchronize")) return SWARM_E_CUDA;
+    int flag = 0;
+    cudaMemcpy(&flag, h->errFlag, 4, cudaMemcpyDeviceToHost);
+    if (flag) return h->fail(SWARM_E_TIMEOUT, "a device-side wait gave up (flag " + std::to_string(flag) + ")");
+    return SWARM_OK;
+}
+
+int swarm_get_grid(SwarmHandle h, uint32_t* grid_id, uint32_t* boid_id, int n) {
+    if (!h || !grid_id || !boid_id) return SWARM_E_INVALID;
+    if (n != h->n) return h->fail(SWARM_E_INVALID, "grid size mismatch");
+    if (!cudaOk(h, cudaStreamSynchronize(h->stream), "sync")) return SWARM_E_CUDA;
+    cudaMemcpy(grid_id, h->skey, size_t(n) * 4, cudaMemcpyDeviceToHost);
+    cudaMemcpy(boid_id, h->sid, size_t(n) * 4, cudaMemcpyDeviceToHost);
+    // the evacuated tail, in id order (CpuCrowdSim's stable counting sort)
+    int first = n;
+    while (first > 0 && grid_id[first - 1] == 0xFFFFFFFFu) --first;
+    std::sort(boid_id + first, boid_id + n);
+    return SWARM_OK;
+}
+
+int swarm_get_cells(SwarmHandle h, uint32_t* start_count, int n_cells) {
+    if (!h) return SWARM_E_INVALID;
+    if (!start_count) return h->ncells;
+    if (n_cells != h->ncells) return h->fail(SWARM_E_INVALID, "cell count mismatch");
+    if (!cudaOk(h, cudaStreamSynchronize(h->stream), "sync")) return SWARM_E_CUDA;
+    return cudaOk(h, cudaMemcpy(start_count, h->cells, size_t(n_cells) * 8, cudaMemcpyDeviceToHost), "cells") ? SWARM_OK : SWARM_E_CUDA;
+}
+
+int swarm_get_contacts(SwarmHandle h, uint8_t* bits, int n) {
+    if (!h || !bits) return SWARM_E_INVALID;
+    if (n != h->n) return h->fail(SWARM_E_INVALID, "contacts size mismatch");
+    if (!cudaOk(h, cudaStreamSynchronize(h->stream), "sync")) return SWARM_E_CUDA;
+    return cudaOk(h, cudaMemcpy(bits, h->contacts, size_t(n), cudaMemcpyDeviceToHost), "contacts") ? SWARM_OK : SWARM_E_CUDA;
+}
+
+int swarm_stage_times(SwarmHandle h, SwarmStageTimes* out) {
+    if (!h || !out) return SWARM_E_INVALID;
+    *out = h->times;
+    return SWARM_OK;
+}
+
+int swarm_launch_count(SwarmHandle h, int64_t* out) {
+    if (!h || !out) return SWARM_E_INVALID;
+    *out = h->launches;
+    return SWARM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,200 @@
+"""Python binding of libswarm_gb300.so (include/swarm_cuda.h): the GB300 crowd step behind a ctypes layer.
+
+The class CrowdSim mirrors the reference's step/state API (DedovSergei/swarm-crowd-simulation
+include/swarm/cpu_crowd_sim.hpp:30-169 and include/swarm/crowd_sim.hpp:53-194): set_state (setState / upload),
+step, state, grid, cells, contacts, set_projection_iterations, set_drive_table. States are numpy float32 arrays of
+shape (n, 8): the reference's GpuBoid (position.xyzw, velocity.xyzw).
+
+There is no CPU fallback: if the library has not been built the import fails with the build command.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from .abi import (SWARM_OK, SWARM_VENUE_GRID, SWARM_VENUE_STADIUM, SwarmParams, SwarmStageTimes, SwarmVenue,
+                  fptr)
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_DIR, "libswarm_gb300.so")
+_lib = None
+
+
+class SwarmError(RuntimeError):
+    pass
+
+
+def lib():
+    """The loaded CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with `python swarm-crowd-simulation_gb300/build.py` "
+                              "(or __graft_entry__.build()); there is no CPU fallback")
+        L = C.CDLL(LIB_PATH)
+        H = C.c_void_p
+        sig = {
+            "swarm_params_reference": [C.POINTER(SwarmParams)],
+            "swarm_params_si": [C.POINTER(SwarmParams)],
+            "swarm_create": [C.POINTER(SwarmParams), C.POINTER(SwarmVenue), C.c_int, C.POINTER(H)],
+            "swarm_destroy": [H],
+            "swarm_set_stream": [H, C.c_void_p],
+            "swarm_last_error": [H, C.c_char_p, C.c_int],
+            "swarm_upload_state": [H, C.POINTER(C.c_float), C.c_int],
+            "swarm_download_state": [H, C.POINTER(C.c_float), C.c_int],
+            "swarm_upload_state_device": [H, C.c_void_p, C.c_int],
+            "swarm_download_state_device": [H, C.c_void_p, C.c_int],
+            "swarm_set_agent_params": [H, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int],
+            "swarm_step": [H, C.c_int],
+            "swarm_set_iterations": [H, C.c_int],
+            "swarm_set_drive_table": [H, C.POINTER(C.c_float), C.c_int],
+            "swarm_set_graph": [H, C.c_int],
+            "swarm_synchronize": [H],
+            "swarm_get_grid": [H, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_int],
+            "swarm_get_cells": [H, C.POINTER(C.c_uint32), C.c_int],
+            "swarm_get_contacts": [H, C.POINTER(C.c_uint8), C.c_int],
+            "swarm_set_timing": [H, C.c_int],
+            "swarm_stage_times": [H, C.POINTER(SwarmStageTimes)],
+            "swarm_launch_count": [H, C.POINTER(C.c_int64)],
+            "swarm_hall_layout": [C.c_void_p, C.POINTER(SwarmVenue)],
+            "swarm_hall_fields": [C.c_void_p, C.POINTER(SwarmVenue), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                  C.POINTER(C.c_float)],
+            "swarm_spawn_lattice": [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_uint64,
+                                    C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                                    C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)],
+        }
+        for name, args in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def params_reference():
+    """The reference's constants (model units, K = 32), folded as the reference folds them."""
+    p = SwarmParams()
+    _check(lib().swarm_params_reference(C.byref(p)), "swarm_params_reference")
+    return p
+
+
+def params_si():
+    """The SI preset of the grid venues (dt 0.05 s, K = 8, tau 0.5 s, per-agent radius and v0)."""
+    p = SwarmParams()
+    _check(lib().swarm_params_si(C.byref(p)), "swarm_params_si")
+    return p
+
+
+def _check(rc, what, h=None):
+    if rc != SWARM_OK:
+        msg = ""
+        if h is not None:
+            buf = C.create_string_buffer(512)
+            lib().swarm_last_error(h, buf, 512)
+            msg = buf.value.decode()
+        raise SwarmError(f"{what} failed ({rc}): {msg}")
+
+
+from .venues import Venue  # noqa: E402  (needs lib())
+
+
+class CrowdSim:
+    """One simulation on the current CUDA device (the reference's CrowdSim / CpuCrowdSim)."""
+
+    def __init__(self, params, venue, capacity):
+        self.params = params
+        self.venue = venue
+        self.capacity = int(capacity)
+        h = C.c_void_p()
+        _check(lib().swarm_create(C.byref(params), C.byref(venue.struct), self.capacity, C.byref(h)), "swarm_create")
+        self._h = h
+        self.n = 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().swarm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc, what):
+        _check(rc, what, self._h)
+
+    # ---- state ----
+    def set_state(self, boids):
+        """CpuCrowdSim::setState / CrowdSim::upload: (n, 8) float32 GpuBoid array."""
+        b = np.ascontiguousarray(boids, dtype=np.float32).reshape(-1, 8)
+        self._ck(lib().swarm_upload_state(self._h, fptr(b), b.shape[0]), "upload")
+        self.n = b.shape[0]
+
+    def set_agent_params(self, radius, v0):
+        r = np.ascontiguousarray(radius, dtype=np.float32)
+        v = np.ascontiguousarray(v0, dtype=np.float32)
+        self._ck(lib().swarm_set_agent_params(self._h, fptr(r), fptr(v), r.shape[0]), "set_agent_params")
+
+    def state(self):
+        out = np.empty((self.n, 8), np.float32)
+        self._ck(lib().swarm_download_state(self._h, fptr(out), self.n), "download")
+        return out
+
+    # ---- stepping ----
+    def step(self, steps=1):
+        self._ck(lib().swarm_step(self._h, int(steps)), "step")
+
+    def synchronize(self):
+        self._ck(lib().swarm_synchronize(self._h), "synchronize")
+
+    def set_projection_iterations(self, k):
+        self._ck(lib().swarm_set_iterations(self._h, int(k)), "set_iterations")
+
+    def set_drive_table(self, dirs):
+        if dirs is None:
+            self._ck(lib().swarm_set_drive_table(self._h, None, 0), "set_drive_table")
+            return
+        d = np.ascontiguousarray(dirs, dtype=np.float32).reshape(-1, 2)
+        self._ck(lib().swarm_set_drive_table(self._h, fptr(d), d.shape[0]), "set_drive_table")
+
+    def set_graph(self, enabled=True):
+        self._ck(lib().swarm_set_graph(self._h, int(bool(enabled))), "set_graph")
+
+    def set_timing(self, enabled=True):
+        self._ck(lib().swarm_set_timing(self._h, int(bool(enabled))), "set_timing")
+
+    def stage_times(self):
+        t = SwarmStageTimes()
+        self._ck(lib().swarm_stage_times(self._h, C.byref(t)), "stage_times")
+        return {k: getattr(t, k) for k, _ in SwarmStageTimes._fields_}
+
+    def launch_count(self):
+        c = C.c_int64()
+        self._ck(lib().swarm_launch_count(self._h, C.byref(c)), "launch_count")
+        return c.value
+
+    # ---- inspection ----
+    def grid(self):
+        """CpuCrowdSim::grid(): the last step's sorted (gridID, boidID) pairs."""
+        g = np.empty(self.n, np.uint32)
+        b = np.empty(self.n, np.uint32)
+        self._ck(lib().swarm_get_grid(self._h, g.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                      b.ctypes.data_as(C.POINTER(C.c_uint32)), self.n), "get_grid")
+        return g, b
+
+    def cells(self):
+        """CpuCrowdSim::cells(): (startIndex, agentCount) per cell, shape (ncells, 2)."""
+        nc = lib().swarm_get_cells(self._h, None, 0)
+        out = np.empty((nc, 2), np.uint32)
+        self._ck(lib().swarm_get_cells(self._h, out.ctypes.data_as(C.POINTER(C.c_uint32)), nc), "get_cells")
+        return out
+
+    def contacts(self):
+        out = np.empty(self.n, np.uint8)
+        self._ck(lib().swarm_get_contacts(self._h, out.ctypes.data_as(C.POINTER(C.c_uint8)), self.n), "get_contacts")
+        return out
+
+
+__all__ = ["CrowdSim", "Venue", "SwarmError", "lib", "params_reference", "params_si", "SwarmParams", "SwarmVenue",
+           "SWARM_VENUE_GRID", "SWARM_VENUE_STADIUM"]

@@ -1,0 +1,132 @@
+"""Venues and spawns: the static inputs of the step.
+
+Venue.stadium(sdf)   the reference's baked terrace (stadium.sdf, 130^3 float32, [x][y][z] z fastest; the terrace's
+                     neighbour grid 40 x 40 over [-1, 1]^2, exit test EXIT_DEPTH 0.93 below EXIT_MAX_Z 0.05:
+                     reference include/swarm/sim_params.hpp:57-70, 349-351)
+Venue.hall(...)      a rectangular hall with door gaps on grids (SI units): the synthetic workloads below
+"""
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _check, lib
+from .abi import SWARM_VENUE_STADIUM, SwarmVenue, fptr
+
+SDF_RES = 130
+
+
+class HallSpec(C.Structure):
+    _fields_ = [("size_x", C.c_float), ("size_y", C.c_float), ("wall_thickness", C.c_float), ("exit_depth", C.c_float),
+                ("margin", C.c_float), ("wall_h", C.c_float), ("nav_h", C.c_float), ("cell", C.c_float),
+                ("n_doors", C.c_int32), ("door_wall", C.c_int32 * 8), ("door_center", C.c_float * 8),
+                ("door_width", C.c_float * 8)]
+
+
+class Venue:
+    """A SwarmVenue plus the host arrays it points to (kept alive with it)."""
+
+    def __init__(self, struct, arrays, name, meta=None):
+        self.struct = struct
+        self.arrays = arrays
+        self.name = name
+        self.meta = meta or {}
+
+    @property
+    def n_cells(self):
+        return self.struct.grid_res_x * self.struct.grid_res_y
+
+    @staticmethod
+    def stadium(sdf):
+        sdf = np.ascontiguousarray(sdf, dtype=np.float32).reshape(-1)
+        if sdf.size != SDF_RES ** 3:
+            raise ValueError(f"stadium.sdf holds {sdf.size} samples, expected {SDF_RES ** 3}")
+        v = SwarmVenue()
+        v.kind = SWARM_VENUE_STADIUM
+        v.grid_res_x = v.grid_res_y = 40
+        v.domain_min_x = v.domain_min_y = -1.0
+        v.domain_span_x = v.domain_span_y = 2.0
+        v.exit_hi_x = 0.930
+        v.exit_max_z = 0.050
+        v.sdf = fptr(sdf)
+        v.sdf_res = SDF_RES
+        v.sdf_origin[:] = [-0.95, -0.95, -0.8092595]
+        v.sdf_spacing = float(np.float32(1.9) / np.float32(127.0))   # SDF_SPACING = 1.9f / 127.0f
+        v.metric_res = 64
+        return Venue(v, {"sdf": sdf}, "terrace")
+
+    @staticmethod
+    def hall(size_x, size_y, doors, wall_thickness=0.3, exit_depth=0.5, margin=1.0, wall_h=0.05, nav_h=0.1, cell=0.5,
+             name="hall"):
+        """doors: [(wall, centre, width)], wall 0: -x, 1: +x, 2: -y, 3: +y; centre along the wall from its midpoint."""
+        spec = HallSpec()
+        spec.size_x, spec.size_y, spec.wall_thickness = size_x, size_y, wall_thickness
+        spec.exit_depth, spec.margin, spec.wall_h, spec.nav_h, spec.cell = exit_depth, margin, wall_h, nav_h, cell
+        if len(doors) > 8:
+            raise ValueError("at most 8 doors")
+        spec.n_doors = len(doors)
+        for i, (w, c, width) in enumerate(doors):
+            spec.door_wall[i], spec.door_center[i], spec.door_width[i] = int(w), float(c), float(width)
+        v = SwarmVenue()
+        _check(lib().swarm_hall_layout(C.byref(spec), C.byref(v)), "swarm_hall_layout")
+        wall = np.empty(v.wall_nx * v.wall_ny, np.float32)
+        nav = np.empty(v.nav_nx * v.nav_ny, np.float32)
+        boxes = np.empty(max(1, 4 * v.n_exits), np.float32)
+        _check(lib().swarm_hall_fields(C.byref(spec), C.byref(v), fptr(wall), fptr(nav), fptr(boxes)), "swarm_hall_fields")
+        v.wall_sdf = fptr(wall)
+        v.nav_dist = fptr(nav)
+        v.exit_boxes = fptr(boxes)
+        meta = {"size": (size_x, size_y), "doors": list(doors), "spec": spec}
+        return Venue(v, {"wall": wall, "nav": nav, "exit_boxes": boxes}, name, meta)
+
+
+def spawn_lattice(nx, ny, n=None, spacing=0.5, center=(0.0, 0.0), jitter=0.05, seed=0, r=(0.20, 0.25),
+                  v=(1.34, 0.26, 0.6, 2.0)):
+    """A jittered lattice spawn: (boids (n, 8), radius (n,), v0 (n,))."""
+    n = nx * ny if n is None else n
+    boids = np.empty((n, 8), np.float32)
+    rad = np.empty(n, np.float32)
+    v0 = np.empty(n, np.float32)
+    _check(lib().swarm_spawn_lattice(nx, ny, n, spacing, center[0], center[1], jitter, seed, r[0], r[1], v[0], v[1], v[2],
+                                     v[3], fptr(boids), fptr(rad), fptr(v0)), "swarm_spawn_lattice")
+    return boids, rad, v0
+
+
+# ---- the synthetic workloads (SI units, 0.5 m hash cells, dt 0.05 s, K = 8) ----
+# Recorded resolutions of specs that cannot hold their lattice as written: a 64 x 64 lattice at 0.5 m spans 31.5 m, so
+# the 40 m x 25 m terrace grows to 40 m x 34 m (its 4 m exit stays centred in a short wall); the 128 x 128 lattice
+# spans 63.5 m, so the 80 m x 60 m hall grows to 80 m x 70 m.
+
+def terrace_c0():
+    """4 096 agents (64 x 64 lattice, 0.5 m) on a 40 m x 34 m terrace, one 4 m exit centred in the +x (short) wall."""
+    venue = Venue.hall(40.0, 34.0, [(1, 0.0, 4.0)], name="terrace 40x34 m, 1 exit")
+    return venue, spawn_lattice(64, 64, seed=0)
+
+
+def hall_c1():
+    """65 536 agents (256 x 256 lattice) in a 140 m x 140 m hall, four 4 m exits, one centred in each wall."""
+    venue = Venue.hall(140.0, 140.0, [(0, 0.0, 4.0), (1, 0.0, 4.0), (2, 0.0, 4.0), (3, 0.0, 4.0)],
+                       name="hall 140x140 m, 4 exits")
+    return venue, spawn_lattice(256, 256, seed=0)
+
+
+def terrace_c4():
+    """16 384 agents (128 x 128 lattice) in an 80 m x 70 m hall, two 4 m exits centred in the +-x walls."""
+    venue = Venue.hall(80.0, 70.0, [(0, 0.0, 4.0), (1, 0.0, 4.0)], name="terrace 80x70 m, 2 exits")
+    return venue, spawn_lattice(128, 128, seed=0)
+
+
+def batch_instances(count=256, seed=0, n_lo=1024, n_hi=65536):
+    """The instances of the batched workload: agent count log-uniform in [n_lo, n_hi], 1 or 2 exits of width
+    U[1.5, 6] m, the hall side sqrt(N / 4) m + 0.5 m (4 agents / m^2 on the lattice), independent seeds."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(n_lo), math.log(n_hi)))))
+        side_agents = int(math.ceil(math.sqrt(n)))
+        side = math.sqrt(n / 4.0) + 0.5
+        k = int(rng.integers(1, 3))
+        walls = rng.choice(4, size=k, replace=False)
+        doors = [(int(w), 0.0, float(rng.uniform(1.5, 6.0))) for w in walls]
+        out.append({"n": n, "side": side, "lattice": side_agents, "doors": doors, "seed": int(rng.integers(1, 2**62))})
+    return out

@@ -1,0 +1,52 @@
+"""Generates the golden fixtures of the terrace from the UNMODIFIED reference CPU step (oracle/_ref/libswarm_ref.so,
+compiled from the reference tree by oracle/Makefile). Run in a container that has the reference tree:
+
+    make -C oracle ref && python tests/golden/make_golden.py
+
+Writes
+  stadium_sdf.zlib   the reference's stadium.sdf (130^3 float32, the terrace's baked SDF), zlib-compressed: the input
+                     data of the terrace venue, needed where the reference tree is absent
+  terrace_ref.npz    spawnBleacherCrowd(4096, seed 1337) (src/crowd_sim.cpp:601-645, this platform's libstdc++
+                     distributions), and CpuCrowdSim (SortMode::Counting) after 1 step (state, sorted pairs, cell table,
+                     contact bits), after 250 steps (state and its FNV-1a hash, tools/golden_state.hpp:121-126) and after
+                     251 steps (one step from the congested state: state, pairs, cells, contacts).
+"""
+import os
+import sys
+import zlib
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", ".."))
+from oracle import oracle as O  # noqa: E402
+
+REF_DIR = os.environ.get("REF_DIR", "/root/reference")
+
+
+def main():
+    sdf_path = os.path.join(REF_DIR, "stadium.sdf")
+    raw = open(sdf_path, "rb").read()
+    with open(os.path.join(HERE, "stadium_sdf.zlib"), "wb") as f:
+        f.write(zlib.compress(raw, 9))
+    assert O.ref_load_sdf(sdf_path)
+    spawn = O.ref_spawn_terrace(4096, 1337)
+    sim = O.RefSim("terrace")
+    sim.set_state(spawn)
+    sim.step(1)
+    out = {"spawn": spawn, "state1": sim.state(), "contacts1": sim.contacts(), "cells1": sim.cells()}
+    out["grid1_key"], out["grid1_id"] = sim.grid()
+    sim.step(249)
+    out["state250"] = sim.state()
+    sim.step(1)
+    out["state251"] = sim.state()
+    out["contacts251"] = sim.contacts()
+    out["cells251"] = sim.cells()
+    out["grid251_key"], out["grid251_id"] = sim.grid()
+    out["hash250"] = np.array([O.state_hash(out["state250"])], dtype=np.uint64)
+    np.savez_compressed(os.path.join(HERE, "terrace_ref.npz"), **out)
+    print("hash after 250 steps: %016x" % int(out["hash250"][0]))
+
+
+if __name__ == "__main__":
+    main()
