@@ -5,12 +5,13 @@ Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this mo
 """
 import ctypes as C
 import os
+import platform
 import subprocess
 
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-ORACLE_SO = os.path.join(HERE, "liboracle.so")
+ORACLE_SO = os.path.join(HERE, "_build", platform.machine(), "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libswarm_ref.so")
 _o = None
 _r = None

@@ -7,12 +7,13 @@ reference's CPU arithmetic (no fused multiply-adds). Objects compile in parallel
 """
 import concurrent.futures as cf
 import os
+import platform
 import subprocess
 import sys
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
-BUILD = os.path.join(PKG, "_build")
+BUILD = os.path.join(PKG, "_build", platform.machine())
 LIB = os.path.join(PKG, "libswarm_gb300.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -47,6 +48,19 @@ def _compile(src, force, hdr_mtime):
     return obj, (r.stdout + r.stderr).strip() or None
 
 
+def _elf_machine(path):
+    """The ELF e_machine of a shared object (62: x86-64, 183: aarch64), None if unreadable."""
+    try:
+        with open(path, "rb") as f:
+            head = f.read(20)
+        return int.from_bytes(head[18:20], "little") if head[:4] == b"\x7fELF" else None
+    except OSError:
+        return None
+
+
+_MACHINE = {"x86_64": 62, "aarch64": 183, "arm64": 183}.get(platform.machine())
+
+
 def build(force=False, verbose=False):
     os.makedirs(BUILD, exist_ok=True)
     cu, cpp = _sources()
@@ -62,7 +76,9 @@ def build(force=False, verbose=False):
             if m:
                 print(m)
     objs = [o for o, _ in results]
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
+    stale = not os.path.exists(LIB) or _elf_machine(LIB) != _MACHINE or \
+        os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs)
+    if force or stale:
         cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
