@@ -1,0 +1,305 @@
+"""Benchmark of the crowd step: agent-steps/s on the 65 536-agent hall, against the HBM roofline.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--no-cpu-baseline]
+
+Workload: the hall 140 m x 140 m with four 4 m exits, 65 536 agents on a 256 x 256 lattice at 0.5 m (jitter 0.05 m,
+radius U[0.20, 0.25] m, desired speed N(1.34, 0.26) clipped to [0.6, 2.0] m/s, seed 0), dt 0.05 s, K = 8 Jacobi
+sweeps, 0.5 m hash cells; synthetic data generated here. One step = hash, key sort, cell ranges + gather, predict,
+7 sweeps, final pass over every agent.
+
+value  agent-steps/s with the state resident in HBM: per timed step, CUDA events on the simulation's stream around
+       the step; the L2 (129 MB, larger than the step's 54 MB working set) is flushed by a 256 MiB write before each
+       timed step, outside the events. Agent-steps count the agents active at the start of each step.
+e2e    the same metric through swarm_step_host: host state in pinned memory -> device, one step, device -> host,
+       every step inside the timed region.
+roofline  the dominant kernel's algorithmic bytes per launch (bytes per agent x active agents) over its mean launch
+       time (CUDA events recorded by the library around each stage during the timed steps), against the measured
+       HBM copy bandwidth (MEASURED_PEAKS.json).
+cpu_baseline  the oracle port of the reference's CPU step (OpenMP, all host threads) on a bounded sample of the same
+       workload.
+--impl reference  the reference's CPU step (the oracle port: the reference's own build needs its source tree, which
+       only exists where the oracle was pinned) on the host cores, same workload, metric and unit.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "swarm-crowd-simulation_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "agent-steps/s vs HBM roofline: plain, 256-batched, adjoint (≤1e-3 FD rel err)"
+UNIT = "agent-steps/s"
+WORKLOAD = ("hall 140x140 m, 4 exits of 4 m, 65536 agents (256x256 lattice, 0.5 m), per-agent radius and v0, "
+            "dt 0.05 s, K=8 Jacobi sweeps, 0.5 m hash cells, FP32")
+# algorithmic bytes per active agent per launch (SoA FP32): predict reads pos, vel, params (48) and writes the
+# predicted position, velocity and wall plane (48); a sweep reads position and plane (32) and writes a position (16);
+# the final pass reads 64 and writes the 32-byte agent record; the sort stage: hash 24 + sort 16 + ranges 4 + gather 100
+BYTES = {"predict": 96.0, "sweep": 48.0, "final": 96.0, "sort": 144.0}
+B_STEP = 336.0 + 48.0 * (8 - 1)   # 672 B per agent-step at K = 8
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampled every 200 ms during the timed region."""
+
+    def __init__(self, index=0):
+        self.rows = []
+        self.proc = None
+        self.index = index
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 4 + i and r[4 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def workload():
+    from swarm_gb300 import venues
+    return venues.hall_c1()
+
+
+def cpu_baseline(budget_s=12.0, max_steps=400):
+    """The oracle port (OpenMP, every host thread) on the same workload: 2 warm-up steps, then steps until the budget."""
+    import numpy as np
+    import swarm_gb300
+    from oracle import oracle as O
+    O.build()
+    venue, (boids, r, v0) = workload()
+    sim = O.OracleSim(swarm_gb300.params_si(), venue.struct)
+    sim.set_state(boids)
+    sim.set_agent_params(r, v0)
+    sim.step(2)
+    agent_steps, t_total, steps = 0, 0.0, 0
+    while t_total < budget_s and steps < max_steps:
+        active = int((sim.state()[:, 3] != 0).sum())
+        t0 = time.perf_counter()
+        sim.step(1)
+        t_total += time.perf_counter() - t0
+        agent_steps += active
+        steps += 1
+    threads = O.lib().oracle_max_threads()
+    return {"value": agent_steps / t_total, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{steps} consecutive steps of the same 65536-agent hall from its spawn (after 2 warm-up steps), "
+                      f"{t_total:.1f} s of wall clock on {threads} OpenMP threads"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    base = cpu_baseline(budget_s=max(5.0, 1.0 * args.steps), max_steps=args.steps)
+    line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 65536.0 / base["value"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD}, "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import numpy as np
+    import torch
+    import __graft_entry__
+    __graft_entry__._pkg_build().build()
+    import swarm_gb300
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    venue, (boids, r, v0) = workload()
+    P = swarm_gb300.params_si()
+    n = boids.shape[0]
+    stream = torch.cuda.Stream()
+    sim = swarm_gb300.CrowdSim(P, venue, n)
+    sim.set_stream(stream.cuda_stream)
+    sim.set_state(boids)
+    sim.set_agent_params(r, v0)
+    sim.set_graph(True)
+    sim.set_timing(True)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            sim.step(1)
+    torch.cuda.synchronize()
+    start_state = sim.state()
+
+    # timed region: K steps, each bracketed by CUDA events on the simulation's stream, L2 flushed before each
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stages = []
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xFF)
+                evs[k][0].record(stream)
+                sim.step(1)
+                evs[k][1].record(stream)
+            stream.synchronize()
+            stages.append(sim.stage_times())
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    total_ms = sum(step_ms)
+    launches = sim.launch_count() * args.steps   # per-step launches of the last call x timed steps
+
+    # exact agent-steps: replay the timed steps (bit-identical) and count the agents active at each step's start
+    rep = swarm_gb300.CrowdSim(P, venue, n)
+    rep.set_state(start_state)
+    rep.set_agent_params(r, v0)
+    agent_steps = 0
+    for _ in range(args.steps):
+        agent_steps += int((rep.state()[:, 3] != 0).sum())
+        rep.step(1)
+    rep.close()
+
+    t_max = total_ms
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+        a = torch.tensor([agent_steps], device="cuda", dtype=torch.float64)
+        dist.all_reduce(a)
+        agent_steps_all = float(a.item())
+    else:
+        agent_steps_all = float(agent_steps)
+    value = agent_steps_all / (t_max * 1e-3)
+
+    # roofline of the dominant kernel, from the library's stage events over the timed steps
+    K = P.proj_iterations
+    active_mean = agent_steps / args.steps
+    per = {
+        "k_predict": (statistics.mean(s["predict"] for s in stages), 1, BYTES["predict"]),
+        "k_project": (statistics.mean(s["project"] for s in stages) / max(K - 1, 1), max(K - 1, 0), BYTES["sweep"]),
+        "k_final": (statistics.mean(s["final_pass"] for s in stages), 1, BYTES["final"]),
+        "sort (4 kernels)": (statistics.mean(s["sort"] for s in stages) / 4.0, 4, BYTES["sort"] / 4.0),
+    }
+    dom = max(per, key=lambda k: per[k][0] * per[k][1])
+    dom_ms, _, dom_bytes = per[dom]
+    hbm, peak_kind = peaks()
+    achieved = dom_bytes * active_mean / (dom_ms * 1e-3) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        traffic = json.load(open(tfile)).get(dom)
+
+    # e2e through swarm_step_host with pinned host buffers
+    e2e_sim = swarm_gb300.CrowdSim(P, venue, n)
+    e2e_sim.set_agent_params(r, v0)
+    e2e_sim.set_graph(True)
+    h_in = torch.from_numpy(start_state.copy()).pin_memory()
+    h_out = torch.empty_like(h_in).pin_memory()
+    for _ in range(2):
+        e2e_sim.step_host(h_in.data_ptr(), h_out.data_ptr(), n, 1)
+    cur_in, cur_out = h_in, h_out
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_sim.step_host(cur_in.data_ptr(), cur_out.data_ptr(), n, 1)
+        cur_in, cur_out = cur_out, cur_in
+    e2e_s = time.perf_counter() - t0
+    e2e_value = agent_steps_all / (e2e_s * (world if False else 1)) if world == 1 else agent_steps_all / e2e_s
+
+    line = None
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (generated hall and lattice spawn, seed 0)",
+            "config": {"workload": WORKLOAD, "agents": n, "active_per_step": active_mean,
+                       "l2": "flushed before every timed step (256 MiB write, outside the timed events)",
+                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+                       "step_fraction_of_hbm_roofline": value * B_STEP / (hbm * 1e9),
+                       "stage_ms_mean": {k: statistics.mean(s[k] for s in stages)
+                                         for k in ("sort", "predict", "project", "final_pass")}},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "peak_kind": peak_kind,
+                         "bytes_per_agent": dom_bytes, "mean_launch_ms": dom_ms,
+                         "traffic": traffic},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 32,
+                    "path": "swarm_step_host (C ABI), pinned host buffers"},
+            "gpu_launches": launches,
+        }
+        line["clocks"] = clk.summary()
+        if not args.no_cpu_baseline and world == 1:
+            try:
+                line["cpu_baseline"] = cpu_baseline()
+            except Exception as e:  # reported, not fatal
+                line["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
+        print(json.dumps(line))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -163,6 +163,9 @@ int swarm_download_state_device(SwarmHandle h, float* d_boids, int n);
  * swarm_step: `steps` x CrowdSim::step (src/crowd_sim.cpp:316-412) = hash, key sort, cell ranges + gather,
  *   predict, K - 1 Jacobi sweeps, final pass; asynchronous on the handle's stream. */
 int swarm_step(SwarmHandle h, int steps);
+/* One call for callers holding the state in host memory: copies in_boids (n x 8 floats) into the device state,
+ * runs `steps` steps, copies the result into out_boids and waits for it. Host buffers (pinned ones copy fastest). */
+int swarm_step_host(SwarmHandle h, const float* in_boids, float* out_boids, int n, int steps);
 /* CpuCrowdSim::setProjectionIterations / CrowdSim::setProjectionIterations (src/crowd_sim.cpp:480-483). */
 int swarm_set_iterations(SwarmHandle h, int k);
 /* CpuCrowdSim::setDriveTable (include/swarm/cpu_crowd_sim.hpp:114): e_goal of agent i is dirs[2i..2i+1];
@@ -179,7 +182,8 @@ int swarm_get_grid(SwarmHandle h, uint32_t* grid_id, uint32_t* boid_id, int n);
 int swarm_get_cells(SwarmHandle h, uint32_t* start_count, int n_cells);
 /* CpuCrowdSim::contacts(): the ContactBits per agent of the last step. */
 int swarm_get_contacts(SwarmHandle h, uint8_t* bits, int n);
-/* Times every stage of the following steps with CUDA events (0: off, the default). */
+/* Records CUDA events around the stages of every following step (0: off, the default); swarm_stage_times waits for
+ * and returns the last step's stage times. */
 int swarm_set_timing(SwarmHandle h, int enabled);
 int swarm_stage_times(SwarmHandle h, SwarmStageTimes* out);
 /* Kernel launches the last swarm_step issued (evidence for benchmarks). */

@@ -51,6 +51,7 @@ struct SwarmSim {
     bool timing = false;
     cudaEvent_t ev[6] = {};
     SwarmStageTimes times{};
+    bool timesValid = false;
     int64_t launches = 0;
     std::vector<void*> allocs;
 
@@ -280,24 +281,23 @@ int swarm_set_graph(SwarmHandle h, int enabled) {
 
 int swarm_set_timing(SwarmHandle h, int enabled) {
     if (!h) return SWARM_E_INVALID;
+    if (h->timing != (enabled != 0)) h->dropGraphs();   // the graphs hold the event records or not
     h->timing = enabled != 0;
     return SWARM_OK;
 }
 
-int swarm_step(SwarmHandle h, int steps) {
-    if (!h) return SWARM_E_INVALID;
-    if (!h->hasState) return h->fail(SWARM_E_STATE, "no state (upload one first)");
-    if (steps < 0) return h->fail(SWARM_E_INVALID, "steps must be >= 0");
+static int stepImpl(SwarmHandle h, int steps) {
     h->launches = 0;
+    const int perStep = 6 + std::max(h->P.proj_iterations - 1, 0);
     for (int s = 0; s < steps; ++s) {
         const int in = h->readIdx;
-        const bool timeThis = h->timing && s == steps - 1;
-        if (h->useGraph && !timeThis) {
+        cudaEvent_t* evs = h->timing ? h->ev : nullptr;
+        if (h->useGraph) {
             if (!h->graph[in]) {
                 cudaGraph_t g = nullptr;
                 if (!cudaOk(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "capture")) return SWARM_E_CUDA;
-                int64_t saved = h->launches;
-                const int rc = h->enqueueStep(in, nullptr);
+                const int64_t saved = h->launches;
+                const int rc = h->enqueueStep(in, evs);
                 h->launches = saved;
                 if (!cudaOk(h, cudaStreamEndCapture(h->stream, &g), "capture end") || rc != SWARM_OK) return SWARM_E_CUDA;
                 const bool inst = cudaOk(h, cudaGraphInstantiate(&h->graph[in], g, 0), "graph instantiate");
@@ -305,23 +305,38 @@ int swarm_step(SwarmHandle h, int steps) {
                 if (!inst) return SWARM_E_CUDA;
             }
             if (!cudaOk(h, cudaGraphLaunch(h->graph[in], h->stream), "graph launch")) return SWARM_E_CUDA;
-            h->launches += 6 + std::max(h->P.proj_iterations - 1, 0);
+            h->launches += perStep;
         } else {
-            const int rc = h->enqueueStep(in, timeThis ? h->ev : nullptr);
+            const int rc = h->enqueueStep(in, evs);
             if (rc != SWARM_OK) return rc;
-        }
-        if (timeThis) {
-            if (!cudaOk(h, cudaEventSynchronize(h->ev[4]), "timing")) return SWARM_E_CUDA;
-            float sort = 0, pred = 0, proj = 0, fin = 0;
-            cudaEventElapsedTime(&sort, h->ev[0], h->ev[1]);
-            cudaEventElapsedTime(&pred, h->ev[1], h->ev[2]);
-            cudaEventElapsedTime(&proj, h->ev[2], h->ev[3]);
-            cudaEventElapsedTime(&fin, h->ev[3], h->ev[4]);
-            h->times = SwarmStageTimes{0.0f, sort, 0.0f, pred, proj, fin, sort + pred + proj + fin};
         }
         h->readIdx ^= 1;
     }
+    h->timesValid = false;
     return SWARM_OK;
+}
+
+int swarm_step(SwarmHandle h, int steps) {
+    if (!h) return SWARM_E_INVALID;
+    if (!h->hasState) return h->fail(SWARM_E_STATE, "no state (upload one first)");
+    if (steps < 0) return h->fail(SWARM_E_INVALID, "steps must be >= 0");
+    return stepImpl(h, steps);
+}
+
+int swarm_step_host(SwarmHandle h, const float* in_boids, float* out_boids, int n, int steps) {
+    if (!h || !in_boids || !out_boids) return SWARM_E_INVALID;
+    if (n <= 0 || n > h->capacity) return h->fail(SWARM_E_INVALID, "agent count " + std::to_string(n) + " outside 1.." + std::to_string(h->capacity));
+    if (steps < 0) return h->fail(SWARM_E_INVALID, "steps must be >= 0");
+    if (n != h->n) h->dropGraphs();
+    h->n = n;
+    h->hasState = true;
+    const size_t bytes = size_t(n) * 32;
+    // the read half only: the final pass writes every agent of the other half
+    if (!cudaOk(h, cudaMemcpyAsync(h->state[h->readIdx], in_boids, bytes, cudaMemcpyHostToDevice, h->stream), "upload")) return SWARM_E_CUDA;
+    const int rc = stepImpl(h, steps);
+    if (rc != SWARM_OK) return rc;
+    if (!cudaOk(h, cudaMemcpyAsync(out_boids, h->state[h->readIdx], bytes, cudaMemcpyDeviceToHost, h->stream), "download")) return SWARM_E_CUDA;
+    return cudaOk(h, cudaStreamSynchronize(h->stream), "step sync") ? SWARM_OK : SWARM_E_CUDA;
 }
 
 int swarm_synchronize(SwarmHandle h) {
@@ -363,6 +378,17 @@ int swarm_get_contacts(SwarmHandle h, uint8_t* bits, int n) {
 
 int swarm_stage_times(SwarmHandle h, SwarmStageTimes* out) {
     if (!h || !out) return SWARM_E_INVALID;
+    if (!h->timing) return h->fail(SWARM_E_STATE, "timing is off (swarm_set_timing)");
+    if (!h->timesValid) {
+        if (!cudaOk(h, cudaEventSynchronize(h->ev[4]), "timing")) return SWARM_E_CUDA;
+        float sort = 0, pred = 0, proj = 0, fin = 0;
+        cudaEventElapsedTime(&sort, h->ev[0], h->ev[1]);
+        cudaEventElapsedTime(&pred, h->ev[1], h->ev[2]);
+        cudaEventElapsedTime(&proj, h->ev[2], h->ev[3]);
+        cudaEventElapsedTime(&fin, h->ev[3], h->ev[4]);
+        h->times = SwarmStageTimes{0.0f, sort, 0.0f, pred, proj, fin, sort + pred + proj + fin};
+        h->timesValid = true;
+    }
     *out = h->times;
     return SWARM_OK;
 }

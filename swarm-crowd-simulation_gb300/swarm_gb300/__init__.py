@@ -47,6 +47,7 @@ def lib():
             "swarm_set_agent_params": [H, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int],
             "swarm_step": [H, C.c_int],
             "swarm_set_iterations": [H, C.c_int],
+            "swarm_step_host": [H, C.c_void_p, C.c_void_p, C.c_int, C.c_int],
             "swarm_set_drive_table": [H, C.POINTER(C.c_float), C.c_int],
             "swarm_set_graph": [H, C.c_int],
             "swarm_synchronize": [H],
@@ -144,6 +145,15 @@ class CrowdSim:
     # ---- stepping ----
     def step(self, steps=1):
         self._ck(lib().swarm_step(self._h, int(steps)), "step")
+
+    def step_host(self, in_ptr, out_ptr, n, steps=1):
+        """swarm_step_host on raw host pointers (e.g. pinned buffers): upload, step, download, wait."""
+        self._ck(lib().swarm_step_host(self._h, C.c_void_p(in_ptr), C.c_void_p(out_ptr), int(n), int(steps)), "step_host")
+        self.n = int(n)
+
+    def set_stream(self, stream_ptr):
+        """Run on the caller's CUDA stream (a cudaStream_t as an int; 0 / None: the handle's own)."""
+        self._ck(lib().swarm_set_stream(self._h, C.c_void_p(stream_ptr or None)), "set_stream")
 
     def synchronize(self):
         self._ck(lib().swarm_synchronize(self._h), "synchronize")
