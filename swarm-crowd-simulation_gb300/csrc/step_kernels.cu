@@ -356,23 +356,28 @@ void launch_sort(const StepArgs& A, cudaStream_t st, int64_t* launches) {
 }
 
 template <class Venue>
-static void physicsImpl(const StepArgs& A, cudaStream_t st, int64_t* launches, cudaEvent_t* ev) {
+static void stageImpl(const StepArgs& A, int stage, cudaStream_t st, int64_t* launches) {
     const int n = A.n, K = A.P.proj_iterations;
-    k_predict<Venue><<<blocks(n, 128), 128, 0, st>>>(A);
-    if (ev) cudaEventRecord(ev[0], st);
-    int in = 0;
-    for (int it = 1; it < K; ++it) {
-        k_project<Venue><<<blocks(n, 128), 128, 0, st>>>(A, in);
-        in ^= 1;
+    if (stage == 1) {
+        k_predict<Venue><<<blocks(n, 128), 128, 0, st>>>(A);
+        *launches += 1;
+    } else if (stage == 2) {
+        int in = 0;
+        for (int it = 1; it < K; ++it) {
+            k_project<Venue><<<blocks(n, 128), 128, 0, st>>>(A, in);
+            in ^= 1;
+        }
+        *launches += K > 1 ? K - 1 : 0;
+    } else if (stage == 3) {
+        k_final<Venue><<<blocks(n, 128), 128, 0, st>>>(A, K > 1 ? (K - 1) & 1 : 0);
+        *launches += 1;
     }
-    if (ev) cudaEventRecord(ev[1], st);
-    k_final<Venue><<<blocks(n, 128), 128, 0, st>>>(A, in);
-    *launches += 2 + (K > 1 ? K - 1 : 0);
 }
 
-void launch_physics(const StepArgs& A, cudaStream_t st, int64_t* launches, cudaEvent_t* ev) {
-    if (A.V.kind == SWARM_VENUE_STADIUM) physicsImpl<Stadium>(A, st, launches, ev);
-    else physicsImpl<GridVenue>(A, st, launches, ev);
+void launch_stage(const StepArgs& A, int stage, cudaStream_t st, int64_t* launches) {
+    if (stage == 0) { launch_sort(A, st, launches); return; }
+    if (A.V.kind == SWARM_VENUE_STADIUM) stageImpl<Stadium>(A, stage, st, launches);
+    else stageImpl<GridVenue>(A, stage, st, launches);
 }
 
 }  // namespace swarm_gpu

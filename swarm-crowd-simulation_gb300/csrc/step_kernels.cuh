@@ -9,7 +9,7 @@ namespace swarm_gpu {
 
 // hash, scan, scatter, rank + gather: 4 launches
 void launch_sort(const StepArgs& A, cudaStream_t st, int64_t* launches);
-// predict, K - 1 sweeps, final; ev (optional): events recorded after predict and after the sweeps
-void launch_physics(const StepArgs& A, cudaStream_t st, int64_t* launches, cudaEvent_t* ev);
+// stage 0: the sort (hash, scan, scatter, rank + gather); 1: predict; 2: the K - 1 sweeps; 3: the final pass
+void launch_stage(const StepArgs& A, int stage, cudaStream_t st, int64_t* launches);
 
 }  // namespace swarm_gpu

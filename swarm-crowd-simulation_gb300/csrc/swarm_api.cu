@@ -47,7 +47,8 @@ struct SwarmSim {
     int ncells = 0;
     // execution
     bool useGraph = false;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};        // a whole step, per state half read
+    cudaGraphExec_t stageGraph[2][4] = {};                  // its four stages (timing on)
     bool timing = false;
     cudaEvent_t ev[6] = {};
     SwarmStageTimes times{};
@@ -59,8 +60,10 @@ struct SwarmSim {
     int fail(int code, const std::string& msg) { err = msg; return code; }
     void dropGraphs() {
         for (auto& g : graph) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+        for (auto& row : stageGraph) for (auto& g : row) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
     }
-    int enqueueStep(int in, cudaEvent_t* evs);
+    int enqueueStages(int in, int s0, int s1);
+    int captureStages(int in, int s0, int s1, cudaGraphExec_t* out);
     ~SwarmSim();
 };
 
@@ -121,14 +124,23 @@ StepArgs SwarmSim::args(int in) const {
     return A;
 }
 
-int SwarmSim::enqueueStep(int in, cudaEvent_t* evs) {
+int SwarmSim::enqueueStages(int in, int s0, int s1) {
     const StepArgs A = args(in);
-    if (evs) cudaEventRecord(evs[0], stream);
-    swarm_gpu::launch_sort(A, stream, &launches);
-    if (evs) cudaEventRecord(evs[1], stream);
-    swarm_gpu::launch_physics(A, stream, &launches, evs ? evs + 2 : nullptr);
-    if (evs) cudaEventRecord(evs[4], stream);
+    for (int st = s0; st < s1; ++st) swarm_gpu::launch_stage(A, st, stream, &launches);
     return cudaOk(this, cudaGetLastError(), "kernel launch") ? SWARM_OK : SWARM_E_CUDA;
+}
+
+// A graph of stages [s0, s1) of a step reading state half `in`
+int SwarmSim::captureStages(int in, int s0, int s1, cudaGraphExec_t* out) {
+    cudaGraph_t g = nullptr;
+    if (!cudaOk(this, cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "capture")) return SWARM_E_CUDA;
+    const int64_t saved = launches;
+    const int rc = enqueueStages(in, s0, s1);
+    launches = saved;
+    if (!cudaOk(this, cudaStreamEndCapture(stream, &g), "capture end") || rc != SWARM_OK) return SWARM_E_CUDA;
+    const bool inst = cudaOk(this, cudaGraphInstantiate(out, g, 0), "graph instantiate");
+    cudaGraphDestroy(g);
+    return inst ? SWARM_OK : SWARM_E_CUDA;
 }
 
 extern "C" {
@@ -286,29 +298,31 @@ int swarm_set_timing(SwarmHandle h, int enabled) {
     return SWARM_OK;
 }
 
+// One step = 4 stages. Timing on: an event before each stage and after the last, recorded on the stream between
+// stage launches (or stage graphs), never inside a capture.
 static int stepImpl(SwarmHandle h, int steps) {
     h->launches = 0;
     const int perStep = 6 + std::max(h->P.proj_iterations - 1, 0);
     for (int s = 0; s < steps; ++s) {
         const int in = h->readIdx;
-        cudaEvent_t* evs = h->timing ? h->ev : nullptr;
-        if (h->useGraph) {
-            if (!h->graph[in]) {
-                cudaGraph_t g = nullptr;
-                if (!cudaOk(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "capture")) return SWARM_E_CUDA;
-                const int64_t saved = h->launches;
-                const int rc = h->enqueueStep(in, evs);
-                h->launches = saved;
-                if (!cudaOk(h, cudaStreamEndCapture(h->stream, &g), "capture end") || rc != SWARM_OK) return SWARM_E_CUDA;
-                const bool inst = cudaOk(h, cudaGraphInstantiate(&h->graph[in], g, 0), "graph instantiate");
-                cudaGraphDestroy(g);
-                if (!inst) return SWARM_E_CUDA;
-            }
+        if (h->useGraph && !h->timing) {
+            if (!h->graph[in] && h->captureStages(in, 0, 4, &h->graph[in]) != SWARM_OK) return SWARM_E_CUDA;
             if (!cudaOk(h, cudaGraphLaunch(h->graph[in], h->stream), "graph launch")) return SWARM_E_CUDA;
             h->launches += perStep;
         } else {
-            const int rc = h->enqueueStep(in, evs);
-            if (rc != SWARM_OK) return rc;
+            for (int st = 0; st < 4; ++st) {
+                if (h->timing && !cudaOk(h, cudaEventRecord(h->ev[st], h->stream), "event")) return SWARM_E_CUDA;
+                if (h->useGraph) {
+                    if (!h->stageGraph[in][st] && h->captureStages(in, st, st + 1, &h->stageGraph[in][st]) != SWARM_OK)
+                        return SWARM_E_CUDA;
+                    if (!cudaOk(h, cudaGraphLaunch(h->stageGraph[in][st], h->stream), "graph launch")) return SWARM_E_CUDA;
+                } else {
+                    const int rc = h->enqueueStages(in, st, st + 1);
+                    if (rc != SWARM_OK) return rc;
+                }
+            }
+            if (h->timing && !cudaOk(h, cudaEventRecord(h->ev[4], h->stream), "event")) return SWARM_E_CUDA;
+            if (h->useGraph) h->launches += perStep;
         }
         h->readIdx ^= 1;
     }

@@ -223,3 +223,20 @@ def test_grid_hall_65536_one_step_vs_oracle_and_invariants(built):
     sim2.set_graph(True)
     sim2.step(1)
     assert np.array_equal(_bits(sim.state()), _bits(sim2.state()))
+
+
+@pytest.mark.parametrize("graph,timing", [(False, True), (True, True), (True, False)])
+def test_execution_modes_are_bit_identical(terrace, terrace_golden, graph, timing):
+    """Kernel-by-kernel launches, whole-step graphs and per-stage graphs with stage events give the same bits."""
+    P, venue = terrace
+    a = _sim(P, venue, terrace_golden["spawn"])
+    b = _sim(P, venue, terrace_golden["spawn"])
+    b.set_graph(graph)
+    b.set_timing(timing)
+    for _ in range(4):
+        a.step(3)
+        b.step(3)
+        if timing:
+            t = b.stage_times()
+            assert t["total"] > 0 and t["predict"] > 0
+    assert np.array_equal(_bits(a.state()), _bits(b.state()))
