@@ -54,6 +54,7 @@ struct StepArgs {
     uint32_t* count;        // agents per cell; ncells + 1 buckets (the last: inactive)
     uint32_t* start;        // exclusive scan of count
     uint2* cells;           // (startIndex, agentCount) per cell, CpuCrowdSim::cells()
+    uint32_t* tileSums;     // the scan's per-tile totals
     uint32_t* sidTmp;       // agent ids in scatter order (any order within a cell)
     uint32_t* sid;          // agent ids in slot order (ascending within a cell)
     uint32_t* skey;         // cell of each slot

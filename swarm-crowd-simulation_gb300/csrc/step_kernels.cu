@@ -3,7 +3,7 @@
 //
 //   k_hash        per agent: cell key (calc_grid.comp / CpuCrowdSim::hash :983-993) and its arrival rank in the cell's
 //                 counter (warp-aggregated atomics: one atomic per distinct cell per warp)
-//   k_scan        exclusive scan of the per-cell counts -> run starts; the cell table (start, count); counts cleared
+//   k_scan_*      exclusive scan of the per-cell counts (two tiled passes) -> run starts; the cell table; counts cleared
 //   k_scatter     agent -> a slot in its cell's run (arrival order)
 //   k_rank_gather per slot: the agent's rank by id among its cell's agents -> the final slot (the key order over
 //                 unique (cell, id) keys = the reference's stable counting sort, CpuCrowdSim::sortCounting :997-1006);
@@ -50,41 +50,72 @@ __global__ void k_hash(StepArgs A) {
     A.rank[i] = base + uint32_t(__popc(peers & ((1u << lane) - 1u)));
 }
 
-// One block of SCAN_THREADS: each thread scans a contiguous chunk; a block-wide scan of the chunk sums links them.
-constexpr int SCAN_THREADS = 1024;
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan(StepArgs A) {
-    __shared__ uint32_t warpSums[32];
-    const int nb = A.V.ncells + 1;
-    const int chunk = (nb + SCAN_THREADS - 1) / SCAN_THREADS;
-    const int t = threadIdx.x;
-    const int b0 = t * chunk, b1 = min(b0 + chunk, nb);
-    uint32_t sum = 0;
-    for (int b = b0; b < b1; ++b) sum += A.count[b];
-    // block exclusive scan of the chunk sums
-    const unsigned lane = t & 31, warp = t >> 5;
-    uint32_t inc = sum;
+// The exclusive scan of the ncells + 1 counts, in tiles of SCAN_TILE: k_scan_reduce writes each tile's total,
+// k_scan_apply scans its tile on top of the totals of the tiles before it, writes the run starts and the cell table,
+// and clears the counts for the next step. No block waits on another.
+constexpr int SCAN_THREADS = 256, SCAN_ITEMS = 8, SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+__device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* warpSums, uint32_t& total) {
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t inc = v;
     for (int o = 1; o < 32; o <<= 1) {
-        uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
-        if (int(lane) >= o) inc += v;
+        const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+        if (int(lane) >= o) inc += u;
     }
     if (lane == 31) warpSums[warp] = inc;
     __syncthreads();
     if (warp == 0) {
-        uint32_t w = warpSums[lane];
+        uint32_t w = lane < SCAN_THREADS / 32 ? warpSums[lane] : 0u;
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t v = __shfl_up_sync(0xffffffffu, w, o);
-            if (int(lane) >= o) w += v;
+            const uint32_t u = __shfl_up_sync(0xffffffffu, w, o);
+            if (int(lane) >= o) w += u;
         }
-        warpSums[lane] = w;   // inclusive
+        if (lane < SCAN_THREADS / 32) warpSums[lane] = w;
     }
     __syncthreads();
-    uint32_t run = inc - sum + (warp > 0 ? warpSums[warp - 1] : 0u);
-    for (int b = b0; b < b1; ++b) {
-        const uint32_t c = A.count[b];
+    total = warpSums[SCAN_THREADS / 32 - 1];
+    return inc - v + (warp > 0 ? warpSums[warp - 1] : 0u);
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(StepArgs A, uint32_t* tileSums) {
+    __shared__ uint32_t warpSums[32];
+    const int nb = A.V.ncells + 1;
+    const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
+    uint32_t sum = 0;
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; ++j) sum += base + j < nb ? A.count[base + j] : 0u;
+    uint32_t total;
+    blockExclusiveScan(sum, warpSums, total);
+    if (threadIdx.x == 0) tileSums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(StepArgs A, const uint32_t* tileSums) {
+    __shared__ uint32_t warpSums[32];
+    __shared__ uint32_t prefix;
+    const int nb = A.V.ncells + 1;
+    // the totals of the tiles before this one
+    uint32_t p = 0;
+    for (int t = threadIdx.x; t < int(blockIdx.x); t += SCAN_THREADS) p += tileSums[t];
+    for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
+    if (threadIdx.x == 0) prefix = 0;
+    __syncthreads();
+    if ((threadIdx.x & 31u) == 0 && p) atomicAdd(&prefix, p);
+    const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
+    uint32_t c[SCAN_ITEMS];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; ++j) { c[j] = base + j < nb ? A.count[base + j] : 0u; sum += c[j]; }
+    uint32_t total;
+    uint32_t run = blockExclusiveScan(sum, warpSums, total);   // its barriers also order the prefix atomics
+    run += prefix;
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; ++j) {
+        const int b = base + j;
+        if (b >= nb) break;
         A.start[b] = run;
-        if (b < A.V.ncells) A.cells[b] = c ? make_uint2(run, c) : make_uint2(0u, 0u);
+        if (b < A.V.ncells) A.cells[b] = c[j] ? make_uint2(run, c[j]) : make_uint2(0u, 0u);
         A.count[b] = 0u;   // ready for the next step's hash
-        run += c;
+        run += c[j];
     }
 }
 
@@ -348,11 +379,13 @@ inline int blocks(int n, int t) { return (n + t - 1) / t; }
 void launch_sort(const StepArgs& A, cudaStream_t st, int64_t* launches) {
     const int n = A.n;
     k_hash<<<blocks(n, 256), 256, 0, st>>>(A);
-    k_scan<<<1, SCAN_THREADS, 0, st>>>(A);
+    const int tiles = (A.V.ncells + 1 + SCAN_TILE - 1) / SCAN_TILE;
+    k_scan_reduce<<<tiles, SCAN_THREADS, 0, st>>>(A, A.tileSums);
+    k_scan_apply<<<tiles, SCAN_THREADS, 0, st>>>(A, A.tileSums);
     k_scatter<<<blocks(n, 256), 256, 0, st>>>(A);
     if (A.P.uniform_body) k_rank_gather<false><<<blocks(n, 256), 256, 0, st>>>(A);
     else k_rank_gather<true><<<blocks(n, 256), 256, 0, st>>>(A);
-    *launches += 4;
+    *launches += 5;
 }
 
 template <class Venue>

@@ -39,6 +39,7 @@ struct SwarmSim {
     uint8_t* contacts = nullptr;
     uint32_t *key = nullptr, *rank = nullptr, *count = nullptr, *start = nullptr, *sidTmp = nullptr, *sid = nullptr, *skey = nullptr;
     uint2* cells = nullptr;
+    uint32_t* tileSums = nullptr;
     float4 *pos0 = nullptr, *vel0 = nullptr, *proj0 = nullptr, *proj1 = nullptr, *vel1 = nullptr, *plane = nullptr;
     float2* prm = nullptr;
     uint8_t* ctc = nullptr;
@@ -117,7 +118,7 @@ StepArgs SwarmSim::args(int in) const {
     A.aparam = aparam;
     A.drive = driveOn ? drive : nullptr;
     A.contacts = contacts;
-    A.key = key; A.rank = rank; A.count = count; A.start = start; A.cells = cells;
+    A.key = key; A.rank = rank; A.count = count; A.start = start; A.cells = cells; A.tileSums = tileSums;
     A.sidTmp = sidTmp; A.sid = sid; A.skey = skey;
     A.pos0 = pos0; A.vel0 = vel0; A.prm = prm; A.proj[0] = proj0; A.proj[1] = proj1;
     A.vel1 = vel1; A.plane = plane; A.ctc = ctc; A.err = errFlag;
@@ -172,7 +173,7 @@ int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capac
     bool ok = devAlloc(h, &h->state[0], 2 * N) && devAlloc(h, &h->state[1], 2 * N) && devAlloc(h, &h->aparam, N) &&
               devAlloc(h, &h->drive, N) && devAlloc(h, &h->contacts, N) && devAlloc(h, &h->key, N) && devAlloc(h, &h->rank, N) &&
               devAlloc(h, &h->count, size_t(h->ncells) + 1) && devAlloc(h, &h->start, size_t(h->ncells) + 1) &&
-              devAlloc(h, &h->cells, size_t(h->ncells)) && devAlloc(h, &h->sidTmp, N) && devAlloc(h, &h->sid, N) &&
+              devAlloc(h, &h->cells, size_t(h->ncells)) && devAlloc(h, &h->tileSums, size_t(h->ncells) / 1024 + 2) && devAlloc(h, &h->sidTmp, N) && devAlloc(h, &h->sid, N) &&
               devAlloc(h, &h->skey, N) && devAlloc(h, &h->pos0, N) && devAlloc(h, &h->vel0, N) && devAlloc(h, &h->proj0, N) &&
               devAlloc(h, &h->proj1, N) && devAlloc(h, &h->vel1, N) && devAlloc(h, &h->plane, N) && devAlloc(h, &h->prm, N) &&
               devAlloc(h, &h->ctc, N) && devAlloc(h, &h->errFlag, 1);
@@ -302,7 +303,7 @@ int swarm_set_timing(SwarmHandle h, int enabled) {
 // stage launches (or stage graphs), never inside a capture.
 static int stepImpl(SwarmHandle h, int steps) {
     h->launches = 0;
-    const int perStep = 6 + std::max(h->P.proj_iterations - 1, 0);
+    const int perStep = 7 + std::max(h->P.proj_iterations - 1, 0);
     for (int s = 0; s < steps; ++s) {
         const int in = h->readIdx;
         if (h->useGraph && !h->timing) {
