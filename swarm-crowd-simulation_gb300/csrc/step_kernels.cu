@@ -196,34 +196,44 @@ __global__ void __launch_bounds__(128) k_predict(StepArgs A) {
     f2 sep{0.0f, 0.0f};
     float sAhead = 1e9f;
     const int R = P.perc_ring;
+    // The neighbour rows: a row of cells is one contiguous run of slots, so each row is [start[a], start[b + 1]) and
+    // walking it visits the reference's order (cells by x, agents by slot). Cells that cannot hold an agent within
+    // R_PERC are left out of each row (every agent lies inside its cell, widened by `margin`): they contribute
+    // nothing, and the nearest-agent-ahead minimum does not depend on the visiting order.
+    const float csx = A.V.dspanX / float(resX), csy = A.V.dspanY / float(resY);
+    const float margin = 0.01f * smax(csx, csy);
+    const float rPerc = sqrtf(P.r_perc2) + margin;
     for (int y = -R; y <= R; y++) {
         const int ny = cy + y;
         if (ny < 0 || ny >= resY) continue;
-        for (int x = -R; x <= R; x++) {
-            const int nx = cx + x;
-            if (nx < 0 || nx >= resX) continue;
-            const uint2 cell = __ldg(reinterpret_cast<const uint2*>(A.cells) + (nx + ny * resX));
-            for (uint32_t k = cell.x; k < cell.x + cell.y; k++) {
-                if (int(k) == s) continue;
-                const float4 op = A.pos0[k];
-                const f3 offset = xyz(p) - xyz(op);
-                const float dxy2 = dot(xy(offset), xy(offset));
-                if (dxy2 < P.r_perc2) {
-                    const uint32_t other = A.sid[k];
-                    float dc, rs, rs2;
-                    if (kUniform) { dc = P.body_diam; rs = P.r_sep; rs2 = P.r_sep2; }
-                    else { dc = ri + A.prm[k].x; rs = dc + P.sep_margin; rs2 = rs * rs; }
-                    sep = sep + separationForce(P, offset, self, other, rs, rs2);
-                    const float ahead = -dot(xy(offset), eGoal);
-                    const float lateral = fabsf(offset.x * eGoal.y - offset.y * eGoal.x);
-                    const float dxy = sqrtf(dxy2);
-                    const float key = kUniform ? dxy : dxy - dc;
-                    if (ahead > 0.0f && lateral < dc && key < sAhead) {
-                        const f2 eOther = goalOf(A, ven, xyz(op), other);
-                        const float aheadOther = dot(xy(offset), eOther);
-                        const bool mutual = aheadOther > 0.0f && fabsf(offset.x * eOther.y - offset.y * eOther.x) < dc;
-                        if (!mutual || ahead > aheadOther || (ahead == aheadOther && self > other)) sAhead = key;
-                    }
+        const float ylo = A.V.dminY + float(ny) * csy - margin, yhi = A.V.dminY + float(ny + 1) * csy + margin;
+        const float dy = fmaxf(0.0f, fmaxf(ylo - p.y, p.y - yhi));
+        if (dy >= rPerc) continue;
+        const float w = sqrtf(rPerc * rPerc - dy * dy) + margin;
+        const int xlo = max(max(cx - R, 0), int(floorf((p.x - w - A.V.dminX) / csx)));
+        const int xhi = min(min(cx + R, resX - 1), int(floorf((p.x + w - A.V.dminX) / csx)));
+        if (xlo > xhi) continue;
+        const uint32_t k0 = __ldg(A.start + (xlo + ny * resX)), k1 = __ldg(A.start + (xhi + 1 + ny * resX));
+        for (uint32_t k = k0; k < k1; k++) {
+            if (int(k) == s) continue;
+            const float4 op = A.pos0[k];
+            const f3 offset = xyz(p) - xyz(op);
+            const float dxy2 = dot(xy(offset), xy(offset));
+            if (dxy2 < P.r_perc2) {
+                const uint32_t other = A.sid[k];
+                float dc, rs, rs2;
+                if (kUniform) { dc = P.body_diam; rs = P.r_sep; rs2 = P.r_sep2; }
+                else { dc = ri + A.prm[k].x; rs = dc + P.sep_margin; rs2 = rs * rs; }
+                sep = sep + separationForce(P, offset, self, other, rs, rs2);
+                const float ahead = -dot(xy(offset), eGoal);
+                const float lateral = fabsf(offset.x * eGoal.y - offset.y * eGoal.x);
+                const float dxy = sqrtf(dxy2);
+                const float key = kUniform ? dxy : dxy - dc;
+                if (ahead > 0.0f && lateral < dc && key < sAhead) {
+                    const f2 eOther = goalOf(A, ven, xyz(op), other);
+                    const float aheadOther = dot(xy(offset), eOther);
+                    const bool mutual = aheadOther > 0.0f && fabsf(offset.x * eOther.y - offset.y * eOther.x) < dc;
+                    if (!mutual || ahead > aheadOther || (ahead == aheadOther && self > other)) sAhead = key;
                 }
             }
         }
@@ -283,30 +293,27 @@ __device__ __forceinline__ float4 projectSlot(const StepArgs& A, const Venue& ve
     const float ri = kUniform ? P.body_radius : A.prm[s].x;
     f2 corr{0.0f, 0.0f};
     int nContacts = 0;
+    const int xlo = max(cx - 1, 0), xhi = min(cx + 1, resX - 1);
     for (int y = -1; y <= 1; y++) {
         const int ny = cy + y;
         if (ny < 0 || ny >= resY) continue;
-        for (int x = -1; x <= 1; x++) {
-            const int nx = cx + x;
-            if (nx < 0 || nx >= resX) continue;
-            const uint2 cell = __ldg(reinterpret_cast<const uint2*>(A.cells) + (nx + ny * resX));
-            for (uint32_t k = cell.x; k < cell.x + cell.y; k++) {
-                if (int(k) == s) continue;
-                const float4 op = in[k];
-                const f3 offset = xyz(b) - xyz(op);
-                float dc, dc2;
-                if (kUniform) { dc = P.body_diam; dc2 = P.body_diam2; }
-                else { dc = ri + A.prm[k].x; dc2 = dc * dc; }
-                const float dxy2 = dot(xy(offset), xy(offset));
-                if (op.w >= 0.0f && fabsf(offset.z) < dc && dxy2 < dc2) {
-                    const float dxy = sqrtf(dxy2);
-                    const float shift = 0.5f * (dc - dxy);
-                    f2 c;
-                    if (dxy2 <= P.stacked_xy2) c = shift * pairDirection(A.sid[s], A.sid[k], P.hash_to_radians);
-                    else c = shift * (xy(offset) / dxy);
-                    corr = corr + c;
-                    ++nContacts;
-                }
+        const uint32_t k0 = __ldg(A.start + (xlo + ny * resX)), k1 = __ldg(A.start + (xhi + 1 + ny * resX));
+        for (uint32_t k = k0; k < k1; k++) {
+            if (int(k) == s) continue;
+            const float4 op = in[k];
+            const f3 offset = xyz(b) - xyz(op);
+            float dc, dc2;
+            if (kUniform) { dc = P.body_diam; dc2 = P.body_diam2; }
+            else { dc = ri + A.prm[k].x; dc2 = dc * dc; }
+            const float dxy2 = dot(xy(offset), xy(offset));
+            if (op.w >= 0.0f && fabsf(offset.z) < dc && dxy2 < dc2) {
+                const float dxy = sqrtf(dxy2);
+                const float shift = 0.5f * (dc - dxy);
+                f2 c;
+                if (dxy2 <= P.stacked_xy2) c = shift * pairDirection(A.sid[s], A.sid[k], P.hash_to_radians);
+                else c = shift * (xy(offset) / dxy);
+                corr = corr + c;
+                ++nContacts;
             }
         }
     }
