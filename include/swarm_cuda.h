@@ -220,6 +220,7 @@ int swarm_spawn_lattice(int nx, int ny, int n, float spacing, float cx, float cy
                         float r_lo, float r_hi, float v_mean, float v_sd, float v_lo, float v_hi,
                         float* boids, float* radius, float* v0);
 
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif

@@ -1,0 +1,72 @@
+"""The synthetic venues and spawns (host code, no GPU): the hall's fields, the lattice spawn's distributions and its
+determinism, the C++ host class compiles against the C ABI."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, PKG
+
+
+@pytest.fixture(scope="module")
+def c0(built):
+    from swarm_gb300 import venues
+    return venues.terrace_c0()
+
+
+def test_hall_fields(c0):
+    venue, _ = c0
+    v = venue.struct
+    wall = venue.arrays["wall"].reshape(v.wall_ny, v.wall_nx)
+    nav = venue.arrays["nav"].reshape(v.nav_ny, v.nav_nx)
+    # the interior is free, the wall ring is solid, the door gap (+x wall, |y| < 2 m) is open
+    def w(x, y):
+        return wall[int(round((y - v.wall_origin_y) / v.wall_h)), int(round((x - v.wall_origin_x) / v.wall_h))]
+    assert w(0.0, 0.0) > 10.0
+    assert w(20.15, 10.0) < 0.0 and w(-20.15, 0.0) < 0.0 and w(0.0, 17.15) < 0.0
+    assert w(20.15, 0.0) > 1.0           # inside the 4 m door gap
+    # the geodesic distance decreases towards the door and is 0 beyond the exit line
+    def d(x, y):
+        return nav[int(round((y - v.nav_origin_y) / v.nav_h)), int(round((x - v.nav_origin_x) / v.nav_h))]
+    assert d(21.5, 0.0) == 0.0
+    assert d(-19.0, 0.0) > d(0.0, 0.0) > d(19.0, 0.0) > 0.0
+    assert abs(d(0.0, 0.0) - 21.0) < 0.3    # 20 m to the wall's inner face + 0.3 wall + 0.5 exit depth, first-order FMM
+    assert d(-19.0, 16.0) > d(-19.0, 0.0)   # around: farther from the door
+
+
+def test_lattice_spawn_distributions_and_determinism(built):
+    from swarm_gb300.venues import spawn_lattice
+    b1, r1, v1 = spawn_lattice(64, 64, seed=0)
+    b2, r2, v2 = spawn_lattice(64, 64, seed=0)
+    b3, _, _ = spawn_lattice(64, 64, seed=1)
+    assert np.array_equal(b1, b2) and np.array_equal(r1, r2) and np.array_equal(v1, v2)
+    assert not np.array_equal(b1, b3)
+    assert r1.min() >= 0.2 and r1.max() <= 0.25 and abs(r1.mean() - 0.225) < 0.003
+    assert v1.min() >= 0.6 and v1.max() <= 2.0 and abs(v1.mean() - 1.34) < 0.02 and abs(v1.std() - 0.26) < 0.02
+    lattice = np.stack(np.meshgrid(np.arange(64) - 31.5, np.arange(64) - 31.5), -1).reshape(-1, 2) * 0.5
+    assert np.abs(b1[:, :2] - lattice).max() <= 0.05 + 1e-6
+    assert np.array_equal(b1[:, 2], r1) and (b1[:, 3] == 1).all() and (b1[:, 4:] == 0).all()
+
+
+def test_batch_instances_spec():
+    import sys
+    sys.path.insert(0, PKG)
+    from swarm_gb300.venues import batch_instances
+    inst = batch_instances(256, seed=0)
+    ns = np.array([i["n"] for i in inst])
+    assert len(inst) == 256 and ns.min() >= 1024 and ns.max() <= 65536
+    assert 10000 < ns.mean() < 22000          # log-uniform mean 64512 / ln 64 = 15.5k
+    assert all(1 <= len(i["doors"]) <= 2 and all(1.5 <= d[2] <= 6.0 for d in i["doors"]) for i in inst)
+
+
+def test_cpp_host_class_compiles_and_links(built, tmp_path):
+    src = tmp_path / "t.cpp"
+    src.write_text('#include "swarm_gb300.hpp"\n#include <cstdio>\n'
+                   'int main(){ SwarmParams p = swarm_gb300::CudaCrowdSim::referenceParams();'
+                   ' std::printf("%d %g\\n", p.proj_iterations, double(p.body_radius)); return 0; }\n')
+    exe = tmp_path / "t"
+    subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe),
+                    "-L", PKG, "-lswarm_gb300", "-Wl,-rpath," + PKG], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    assert out == ["32", "0.0064"]
