@@ -220,6 +220,18 @@ int swarm_spawn_lattice(int nx, int ny, int n, float spacing, float cx, float cy
                         float r_lo, float r_hi, float v_mean, float v_sd, float v_lo, float v_hi,
                         float* boids, float* radius, float* v0);
 
+/* ---- the key sort without device allocation ----
+ * No counterpart in the reference. For callers that cannot allocate device memory while they run (host callbacks,
+ * allocator-free deployments that fix their footprint at start-up): sorts one state already in device memory --
+ * d_boids, n x 8 floats -- by cell over the given hash grid, exactly as the step's own sort, and writes the sorted
+ * pairs (d_grid_id, d_boid_id: n each) and the cell table (d_cells: 2 x grid_res_x x grid_res_y) to the caller's
+ * device arrays. Its working memory is a fixed array compiled into this library (about 1.8 MB per GPU that loads
+ * it, held until exit): at most 65536 agents and 131072 cells, larger sizes return SWARM_E_INVALID. It calls no
+ * allocator. The first call on a device looks up the array's address and should come before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race, so order them (one stream, or events). */
+int swarm_sort_grid_noalloc(const float* d_boids, int n, int grid_res_x, int grid_res_y, float domain_min_x,
+                            float domain_min_y, float domain_span_x, float domain_span_y, uint32_t* d_grid_id,
+                            uint32_t* d_boid_id, uint32_t* d_cells, void* stream);
 
 #ifdef __cplusplus
 }  /* extern "C" */
