@@ -173,6 +173,14 @@ int swarm_set_iterations(SwarmHandle h, int k);
 int swarm_set_drive_table(SwarmHandle h, const float* dirs, int n);
 /* Captures one step in a CUDA graph and replays it (1) or launches kernel by kernel (0, the default). */
 int swarm_set_graph(SwarmHandle h, int enabled);
+/* 1 (the default): each step is one persistent cooperative kernel whose phases are separated by grid barriers (the
+ * grid is sized to stay resident); 0: one kernel per phase (hash, scan x2, scatter, rank + gather, predict, K - 1
+ * sweeps, final), replayed from CUDA graphs when swarm_set_graph is on. Both give the same bits. */
+int swarm_set_fused(SwarmHandle h, int enabled);
+/* Failure-path test: the next fused step's first grid barrier waits for one block more than the launch has, runs
+ * out its 1 s limit, records the timeout and ends the launch early; the next swarm_synchronize (or download)
+ * returns SWARM_E_TIMEOUT and the handle stays usable. For tests only. */
+int swarm_test_barrier_timeout(SwarmHandle h);
 int swarm_synchronize(SwarmHandle h);
 
 /* ---- inspection (the reference's parity tests read these) ----

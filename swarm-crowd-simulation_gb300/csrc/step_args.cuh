@@ -67,6 +67,8 @@ struct StepArgs {
     float4* plane;          // wall plane (n.xy, offset) and flags
     uint8_t* ctc;           // the predict pass's contact bits
     int* err;
+    unsigned* barrier;      // the fused kernel's grid barrier: arrival counter, generation
+    int32_t barrierExtra;   // 0; 1 only in the timeout test: the first barrier waits for a block that never arrives
 };
 
 }  // namespace swarm_gpu

@@ -19,6 +19,8 @@
 
 #include <type_traits>
 
+#include <cuda/atomic>
+
 #include "device_math.cuh"
 #include "venue_grid.cuh"
 #include "venue_stadium.cuh"
@@ -31,17 +33,17 @@ __device__ __forceinline__ uint32_t cellID(const VenueArgs& V, float4 p) {
     return uint32_t(x + y * V.resX);
 }
 
-__global__ void k_hash(StepArgs A) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= A.n) return;
-    float4 p = A.stateIn[2 * i];
-    if (isnan(p.x)) { p = make_float4(0.0f, 0.0f, 0.0f, 1.0f); A.stateIn[2 * i] = p; }
+// Called by all 32 lanes of a warp together (warp-aggregated atomics); lanes with i >= n take no part.
+__device__ __forceinline__ void hashItem(const StepArgs& A, int i) {
+    const bool valid = i < A.n;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned mask = __ballot_sync(0xffffffffu, valid);
+    if (!valid) return;
+    float4 p = A.stateIn[2 * size_t(i)];
+    if (isnan(p.x)) { p = make_float4(0.0f, 0.0f, 0.0f, 1.0f); A.stateIn[2 * size_t(i)] = p; }
     const uint32_t key = p.w == 0.0f ? INACTIVE_CELL : cellID(A.V, p);
     const uint32_t bucket = key == INACTIVE_CELL ? uint32_t(A.V.ncells) : key;
-    const unsigned lane = threadIdx.x & 31u;
-    const int warpBase = i - int(lane);
-    const unsigned valid = A.n - warpBase >= 32 ? 0xffffffffu : ((1u << (A.n - warpBase)) - 1u);
-    const unsigned peers = __match_any_sync(valid, bucket);
+    const unsigned peers = __match_any_sync(mask, bucket);
     const int leader = __ffs(peers) - 1;
     uint32_t base = 0;
     if (int(lane) == leader) base = atomicAdd(A.count + bucket, uint32_t(__popc(peers)));
@@ -50,11 +52,15 @@ __global__ void k_hash(StepArgs A) {
     A.rank[i] = base + uint32_t(__popc(peers & ((1u << lane) - 1u)));
 }
 
+__global__ void k_hash(StepArgs A) { hashItem(A, blockIdx.x * blockDim.x + threadIdx.x); }
+
 // The exclusive scan of the ncells + 1 counts, in tiles of SCAN_TILE: k_scan_reduce writes each tile's total,
 // k_scan_apply scans its tile on top of the totals of the tiles before it, writes the run starts and the cell table,
 // and clears the counts for the next step. No block waits on another.
 constexpr int SCAN_THREADS = 256, SCAN_ITEMS = 8, SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+constexpr int FUSED_THREADS = 128;   // the fused kernel's blocks (they also run the scan, in tiles of 1 024 counts)
 
+template <int T>
 __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* warpSums, uint32_t& total) {
     const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     uint32_t inc = v;
@@ -65,49 +71,51 @@ __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* war
     if (lane == 31) warpSums[warp] = inc;
     __syncthreads();
     if (warp == 0) {
-        uint32_t w = lane < SCAN_THREADS / 32 ? warpSums[lane] : 0u;
+        uint32_t w = lane < T / 32 ? warpSums[lane] : 0u;
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t u = __shfl_up_sync(0xffffffffu, w, o);
             if (int(lane) >= o) w += u;
         }
-        if (lane < SCAN_THREADS / 32) warpSums[lane] = w;
+        if (lane < T / 32) warpSums[lane] = w;
     }
     __syncthreads();
-    total = warpSums[SCAN_THREADS / 32 - 1];
+    total = warpSums[T / 32 - 1];
     return inc - v + (warp > 0 ? warpSums[warp - 1] : 0u);
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(StepArgs A, uint32_t* tileSums) {
-    __shared__ uint32_t warpSums[32];
+// Block-level (blockDim.x == T): the total of tile `tile` (T * SCAN_ITEMS counts) into A.tileSums
+template <int T>
+__device__ __forceinline__ void scanReduceTile(const StepArgs& A, int tile, uint32_t* warpSums) {
     const int nb = A.V.ncells + 1;
-    const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
+    const int base = tile * (T * SCAN_ITEMS) + threadIdx.x * SCAN_ITEMS;
     uint32_t sum = 0;
 #pragma unroll
     for (int j = 0; j < SCAN_ITEMS; ++j) sum += base + j < nb ? A.count[base + j] : 0u;
     uint32_t total;
-    blockExclusiveScan(sum, warpSums, total);
-    if (threadIdx.x == 0) tileSums[blockIdx.x] = total;
+    blockExclusiveScan<T>(sum, warpSums, total);
+    if (threadIdx.x == 0) A.tileSums[tile] = total;
+    __syncthreads();   // warpSums is reused by the next tile
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(StepArgs A, const uint32_t* tileSums) {
-    __shared__ uint32_t warpSums[32];
-    __shared__ uint32_t prefix;
+// Block-level (blockDim.x == T): scan tile `tile` on top of the totals of the tiles before it; run starts, cell table,
+// counts cleared
+template <int T>
+__device__ __forceinline__ void scanApplyTile(const StepArgs& A, int tile, uint32_t* warpSums, uint32_t* prefix) {
     const int nb = A.V.ncells + 1;
-    // the totals of the tiles before this one
     uint32_t p = 0;
-    for (int t = threadIdx.x; t < int(blockIdx.x); t += SCAN_THREADS) p += tileSums[t];
+    for (int t = threadIdx.x; t < tile; t += T) p += A.tileSums[t];
     for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
-    if (threadIdx.x == 0) prefix = 0;
+    if (threadIdx.x == 0) *prefix = 0;
     __syncthreads();
-    if ((threadIdx.x & 31u) == 0 && p) atomicAdd(&prefix, p);
-    const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
+    if ((threadIdx.x & 31u) == 0 && p) atomicAdd(prefix, p);
+    const int base = tile * (T * SCAN_ITEMS) + threadIdx.x * SCAN_ITEMS;
     uint32_t c[SCAN_ITEMS];
     uint32_t sum = 0;
 #pragma unroll
     for (int j = 0; j < SCAN_ITEMS; ++j) { c[j] = base + j < nb ? A.count[base + j] : 0u; sum += c[j]; }
     uint32_t total;
-    uint32_t run = blockExclusiveScan(sum, warpSums, total);   // its barriers also order the prefix atomics
-    run += prefix;
+    uint32_t run = blockExclusiveScan<T>(sum, warpSums, total);   // its barriers also order the prefix atomics
+    run += *prefix;
 #pragma unroll
     for (int j = 0; j < SCAN_ITEMS; ++j) {
         const int b = base + j;
@@ -117,11 +125,21 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(StepArgs A, const u
         A.count[b] = 0u;   // ready for the next step's hash
         run += c[j];
     }
+    __syncthreads();   // prefix and warpSums are reused by the next tile
 }
 
-__global__ void k_scatter(StepArgs A) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= A.n) return;
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(StepArgs A) {
+    __shared__ uint32_t warpSums[32];
+    scanReduceTile<SCAN_THREADS>(A, blockIdx.x, warpSums);
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(StepArgs A) {
+    __shared__ uint32_t warpSums[32];
+    __shared__ uint32_t prefix;
+    scanApplyTile<SCAN_THREADS>(A, blockIdx.x, warpSums, &prefix);
+}
+
+__device__ __forceinline__ void scatterItem(const StepArgs& A, int i) {
     const uint32_t key = A.key[i];
     const uint32_t bucket = key == INACTIVE_CELL ? uint32_t(A.V.ncells) : key;
     const uint32_t slot = A.start[bucket] + A.rank[i];
@@ -129,10 +147,13 @@ __global__ void k_scatter(StepArgs A) {
     A.sidTmp[slot] = uint32_t(i);
 }
 
+__global__ void k_scatter(StepArgs A) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < A.n) scatterItem(A, i);
+}
+
 template <bool kPerAgent>
-__global__ void k_rank_gather(StepArgs A) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= A.n) return;
+__device__ __forceinline__ void rankGatherItem(const StepArgs& A, int s) {
     const int nActive = int(A.start[A.V.ncells]);
     const uint32_t me = A.sidTmp[s];
     if (me >= uint32_t(A.n)) { atomicOr(A.err, ERR_BOUNDS); return; }
@@ -147,6 +168,12 @@ __global__ void k_rank_gather(StepArgs A) {
     A.pos0[t] = A.stateIn[2 * size_t(me)];
     A.vel0[t] = A.stateIn[2 * size_t(me) + 1];
     if (kPerAgent) A.prm[t] = A.aparam[me];
+}
+
+template <bool kPerAgent>
+__global__ void k_rank_gather(StepArgs A) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < A.n) rankGatherItem<kPerAgent>(A, s);
 }
 
 // ---- the physics passes ----
@@ -172,10 +199,8 @@ __device__ __forceinline__ f2 separationForce(const SwarmParams& P, f3 offset, u
 }
 
 template <class Venue>
-__global__ void __launch_bounds__(128) k_predict(StepArgs A) {
+__device__ __forceinline__ void predictItem(const StepArgs& A, int s) {
     constexpr bool kUniform = Body<Venue>::kUniform;
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= A.n) return;
     const int nActive = int(A.start[A.V.ncells]);
     if (s >= nActive) return;
     const SwarmParams& P = A.P;
@@ -213,7 +238,7 @@ __global__ void __launch_bounds__(128) k_predict(StepArgs A) {
         const int xlo = max(max(cx - R, 0), int(floorf((p.x - w - A.V.dminX) / csx)));
         const int xhi = min(min(cx + R, resX - 1), int(floorf((p.x + w - A.V.dminX) / csx)));
         if (xlo > xhi) continue;
-        const uint32_t k0 = __ldg(A.start + (xlo + ny * resX)), k1 = __ldg(A.start + (xhi + 1 + ny * resX));
+        const uint32_t k0 = A.start[xlo + ny * resX], k1 = A.start[xhi + 1 + ny * resX];
         for (uint32_t k = k0; k < k1; k++) {
             if (int(k) == s) continue;
             const float4 op = A.pos0[k];
@@ -280,6 +305,12 @@ __global__ void __launch_bounds__(128) k_predict(StepArgs A) {
     A.ctc[s] = uint8_t(contact);
 }
 
+template <class Venue>
+__global__ void __launch_bounds__(128) k_predict(StepArgs A) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < A.n) predictItem<Venue>(A, s);
+}
+
 // One Jacobi sweep for slot s reading `in` (cpu_crowd_sim.cpp:781-822 projectSlot); w of the result: displacement
 template <class Venue>
 __device__ __forceinline__ float4 projectSlot(const StepArgs& A, const Venue& ven, const float4* __restrict__ in, int s) {
@@ -297,7 +328,7 @@ __device__ __forceinline__ float4 projectSlot(const StepArgs& A, const Venue& ve
     for (int y = -1; y <= 1; y++) {
         const int ny = cy + y;
         if (ny < 0 || ny >= resY) continue;
-        const uint32_t k0 = __ldg(A.start + (xlo + ny * resX)), k1 = __ldg(A.start + (xhi + 1 + ny * resX));
+        const uint32_t k0 = A.start[xlo + ny * resX], k1 = A.start[xhi + 1 + ny * resX];
         for (uint32_t k = k0; k < k1; k++) {
             if (int(k) == s) continue;
             const float4 op = in[k];
@@ -333,18 +364,20 @@ __device__ __forceinline__ float4 projectSlot(const StepArgs& A, const Venue& ve
 }
 
 template <class Venue>
-__global__ void __launch_bounds__(128) k_project(StepArgs A, int inBuf) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= A.n) return;
+__device__ __forceinline__ void projectItem(const StepArgs& A, int s, int inBuf) {
     if (s >= int(A.start[A.V.ncells])) return;
     const Venue ven{A.P, A.V};
     A.proj[inBuf ^ 1][s] = projectSlot(A, ven, A.proj[inBuf], s);
 }
 
 template <class Venue>
-__global__ void __launch_bounds__(128) k_final(StepArgs A, int inBuf) {
+__global__ void __launch_bounds__(128) k_project(StepArgs A, int inBuf) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= A.n) return;
+    if (s < A.n) projectItem<Venue>(A, s, inBuf);
+}
+
+template <class Venue>
+__device__ __forceinline__ void finalItem(const StepArgs& A, int s, int inBuf) {
     const uint32_t self = A.sid[s];
     if (s >= int(A.start[A.V.ncells])) {   // evacuated before this step: carried over
         A.stateOut[2 * size_t(self)] = A.stateIn[2 * size_t(self)];
@@ -378,6 +411,78 @@ __global__ void __launch_bounds__(128) k_final(StepArgs A, int inBuf) {
     A.contacts[self] = uint8_t(contact);
 }
 
+template <class Venue>
+__global__ void __launch_bounds__(128) k_final(StepArgs A, int inBuf) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < A.n) finalItem<Venue>(A, s, inBuf);
+}
+
+// ---- the whole step as one persistent kernel ----
+// Every block stays resident (a cooperative launch) and the phases are separated by grid barriers. A barrier is a
+// counter and a generation word: the last block to arrive resets the counter and advances the generation (release);
+// the others wait for the generation to move (acquire) for at most BARRIER_WAIT_NS of wall-clock time (%globaltimer),
+// after which the kernel records ERR_TIMEOUT and stops waiting: every later barrier of the launch returns at once,
+// the launch ends, and the host reports SWARM_E_TIMEOUT and resets the barrier words.
+constexpr uint64_t BARRIER_WAIT_NS = 1000000000ull;   // 1 s; a healthy barrier waits microseconds
+
+__device__ __forceinline__ uint64_t globalNs() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void gridBarrier(const StepArgs& A, unsigned expected) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        cuda::atomic_ref<int, cuda::thread_scope_device> err(*A.err);
+        if (!(err.load(cuda::memory_order_relaxed) & ERR_TIMEOUT)) {
+            cuda::atomic_ref<unsigned, cuda::thread_scope_device> count(A.barrier[0]), gen(A.barrier[1]);
+            const unsigned g0 = gen.load(cuda::memory_order_relaxed);
+            if (count.fetch_add(1u, cuda::memory_order_acq_rel) == expected - 1) {
+                count.store(0u, cuda::memory_order_relaxed);
+                gen.fetch_add(1u, cuda::memory_order_release);
+            } else {
+                const uint64_t t0 = globalNs();
+                while (gen.load(cuda::memory_order_acquire) == g0) {
+                    if (globalNs() - t0 > BARRIER_WAIT_NS) { err.fetch_or(ERR_TIMEOUT, cuda::memory_order_relaxed); break; }
+                    __nanosleep(64);
+                }
+            }
+        }
+    }
+    __syncthreads();
+}
+
+template <class Venue, bool kPerAgent>
+__global__ void __launch_bounds__(FUSED_THREADS) k_step_fused(StepArgs A) {
+    __shared__ uint32_t warpSums[32];
+    __shared__ uint32_t prefix;
+    const int n = A.n;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    for (int base = tid - int(threadIdx.x & 31u); base < n; base += stride) hashItem(A, base + int(threadIdx.x & 31u));
+    gridBarrier(A, gridDim.x + unsigned(A.barrierExtra));   // barrierExtra: the timeout test's block that never arrives
+    constexpr int TILE = FUSED_THREADS * SCAN_ITEMS;
+    const int tiles = (A.V.ncells + 1 + TILE - 1) / TILE;
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x) scanReduceTile<FUSED_THREADS>(A, t, warpSums);
+    gridBarrier(A, gridDim.x);
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x) scanApplyTile<FUSED_THREADS>(A, t, warpSums, &prefix);
+    gridBarrier(A, gridDim.x);
+    for (int i = tid; i < n; i += stride) scatterItem(A, i);
+    gridBarrier(A, gridDim.x);
+    for (int s = tid; s < n; s += stride) rankGatherItem<kPerAgent>(A, s);
+    gridBarrier(A, gridDim.x);
+    for (int s = tid; s < n; s += stride) predictItem<Venue>(A, s);
+    gridBarrier(A, gridDim.x);
+    const int K = A.P.proj_iterations;
+    int in = 0;
+    for (int it = 1; it < K; ++it) {
+        for (int s = tid; s < n; s += stride) projectItem<Venue>(A, s, in);
+        in ^= 1;
+        gridBarrier(A, gridDim.x);
+    }
+    for (int s = tid; s < n; s += stride) finalItem<Venue>(A, s, in);
+}
+
 // ---- host launchers ----
 namespace {
 inline int blocks(int n, int t) { return (n + t - 1) / t; }
@@ -387,8 +492,8 @@ void launch_sort(const StepArgs& A, cudaStream_t st, int64_t* launches) {
     const int n = A.n;
     k_hash<<<blocks(n, 256), 256, 0, st>>>(A);
     const int tiles = (A.V.ncells + 1 + SCAN_TILE - 1) / SCAN_TILE;
-    k_scan_reduce<<<tiles, SCAN_THREADS, 0, st>>>(A, A.tileSums);
-    k_scan_apply<<<tiles, SCAN_THREADS, 0, st>>>(A, A.tileSums);
+    k_scan_reduce<<<tiles, SCAN_THREADS, 0, st>>>(A);
+    k_scan_apply<<<tiles, SCAN_THREADS, 0, st>>>(A);
     k_scatter<<<blocks(n, 256), 256, 0, st>>>(A);
     if (A.P.uniform_body) k_rank_gather<false><<<blocks(n, 256), 256, 0, st>>>(A);
     else k_rank_gather<true><<<blocks(n, 256), 256, 0, st>>>(A);
@@ -412,6 +517,41 @@ static void stageImpl(const StepArgs& A, int stage, cudaStream_t st, int64_t* la
         k_final<Venue><<<blocks(n, 128), 128, 0, st>>>(A, K > 1 ? (K - 1) & 1 : 0);
         *launches += 1;
     }
+}
+
+template <class Venue, bool kPerAgent>
+static int fusedBlocks() {
+    static int cached = -1;
+    if (cached < 0) {
+        int dev = 0, sms = 0, perSm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_step_fused<Venue, kPerAgent>, FUSED_THREADS, 0);
+        cached = sms * perSm;
+    }
+    return cached;
+}
+
+template <class Venue, bool kPerAgent>
+static cudaError_t fusedImpl(const StepArgs& A, cudaStream_t st) {
+    const int resident = fusedBlocks<Venue, kPerAgent>();
+    if (resident <= 0) return cudaErrorCooperativeLaunchTooLarge;
+    const int want = blocks(A.n, FUSED_THREADS);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(unsigned(want < resident ? want : resident));
+    cfg.blockDim = dim3(FUSED_THREADS);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_step_fused<Venue, kPerAgent>, A);
+}
+
+cudaError_t launch_step_fused(const StepArgs& A, cudaStream_t st) {
+    if (A.V.kind == SWARM_VENUE_STADIUM) return fusedImpl<Stadium, false>(A, st);
+    return fusedImpl<GridVenue, true>(A, st);
 }
 
 void launch_stage(const StepArgs& A, int stage, cudaStream_t st, int64_t* launches) {

@@ -11,5 +11,7 @@ namespace swarm_gpu {
 void launch_sort(const StepArgs& A, cudaStream_t st, int64_t* launches);
 // stage 0: the sort (hash, scan, scatter, rank + gather); 1: predict; 2: the K - 1 sweeps; 3: the final pass
 void launch_stage(const StepArgs& A, int stage, cudaStream_t st, int64_t* launches);
+// the whole step as one cooperative persistent kernel (grid barriers between the phases)
+cudaError_t launch_step_fused(const StepArgs& A, cudaStream_t st);
 
 }  // namespace swarm_gpu

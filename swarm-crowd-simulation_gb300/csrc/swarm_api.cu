@@ -44,6 +44,9 @@ struct SwarmSim {
     float2* prm = nullptr;
     uint8_t* ctc = nullptr;
     int* errFlag = nullptr;
+    unsigned* barrier = nullptr;
+    bool fused = true;          // the whole step as one persistent kernel when the grid fits on the GPU
+    int barrierExtra = 0;       // the timeout test's missing block (swarm_test_barrier_timeout)
     float *dSdf = nullptr, *dWall = nullptr, *dNav = nullptr, *dFloor = nullptr, *dSpeed = nullptr;
     int ncells = 0;
     // execution
@@ -121,7 +124,7 @@ StepArgs SwarmSim::args(int in) const {
     A.key = key; A.rank = rank; A.count = count; A.start = start; A.cells = cells; A.tileSums = tileSums;
     A.sidTmp = sidTmp; A.sid = sid; A.skey = skey;
     A.pos0 = pos0; A.vel0 = vel0; A.prm = prm; A.proj[0] = proj0; A.proj[1] = proj1;
-    A.vel1 = vel1; A.plane = plane; A.ctc = ctc; A.err = errFlag;
+    A.vel1 = vel1; A.plane = plane; A.ctc = ctc; A.err = errFlag; A.barrier = barrier; A.barrierExtra = barrierExtra;
     return A;
 }
 
@@ -176,7 +179,7 @@ int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capac
               devAlloc(h, &h->cells, size_t(h->ncells)) && devAlloc(h, &h->tileSums, size_t(h->ncells) / 1024 + 2) && devAlloc(h, &h->sidTmp, N) && devAlloc(h, &h->sid, N) &&
               devAlloc(h, &h->skey, N) && devAlloc(h, &h->pos0, N) && devAlloc(h, &h->vel0, N) && devAlloc(h, &h->proj0, N) &&
               devAlloc(h, &h->proj1, N) && devAlloc(h, &h->vel1, N) && devAlloc(h, &h->plane, N) && devAlloc(h, &h->prm, N) &&
-              devAlloc(h, &h->ctc, N) && devAlloc(h, &h->errFlag, 1);
+              devAlloc(h, &h->ctc, N) && devAlloc(h, &h->errFlag, 1) && devAlloc(h, &h->barrier, 2);
     if (ok && V.kind == SWARM_VENUE_STADIUM) {
         const size_t nv = size_t(V.sdf_res) * size_t(V.sdf_res) * size_t(V.sdf_res);
         ok = devAlloc(h, &h->dSdf, nv) && cudaMemcpy(h->dSdf, V.sdf, nv * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
@@ -195,6 +198,7 @@ int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capac
     h->V.speed_factor = nullptr; h->V.exit_boxes = nullptr;
     if (!ok) { delete h; return SWARM_E_OOM; }
     if (cudaMemset(h->count, 0, (size_t(h->ncells) + 1) * 4) != cudaSuccess || cudaMemset(h->errFlag, 0, 4) != cudaSuccess ||
+        cudaMemset(h->barrier, 0, 8) != cudaSuccess ||
         cudaMemset(h->contacts, 0, N) != cudaSuccess) {
         delete h;
         return SWARM_E_CUDA;
@@ -250,7 +254,7 @@ static int downloadImpl(SwarmHandle h, float* boids, int n, cudaMemcpyKind kind)
     if (!h->hasState) return h->fail(SWARM_E_STATE, "no state uploaded");
     if (n != h->n) return h->fail(SWARM_E_INVALID, "download size " + std::to_string(n) + " != state size " + std::to_string(h->n));
     if (!cudaOk(h, cudaMemcpyAsync(boids, h->state[h->readIdx], size_t(n) * 32, kind, h->stream), "download")) return SWARM_E_CUDA;
-    if (kind == cudaMemcpyDeviceToHost && !cudaOk(h, cudaStreamSynchronize(h->stream), "download sync")) return SWARM_E_CUDA;
+    if (kind == cudaMemcpyDeviceToHost) return swarm_synchronize(h);
     return SWARM_OK;
 }
 
@@ -292,6 +296,18 @@ int swarm_set_graph(SwarmHandle h, int enabled) {
     return SWARM_OK;
 }
 
+int swarm_test_barrier_timeout(SwarmHandle h) {
+    if (!h) return SWARM_E_INVALID;
+    h->barrierExtra = 1;
+    return SWARM_OK;
+}
+
+int swarm_set_fused(SwarmHandle h, int enabled) {
+    if (!h) return SWARM_E_INVALID;
+    h->fused = enabled != 0;
+    return SWARM_OK;
+}
+
 int swarm_set_timing(SwarmHandle h, int enabled) {
     if (!h) return SWARM_E_INVALID;
     if (h->timing != (enabled != 0)) h->dropGraphs();   // the graphs hold the event records or not
@@ -306,7 +322,13 @@ static int stepImpl(SwarmHandle h, int steps) {
     const int perStep = 7 + std::max(h->P.proj_iterations - 1, 0);
     for (int s = 0; s < steps; ++s) {
         const int in = h->readIdx;
-        if (h->useGraph && !h->timing) {
+        if (h->fused) {
+            if (h->timing && !cudaOk(h, cudaEventRecord(h->ev[0], h->stream), "event")) return SWARM_E_CUDA;
+            if (!cudaOk(h, swarm_gpu::launch_step_fused(h->args(in), h->stream), "fused step launch")) return SWARM_E_CUDA;
+            h->barrierExtra = 0;
+            if (h->timing && !cudaOk(h, cudaEventRecord(h->ev[4], h->stream), "event")) return SWARM_E_CUDA;
+            h->launches += 1;
+        } else if (h->useGraph && !h->timing) {
             if (!h->graph[in] && h->captureStages(in, 0, 4, &h->graph[in]) != SWARM_OK) return SWARM_E_CUDA;
             if (!cudaOk(h, cudaGraphLaunch(h->graph[in], h->stream), "graph launch")) return SWARM_E_CUDA;
             h->launches += perStep;
@@ -359,7 +381,12 @@ int swarm_synchronize(SwarmHandle h) {
     if (!cudaOk(h, cudaStreamSynchronize(h->stream), "synchronize")) return SWARM_E_CUDA;
     int flag = 0;
     cudaMemcpy(&flag, h->errFlag, 4, cudaMemcpyDeviceToHost);
-    if (flag) return h->fail(SWARM_E_TIMEOUT, "a device-side wait gave up (flag " + std::to_string(flag) + ")");
+    if (flag) {
+        cudaMemset(h->errFlag, 0, 4);
+        cudaMemset(h->barrier, 0, 8);   // a barrier that gave up leaves its counter behind
+        if (flag & 1) return h->fail(SWARM_E_TIMEOUT, "a device-side wait gave up (flag " + std::to_string(flag) + ")");
+        return h->fail(SWARM_E_CUDA, "a device-side bounds check failed (flag " + std::to_string(flag) + ")");
+    }
     return SWARM_OK;
 }
 
@@ -394,6 +421,13 @@ int swarm_get_contacts(SwarmHandle h, uint8_t* bits, int n) {
 int swarm_stage_times(SwarmHandle h, SwarmStageTimes* out) {
     if (!h || !out) return SWARM_E_INVALID;
     if (!h->timing) return h->fail(SWARM_E_STATE, "timing is off (swarm_set_timing)");
+    if (!h->timesValid && h->fused) {
+        if (!cudaOk(h, cudaEventSynchronize(h->ev[4]), "timing")) return SWARM_E_CUDA;
+        float total = 0;
+        cudaEventElapsedTime(&total, h->ev[0], h->ev[4]);
+        h->times = SwarmStageTimes{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, total};
+        h->timesValid = true;
+    }
     if (!h->timesValid) {
         if (!cudaOk(h, cudaEventSynchronize(h->ev[4]), "timing")) return SWARM_E_CUDA;
         float sort = 0, pred = 0, proj = 0, fin = 0;

@@ -50,6 +50,8 @@ def lib():
             "swarm_step_host": [H, C.c_void_p, C.c_void_p, C.c_int, C.c_int],
             "swarm_set_drive_table": [H, C.POINTER(C.c_float), C.c_int],
             "swarm_set_graph": [H, C.c_int],
+            "swarm_set_fused": [H, C.c_int],
+            "swarm_test_barrier_timeout": [H],
             "swarm_synchronize": [H],
             "swarm_get_grid": [H, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_int],
             "swarm_get_cells": [H, C.POINTER(C.c_uint32), C.c_int],
@@ -170,6 +172,10 @@ class CrowdSim:
 
     def set_graph(self, enabled=True):
         self._ck(lib().swarm_set_graph(self._h, int(bool(enabled))), "set_graph")
+
+    def set_fused(self, enabled=True):
+        """One persistent kernel per step (True, the default) or one kernel per phase (False)."""
+        self._ck(lib().swarm_set_fused(self._h, int(bool(enabled))), "set_fused")
 
     def set_timing(self, enabled=True):
         self._ck(lib().swarm_set_timing(self._h, int(bool(enabled))), "set_timing")

@@ -225,12 +225,15 @@ def test_grid_hall_65536_one_step_vs_oracle_and_invariants(built):
     assert np.array_equal(_bits(sim.state()), _bits(sim2.state()))
 
 
-@pytest.mark.parametrize("graph,timing", [(False, True), (True, True), (True, False)])
-def test_execution_modes_are_bit_identical(terrace, terrace_golden, graph, timing):
-    """Kernel-by-kernel launches, whole-step graphs and per-stage graphs with stage events give the same bits."""
+@pytest.mark.parametrize("fused,graph,timing", [(False, False, False), (False, False, True), (False, True, True),
+                                               (False, True, False), (True, False, True)])
+def test_execution_modes_are_bit_identical(terrace, terrace_golden, fused, graph, timing):
+    """The persistent one-kernel step, kernel-by-kernel launches, whole-step graphs and per-stage graphs with stage
+    events give the same bits."""
     P, venue = terrace
     a = _sim(P, venue, terrace_golden["spawn"])
     b = _sim(P, venue, terrace_golden["spawn"])
+    b.set_fused(fused)
     b.set_graph(graph)
     b.set_timing(timing)
     for _ in range(4):
@@ -240,3 +243,37 @@ def test_execution_modes_are_bit_identical(terrace, terrace_golden, graph, timin
             t = b.stage_times()
             assert t["total"] > 0 and t["predict"] > 0
     assert np.array_equal(_bits(a.state()), _bits(b.state()))
+
+
+def test_fused_and_phase_kernels_agree_on_the_grid_hall(built):
+    import swarm_gb300
+    from swarm_gb300 import venues
+    venue, (boids, r, v0) = venues.hall_c1()
+    P = swarm_gb300.params_si()
+    a = _sim(P, venue, boids, r, v0)
+    b = _sim(P, venue, boids, r, v0)
+    b.set_fused(False)
+    b.set_graph(True)
+    for _ in range(3):
+        a.step(4)
+        b.step(4)
+        assert np.array_equal(_bits(a.state()), _bits(b.state()))
+    assert np.array_equal(a.cells(), b.cells())
+    assert np.array_equal(a.contacts(), b.contacts())
+
+
+def test_barrier_timeout_is_reported_and_the_handle_recovers(terrace, terrace_golden):
+    """A grid barrier that waits for a block that never arrives gives up after its 1 s limit: the step ends, the host
+    reads SWARM_E_TIMEOUT, and the next steps run normally (no fault, no hang)."""
+    import swarm_gb300
+    P, venue = terrace
+    st = terrace_golden["spawn"]
+    sim = _sim(P, venue, st)
+    assert swarm_gb300.lib().swarm_test_barrier_timeout(sim._h) == 0
+    sim.step(1)
+    with pytest.raises(swarm_gb300.SwarmError, match="gave up"):
+        sim.synchronize()
+    sim.set_state(st)
+    sim.step(1)
+    sim.synchronize()
+    assert np.array_equal(_bits(sim.state()), _bits(terrace_golden["state1"]))
