@@ -151,6 +151,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--phase-kernels", action="store_true", help="one kernel per phase instead of the fused step")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -181,6 +182,7 @@ def main():
     sim.set_state(boids)
     sim.set_agent_params(r, v0)
     sim.set_graph(True)
+    sim.set_fused(not args.phase_kernels)
     sim.set_timing(True)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
@@ -213,6 +215,7 @@ def main():
     launches = sim.launch_count() * args.steps   # per-step launches of the last call x timed steps
 
     # exact agent-steps: replay the timed steps (bit-identical) and count the agents active at each step's start
+    sim.synchronize()   # raises if a device-side check or wait failed during the timed steps
     rep = swarm_gb300.CrowdSim(P, venue, n)
     rep.set_state(start_state)
     rep.set_agent_params(r, v0)
@@ -234,15 +237,19 @@ def main():
         agent_steps_all = float(agent_steps)
     value = agent_steps_all / (t_max * 1e-3)
 
-    # roofline of the dominant kernel, from the library's stage events over the timed steps
+    # roofline of the dominant kernel, from the library's events over the timed steps. The default path runs each
+    # step as one persistent kernel (k_step_fused): its algorithmic bytes are the whole step's, B_step per agent.
     K = P.proj_iterations
     active_mean = agent_steps / args.steps
-    per = {
-        "k_predict": (statistics.mean(s["predict"] for s in stages), 1, BYTES["predict"]),
-        "k_project": (statistics.mean(s["project"] for s in stages) / max(K - 1, 1), max(K - 1, 0), BYTES["sweep"]),
-        "k_final": (statistics.mean(s["final_pass"] for s in stages), 1, BYTES["final"]),
-        "sort (4 kernels)": (statistics.mean(s["sort"] for s in stages) / 4.0, 4, BYTES["sort"] / 4.0),
-    }
+    if args.phase_kernels:
+        per = {
+            "k_predict": (statistics.mean(s["predict"] for s in stages), 1, BYTES["predict"]),
+            "k_project": (statistics.mean(s["project"] for s in stages) / max(K - 1, 1), max(K - 1, 0), BYTES["sweep"]),
+            "k_final": (statistics.mean(s["final_pass"] for s in stages), 1, BYTES["final"]),
+            "sort (5 kernels)": (statistics.mean(s["sort"] for s in stages) / 5.0, 5, BYTES["sort"] / 5.0),
+        }
+    else:
+        per = {"k_step_fused": (statistics.mean(s["total"] for s in stages), 1, B_STEP)}
     dom = max(per, key=lambda k: per[k][0] * per[k][1])
     dom_ms, _, dom_bytes = per[dom]
     hbm, peak_kind = peaks()
@@ -256,6 +263,7 @@ def main():
     e2e_sim = swarm_gb300.CrowdSim(P, venue, n)
     e2e_sim.set_agent_params(r, v0)
     e2e_sim.set_graph(True)
+    e2e_sim.set_fused(not args.phase_kernels)
     h_in = torch.from_numpy(start_state.copy()).pin_memory()
     h_out = torch.empty_like(h_in).pin_memory()
     for _ in range(2):
@@ -278,8 +286,10 @@ def main():
                        "l2": "flushed before every timed step (256 MiB write, outside the timed events)",
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
                        "step_fraction_of_hbm_roofline": value * B_STEP / (hbm * 1e9),
+                       "path": "one kernel per phase (CUDA graphs)" if args.phase_kernels else
+                               "one persistent cooperative kernel per step",
                        "stage_ms_mean": {k: statistics.mean(s[k] for s in stages)
-                                         for k in ("sort", "predict", "project", "final_pass")}},
+                                         for k in ("sort", "predict", "project", "final_pass", "total")}},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "peak_kind": peak_kind,
                          "bytes_per_agent": dom_bytes, "mean_launch_ms": dom_ms,
