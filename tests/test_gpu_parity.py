@@ -241,7 +241,7 @@ def test_execution_modes_are_bit_identical(terrace, terrace_golden, fused, graph
         b.step(3)
         if timing:
             t = b.stage_times()
-            assert t["total"] > 0 and t["predict"] > 0
+            assert t["total"] > 0 and (fused or t["predict"] > 0)
     assert np.array_equal(_bits(a.state()), _bits(b.state()))
 
 
