@@ -228,9 +228,15 @@ __device__ __forceinline__ void predictItem(const StepArgs& A, int s) {
     const float csx = A.V.dspanX / float(resX), csy = A.V.dspanY / float(resY);
     const float margin = 0.01f * smax(csx, csy);
     const float rPerc = sqrtf(P.r_perc2) + margin;
-    for (int y = -R; y <= R; y++) {
+    // every row's slot range first (independent loads, issued together), then the rows in order
+    constexpr int MAXR = 2 * 4 + 1;   // PERC_RING <= 4
+    uint32_t rk0[MAXR], rk1[MAXR];
+#pragma unroll
+    for (int j = 0; j < MAXR; ++j) {
+        rk0[j] = rk1[j] = 0;
+        const int y = j - R;
         const int ny = cy + y;
-        if (ny < 0 || ny >= resY) continue;
+        if (y > R || ny < 0 || ny >= resY) continue;
         const float ylo = A.V.dminY + float(ny) * csy - margin, yhi = A.V.dminY + float(ny + 1) * csy + margin;
         const float dy = fmaxf(0.0f, fmaxf(ylo - p.y, p.y - yhi));
         if (dy >= rPerc) continue;
@@ -238,17 +244,22 @@ __device__ __forceinline__ void predictItem(const StepArgs& A, int s) {
         const int xlo = max(max(cx - R, 0), int(floorf((p.x - w - A.V.dminX) / csx)));
         const int xhi = min(min(cx + R, resX - 1), int(floorf((p.x + w - A.V.dminX) / csx)));
         if (xlo > xhi) continue;
-        const uint32_t k0 = A.start[xlo + ny * resX], k1 = A.start[xhi + 1 + ny * resX];
-        for (uint32_t k = k0; k < k1; k++) {
+        rk0[j] = A.start[xlo + ny * resX];
+        rk1[j] = A.start[xhi + 1 + ny * resX];
+    }
+#pragma unroll
+    for (int j = 0; j < MAXR; ++j) {
+        for (uint32_t k = rk0[j]; k < rk1[j]; k++) {
             if (int(k) == s) continue;
             const float4 op = A.pos0[k];
+            const uint32_t other = A.sid[k];
+            const float rj = kUniform ? 0.0f : A.prm[k].x;
             const f3 offset = xyz(p) - xyz(op);
             const float dxy2 = dot(xy(offset), xy(offset));
             if (dxy2 < P.r_perc2) {
-                const uint32_t other = A.sid[k];
                 float dc, rs, rs2;
                 if (kUniform) { dc = P.body_diam; rs = P.r_sep; rs2 = P.r_sep2; }
-                else { dc = ri + A.prm[k].x; rs = dc + P.sep_margin; rs2 = rs * rs; }
+                else { dc = ri + rj; rs = dc + P.sep_margin; rs2 = rs * rs; }
                 sep = sep + separationForce(P, offset, self, other, rs, rs2);
                 const float ahead = -dot(xy(offset), eGoal);
                 const float lateral = fabsf(offset.x * eGoal.y - offset.y * eGoal.x);
@@ -325,17 +336,24 @@ __device__ __forceinline__ float4 projectSlot(const StepArgs& A, const Venue& ve
     f2 corr{0.0f, 0.0f};
     int nContacts = 0;
     const int xlo = max(cx - 1, 0), xhi = min(cx + 1, resX - 1);
-    for (int y = -1; y <= 1; y++) {
-        const int ny = cy + y;
-        if (ny < 0 || ny >= resY) continue;
-        const uint32_t k0 = A.start[xlo + ny * resX], k1 = A.start[xhi + 1 + ny * resX];
-        for (uint32_t k = k0; k < k1; k++) {
+    uint32_t rk0[3], rk1[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        const int ny = cy + j - 1;
+        const bool ok = ny >= 0 && ny < resY;
+        rk0[j] = ok ? A.start[xlo + ny * resX] : 0u;
+        rk1[j] = ok ? A.start[xhi + 1 + ny * resX] : 0u;
+    }
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        for (uint32_t k = rk0[j]; k < rk1[j]; k++) {
             if (int(k) == s) continue;
             const float4 op = in[k];
+            const float rj = kUniform ? 0.0f : A.prm[k].x;
             const f3 offset = xyz(b) - xyz(op);
             float dc, dc2;
             if (kUniform) { dc = P.body_diam; dc2 = P.body_diam2; }
-            else { dc = ri + A.prm[k].x; dc2 = dc * dc; }
+            else { dc = ri + rj; dc2 = dc * dc; }
             const float dxy2 = dot(xy(offset), xy(offset));
             if (op.w >= 0.0f && fabsf(offset.z) < dc && dxy2 < dc2) {
                 const float dxy = sqrtf(dxy2);
@@ -445,7 +463,6 @@ __device__ __forceinline__ void gridBarrier(const StepArgs& A, unsigned expected
                 const uint64_t t0 = globalNs();
                 while (gen.load(cuda::memory_order_acquire) == g0) {
                     if (globalNs() - t0 > BARRIER_WAIT_NS) { err.fetch_or(ERR_TIMEOUT, cuda::memory_order_relaxed); break; }
-                    __nanosleep(64);
                 }
             }
         }

@@ -161,7 +161,7 @@ int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capac
     auto bad = [&](const char* m) { delete h; (void)m; return SWARM_E_INVALID; };
     if (V.kind != SWARM_VENUE_STADIUM && V.kind != SWARM_VENUE_GRID) return bad("venue kind");
     if (V.grid_res_x <= 0 || V.grid_res_y <= 0 || !(V.domain_span_x > 0.0f) || !(V.domain_span_y > 0.0f)) return bad("grid");
-    if (params->proj_iterations < 0 || params->perc_ring < 1) return bad("params");
+    if (params->proj_iterations < 0 || params->perc_ring < 1 || params->perc_ring > 4) return bad("params");   // the predict pass holds <= 9 rows
     if (V.kind == SWARM_VENUE_STADIUM && (!V.sdf || V.sdf_res < 2 || !(V.sdf_spacing > 0.0f))) return bad("sdf");
     if (V.kind == SWARM_VENUE_GRID && (!V.wall_sdf || !V.nav_dist || V.wall_nx < 2 || V.wall_ny < 2 || V.nav_nx < 2 || V.nav_ny < 2 ||
                                        !(V.wall_h > 0.0f) || !(V.nav_h > 0.0f)))
