@@ -69,6 +69,7 @@ struct StepArgs {
     int* err;
     unsigned* barrier;      // the fused kernel's grid barrier: arrival counter, generation
     int32_t barrierExtra;   // 0; 1 only in the timeout test: the first barrier waits for a block that never arrives
+    unsigned long long* stamps;   // timing on: the fused kernel's stage boundaries (%globaltimer, ns), else null
 };
 
 }  // namespace swarm_gpu

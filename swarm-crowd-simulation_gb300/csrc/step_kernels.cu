@@ -247,31 +247,45 @@ __device__ __forceinline__ void predictItem(const StepArgs& A, int s) {
         rk0[j] = A.start[xlo + ny * resX];
         rk1[j] = A.start[xhi + 1 + ny * resX];
     }
+    // each row in groups of four neighbours: the group's loads are issued together, then its neighbours are taken
+    // in order (the accumulation order is unchanged)
+    auto visit = [&](uint32_t k, float4 op, uint32_t other, float rj) {
+        if (int(k) == s) return;
+        const f3 offset = xyz(p) - xyz(op);
+        const float dxy2 = dot(xy(offset), xy(offset));
+        if (dxy2 < P.r_perc2) {
+            float dc, rs, rs2;
+            if (kUniform) { dc = P.body_diam; rs = P.r_sep; rs2 = P.r_sep2; }
+            else { dc = ri + rj; rs = dc + P.sep_margin; rs2 = rs * rs; }
+            sep = sep + separationForce(P, offset, self, other, rs, rs2);
+            const float ahead = -dot(xy(offset), eGoal);
+            const float lateral = fabsf(offset.x * eGoal.y - offset.y * eGoal.x);
+            const float dxy = sqrtf(dxy2);
+            const float key = kUniform ? dxy : dxy - dc;
+            if (ahead > 0.0f && lateral < dc && key < sAhead) {
+                const f2 eOther = goalOf(A, ven, xyz(op), other);
+                const float aheadOther = dot(xy(offset), eOther);
+                const bool mutual = aheadOther > 0.0f && fabsf(offset.x * eOther.y - offset.y * eOther.x) < dc;
+                if (!mutual || ahead > aheadOther || (ahead == aheadOther && self > other)) sAhead = key;
+            }
+        }
+    };
 #pragma unroll
     for (int j = 0; j < MAXR; ++j) {
-        for (uint32_t k = rk0[j]; k < rk1[j]; k++) {
-            if (int(k) == s) continue;
-            const float4 op = A.pos0[k];
-            const uint32_t other = A.sid[k];
-            const float rj = kUniform ? 0.0f : A.prm[k].x;
-            const f3 offset = xyz(p) - xyz(op);
-            const float dxy2 = dot(xy(offset), xy(offset));
-            if (dxy2 < P.r_perc2) {
-                float dc, rs, rs2;
-                if (kUniform) { dc = P.body_diam; rs = P.r_sep; rs2 = P.r_sep2; }
-                else { dc = ri + rj; rs = dc + P.sep_margin; rs2 = rs * rs; }
-                sep = sep + separationForce(P, offset, self, other, rs, rs2);
-                const float ahead = -dot(xy(offset), eGoal);
-                const float lateral = fabsf(offset.x * eGoal.y - offset.y * eGoal.x);
-                const float dxy = sqrtf(dxy2);
-                const float key = kUniform ? dxy : dxy - dc;
-                if (ahead > 0.0f && lateral < dc && key < sAhead) {
-                    const f2 eOther = goalOf(A, ven, xyz(op), other);
-                    const float aheadOther = dot(xy(offset), eOther);
-                    const bool mutual = aheadOther > 0.0f && fabsf(offset.x * eOther.y - offset.y * eOther.x) < dc;
-                    if (!mutual || ahead > aheadOther || (ahead == aheadOther && self > other)) sAhead = key;
-                }
+        for (uint32_t k = rk0[j]; k < rk1[j]; k += 4) {
+            float4 op[4];
+            uint32_t oth[4];
+            float rj[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t kk = k + u < rk1[j] ? k + u : k;
+                op[u] = A.pos0[kk];
+                oth[u] = A.sid[kk];
+                rj[u] = kUniform ? 0.0f : A.prm[kk].x;
             }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (k + u < rk1[j]) visit(k + u, op[u], oth[u], rj[u]);
         }
     }
     float vDes;
@@ -344,26 +358,37 @@ __device__ __forceinline__ float4 projectSlot(const StepArgs& A, const Venue& ve
         rk0[j] = ok ? A.start[xlo + ny * resX] : 0u;
         rk1[j] = ok ? A.start[xhi + 1 + ny * resX] : 0u;
     }
+    auto visit = [&](uint32_t k, float4 op, float rj) {
+        if (int(k) == s) return;
+        const f3 offset = xyz(b) - xyz(op);
+        float dc, dc2;
+        if (kUniform) { dc = P.body_diam; dc2 = P.body_diam2; }
+        else { dc = ri + rj; dc2 = dc * dc; }
+        const float dxy2 = dot(xy(offset), xy(offset));
+        if (op.w >= 0.0f && fabsf(offset.z) < dc && dxy2 < dc2) {
+            const float dxy = sqrtf(dxy2);
+            const float shift = 0.5f * (dc - dxy);
+            f2 c;
+            if (dxy2 <= P.stacked_xy2) c = shift * pairDirection(A.sid[s], A.sid[k], P.hash_to_radians);
+            else c = shift * (xy(offset) / dxy);
+            corr = corr + c;
+            ++nContacts;
+        }
+    };
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-        for (uint32_t k = rk0[j]; k < rk1[j]; k++) {
-            if (int(k) == s) continue;
-            const float4 op = in[k];
-            const float rj = kUniform ? 0.0f : A.prm[k].x;
-            const f3 offset = xyz(b) - xyz(op);
-            float dc, dc2;
-            if (kUniform) { dc = P.body_diam; dc2 = P.body_diam2; }
-            else { dc = ri + rj; dc2 = dc * dc; }
-            const float dxy2 = dot(xy(offset), xy(offset));
-            if (op.w >= 0.0f && fabsf(offset.z) < dc && dxy2 < dc2) {
-                const float dxy = sqrtf(dxy2);
-                const float shift = 0.5f * (dc - dxy);
-                f2 c;
-                if (dxy2 <= P.stacked_xy2) c = shift * pairDirection(A.sid[s], A.sid[k], P.hash_to_radians);
-                else c = shift * (xy(offset) / dxy);
-                corr = corr + c;
-                ++nContacts;
+        for (uint32_t k = rk0[j]; k < rk1[j]; k += 4) {
+            float4 op[4];
+            float rj[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t kk = k + u < rk1[j] ? k + u : k;
+                op[u] = in[kk];
+                rj[u] = kUniform ? 0.0f : A.prm[kk].x;
             }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (k + u < rk1[j]) visit(k + u, op[u], rj[u]);
         }
     }
     corr = corr * (P.proj_relax / float(smax(nContacts, 1)));
@@ -449,6 +474,11 @@ __device__ __forceinline__ uint64_t globalNs() {
     return t;
 }
 
+// The fused kernel's stage boundaries (timing on): block 0 records %globaltimer after each barrier
+__device__ __forceinline__ void stamp(const StepArgs& A, int i) {
+    if (A.stamps && blockIdx.x == 0 && threadIdx.x == 0) A.stamps[i] = globalNs();
+}
+
 __device__ __forceinline__ void gridBarrier(const StepArgs& A, unsigned expected) {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -476,6 +506,7 @@ __global__ void __launch_bounds__(FUSED_THREADS) k_step_fused(StepArgs A) {
     __shared__ uint32_t prefix;
     const int n = A.n;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    stamp(A, 0);
     for (int base = tid - int(threadIdx.x & 31u); base < n; base += stride) hashItem(A, base + int(threadIdx.x & 31u));
     gridBarrier(A, gridDim.x + unsigned(A.barrierExtra));   // barrierExtra: the timeout test's block that never arrives
     constexpr int TILE = FUSED_THREADS * SCAN_ITEMS;
@@ -488,8 +519,10 @@ __global__ void __launch_bounds__(FUSED_THREADS) k_step_fused(StepArgs A) {
     gridBarrier(A, gridDim.x);
     for (int s = tid; s < n; s += stride) rankGatherItem<kPerAgent>(A, s);
     gridBarrier(A, gridDim.x);
+    stamp(A, 1);
     for (int s = tid; s < n; s += stride) predictItem<Venue>(A, s);
     gridBarrier(A, gridDim.x);
+    stamp(A, 2);
     const int K = A.P.proj_iterations;
     int in = 0;
     for (int it = 1; it < K; ++it) {
@@ -497,7 +530,19 @@ __global__ void __launch_bounds__(FUSED_THREADS) k_step_fused(StepArgs A) {
         in ^= 1;
         gridBarrier(A, gridDim.x);
     }
+    stamp(A, 3);
     for (int s = tid; s < n; s += stride) finalItem<Venue>(A, s, in);
+    if (A.stamps) {   // the end: the last block out records it
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            cuda::atomic_ref<unsigned, cuda::thread_scope_device> done(A.barrier[2]);
+            if (done.fetch_add(1u, cuda::memory_order_acq_rel) == gridDim.x - 1) {
+                A.stamps[4] = globalNs();
+                done.store(0u, cuda::memory_order_relaxed);
+            }
+        }
+    }
 }
 
 // ---- host launchers ----

@@ -45,6 +45,7 @@ struct SwarmSim {
     uint8_t* ctc = nullptr;
     int* errFlag = nullptr;
     unsigned* barrier = nullptr;
+    unsigned long long* stamps = nullptr;
     bool fused = true;          // the whole step as one persistent kernel when the grid fits on the GPU
     int barrierExtra = 0;       // the timeout test's missing block (swarm_test_barrier_timeout)
     float *dSdf = nullptr, *dWall = nullptr, *dNav = nullptr, *dFloor = nullptr, *dSpeed = nullptr;
@@ -125,6 +126,7 @@ StepArgs SwarmSim::args(int in) const {
     A.sidTmp = sidTmp; A.sid = sid; A.skey = skey;
     A.pos0 = pos0; A.vel0 = vel0; A.prm = prm; A.proj[0] = proj0; A.proj[1] = proj1;
     A.vel1 = vel1; A.plane = plane; A.ctc = ctc; A.err = errFlag; A.barrier = barrier; A.barrierExtra = barrierExtra;
+    A.stamps = timing ? stamps : nullptr;
     return A;
 }
 
@@ -179,7 +181,7 @@ int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capac
               devAlloc(h, &h->cells, size_t(h->ncells)) && devAlloc(h, &h->tileSums, size_t(h->ncells) / 1024 + 2) && devAlloc(h, &h->sidTmp, N) && devAlloc(h, &h->sid, N) &&
               devAlloc(h, &h->skey, N) && devAlloc(h, &h->pos0, N) && devAlloc(h, &h->vel0, N) && devAlloc(h, &h->proj0, N) &&
               devAlloc(h, &h->proj1, N) && devAlloc(h, &h->vel1, N) && devAlloc(h, &h->plane, N) && devAlloc(h, &h->prm, N) &&
-              devAlloc(h, &h->ctc, N) && devAlloc(h, &h->errFlag, 1) && devAlloc(h, &h->barrier, 2);
+              devAlloc(h, &h->ctc, N) && devAlloc(h, &h->errFlag, 1) && devAlloc(h, &h->barrier, 4) && devAlloc(h, &h->stamps, 8);
     if (ok && V.kind == SWARM_VENUE_STADIUM) {
         const size_t nv = size_t(V.sdf_res) * size_t(V.sdf_res) * size_t(V.sdf_res);
         ok = devAlloc(h, &h->dSdf, nv) && cudaMemcpy(h->dSdf, V.sdf, nv * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
@@ -198,7 +200,7 @@ int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capac
     h->V.speed_factor = nullptr; h->V.exit_boxes = nullptr;
     if (!ok) { delete h; return SWARM_E_OOM; }
     if (cudaMemset(h->count, 0, (size_t(h->ncells) + 1) * 4) != cudaSuccess || cudaMemset(h->errFlag, 0, 4) != cudaSuccess ||
-        cudaMemset(h->barrier, 0, 8) != cudaSuccess ||
+        cudaMemset(h->barrier, 0, 16) != cudaSuccess ||
         cudaMemset(h->contacts, 0, N) != cudaSuccess) {
         delete h;
         return SWARM_E_CUDA;
@@ -383,7 +385,7 @@ int swarm_synchronize(SwarmHandle h) {
     cudaMemcpy(&flag, h->errFlag, 4, cudaMemcpyDeviceToHost);
     if (flag) {
         cudaMemset(h->errFlag, 0, 4);
-        cudaMemset(h->barrier, 0, 8);   // a barrier that gave up leaves its counter behind
+        cudaMemset(h->barrier, 0, 16);   // a barrier that gave up leaves its counter behind
         if (flag & 1) return h->fail(SWARM_E_TIMEOUT, "a device-side wait gave up (flag " + std::to_string(flag) + ")");
         return h->fail(SWARM_E_CUDA, "a device-side bounds check failed (flag " + std::to_string(flag) + ")");
     }
@@ -425,7 +427,10 @@ int swarm_stage_times(SwarmHandle h, SwarmStageTimes* out) {
         if (!cudaOk(h, cudaEventSynchronize(h->ev[4]), "timing")) return SWARM_E_CUDA;
         float total = 0;
         cudaEventElapsedTime(&total, h->ev[0], h->ev[4]);
-        h->times = SwarmStageTimes{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, total};
+        unsigned long long st[5] = {};
+        cudaMemcpy(st, h->stamps, sizeof st, cudaMemcpyDeviceToHost);
+        auto ms = [&](int a, int b) { return st[b] > st[a] ? float(double(st[b] - st[a]) * 1e-6) : 0.0f; };
+        h->times = SwarmStageTimes{0.0f, ms(0, 1), 0.0f, ms(1, 2), ms(2, 3), ms(3, 4), total};
         h->timesValid = true;
     }
     if (!h->timesValid) {
