@@ -91,7 +91,8 @@ typedef struct SwarmParams {
     /* metrics (fixed-point cloud-in-cell density; include/swarm/metrics.hpp) */
     float metric_cells_per_unit;  /* metric cells per length unit */
     float metric_speed_scale;     /* m/s per speed unit */
-    float pad2[6];
+    float r_pair_max;             /* per-agent body: the largest radius any agent may have (bounds the search disk) */
+    float pad2[5];
 } SwarmParams;
 
 /* The venue: the neighbour grid, the exit test, and the static fields of its kind. Host pointers; swarm_create

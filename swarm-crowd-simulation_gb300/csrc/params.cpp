@@ -135,6 +135,7 @@ extern "C" int swarm_params_reference(SwarmParams* p) {
     p->park_coord = 1000.0f;
     p->metric_cells_per_unit = 31.25f;
     p->metric_speed_scale = float(double(kWorldScale) / double(kTimeScale));
+    p->r_pair_max = bodyRadius;
     return SWARM_OK;
 }
 
@@ -197,5 +198,6 @@ extern "C" int swarm_params_si(SwarmParams* p) {
     p->park_coord = 1000.0f;
     p->metric_cells_per_unit = 1.0f;
     p->metric_speed_scale = 1.0f;
+    p->r_pair_max = 0.25f;   // the spawn's largest radius; swarm_set_agent_params checks every radius against it
     return SWARM_OK;
 }

@@ -227,7 +227,13 @@ __device__ __forceinline__ void predictItem(const StepArgs& A, int s) {
     // nothing, and the nearest-agent-ahead minimum does not depend on the visiting order.
     const float csx = A.V.dspanX / float(resX), csy = A.V.dspanY / float(resY);
     const float margin = 0.01f * smax(csx, csy);
-    const float rPerc = sqrtf(P.r_perc2) + margin;
+    // The search disk: R_PERC, or less where that cannot change the result. A neighbour farther than
+    // (largest pair contact distance) + vFree * T_HEADWAY leaves a gap whose headway speed is above vFree, so it
+    // cannot lower v_des; the separation ends at R_SEP_ij, nearer still. 1 % slack covers the float rounding.
+    const float vFreeSelf = kUniform ? P.v_max : A.prm[s].y * ven.speedFactor(xyz(p));
+    const float dcMax = kUniform ? P.body_diam : ri + P.r_pair_max;
+    const float reach = smax(dcMax + vFreeSelf / P.headway_rate, kUniform ? P.r_sep : dcMax + P.sep_margin) * 1.01f + margin;
+    const float rPerc = smin(sqrtf(P.r_perc2) + margin, reach);
     // every row's slot range first (independent loads, issued together), then the rows in order
     constexpr int MAXR = 2 * 4 + 1;   // PERC_RING <= 4
     uint32_t rk0[MAXR], rk1[MAXR];
@@ -247,45 +253,47 @@ __device__ __forceinline__ void predictItem(const StepArgs& A, int s) {
         rk0[j] = A.start[xlo + ny * resX];
         rk1[j] = A.start[xhi + 1 + ny * resX];
     }
-    // each row in groups of four neighbours: the group's loads are issued together, then its neighbours are taken
-    // in order (the accumulation order is unchanged)
-    auto visit = [&](uint32_t k, float4 op, uint32_t other, float rj) {
-        if (int(k) == s) return;
-        const f3 offset = xyz(p) - xyz(op);
-        const float dxy2 = dot(xy(offset), xy(offset));
-        if (dxy2 < P.r_perc2) {
-            float dc, rs, rs2;
-            if (kUniform) { dc = P.body_diam; rs = P.r_sep; rs2 = P.r_sep2; }
-            else { dc = ri + rj; rs = dc + P.sep_margin; rs2 = rs * rs; }
-            sep = sep + separationForce(P, offset, self, other, rs, rs2);
-            const float ahead = -dot(xy(offset), eGoal);
-            const float lateral = fabsf(offset.x * eGoal.y - offset.y * eGoal.x);
-            const float dxy = sqrtf(dxy2);
-            const float key = kUniform ? dxy : dxy - dc;
-            if (ahead > 0.0f && lateral < dc && key < sAhead) {
-                const f2 eOther = goalOf(A, ven, xyz(op), other);
-                const float aheadOther = dot(xy(offset), eOther);
-                const bool mutual = aheadOther > 0.0f && fabsf(offset.x * eOther.y - offset.y * eOther.x) < dc;
-                if (!mutual || ahead > aheadOther || (ahead == aheadOther && self > other)) sAhead = key;
-            }
-        }
-    };
 #pragma unroll
     for (int j = 0; j < MAXR; ++j) {
-        for (uint32_t k = rk0[j]; k < rk1[j]; k += 4) {
-            float4 op[4];
-            uint32_t oth[4];
-            float rj[4];
+        rk0[j] = rk1[j] = 0;
+        const int y = j - R;
+        const int ny = cy + y;
+        if (y > R || ny < 0 || ny >= resY) continue;
+        const float ylo = A.V.dminY + float(ny) * csy - margin, yhi = A.V.dminY + float(ny + 1) * csy + margin;
+        const float dy = fmaxf(0.0f, fmaxf(ylo - p.y, p.y - yhi));
+        if (dy >= rPerc) continue;
+        const float w = sqrtf(rPerc * rPerc - dy * dy) + margin;
+        const int xlo = max(max(cx - R, 0), int(floorf((p.x - w - A.V.dminX) / csx)));
+        const int xhi = min(min(cx + R, resX - 1), int(floorf((p.x + w - A.V.dminX) / csx)));
+        if (xlo > xhi) continue;
+        rk0[j] = A.start[xlo + ny * resX];
+        rk1[j] = A.start[xhi + 1 + ny * resX];
+    }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const uint32_t kk = k + u < rk1[j] ? k + u : k;
-                op[u] = A.pos0[kk];
-                oth[u] = A.sid[kk];
-                rj[u] = kUniform ? 0.0f : A.prm[kk].x;
+    for (int j = 0; j < MAXR; ++j) {
+        for (uint32_t k = rk0[j]; k < rk1[j]; k++) {
+            if (int(k) == s) continue;
+            const float4 op = A.pos0[k];
+            const uint32_t other = A.sid[k];
+            const float rj = kUniform ? 0.0f : A.prm[k].x;
+            const f3 offset = xyz(p) - xyz(op);
+            const float dxy2 = dot(xy(offset), xy(offset));
+            if (dxy2 < P.r_perc2) {
+                float dc, rs, rs2;
+                if (kUniform) { dc = P.body_diam; rs = P.r_sep; rs2 = P.r_sep2; }
+                else { dc = ri + rj; rs = dc + P.sep_margin; rs2 = rs * rs; }
+                sep = sep + separationForce(P, offset, self, other, rs, rs2);
+                const float ahead = -dot(xy(offset), eGoal);
+                const float lateral = fabsf(offset.x * eGoal.y - offset.y * eGoal.x);
+                const float dxy = sqrtf(dxy2);
+                const float key = kUniform ? dxy : dxy - dc;
+                if (ahead > 0.0f && lateral < dc && key < sAhead) {
+                    const f2 eOther = goalOf(A, ven, xyz(op), other);
+                    const float aheadOther = dot(xy(offset), eOther);
+                    const bool mutual = aheadOther > 0.0f && fabsf(offset.x * eOther.y - offset.y * eOther.x) < dc;
+                    if (!mutual || ahead > aheadOther || (ahead == aheadOther && self > other)) sAhead = key;
+                }
             }
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-                if (k + u < rk1[j]) visit(k + u, op[u], oth[u], rj[u]);
         }
     }
     float vDes;
@@ -358,37 +366,26 @@ __device__ __forceinline__ float4 projectSlot(const StepArgs& A, const Venue& ve
         rk0[j] = ok ? A.start[xlo + ny * resX] : 0u;
         rk1[j] = ok ? A.start[xhi + 1 + ny * resX] : 0u;
     }
-    auto visit = [&](uint32_t k, float4 op, float rj) {
-        if (int(k) == s) return;
-        const f3 offset = xyz(b) - xyz(op);
-        float dc, dc2;
-        if (kUniform) { dc = P.body_diam; dc2 = P.body_diam2; }
-        else { dc = ri + rj; dc2 = dc * dc; }
-        const float dxy2 = dot(xy(offset), xy(offset));
-        if (op.w >= 0.0f && fabsf(offset.z) < dc && dxy2 < dc2) {
-            const float dxy = sqrtf(dxy2);
-            const float shift = 0.5f * (dc - dxy);
-            f2 c;
-            if (dxy2 <= P.stacked_xy2) c = shift * pairDirection(A.sid[s], A.sid[k], P.hash_to_radians);
-            else c = shift * (xy(offset) / dxy);
-            corr = corr + c;
-            ++nContacts;
-        }
-    };
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-        for (uint32_t k = rk0[j]; k < rk1[j]; k += 4) {
-            float4 op[4];
-            float rj[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const uint32_t kk = k + u < rk1[j] ? k + u : k;
-                op[u] = in[kk];
-                rj[u] = kUniform ? 0.0f : A.prm[kk].x;
+        for (uint32_t k = rk0[j]; k < rk1[j]; k++) {
+            if (int(k) == s) continue;
+            const float4 op = in[k];
+            const float rj = kUniform ? 0.0f : A.prm[k].x;
+            const f3 offset = xyz(b) - xyz(op);
+            float dc, dc2;
+            if (kUniform) { dc = P.body_diam; dc2 = P.body_diam2; }
+            else { dc = ri + rj; dc2 = dc * dc; }
+            const float dxy2 = dot(xy(offset), xy(offset));
+            if (op.w >= 0.0f && fabsf(offset.z) < dc && dxy2 < dc2) {
+                const float dxy = sqrtf(dxy2);
+                const float shift = 0.5f * (dc - dxy);
+                f2 c;
+                if (dxy2 <= P.stacked_xy2) c = shift * pairDirection(A.sid[s], A.sid[k], P.hash_to_radians);
+                else c = shift * (xy(offset) / dxy);
+                corr = corr + c;
+                ++nContacts;
             }
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-                if (k + u < rk1[j]) visit(k + u, op[u], rj[u]);
         }
     }
     corr = corr * (P.proj_relax / float(smax(nContacts, 1)));

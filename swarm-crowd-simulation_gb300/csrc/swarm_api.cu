@@ -266,7 +266,11 @@ int swarm_download_state_device(SwarmHandle h, float* d, int n) { return downloa
 int swarm_set_agent_params(SwarmHandle h, const float* radius, const float* v0, int n) {
     if (!h || !radius || !v0 || n <= 0 || n > h->capacity) return SWARM_E_INVALID;
     std::vector<float2> ap(static_cast<size_t>(n));
-    for (int i = 0; i < n; ++i) ap[size_t(i)] = make_float2(radius[i], v0[i]);
+    for (int i = 0; i < n; ++i) {
+        if (!(radius[i] > 0.0f) || radius[i] > h->P.r_pair_max || !(v0[i] >= 0.0f) || v0[i] > h->P.v_max)
+            return h->fail(SWARM_E_INVALID, "agent " + std::to_string(i) + ": radius must lie in (0, r_pair_max] and v0 in [0, v_max]");
+        ap[size_t(i)] = make_float2(radius[i], v0[i]);
+    }
     if (!cudaOk(h, cudaMemcpyAsync(h->aparam, ap.data(), size_t(n) * sizeof(float2), cudaMemcpyHostToDevice, h->stream), "params"))
         return SWARM_E_CUDA;
     return cudaOk(h, cudaStreamSynchronize(h->stream), "params") ? SWARM_OK : SWARM_E_CUDA;

@@ -46,7 +46,7 @@ class SwarmParams(C.Structure):
         ("avenue_half", _f), ("walkway_min", _f), ("walkway_max", _f), ("walkway_centre", _f),
         ("aisle_max", _f), ("aisle_centre", _f), ("avenue_target_depth", _f), ("pitch_recovery_depth", _f),
         ("park_coord", _f),
-        ("metric_cells_per_unit", _f), ("metric_speed_scale", _f), ("pad2", _f * 6),
+        ("metric_cells_per_unit", _f), ("metric_speed_scale", _f), ("r_pair_max", _f), ("pad2", _f * 5),
     ]
 
 
