@@ -66,6 +66,9 @@ struct StepArgs {
     float4* vel1;           // predicted velocity
     float4* plane;          // wall plane (n.xy, offset) and flags
     uint8_t* ctc;           // the predict pass's contact bits
+    uint4* rowsA;           // fused step: each slot's 3 x 3 neighbour rows (row 0 and row 1 ranges)
+    uint2* rowsB;           //   (row 2 range)
+    uint2* tileWin;         //   each tile's neighbour window [lo, hi) in slots
     int* err;
     unsigned* barrier;      // the fused kernel's grid barrier: arrival counter, generation
     int32_t barrierExtra;   // 0; 1 only in the timeout test: the first barrier waits for a block that never arrives

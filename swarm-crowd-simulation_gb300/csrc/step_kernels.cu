@@ -344,21 +344,26 @@ __global__ void __launch_bounds__(128) k_predict(StepArgs A) {
     if (s < A.n) predictItem<Venue>(A, s);
 }
 
-// One Jacobi sweep for slot s reading `in` (cpu_crowd_sim.cpp:781-822 projectSlot); w of the result: displacement
-template <class Venue>
-__device__ __forceinline__ float4 projectSlot(const StepArgs& A, const Venue& ven, const float4* __restrict__ in, int s) {
-    constexpr bool kUniform = Body<Venue>::kUniform;
-    const SwarmParams& P = A.P;
-    const float4 b = in[s];
-    if (b.w < 0.0f) return b;   // parked this step
-    const uint32_t cid = A.skey[s];
+// Where a sweep reads its neighbours: global memory, or a tile's window of slots staged in shared memory
+struct GlobalNbr {
+    const float4* in;
+    const float2* prm;
+    __device__ __forceinline__ float4 pos(uint32_t k) const { return in[k]; }
+    __device__ __forceinline__ float r(uint32_t k) const { return prm[k].x; }
+};
+struct WindowNbr {
+    const float4* pos_;
+    const float* r_;
+    uint32_t lo;
+    __device__ __forceinline__ float4 pos(uint32_t k) const { return pos_[k - lo]; }
+    __device__ __forceinline__ float r(uint32_t k) const { return r_[k - lo]; }
+};
+
+// The 3 x 3 neighbour rows of slot s: slot ranges [rk0[j], rk1[j]) for the rows cy - 1 .. cy + 1
+__device__ __forceinline__ void sweepRows(const StepArgs& A, uint32_t cid, uint32_t* rk0, uint32_t* rk1) {
     const int resX = A.V.resX, resY = A.V.resY;
     const int cx = int(cid % uint32_t(resX)), cy = int(cid / uint32_t(resX));
-    const float ri = kUniform ? P.body_radius : A.prm[s].x;
-    f2 corr{0.0f, 0.0f};
-    int nContacts = 0;
     const int xlo = max(cx - 1, 0), xhi = min(cx + 1, resX - 1);
-    uint32_t rk0[3], rk1[3];
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
         const int ny = cy + j - 1;
@@ -366,12 +371,22 @@ __device__ __forceinline__ float4 projectSlot(const StepArgs& A, const Venue& ve
         rk0[j] = ok ? A.start[xlo + ny * resX] : 0u;
         rk1[j] = ok ? A.start[xhi + 1 + ny * resX] : 0u;
     }
+}
+
+// One Jacobi sweep of an unparked slot s at b (cpu_crowd_sim.cpp:781-822 projectSlot); w of the result: displacement
+template <class Venue, class Nbr>
+__device__ __forceinline__ float4 projectCore(const StepArgs& A, const Venue& ven, float4 b, int s, float ri,
+                                             const uint32_t* rk0, const uint32_t* rk1, float4 plane, const Nbr& nb) {
+    constexpr bool kUniform = Body<Venue>::kUniform;
+    const SwarmParams& P = A.P;
+    f2 corr{0.0f, 0.0f};
+    int nContacts = 0;
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
         for (uint32_t k = rk0[j]; k < rk1[j]; k++) {
             if (int(k) == s) continue;
-            const float4 op = in[k];
-            const float rj = kUniform ? 0.0f : A.prm[k].x;
+            const float4 op = nb.pos(k);
+            const float rj = kUniform ? 0.0f : nb.r(k);
             const f3 offset = xyz(b) - xyz(op);
             float dc, dc2;
             if (kUniform) { dc = P.body_diam; dc2 = P.body_diam2; }
@@ -394,13 +409,24 @@ __device__ __forceinline__ float4 projectSlot(const StepArgs& A, const Venue& ve
     f3 q = xyz(b);
     setXY(q, xy(q) + corr);
     ven.fenceProject(q);
-    const float4 plane = A.plane[s];
     if (plane.w == PLANE_WALL || plane.w == PLANE_WALL + PLANE_GROUNDED) {   // fmod(w, 2) == PLANE_WALL, w in {0, 1, 2, 3}
         const float sd = plane.z - dot(xy(q), f2{plane.x, plane.y});
         if (sd > 0.0f) setXY(q, xy(q) + f2{plane.x, plane.y} * sd);
     }
     const f2 d = xy(q) - xy(b);
     return make_float4(q.x, q.y, b.z, b.w + length(d));
+}
+
+// One Jacobi sweep for slot s reading `in` from global memory
+template <class Venue>
+__device__ __forceinline__ float4 projectSlot(const StepArgs& A, const Venue& ven, const float4* __restrict__ in, int s) {
+    constexpr bool kUniform = Body<Venue>::kUniform;
+    const float4 b = in[s];
+    if (b.w < 0.0f) return b;   // parked this step
+    uint32_t rk0[3], rk1[3];
+    sweepRows(A, A.skey[s], rk0, rk1);
+    const float ri = kUniform ? A.P.body_radius : A.prm[s].x;
+    return projectCore(A, ven, b, s, ri, rk0, rk1, A.plane[s], GlobalNbr{in, A.prm});
 }
 
 template <class Venue>
@@ -416,18 +442,11 @@ __global__ void __launch_bounds__(128) k_project(StepArgs A, int inBuf) {
     if (s < A.n) projectItem<Venue>(A, s, inBuf);
 }
 
+// The final pass of an active slot whose last sweep gave b (cpu_crowd_sim.cpp:835-866)
 template <class Venue>
-__device__ __forceinline__ void finalItem(const StepArgs& A, int s, int inBuf) {
-    const uint32_t self = A.sid[s];
-    if (s >= int(A.start[A.V.ncells])) {   // evacuated before this step: carried over
-        A.stateOut[2 * size_t(self)] = A.stateIn[2 * size_t(self)];
-        A.stateOut[2 * size_t(self) + 1] = A.stateIn[2 * size_t(self) + 1];
-        A.contacts[self] = 0;
-        return;
-    }
+__device__ __forceinline__ void finalActive(const StepArgs& A, const Venue& ven, int s, float4 b) {
     const SwarmParams& P = A.P;
-    const Venue ven{A.P, A.V};
-    const float4 b = A.projectInFinal ? projectSlot(A, ven, A.proj[inBuf], s) : A.proj[inBuf][s];
+    const uint32_t self = A.sid[s];
     if (b.w < 0.0f) {   // parked this step
         A.stateOut[2 * size_t(self)] = make_float4(P.park_coord, P.park_coord, P.park_coord, 0.0f);
         A.stateOut[2 * size_t(self) + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -449,6 +468,22 @@ __device__ __forceinline__ void finalItem(const StepArgs& A, int s, int inBuf) {
     A.stateOut[2 * size_t(self)] = make_float4(np.x, np.y, np.z, 1.0f);
     A.stateOut[2 * size_t(self) + 1] = make_float4(nv.x, nv.y, nv.z, length(nv));
     A.contacts[self] = uint8_t(contact);
+}
+
+// An agent evacuated before this step: carried over
+__device__ __forceinline__ void finalInactive(const StepArgs& A, int s) {
+    const uint32_t self = A.sid[s];
+    A.stateOut[2 * size_t(self)] = A.stateIn[2 * size_t(self)];
+    A.stateOut[2 * size_t(self) + 1] = A.stateIn[2 * size_t(self) + 1];
+    A.contacts[self] = 0;
+}
+
+template <class Venue>
+__device__ __forceinline__ void finalItem(const StepArgs& A, int s, int inBuf) {
+    if (s >= int(A.start[A.V.ncells])) { finalInactive(A, s); return; }
+    const Venue ven{A.P, A.V};
+    const float4 b = A.projectInFinal ? projectSlot(A, ven, A.proj[inBuf], s) : A.proj[inBuf][s];
+    finalActive(A, ven, s, b);
 }
 
 template <class Venue>
@@ -497,10 +532,32 @@ __device__ __forceinline__ void gridBarrier(const StepArgs& A, unsigned expected
     __syncthreads();
 }
 
+// The sweeps' neighbour data for the fused kernel, once per step: each active slot's 3 x 3 rows, and each tile of
+// FUSED_THREADS slots' window [lo, hi) -- every slot any of its slots can read (cells c - resX - 1 .. c + resX + 1 of
+// its first and last cells), a contiguous range in key order.
+__device__ __forceinline__ void prepareSweepItem(const StepArgs& A, int s, int nActive) {
+    const uint32_t cid = A.skey[s];
+    uint32_t rk0[3], rk1[3];
+    sweepRows(A, cid, rk0, rk1);
+    A.rowsA[s] = make_uint4(rk0[0], rk1[0], rk0[1], rk1[1]);
+    A.rowsB[s] = make_uint2(rk0[2], rk1[2]);
+    if (s % FUSED_THREADS == 0) {
+        const int last = min(s + FUSED_THREADS, nActive) - 1;
+        const int resX = A.V.resX, ncells = A.V.ncells;
+        const int c0 = int(cid), c1 = int(A.skey[last]);
+        A.tileWin[s / FUSED_THREADS] = make_uint2(A.start[max(c0 - resX - 1, 0)], A.start[min(c1 + resX + 2, ncells)]);
+    }
+}
+
+constexpr int WIN_CAP = 2048;   // slots a tile window may hold in shared memory (40 KB); larger windows read global memory
+
 template <class Venue, bool kPerAgent>
 __global__ void __launch_bounds__(FUSED_THREADS) k_step_fused(StepArgs A) {
+    constexpr bool kUniform = Body<Venue>::kUniform;
     __shared__ uint32_t warpSums[32];
     __shared__ uint32_t prefix;
+    extern __shared__ float4 smPos[];                    // WIN_CAP positions, then WIN_CAP radii
+    float* smR = reinterpret_cast<float*>(smPos + WIN_CAP);
     const int n = A.n;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
     stamp(A, 0);
@@ -517,18 +574,70 @@ __global__ void __launch_bounds__(FUSED_THREADS) k_step_fused(StepArgs A) {
     for (int s = tid; s < n; s += stride) rankGatherItem<kPerAgent>(A, s);
     gridBarrier(A, gridDim.x);
     stamp(A, 1);
-    for (int s = tid; s < n; s += stride) predictItem<Venue>(A, s);
+    const int nActive = int(A.start[A.V.ncells]);
+    for (int s = tid; s < n; s += stride) {
+        predictItem<Venue>(A, s);
+        if (s < nActive) prepareSweepItem(A, s, nActive);
+    }
     gridBarrier(A, gridDim.x);
     stamp(A, 2);
+    const Venue ven{A.P, A.V};
     const int K = A.P.proj_iterations;
+    const int activeTiles = (nActive + FUSED_THREADS - 1) / FUSED_THREADS;
+    // one sweep (or the final pass) over tile t: stage its window, then each slot reads its neighbours from it
+    auto sweepTile = [&](int t, const float4* in, float4& result, bool& own) {
+        const int s = t * FUSED_THREADS + int(threadIdx.x);
+        own = s < nActive;
+        const uint2 win = t < activeTiles ? A.tileWin[t] : make_uint2(0u, 0u);
+        const bool useWin = win.y - win.x <= uint32_t(WIN_CAP);
+        float4 b = make_float4(0.0f, 0.0f, 0.0f, 0.0f), plane = b;
+        uint4 ra = make_uint4(0u, 0u, 0u, 0u);
+        uint2 rb = make_uint2(0u, 0u);
+        float ri = A.P.body_radius;
+        if (own) {
+            b = in[s];
+            ra = A.rowsA[s];
+            rb = A.rowsB[s];
+            plane = A.plane[s];
+            if (!kUniform) ri = A.prm[s].x;
+        }
+        if (useWin) {
+            for (uint32_t k = win.x + threadIdx.x; k < win.y; k += blockDim.x) {
+                smPos[k - win.x] = in[k];
+                if (!kUniform) smR[k - win.x] = A.prm[k].x;
+            }
+        }
+        __syncthreads();
+        if (own && b.w >= 0.0f) {
+            const uint32_t rk0[3] = {ra.x, ra.z, rb.x}, rk1[3] = {ra.y, ra.w, rb.y};
+            b = useWin ? projectCore(A, ven, b, s, ri, rk0, rk1, plane, WindowNbr{smPos, smR, win.x})
+                       : projectCore(A, ven, b, s, ri, rk0, rk1, plane, GlobalNbr{in, A.prm});
+        }
+        result = b;
+        __syncthreads();   // the window is reused by the next tile
+    };
     int in = 0;
     for (int it = 1; it < K; ++it) {
-        for (int s = tid; s < n; s += stride) projectItem<Venue>(A, s, in);
+        for (int t = blockIdx.x; t < activeTiles; t += gridDim.x) {
+            float4 r;
+            bool own;
+            sweepTile(t, A.proj[in], r, own);
+            if (own) A.proj[in ^ 1][t * FUSED_THREADS + int(threadIdx.x)] = r;
+        }
         in ^= 1;
         gridBarrier(A, gridDim.x);
     }
     stamp(A, 3);
-    for (int s = tid; s < n; s += stride) finalItem<Venue>(A, s, in);
+    const int allTiles = (n + FUSED_THREADS - 1) / FUSED_THREADS;
+    for (int t = blockIdx.x; t < allTiles; t += gridDim.x) {
+        const int s = t * FUSED_THREADS + int(threadIdx.x);
+        float4 b;
+        bool own;
+        if (A.projectInFinal) sweepTile(t, A.proj[in], b, own);
+        else { own = s < nActive; b = own ? A.proj[in][s] : make_float4(0.0f, 0.0f, 0.0f, 0.0f); }
+        if (own) finalActive(A, ven, s, b);
+        else if (s < n) finalInactive(A, s);
+    }
     if (A.stamps) {   // the end: the last block out records it
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -578,6 +687,8 @@ static void stageImpl(const StepArgs& A, int stage, cudaStream_t st, int64_t* la
     }
 }
 
+constexpr int FUSED_SMEM = WIN_CAP * (int(sizeof(float4)) + int(sizeof(float)));
+
 template <class Venue, bool kPerAgent>
 static int fusedBlocks() {
     static int cached = -1;
@@ -585,7 +696,8 @@ static int fusedBlocks() {
         int dev = 0, sms = 0, perSm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_step_fused<Venue, kPerAgent>, FUSED_THREADS, 0);
+        cudaFuncSetAttribute(k_step_fused<Venue, kPerAgent>, cudaFuncAttributeMaxDynamicSharedMemorySize, FUSED_SMEM);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_step_fused<Venue, kPerAgent>, FUSED_THREADS, FUSED_SMEM);
         cached = sms * perSm;
     }
     return cached;
@@ -599,6 +711,7 @@ static cudaError_t fusedImpl(const StepArgs& A, cudaStream_t st) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(unsigned(want < resident ? want : resident));
     cfg.blockDim = dim3(FUSED_THREADS);
+    cfg.dynamicSmemBytes = FUSED_SMEM;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
