@@ -73,6 +73,8 @@ struct StepArgs {
     unsigned* barrier;      // the fused kernel's grid barrier: arrival counter, generation
     int32_t barrierExtra;   // 0; 1 only in the timeout test: the first barrier waits for a block that never arrives
     unsigned long long* stamps;   // timing on: the fused kernel's stage boundaries (%globaltimer, ns), else null
+    int32_t hashed;         // fused step: the keys and counts of this step's input were counted by the last final pass
+    int32_t hashNext;       // fused step: count the next step's keys in the final pass
 };
 
 }  // namespace swarm_gpu

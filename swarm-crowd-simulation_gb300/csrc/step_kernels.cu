@@ -33,15 +33,12 @@ __device__ __forceinline__ uint32_t cellID(const VenueArgs& V, float4 p) {
     return uint32_t(x + y * V.resX);
 }
 
-// Called by all 32 lanes of a warp together (warp-aggregated atomics); lanes with i >= n take no part.
-__device__ __forceinline__ void hashItem(const StepArgs& A, int i) {
-    const bool valid = i < A.n;
+// Counts agent i's key in its cell's counter and records its arrival rank. Called by all 32 lanes of a warp together
+// (warp-aggregated atomics: one atomic per distinct cell per warp); lanes with valid == false take no part.
+__device__ __forceinline__ void countKey(const StepArgs& A, uint32_t i, uint32_t key, bool valid) {
     const unsigned lane = threadIdx.x & 31u;
     const unsigned mask = __ballot_sync(0xffffffffu, valid);
     if (!valid) return;
-    float4 p = A.stateIn[2 * size_t(i)];
-    if (isnan(p.x)) { p = make_float4(0.0f, 0.0f, 0.0f, 1.0f); A.stateIn[2 * size_t(i)] = p; }
-    const uint32_t key = p.w == 0.0f ? INACTIVE_CELL : cellID(A.V, p);
     const uint32_t bucket = key == INACTIVE_CELL ? uint32_t(A.V.ncells) : key;
     const unsigned peers = __match_any_sync(mask, bucket);
     const int leader = __ffs(peers) - 1;
@@ -52,17 +49,29 @@ __device__ __forceinline__ void hashItem(const StepArgs& A, int i) {
     A.rank[i] = base + uint32_t(__popc(peers & ((1u << lane) - 1u)));
 }
 
+// calc_grid.comp (CpuCrowdSim::hash, cpu_crowd_sim.cpp:983-993), with its NaN sanitiser. All lanes of a warp together.
+__device__ __forceinline__ void hashItem(const StepArgs& A, int i) {
+    const bool valid = i < A.n;
+    uint32_t key = 0;
+    if (valid) {
+        float4 p = A.stateIn[2 * size_t(i)];
+        if (isnan(p.x)) { p = make_float4(0.0f, 0.0f, 0.0f, 1.0f); A.stateIn[2 * size_t(i)] = p; }
+        key = p.w == 0.0f ? INACTIVE_CELL : cellID(A.V, p);
+    }
+    countKey(A, uint32_t(valid ? i : 0), key, valid);
+}
+
 __global__ void k_hash(StepArgs A) { hashItem(A, blockIdx.x * blockDim.x + threadIdx.x); }
 
 // The exclusive scan of the ncells + 1 counts, in tiles of SCAN_TILE: k_scan_reduce writes each tile's total,
 // k_scan_apply scans its tile on top of the totals of the tiles before it, writes the run starts and the cell table,
 // and clears the counts for the next step. No block waits on another.
 constexpr int SCAN_THREADS = 256, SCAN_ITEMS = 8, SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
-constexpr int FUSED_THREADS = 128;   // the fused kernel's blocks (they also run the scan, in tiles of 1 024 counts)
+constexpr int FUSED_MAX_THREADS = 512;   // the fused kernel's largest block (one block per SM, sized to the state)
 
-template <int T>
+// Block-wide exclusive scan of one value per thread (any block size that is a multiple of 32, up to 1024)
 __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* warpSums, uint32_t& total) {
-    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     uint32_t inc = v;
     for (int o = 1; o < 32; o <<= 1) {
         const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
@@ -71,50 +80,47 @@ __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* war
     if (lane == 31) warpSums[warp] = inc;
     __syncthreads();
     if (warp == 0) {
-        uint32_t w = lane < T / 32 ? warpSums[lane] : 0u;
+        uint32_t w = lane < nw ? warpSums[lane] : 0u;
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t u = __shfl_up_sync(0xffffffffu, w, o);
             if (int(lane) >= o) w += u;
         }
-        if (lane < T / 32) warpSums[lane] = w;
+        if (lane < nw) warpSums[lane] = w;
     }
     __syncthreads();
-    total = warpSums[T / 32 - 1];
+    total = warpSums[nw - 1];
     return inc - v + (warp > 0 ? warpSums[warp - 1] : 0u);
 }
 
-// Block-level (blockDim.x == T): the total of tile `tile` (T * SCAN_ITEMS counts) into A.tileSums
-template <int T>
+// Block-level: the total of tile `tile` (blockDim.x * SCAN_ITEMS counts) into A.tileSums
 __device__ __forceinline__ void scanReduceTile(const StepArgs& A, int tile, uint32_t* warpSums) {
     const int nb = A.V.ncells + 1;
-    const int base = tile * (T * SCAN_ITEMS) + threadIdx.x * SCAN_ITEMS;
+    const int base = tile * int(blockDim.x * SCAN_ITEMS) + int(threadIdx.x) * SCAN_ITEMS;
     uint32_t sum = 0;
 #pragma unroll
     for (int j = 0; j < SCAN_ITEMS; ++j) sum += base + j < nb ? A.count[base + j] : 0u;
     uint32_t total;
-    blockExclusiveScan<T>(sum, warpSums, total);
+    blockExclusiveScan(sum, warpSums, total);
     if (threadIdx.x == 0) A.tileSums[tile] = total;
     __syncthreads();   // warpSums is reused by the next tile
 }
 
-// Block-level (blockDim.x == T): scan tile `tile` on top of the totals of the tiles before it; run starts, cell table,
-// counts cleared
-template <int T>
+// Block-level: scan tile `tile` on top of the totals of the tiles before it; run starts, cell table, counts cleared
 __device__ __forceinline__ void scanApplyTile(const StepArgs& A, int tile, uint32_t* warpSums, uint32_t* prefix) {
     const int nb = A.V.ncells + 1;
     uint32_t p = 0;
-    for (int t = threadIdx.x; t < tile; t += T) p += A.tileSums[t];
+    for (int t = threadIdx.x; t < tile; t += blockDim.x) p += A.tileSums[t];
     for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
     if (threadIdx.x == 0) *prefix = 0;
     __syncthreads();
     if ((threadIdx.x & 31u) == 0 && p) atomicAdd(prefix, p);
-    const int base = tile * (T * SCAN_ITEMS) + threadIdx.x * SCAN_ITEMS;
+    const int base = tile * int(blockDim.x * SCAN_ITEMS) + int(threadIdx.x) * SCAN_ITEMS;
     uint32_t c[SCAN_ITEMS];
     uint32_t sum = 0;
 #pragma unroll
     for (int j = 0; j < SCAN_ITEMS; ++j) { c[j] = base + j < nb ? A.count[base + j] : 0u; sum += c[j]; }
     uint32_t total;
-    uint32_t run = blockExclusiveScan<T>(sum, warpSums, total);   // its barriers also order the prefix atomics
+    uint32_t run = blockExclusiveScan(sum, warpSums, total);   // its barriers also order the prefix atomics
     run += *prefix;
 #pragma unroll
     for (int j = 0; j < SCAN_ITEMS; ++j) {
@@ -130,13 +136,13 @@ __device__ __forceinline__ void scanApplyTile(const StepArgs& A, int tile, uint3
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(StepArgs A) {
     __shared__ uint32_t warpSums[32];
-    scanReduceTile<SCAN_THREADS>(A, blockIdx.x, warpSums);
+    scanReduceTile(A, blockIdx.x, warpSums);
 }
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(StepArgs A) {
     __shared__ uint32_t warpSums[32];
     __shared__ uint32_t prefix;
-    scanApplyTile<SCAN_THREADS>(A, blockIdx.x, warpSums, &prefix);
+    scanApplyTile(A, blockIdx.x, warpSums, &prefix);
 }
 
 __device__ __forceinline__ void scatterItem(const StepArgs& A, int i) {
@@ -165,7 +171,9 @@ __device__ __forceinline__ void rankGatherItem(const StepArgs& A, int s) {
     const uint32_t t = cs.x + r;
     A.sid[t] = me;
     A.skey[t] = c;
-    A.pos0[t] = A.stateIn[2 * size_t(me)];
+    float4 p = A.stateIn[2 * size_t(me)];
+    if (isnan(p.x)) { p = make_float4(0.0f, 0.0f, 0.0f, 1.0f); A.stateIn[2 * size_t(me)] = p; }
+    A.pos0[t] = p;
     A.vel0[t] = A.stateIn[2 * size_t(me) + 1];
     if (kPerAgent) A.prm[t] = A.aparam[me];
 }
@@ -443,15 +451,16 @@ __global__ void __launch_bounds__(128) k_project(StepArgs A, int inBuf) {
 }
 
 // The final pass of an active slot whose last sweep gave b (cpu_crowd_sim.cpp:835-866)
+// Returns the agent's cell key for the next step (INACTIVE_CELL once parked; a NaN position hashes as (0, 0, 0, 1))
 template <class Venue>
-__device__ __forceinline__ void finalActive(const StepArgs& A, const Venue& ven, int s, float4 b) {
+__device__ __forceinline__ uint32_t finalActive(const StepArgs& A, const Venue& ven, int s, float4 b) {
     const SwarmParams& P = A.P;
     const uint32_t self = A.sid[s];
     if (b.w < 0.0f) {   // parked this step
         A.stateOut[2 * size_t(self)] = make_float4(P.park_coord, P.park_coord, P.park_coord, 0.0f);
         A.stateOut[2 * size_t(self) + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         A.contacts[self] = A.ctc[s];
-        return;
+        return INACTIVE_CELL;
     }
     constexpr bool kUniform = Body<Venue>::kUniform;
     const float ri = kUniform ? P.body_radius : A.prm[s].x;
@@ -465,12 +474,14 @@ __device__ __forceinline__ void finalActive(const StepArgs& A, const Venue& ven,
         ven.resolveStatic(pOld, np, nv, A.plane[s].w >= PLANE_GROUNDED, wall, contact, ri);
     }
     if (ven.limitStepUp(pOld, np, nv, ri)) contact |= C_STEP_UP;
-    A.stateOut[2 * size_t(self)] = make_float4(np.x, np.y, np.z, 1.0f);
+    const float4 out = make_float4(np.x, np.y, np.z, 1.0f);
+    A.stateOut[2 * size_t(self)] = out;
     A.stateOut[2 * size_t(self) + 1] = make_float4(nv.x, nv.y, nv.z, length(nv));
     A.contacts[self] = uint8_t(contact);
+    return cellID(A.V, isnan(out.x) ? make_float4(0.0f, 0.0f, 0.0f, 1.0f) : out);
 }
 
-// An agent evacuated before this step: carried over
+// An agent evacuated before this step: carried over (its next key: inactive)
 __device__ __forceinline__ void finalInactive(const StepArgs& A, int s) {
     const uint32_t self = A.sid[s];
     A.stateOut[2 * size_t(self)] = A.stateIn[2 * size_t(self)];
@@ -511,21 +522,20 @@ __device__ __forceinline__ void stamp(const StepArgs& A, int i) {
     if (A.stamps && blockIdx.x == 0 && threadIdx.x == 0) A.stamps[i] = globalNs();
 }
 
+// One word per barrier: block 0 adds 2^31 - (expected - 1), every other block adds 1, so the word's top bit flips
+// exactly when all `expected` blocks have arrived; each block waits for the flip of the value it saw (the scheme of
+// CUDA's cooperative groups grid sync). Release before the add, acquire on the poll.
 __device__ __forceinline__ void gridBarrier(const StepArgs& A, unsigned expected) {
     __syncthreads();
     if (threadIdx.x == 0) {
         cuda::atomic_ref<int, cuda::thread_scope_device> err(*A.err);
         if (!(err.load(cuda::memory_order_relaxed) & ERR_TIMEOUT)) {
-            cuda::atomic_ref<unsigned, cuda::thread_scope_device> count(A.barrier[0]), gen(A.barrier[1]);
-            const unsigned g0 = gen.load(cuda::memory_order_relaxed);
-            if (count.fetch_add(1u, cuda::memory_order_acq_rel) == expected - 1) {
-                count.store(0u, cuda::memory_order_relaxed);
-                gen.fetch_add(1u, cuda::memory_order_release);
-            } else {
-                const uint64_t t0 = globalNs();
-                while (gen.load(cuda::memory_order_acquire) == g0) {
-                    if (globalNs() - t0 > BARRIER_WAIT_NS) { err.fetch_or(ERR_TIMEOUT, cuda::memory_order_relaxed); break; }
-                }
+            cuda::atomic_ref<unsigned, cuda::thread_scope_device> word(A.barrier[0]);
+            const unsigned add = blockIdx.x == 0 ? 0x80000000u - (expected - 1u) : 1u;
+            const unsigned old = word.fetch_add(add, cuda::memory_order_release);
+            const uint64_t t0 = globalNs();
+            while (((word.load(cuda::memory_order_acquire) ^ old) & 0x80000000u) == 0u) {
+                if (globalNs() - t0 > BARRIER_WAIT_NS) { err.fetch_or(ERR_TIMEOUT, cuda::memory_order_relaxed); break; }
             }
         }
     }
@@ -535,39 +545,41 @@ __device__ __forceinline__ void gridBarrier(const StepArgs& A, unsigned expected
 // The sweeps' neighbour data for the fused kernel, once per step: each active slot's 3 x 3 rows, and each tile of
 // FUSED_THREADS slots' window [lo, hi) -- every slot any of its slots can read (cells c - resX - 1 .. c + resX + 1 of
 // its first and last cells), a contiguous range in key order.
-__device__ __forceinline__ void prepareSweepItem(const StepArgs& A, int s, int nActive) {
+__device__ __forceinline__ void prepareSweepItem(const StepArgs& A, int s, int nActive, int tile) {
     const uint32_t cid = A.skey[s];
     uint32_t rk0[3], rk1[3];
     sweepRows(A, cid, rk0, rk1);
     A.rowsA[s] = make_uint4(rk0[0], rk1[0], rk0[1], rk1[1]);
     A.rowsB[s] = make_uint2(rk0[2], rk1[2]);
-    if (s % FUSED_THREADS == 0) {
-        const int last = min(s + FUSED_THREADS, nActive) - 1;
+    if (s % tile == 0) {
+        const int last = min(s + tile, nActive) - 1;
         const int resX = A.V.resX, ncells = A.V.ncells;
         const int c0 = int(cid), c1 = int(A.skey[last]);
-        A.tileWin[s / FUSED_THREADS] = make_uint2(A.start[max(c0 - resX - 1, 0)], A.start[min(c1 + resX + 2, ncells)]);
+        A.tileWin[s / tile] = make_uint2(A.start[max(c0 - resX - 1, 0)], A.start[min(c1 + resX + 2, ncells)]);
     }
 }
 
 constexpr int WIN_CAP = 2048;   // slots a tile window may hold in shared memory (40 KB); larger windows read global memory
 
 template <class Venue, bool kPerAgent>
-__global__ void __launch_bounds__(FUSED_THREADS) k_step_fused(StepArgs A) {
+__global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A) {
     constexpr bool kUniform = Body<Venue>::kUniform;
     __shared__ uint32_t warpSums[32];
     __shared__ uint32_t prefix;
     extern __shared__ float4 smPos[];                    // WIN_CAP positions, then WIN_CAP radii
     float* smR = reinterpret_cast<float*>(smPos + WIN_CAP);
     const int n = A.n;
+    const int T = int(blockDim.x);   // the tile of slots a block handles at a time
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
     stamp(A, 0);
-    for (int base = tid - int(threadIdx.x & 31u); base < n; base += stride) hashItem(A, base + int(threadIdx.x & 31u));
+    if (!A.hashed) {   // (the previous fused step's final pass counted the keys already)
+        for (int base = tid - int(threadIdx.x & 31u); base < n; base += stride) hashItem(A, base + int(threadIdx.x & 31u));
+        gridBarrier(A, gridDim.x);
+    }
+    const int tiles = (A.V.ncells + 1 + T * SCAN_ITEMS - 1) / (T * SCAN_ITEMS);
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x) scanReduceTile(A, t, warpSums);
     gridBarrier(A, gridDim.x + unsigned(A.barrierExtra));   // barrierExtra: the timeout test's block that never arrives
-    constexpr int TILE = FUSED_THREADS * SCAN_ITEMS;
-    const int tiles = (A.V.ncells + 1 + TILE - 1) / TILE;
-    for (int t = blockIdx.x; t < tiles; t += gridDim.x) scanReduceTile<FUSED_THREADS>(A, t, warpSums);
-    gridBarrier(A, gridDim.x);
-    for (int t = blockIdx.x; t < tiles; t += gridDim.x) scanApplyTile<FUSED_THREADS>(A, t, warpSums, &prefix);
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x) scanApplyTile(A, t, warpSums, &prefix);
     gridBarrier(A, gridDim.x);
     for (int i = tid; i < n; i += stride) scatterItem(A, i);
     gridBarrier(A, gridDim.x);
@@ -577,16 +589,16 @@ __global__ void __launch_bounds__(FUSED_THREADS) k_step_fused(StepArgs A) {
     const int nActive = int(A.start[A.V.ncells]);
     for (int s = tid; s < n; s += stride) {
         predictItem<Venue>(A, s);
-        if (s < nActive) prepareSweepItem(A, s, nActive);
+        if (s < nActive) prepareSweepItem(A, s, nActive, T);
     }
     gridBarrier(A, gridDim.x);
     stamp(A, 2);
     const Venue ven{A.P, A.V};
     const int K = A.P.proj_iterations;
-    const int activeTiles = (nActive + FUSED_THREADS - 1) / FUSED_THREADS;
+    const int activeTiles = (nActive + T - 1) / T;
     // one sweep (or the final pass) over tile t: stage its window, then each slot reads its neighbours from it
     auto sweepTile = [&](int t, const float4* in, float4& result, bool& own) {
-        const int s = t * FUSED_THREADS + int(threadIdx.x);
+        const int s = t * T + int(threadIdx.x);
         own = s < nActive;
         const uint2 win = t < activeTiles ? A.tileWin[t] : make_uint2(0u, 0u);
         const bool useWin = win.y - win.x <= uint32_t(WIN_CAP);
@@ -622,21 +634,24 @@ __global__ void __launch_bounds__(FUSED_THREADS) k_step_fused(StepArgs A) {
             float4 r;
             bool own;
             sweepTile(t, A.proj[in], r, own);
-            if (own) A.proj[in ^ 1][t * FUSED_THREADS + int(threadIdx.x)] = r;
+            if (own) A.proj[in ^ 1][t * T + int(threadIdx.x)] = r;
         }
         in ^= 1;
         gridBarrier(A, gridDim.x);
     }
     stamp(A, 3);
-    const int allTiles = (n + FUSED_THREADS - 1) / FUSED_THREADS;
+    const int allTiles = (n + T - 1) / T;
     for (int t = blockIdx.x; t < allTiles; t += gridDim.x) {
-        const int s = t * FUSED_THREADS + int(threadIdx.x);
+        const int s = t * T + int(threadIdx.x);
         float4 b;
         bool own;
         if (A.projectInFinal) sweepTile(t, A.proj[in], b, own);
         else { own = s < nActive; b = own ? A.proj[in][s] : make_float4(0.0f, 0.0f, 0.0f, 0.0f); }
-        if (own) finalActive(A, ven, s, b);
+        uint32_t nextKey = INACTIVE_CELL;
+        if (own) nextKey = finalActive(A, ven, s, b);
         else if (s < n) finalInactive(A, s);
+        // the next step's hash, counted here (all lanes of the warp together)
+        if (A.hashNext) countKey(A, s < n ? A.sid[s] : 0u, nextKey, s < n);
     }
     if (A.stamps) {   // the end: the last block out records it
         __syncthreads();
@@ -689,28 +704,27 @@ static void stageImpl(const StepArgs& A, int stage, cudaStream_t st, int64_t* la
 
 constexpr int FUSED_SMEM = WIN_CAP * (int(sizeof(float4)) + int(sizeof(float)));
 
+// The fused grid: one block per SM when the state fits (threads = n / SMs rounded up to a warp, 128..512), else as
+// many blocks as stay resident, each taking several tiles per phase
 template <class Venue, bool kPerAgent>
-static int fusedBlocks() {
-    static int cached = -1;
-    if (cached < 0) {
-        int dev = 0, sms = 0, perSm = 0;
+static cudaError_t fusedImpl(const StepArgs& A, cudaStream_t st) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaFuncSetAttribute(k_step_fused<Venue, kPerAgent>, cudaFuncAttributeMaxDynamicSharedMemorySize, FUSED_SMEM);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_step_fused<Venue, kPerAgent>, FUSED_THREADS, FUSED_SMEM);
-        cached = sms * perSm;
     }
-    return cached;
-}
-
-template <class Venue, bool kPerAgent>
-static cudaError_t fusedImpl(const StepArgs& A, cudaStream_t st) {
-    const int resident = fusedBlocks<Venue, kPerAgent>();
+    int threads = ((A.n + sms - 1) / sms + 31) / 32 * 32;
+    threads = threads < 128 ? 128 : (threads > FUSED_MAX_THREADS ? FUSED_MAX_THREADS : threads);
+    int perSm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_step_fused<Venue, kPerAgent>, threads, FUSED_SMEM);
+    const int resident = perSm * sms;
     if (resident <= 0) return cudaErrorCooperativeLaunchTooLarge;
-    const int want = blocks(A.n, FUSED_THREADS);
+    const int want = blocks(A.n, threads);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(unsigned(want < resident ? want : resident));
-    cfg.blockDim = dim3(FUSED_THREADS);
+    cfg.blockDim = dim3(unsigned(threads));
     cfg.dynamicSmemBytes = FUSED_SMEM;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];

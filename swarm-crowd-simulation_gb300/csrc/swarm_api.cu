@@ -51,6 +51,7 @@ struct SwarmSim {
     unsigned long long* stamps = nullptr;
     bool fused = true;          // the whole step as one persistent kernel when the grid fits on the GPU
     int barrierExtra = 0;       // the timeout test's missing block (swarm_test_barrier_timeout)
+    bool counted = false;       // the counts hold the current state's keys (a fused step's final pass counted them)
     float *dSdf = nullptr, *dWall = nullptr, *dNav = nullptr, *dFloor = nullptr, *dSpeed = nullptr;
     int ncells = 0;
     // execution
@@ -66,6 +67,11 @@ struct SwarmSim {
 
     StepArgs args(int in) const;
     int fail(int code, const std::string& msg) { err = msg; return code; }
+    // The per-phase path hashes from zeroed counts: drop what a fused final pass counted ahead
+    bool clearCounts() {
+        counted = false;
+        return cudaMemsetAsync(count, 0, (size_t(ncells) + 1) * 4, stream) == cudaSuccess;
+    }
     void dropGraphs() {
         for (auto& g : graph) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
         for (auto& row : stageGraph) for (auto& g : row) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
@@ -241,6 +247,7 @@ static int uploadImpl(SwarmHandle h, const float* boids, int n, cudaMemcpyKind k
     if (!h || !boids) return SWARM_E_INVALID;
     if (n <= 0 || n > h->capacity) return h->fail(SWARM_E_INVALID, "agent count " + std::to_string(n) + " outside 1.." + std::to_string(h->capacity));
     if (n != h->n) h->dropGraphs();
+    if (h->counted && !h->clearCounts()) return h->fail(SWARM_E_CUDA, "clearing the counts");
     h->n = n;
     h->readIdx = 0;
     const size_t bytes = size_t(n) * 32;
@@ -334,10 +341,16 @@ static int stepImpl(SwarmHandle h, int steps) {
         const int in = h->readIdx;
         if (h->fused) {
             if (h->timing && !cudaOk(h, cudaEventRecord(h->ev[0], h->stream), "event")) return SWARM_E_CUDA;
-            if (!cudaOk(h, swarm_gpu::launch_step_fused(h->args(in), h->stream), "fused step launch")) return SWARM_E_CUDA;
+            StepArgs A = h->args(in);
+            A.hashed = h->counted ? 1 : 0;
+            A.hashNext = 1;
+            if (!cudaOk(h, swarm_gpu::launch_step_fused(A, h->stream), "fused step launch")) return SWARM_E_CUDA;
             h->barrierExtra = 0;
+            h->counted = true;
             if (h->timing && !cudaOk(h, cudaEventRecord(h->ev[4], h->stream), "event")) return SWARM_E_CUDA;
             h->launches += 1;
+        } else if (h->counted && !h->clearCounts()) {
+            return SWARM_E_CUDA;
         } else if (h->useGraph && !h->timing) {
             if (!h->graph[in] && h->captureStages(in, 0, 4, &h->graph[in]) != SWARM_OK) return SWARM_E_CUDA;
             if (!cudaOk(h, cudaGraphLaunch(h->graph[in], h->stream), "graph launch")) return SWARM_E_CUDA;
@@ -375,6 +388,7 @@ int swarm_step_host(SwarmHandle h, const float* in_boids, float* out_boids, int 
     if (n <= 0 || n > h->capacity) return h->fail(SWARM_E_INVALID, "agent count " + std::to_string(n) + " outside 1.." + std::to_string(h->capacity));
     if (steps < 0) return h->fail(SWARM_E_INVALID, "steps must be >= 0");
     if (n != h->n) h->dropGraphs();
+    if (h->counted && !h->clearCounts()) return h->fail(SWARM_E_CUDA, "clearing the counts");
     h->n = n;
     h->hasState = true;
     const size_t bytes = size_t(n) * 32;
@@ -394,6 +408,8 @@ int swarm_synchronize(SwarmHandle h) {
     if (flag) {
         cudaMemset(h->errFlag, 0, 4);
         cudaMemset(h->barrier, 0, 16);   // a barrier that gave up leaves its counter behind
+        cudaMemset(h->count, 0, (size_t(h->ncells) + 1) * 4);
+        h->counted = false;
         if (flag & 1) return h->fail(SWARM_E_TIMEOUT, "a device-side wait gave up (flag " + std::to_string(flag) + ")");
         return h->fail(SWARM_E_CUDA, "a device-side bounds check failed (flag " + std::to_string(flag) + ")");
     }
