@@ -255,9 +255,12 @@ def main():
     hbm, peak_kind = peaks()
     achieved = dom_bytes * active_mean / (dom_ms * 1e-3) / 1e9
     traffic = None
-    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    tfile = os.path.join(ROOT, "profiles", "traffic.txt")   # measured by ncu, one line per kernel: name bytes
     if os.path.exists(tfile):
-        traffic = json.load(open(tfile)).get(dom)
+        for line in open(tfile):
+            parts = line.split()
+            if len(parts) == 2 and not line.startswith("#") and parts[0] == dom:
+                traffic = int(parts[1])
 
     # e2e through swarm_step_host with pinned host buffers
     e2e_sim = swarm_gb300.CrowdSim(P, venue, n)
