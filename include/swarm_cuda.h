@@ -242,6 +242,36 @@ int swarm_sort_grid_noalloc(const float* d_boids, int n, int grid_res_x, int gri
                             float domain_min_y, float domain_span_x, float domain_span_y, uint32_t* d_grid_id,
                             uint32_t* d_boid_id, uint32_t* d_cells, void* stream);
 
+/* ---- safety metrics: write-only side outputs of each step (the reference's metrics_deposit.comp and
+ * metrics_finalize.comp; CPU mirror MetricsReference, src/metrics.cpp:429-476) ----
+ * Per step: every agent active in the step's input and evacuated in its output counts towards the exit at its last
+ * active position (stadium: the avenue gap it crossed; grid venues: the exit box holding it, slot 5 + box index, else
+ * slot 4) and records the step index; every active agent deposits one person onto the 4 floor cells around it
+ * (cloud-in-cell on a metric_res^2 grid of 1 m cells, position quantised to 1/256 cell, integer weights summing to
+ * 65536) with its horizontal speed; then each cell updates its peak, occupied steps, steps at or above the three
+ * density thresholds (as integer masses), and 64-bit sums. All integer: the result does not depend on order. */
+typedef struct SwarmMetricCounters {   /* GpuMetricCounters (include/swarm/gpu_types.hpp), 784 bytes */
+    uint32_t step, active, evacuated, active_accum;
+    uint32_t exits[61];
+    uint32_t pad[3];
+    uint32_t gangway_visits[64], gangway_last[64];
+} SwarmMetricCounters;
+typedef struct SwarmMetricCell {       /* GpuMetricCell, 64 bytes */
+    uint32_t last_mass, last_speed_mass, peak_mass, occupied_steps;
+    uint32_t steps_above[4];
+    uint32_t mass_steps[2], speed_mass_steps[2], exposure_mass_steps[2], pad[2];
+} SwarmMetricCell;
+/* Enables the metrics after every following step: the metric grid (res x res cells of 1 metre, res a multiple of 16,
+ * centred on the venue's metric_center) and each cell's threshold masses (4 per cell: LoS E, LoS F, crush, unused;
+ * 0xFFFFFFFF: never; the reference's GpuMetricCellInfo::thresholdMass). Resets the accumulators. */
+int swarm_metrics_enable(SwarmHandle h, int res, const uint32_t* threshold_mass);
+int swarm_metrics_reset(SwarmHandle h);
+/* Reads the counters, the res^2 cells and the per-agent evacuation step (0: not evacuated); any may be NULL. */
+int swarm_metrics_read(SwarmHandle h, SwarmMetricCounters* counters, SwarmMetricCell* cells, uint32_t* evac_step, int n);
+/* Threshold masses of a grid venue (host): each 1 m cell's walkable area is sampled on a 40 x 40 lattice (free where
+ * the wall SDF is positive, inside the exit line); cells under 0.1 m^2 never reach a threshold. */
+int swarm_metric_thresholds_grid(const SwarmVenue* venue, int res, uint32_t* threshold_mass);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif

@@ -121,6 +121,37 @@ class OracleSim:
         return out
 
 
+class OracleMetrics:
+    """The metrics restatement (MetricsReference::record): record(prev, cur) after each step."""
+
+    def __init__(self, params, venue_struct, res, threshold_mass, n):
+        L = lib()
+        L.oracle_metrics_create.restype = C.c_void_p
+        L.oracle_metrics_create.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int]
+        L.oracle_metrics_record.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        L.oracle_metrics_read.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.oracle_metrics_destroy.argtypes = [C.c_void_p]
+        self.thr = np.ascontiguousarray(threshold_mass, dtype=np.uint32)
+        self._h = L.oracle_metrics_create(C.byref(params), C.byref(venue_struct), res, _p(self.thr), n)
+        self.res, self.n = res, n
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().oracle_metrics_destroy(self._h)
+
+    def record(self, prev, cur):
+        a = np.ascontiguousarray(prev, dtype=np.float32)
+        b = np.ascontiguousarray(cur, dtype=np.float32)
+        lib().oracle_metrics_record(self._h, _p(a), _p(b), self.n)
+
+    def read(self):
+        ctr = np.zeros(196, np.uint32)   # SwarmMetricCounters, 784 bytes
+        cells = np.zeros((self.res * self.res, 16), np.uint32)
+        evac = np.zeros(self.n, np.uint32)
+        lib().oracle_metrics_read(self._h, _p(ctr), _p(cells), _p(evac))
+        return ctr, cells, evac
+
+
 # ---- the unmodified reference (this container only) ----
 def ref_available():
     return os.path.exists(REF_SO)
@@ -194,6 +225,48 @@ class RefSim:
         out = np.empty(self.n, np.uint8)
         ref_lib().ref_get_contacts(self._h, _p(out))
         return out
+
+
+class RefMetrics:
+    """swarm::metrics::MetricsReference itself (the terrace's exits)."""
+
+    def __init__(self, n, threshold_mass):
+        L = ref_lib()
+        L.ref_metrics_create.restype = C.c_void_p
+        L.ref_metrics_create.argtypes = [C.c_int, C.c_void_p, C.c_int]
+        L.ref_metrics_record.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        L.ref_metrics_read.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.ref_metrics_destroy.argtypes = [C.c_void_p]
+        self.thr = np.ascontiguousarray(threshold_mass, dtype=np.uint32)
+        self.cells = self.thr.size // 4
+        self._h = L.ref_metrics_create(n, _p(self.thr), self.cells)
+        self.n = n
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            ref_lib().ref_metrics_destroy(self._h)
+
+    def record(self, prev, cur):
+        a = np.ascontiguousarray(prev, dtype=np.float32)
+        b = np.ascontiguousarray(cur, dtype=np.float32)
+        assert ref_lib().ref_metrics_record(self._h, _p(a), _p(b), self.n) == 0
+
+    def read(self):
+        ctr = np.zeros(196, np.uint32)
+        cells = np.zeros((self.cells, 16), np.uint32)
+        evac = np.zeros(self.n, np.uint32)
+        ref_lib().ref_metrics_read(self._h, _p(ctr), _p(cells), _p(evac))
+        return ctr, cells, evac
+
+
+def ref_terrace_metric_cells():
+    """computeMetricVenue(stadium.sdf).cellInfo(): (threshold_mass (4096, 4), walkable m^2 (4096,))."""
+    L = ref_lib()
+    L.ref_metrics_terrace_cells.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+    thr = np.zeros((4096, 4), np.uint32)
+    area = np.zeros(4096, np.float32)
+    assert L.ref_metrics_terrace_cells(_p(thr), _p(area), 4096) == 4096
+    return thr, area
 
 
 def ref_load_sdf(path):

@@ -9,6 +9,7 @@
 
 #include <swarm/cpu_crowd_sim.hpp>
 #include <swarm/crowd_sim.hpp>
+#include <swarm/metrics.hpp>
 #include <swarm/sdf.hpp>
 #include <swarm/venue.hpp>
 
@@ -149,6 +150,51 @@ int ref_venue_grid(const char* venue, int* grid_res, float* domain_min, float* d
         *exit_depth = v.exitDepth; *exit_max_z = v.exitMaxZ;
         return 0;
     } catch (const std::exception& e) { g_err = e.what(); return -1; }
+}
+
+// ---- safety metrics: MetricsReference (src/metrics.cpp:429-476), the CPU mirror of metrics_deposit/finalize.comp ----
+
+// The terrace's metric cell table (computeMetricVenue, src/metrics.cpp:122): per cell thresholdMass[4], walkable m^2
+int ref_metrics_terrace_cells(uint32_t* threshold_mass, float* walkable_m2, int capacity) {
+    try {
+        const swarm::metrics::MetricVenue mv = swarm::metrics::computeMetricVenue(swarm::sdfVolumeCPU());
+        const std::vector<swarm::GpuMetricCellInfo> info = mv.cellInfo();
+        const int n = int(info.size());
+        for (int c = 0; c < n && c < capacity; ++c) {
+            for (int k = 0; k < 4; ++k) threshold_mass[4 * c + k] = info[size_t(c)].thresholdMass[k];
+            walkable_m2[c] = info[size_t(c)].walkableM2;
+        }
+        return n;
+    } catch (const std::exception& e) { g_err = e.what(); return -1; }
+}
+
+void* ref_metrics_create(int n, const uint32_t* threshold_mass, int cells) {
+    try {
+        std::vector<swarm::GpuMetricCellInfo> info(size_t(cells), swarm::GpuMetricCellInfo{});
+        for (int c = 0; c < cells; ++c)
+            for (int k = 0; k < 4; ++k) info[size_t(c)].thresholdMass[k] = threshold_mass[4 * c + k];
+        return new swarm::metrics::MetricsReference(n, std::move(info));
+    } catch (const std::exception& e) { g_err = e.what(); return nullptr; }
+}
+void ref_metrics_destroy(void* h) { delete static_cast<swarm::metrics::MetricsReference*>(h); }
+
+int ref_metrics_record(void* h, const float* prev, const float* cur, int n) {
+    try {
+        std::vector<swarm::GpuBoid> a(static_cast<size_t>(n)), b(static_cast<size_t>(n));
+        std::memcpy(a.data(), prev, size_t(n) * sizeof(swarm::GpuBoid));
+        std::memcpy(b.data(), cur, size_t(n) * sizeof(swarm::GpuBoid));
+        static_cast<swarm::metrics::MetricsReference*>(h)->record(a, b);
+        return 0;
+    } catch (const std::exception& e) { g_err = e.what(); return -1; }
+}
+
+// counters: 784 bytes (GpuMetricCounters); cells: 64 bytes each (GpuMetricCell); evac_step: n
+int ref_metrics_read(void* h, void* counters, void* cells, uint32_t* evac_step) {
+    auto* m = static_cast<swarm::metrics::MetricsReference*>(h);
+    std::memcpy(counters, &m->counters, sizeof m->counters);
+    std::memcpy(cells, m->cells.data(), m->cells.size() * sizeof(swarm::GpuMetricCell));
+    std::memcpy(evac_step, m->evacStep.data(), m->evacStep.size() * sizeof(uint32_t));
+    return 0;
 }
 
 }  // extern "C"

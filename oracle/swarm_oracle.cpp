@@ -1155,3 +1155,113 @@ int oracle_get_contacts(void* h, uint8_t* out) {
 int oracle_max_threads() { return omp_get_max_threads(); }
 
 }  // extern "C"
+
+// ================================================================================================================
+// Safety metrics (src/metrics.cpp:249-268 cicDeposit / speedMass, :429-476 MetricsReference::record; the exit slot
+// rule :40-51 for the stadium, exit boxes for grid venues)
+// ================================================================================================================
+namespace oracle {
+namespace {
+struct Metrics {
+    SwarmParams P;
+    SwarmVenue V;
+    std::vector<float> boxes;
+    int res;
+    std::vector<uint32_t> thr;         // 4 per cell
+    SwarmMetricCounters ctr{};
+    std::vector<SwarmMetricCell> cells;
+    std::vector<uint32_t> evac;
+    uint32_t steps = 0;
+
+    int exitSlot(F4 p) const {
+        if (V.kind == SWARM_VENUE_STADIUM) {
+            const float ax = std::abs(p.x), ay = std::abs(p.y);
+            const bool alongY = ay >= ax;
+            const float lat = alongY ? ax : ay;
+            if (lat >= P.avenue_half) return 4;
+            return alongY ? (p.y > 0.0f ? 2 : 3) : (p.x > 0.0f ? 0 : 1);
+        }
+        for (int e = 0; e < V.n_exits && e < 56; ++e) {
+            const float* b = boxes.data() + 4 * e;
+            if (p.x >= b[0] && p.x <= b[2] && p.y >= b[1] && p.y <= b[3]) return 5 + e;
+        }
+        return 4;
+    }
+    void record(const Boid* prev, const Boid* cur, int n) {
+        ++steps;
+        std::vector<uint32_t> mass(size_t(res) * size_t(res), 0u), smass(mass.size(), 0u);
+        uint32_t active = 0;
+        const float off = float(0.5 * res - 0.5);
+        for (int i = 0; i < n; ++i) {
+            const F4 p0 = prev[i].pos, p1 = cur[i].pos;
+            if (p0.w != 0.0f && p1.w == 0.0f) {
+                ++ctr.exits[exitSlot(p0)];
+                ++ctr.evacuated;
+                evac[size_t(i)] = steps;
+            }
+            if (p1.w != 0.0f) {
+                ++active;
+                const float gx = (p1.x - V.metric_center_x) * P.metric_cells_per_unit + off;
+                const float gy = (p1.y - V.metric_center_y) * P.metric_cells_per_unit + off;
+                const float fx = std::floor(gx), fy = std::floor(gy);
+                const float tx = gx - fx, ty = gy - fy;
+                const uint32_t qx = uint32_t(std::floor(tx * 256.0f + 0.5f)), qy = uint32_t(std::floor(ty * 256.0f + 0.5f));
+                const uint32_t rx = 256u - qx, ry = 256u - qy;
+                const int ix = int(fx), iy = int(fy);
+                auto idx = [this](int x, int y) { return std::clamp(x, 0, res - 1) + std::clamp(y, 0, res - 1) * res; };
+                const int c[4] = {idx(ix, iy), idx(ix + 1, iy), idx(ix, iy + 1), idx(ix + 1, iy + 1)};
+                const uint32_t w[4] = {rx * ry, qx * ry, rx * qy, qx * qy};
+                const float v = std::sqrt(cur[i].vel.x * cur[i].vel.x + cur[i].vel.y * cur[i].vel.y) * P.metric_speed_scale;
+                for (int k = 0; k < 4; ++k) {
+                    if (w[k] == 0) continue;
+                    mass[size_t(c[k])] += w[k];
+                    smass[size_t(c[k])] += uint32_t(std::floor(float(w[k]) * v + 0.5f));
+                }
+            }
+        }
+        ctr.active = active;
+        ctr.active_accum = 0;
+        ctr.step = steps;
+        auto add64 = [](uint32_t* a, uint32_t b) {
+            const uint64_t x = (uint64_t(a[0]) | (uint64_t(a[1]) << 32)) + b;
+            a[0] = uint32_t(x); a[1] = uint32_t(x >> 32);
+        };
+        for (size_t c = 0; c < cells.size(); ++c) {
+            const uint32_t m = mass[c], sm = smass[c];
+            SwarmMetricCell& s = cells[c];
+            s.last_mass = m;
+            s.last_speed_mass = sm;
+            s.peak_mass = std::max(s.peak_mass, m);
+            s.occupied_steps += m != 0;
+            for (int k = 0; k < 4; ++k) s.steps_above[k] += m >= thr[4 * c + size_t(k)];
+            add64(s.mass_steps, m);
+            add64(s.speed_mass_steps, sm);
+            if (m >= thr[4 * c + 2]) add64(s.exposure_mass_steps, m);
+        }
+    }
+};
+}  // namespace
+}  // namespace oracle
+
+extern "C" {
+void* oracle_metrics_create(const SwarmParams* p, const SwarmVenue* v, int res, const uint32_t* threshold_mass, int n) {
+    auto* m = new oracle::Metrics{*p, *v, {}, res, {}, {}, {}, {}, 0};
+    if (v->n_exits > 0 && v->exit_boxes) m->boxes.assign(v->exit_boxes, v->exit_boxes + 4 * v->n_exits);
+    m->thr.assign(threshold_mass, threshold_mass + 4 * size_t(res) * size_t(res));
+    m->cells.assign(size_t(res) * size_t(res), SwarmMetricCell{});
+    m->evac.assign(size_t(n), 0u);
+    return m;
+}
+void oracle_metrics_destroy(void* h) { delete static_cast<oracle::Metrics*>(h); }
+int oracle_metrics_record(void* h, const float* prev, const float* cur, int n) {
+    static_cast<oracle::Metrics*>(h)->record(reinterpret_cast<const oracle::Boid*>(prev), reinterpret_cast<const oracle::Boid*>(cur), n);
+    return 0;
+}
+int oracle_metrics_read(void* h, SwarmMetricCounters* ctr, SwarmMetricCell* cells, uint32_t* evac) {
+    auto* m = static_cast<oracle::Metrics*>(h);
+    if (ctr) *ctr = m->ctr;
+    if (cells) std::memcpy(cells, m->cells.data(), m->cells.size() * sizeof(SwarmMetricCell));
+    if (evac) std::memcpy(evac, m->evac.data(), m->evac.size() * 4);
+    return 0;
+}
+}

@@ -7,6 +7,7 @@
 // No exception crosses the boundary: every entry returns a status, swarm_last_error the message.
 
 #include "../../include/swarm_cuda.h"
+#include "metrics.cuh"
 #include "step_kernels.cuh"
 
 #include <cuda_runtime.h>
@@ -52,6 +53,17 @@ struct SwarmSim {
     bool fused = true;          // the whole step as one persistent kernel when the grid fits on the GPU
     int barrierExtra = 0;       // the timeout test's missing block (swarm_test_barrier_timeout)
     bool counted = false;       // the counts hold the current state's keys (a fused step's final pass counted them)
+    // safety metrics (swarm_metrics_enable)
+    int metricRes = 0;
+    uint32_t metricStep = 0;
+    SwarmMetricCounters* mCounters = nullptr;
+    uint32_t* mEvac = nullptr;
+    uint2* mMass = nullptr;
+    uint4* mThr = nullptr;
+    SwarmMetricCell* mCells = nullptr;
+    float4* mBoxes = nullptr;
+    std::vector<float> exitBoxesHost;
+    int enqueueMetrics(int in);
     float *dSdf = nullptr, *dWall = nullptr, *dNav = nullptr, *dFloor = nullptr, *dSpeed = nullptr;
     int ncells = 0;
     // execution
@@ -139,6 +151,33 @@ StepArgs SwarmSim::args(int in) const {
     return A;
 }
 
+int SwarmSim::enqueueMetrics(int in) {
+    if (!metricRes) return SWARM_OK;
+    swarm_gpu::MetricArgs M{};
+    M.prev = state[in];
+    M.cur = state[in ^ 1];
+    M.n = n;
+    M.res = metricRes;
+    M.cellsPerUnit = P.metric_cells_per_unit;
+    M.offset = float(0.5 * metricRes - 0.5);
+    M.centerX = V.metric_center_x;
+    M.centerY = V.metric_center_y;
+    M.speedScale = P.metric_speed_scale;
+    M.stadium = V.kind == SWARM_VENUE_STADIUM ? 1 : 0;
+    M.avenueHalf = P.avenue_half;
+    M.nExits = std::min(V.n_exits, 56);
+    M.exitBoxes = mBoxes;
+    M.counters = mCounters;
+    M.evacStep = mEvac;
+    M.mass = mMass;
+    M.thresholds = mThr;
+    M.cells = mCells;
+    M.stepIndex = ++metricStep;
+    swarm_gpu::launch_metrics(M, stream);
+    launches += 2;
+    return cudaOk(this, cudaGetLastError(), "metrics launch") ? SWARM_OK : SWARM_E_CUDA;
+}
+
 int SwarmSim::enqueueStages(int in, int s0, int s1) {
     const StepArgs A = args(in);
     for (int st = s0; st < s1; ++st) swarm_gpu::launch_stage(A, st, stream, &launches);
@@ -205,6 +244,7 @@ int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capac
         if (ok && V.speed_factor)
             ok = devAlloc(h, &h->dSpeed, nw) && cudaMemcpy(h->dSpeed, V.speed_factor, nw * 4, cudaMemcpyHostToDevice) == cudaSuccess;
     }
+    if (V.n_exits > 0 && V.exit_boxes) h->exitBoxesHost.assign(V.exit_boxes, V.exit_boxes + 4 * size_t(V.n_exits));
     // host pointers of the venue are not kept
     h->V.sdf = nullptr; h->V.wall_sdf = nullptr; h->V.nav_dist = nullptr; h->V.floor_height = nullptr;
     h->V.speed_factor = nullptr; h->V.exit_boxes = nullptr;
@@ -313,6 +353,51 @@ int swarm_set_graph(SwarmHandle h, int enabled) {
     return SWARM_OK;
 }
 
+int swarm_metrics_enable(SwarmHandle h, int res, const uint32_t* threshold_mass) {
+    if (!h || !threshold_mass || res <= 0 || res % 16 != 0 || res > 4096) return SWARM_E_INVALID;
+    if (!h->metricRes) {
+        const size_t cells = size_t(res) * size_t(res), N = size_t(h->capacity);
+        const size_t boxes = std::max<size_t>(h->exitBoxesHost.size() / 4, 1);
+        if (!(devAlloc(h, &h->mCounters, 1) && devAlloc(h, &h->mEvac, N) && devAlloc(h, &h->mMass, cells) &&
+              devAlloc(h, &h->mThr, cells) && devAlloc(h, &h->mCells, cells) && devAlloc(h, &h->mBoxes, boxes)))
+            return h->fail(SWARM_E_OOM, "metrics buffers");
+        if (!h->exitBoxesHost.empty() &&
+            !cudaOk(h, cudaMemcpy(h->mBoxes, h->exitBoxesHost.data(), h->exitBoxesHost.size() * 4, cudaMemcpyHostToDevice), "boxes"))
+            return SWARM_E_CUDA;
+        h->metricRes = res;
+    } else if (res != h->metricRes) {
+        return h->fail(SWARM_E_INVALID, "the metric grid's resolution is fixed once enabled");
+    }
+    const size_t cells = size_t(res) * size_t(res);
+    if (!cudaOk(h, cudaMemcpy(h->mThr, threshold_mass, cells * 16, cudaMemcpyHostToDevice), "thresholds")) return SWARM_E_CUDA;
+    return swarm_metrics_reset(h);
+}
+
+int swarm_metrics_reset(SwarmHandle h) {
+    if (!h) return SWARM_E_INVALID;
+    if (!h->metricRes) return h->fail(SWARM_E_STATE, "metrics are not enabled");
+    const size_t cells = size_t(h->metricRes) * size_t(h->metricRes);
+    h->metricStep = 0;
+    const bool ok = cudaMemsetAsync(h->mCounters, 0, sizeof(SwarmMetricCounters), h->stream) == cudaSuccess &&
+                    cudaMemsetAsync(h->mEvac, 0, size_t(h->capacity) * 4, h->stream) == cudaSuccess &&
+                    cudaMemsetAsync(h->mMass, 0, cells * 8, h->stream) == cudaSuccess &&
+                    cudaMemsetAsync(h->mCells, 0, cells * sizeof(SwarmMetricCell), h->stream) == cudaSuccess;
+    return ok ? SWARM_OK : h->fail(SWARM_E_CUDA, "metrics reset");
+}
+
+int swarm_metrics_read(SwarmHandle h, SwarmMetricCounters* counters, SwarmMetricCell* cells, uint32_t* evac_step, int n) {
+    if (!h) return SWARM_E_INVALID;
+    if (!h->metricRes) return h->fail(SWARM_E_STATE, "metrics are not enabled");
+    if (!cudaOk(h, cudaStreamSynchronize(h->stream), "sync")) return SWARM_E_CUDA;
+    if (counters) cudaMemcpy(counters, h->mCounters, sizeof *counters, cudaMemcpyDeviceToHost);
+    if (cells) cudaMemcpy(cells, h->mCells, size_t(h->metricRes) * size_t(h->metricRes) * sizeof(SwarmMetricCell), cudaMemcpyDeviceToHost);
+    if (evac_step) {
+        if (n != h->n) return h->fail(SWARM_E_INVALID, "evac_step size mismatch");
+        cudaMemcpy(evac_step, h->mEvac, size_t(n) * 4, cudaMemcpyDeviceToHost);
+    }
+    return cudaOk(h, cudaGetLastError(), "metrics read") ? SWARM_OK : SWARM_E_CUDA;
+}
+
 int swarm_test_barrier_timeout(SwarmHandle h) {
     if (!h) return SWARM_E_INVALID;
     h->barrierExtra = 1;
@@ -370,6 +455,7 @@ static int stepImpl(SwarmHandle h, int steps) {
             if (h->timing && !cudaOk(h, cudaEventRecord(h->ev[4], h->stream), "event")) return SWARM_E_CUDA;
             if (h->useGraph) h->launches += perStep;
         }
+        if (h->metricRes && h->enqueueMetrics(in) != SWARM_OK) return SWARM_E_CUDA;
         h->readIdx ^= 1;
     }
     h->timesValid = false;

@@ -205,3 +205,41 @@ extern "C" int swarm_spawn_lattice(int nx, int ny, int n, float spacing, float c
     }
     return SWARM_OK;
 }
+
+extern "C" int swarm_metric_thresholds_grid(const SwarmVenue* v, int res, uint32_t* out) {
+    if (!v || !out || res <= 0 || !v->wall_sdf || v->wall_nx < 2 || v->wall_ny < 2 || !(v->wall_h > 0)) return SWARM_E_INVALID;
+    // persons per m^2: Fruin's LoS E and LoS F, and the crush level (the reference's metrics.hpp thresholds)
+    const double thresholds[3] = {1.08, 2.17, 5.0};
+    const int sub = 40;
+    const double inv = 1.0 / v->wall_h;
+    auto wallAt = [&](double x, double y) {
+        double fx = (x - v->wall_origin_x) * inv, fy = (y - v->wall_origin_y) * inv;
+        if (fx < 0 || fy < 0 || fx > v->wall_nx - 1 || fy > v->wall_ny - 1) return 1.0;
+        int ix = std::min(int(fx), v->wall_nx - 2), iy = std::min(int(fy), v->wall_ny - 2);
+        double wx = fx - ix, wy = fy - iy;
+        const float* W = v->wall_sdf;
+        size_t r0 = size_t(iy) * size_t(v->wall_nx) + size_t(ix), r1 = r0 + size_t(v->wall_nx);
+        return (W[r0] * (1 - wx) + W[r0 + 1] * wx) * (1 - wy) + (W[r1] * (1 - wx) + W[r1 + 1] * wx) * wy;
+    };
+    for (int iy = 0; iy < res; ++iy) {
+        for (int ix = 0; ix < res; ++ix) {
+            int free = 0;
+            for (int sy = 0; sy < sub; ++sy) {
+                for (int sx = 0; sx < sub; ++sx) {
+                    const double x = v->metric_center_x + (ix - 0.5 * res) + (sx + 0.5) / sub;
+                    const double y = v->metric_center_y + (iy - 0.5 * res) + (sy + 0.5) / sub;
+                    if (x < v->exit_lo_x || x > v->exit_hi_x || y < v->exit_lo_y || y > v->exit_hi_y) continue;
+                    free += wallAt(x, y) > 0.0;
+                }
+            }
+            const double area = double(free) / double(sub * sub);
+            uint32_t* t = out + 4 * (size_t(iy) * size_t(res) + size_t(ix));
+            for (int k = 0; k < 3; ++k) {
+                const double m = std::ceil(thresholds[k] * area * 65536.0);
+                t[k] = area < 0.1 ? 0xFFFFFFFFu : uint32_t(std::min(std::max(m, 1.0), 4294967295.0));
+            }
+            t[3] = 0xFFFFFFFFu;
+        }
+    }
+    return SWARM_OK;
+}

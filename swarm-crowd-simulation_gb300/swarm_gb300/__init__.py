@@ -12,8 +12,8 @@ import os
 
 import numpy as np
 
-from .abi import (SWARM_OK, SWARM_VENUE_GRID, SWARM_VENUE_STADIUM, SwarmParams, SwarmStageTimes, SwarmVenue,
-                  fptr)
+from .abi import (METRIC_CELL_WORDS, SWARM_OK, SWARM_VENUE_GRID, SWARM_VENUE_STADIUM, SwarmMetricCounters, SwarmParams,
+                  SwarmStageTimes, SwarmVenue, fptr)
 
 PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG_DIR, "libswarm_gb300.so")
@@ -59,6 +59,10 @@ def lib():
             "swarm_set_timing": [H, C.c_int],
             "swarm_stage_times": [H, C.POINTER(SwarmStageTimes)],
             "swarm_launch_count": [H, C.POINTER(C.c_int64)],
+            "swarm_metrics_enable": [H, C.c_int, C.c_void_p],
+            "swarm_metrics_reset": [H],
+            "swarm_metrics_read": [H, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int],
+            "swarm_metric_thresholds_grid": [C.POINTER(SwarmVenue), C.c_int, C.c_void_p],
             "swarm_hall_layout": [C.c_void_p, C.POINTER(SwarmVenue)],
             "swarm_hall_fields": [C.c_void_p, C.POINTER(SwarmVenue), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                   C.POINTER(C.c_float)],
@@ -189,6 +193,26 @@ class CrowdSim:
         c = C.c_int64()
         self._ck(lib().swarm_launch_count(self._h, C.byref(c)), "launch_count")
         return c.value
+
+    # ---- safety metrics ----
+    def metrics_enable(self, res, threshold_mass):
+        """Metrics after every step: res x res 1 m cells; threshold_mass (res*res, 4) uint32 (LoS E, LoS F, crush, -)."""
+        t = np.ascontiguousarray(threshold_mass, dtype=np.uint32).reshape(-1, 4)
+        assert t.shape[0] == res * res
+        self._ck(lib().swarm_metrics_enable(self._h, int(res), t.ctypes.data_as(C.c_void_p)), "metrics_enable")
+        self.metric_res = int(res)
+
+    def metrics_reset(self):
+        self._ck(lib().swarm_metrics_reset(self._h), "metrics_reset")
+
+    def metrics(self):
+        """(counters struct, cells (res*res, 16) uint32, evacuation step per agent)."""
+        ctr = SwarmMetricCounters()
+        cells = np.empty((self.metric_res * self.metric_res, METRIC_CELL_WORDS), np.uint32)
+        evac = np.empty(self.n, np.uint32)
+        self._ck(lib().swarm_metrics_read(self._h, C.byref(ctr), cells.ctypes.data_as(C.c_void_p),
+                                          evac.ctypes.data_as(C.c_void_p), self.n), "metrics_read")
+        return ctr, cells, evac
 
     # ---- inspection ----
     def grid(self):

@@ -76,3 +76,13 @@ def fptr(a):
         return None
     assert a.dtype.name == "float32" and a.flags["C_CONTIGUOUS"]
     return a.ctypes.data_as(C.POINTER(_f))
+
+
+class SwarmMetricCounters(C.Structure):
+    _fields_ = [("step", C.c_uint32), ("active", C.c_uint32), ("evacuated", C.c_uint32), ("active_accum", C.c_uint32),
+                ("exits", C.c_uint32 * 61), ("pad", C.c_uint32 * 3), ("gangway_visits", C.c_uint32 * 64),
+                ("gangway_last", C.c_uint32 * 64)]
+
+
+METRIC_CELL_WORDS = 16   # SwarmMetricCell: 16 uint32 (last_mass, last_speed_mass, peak_mass, occupied_steps,
+                         # steps_above[4], mass_steps[2], speed_mass_steps[2], exposure_mass_steps[2], pad[2])

@@ -36,6 +36,14 @@ class Venue:
     def n_cells(self):
         return self.struct.grid_res_x * self.struct.grid_res_y
 
+    def metric_thresholds(self, res=None):
+        """Per 1 m cell threshold masses of a grid venue (walkable area sampled from its wall SDF)."""
+        res = res or self.struct.metric_res
+        out = np.empty((res * res, 4), np.uint32)
+        _check(lib().swarm_metric_thresholds_grid(C.byref(self.struct), int(res), out.ctypes.data_as(C.c_void_p)),
+               "swarm_metric_thresholds_grid")
+        return res, out
+
     @staticmethod
     def stadium(sdf):
         sdf = np.ascontiguousarray(sdf, dtype=np.float32).reshape(-1)

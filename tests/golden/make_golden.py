@@ -10,6 +10,9 @@ Writes
                      distributions), and CpuCrowdSim (SortMode::Counting) after 1 step (state, sorted pairs, cell table,
                      contact bits), after 250 steps (state and its FNV-1a hash, tools/golden_state.hpp:121-126) and after
                      251 steps (one step from the congested state: state, pairs, cells, contacts).
+  terrace_metrics_ref.npz  the terrace's metric cell table (computeMetricVenue: threshold masses, walkable area) and
+                     MetricsReference (src/metrics.cpp:429-476) after recording the first 250 steps from the spawn:
+                     counters, per-cell accumulators, evacuation step per agent.
 """
 import os
 import sys
@@ -45,6 +48,21 @@ def main():
     out["grid251_key"], out["grid251_id"] = sim.grid()
     out["hash250"] = np.array([O.state_hash(out["state250"])], dtype=np.uint64)
     np.savez_compressed(os.path.join(HERE, "terrace_ref.npz"), **out)
+
+    thr, area = O.ref_terrace_metric_cells()
+    met = O.RefMetrics(4096, thr)
+    sim = O.RefSim("terrace")
+    sim.set_state(spawn)
+    prev = spawn
+    for _ in range(250):
+        sim.step(1)
+        cur = sim.state()
+        met.record(prev, cur)
+        prev = cur
+    ctr, cells, evac = met.read()
+    np.savez_compressed(os.path.join(HERE, "terrace_metrics_ref.npz"), threshold_mass=thr, walkable_m2=area,
+                        counters=ctr, cells=cells, evac_step=evac)
+    print("metrics: %d evacuated, exits %s" % (ctr[2], list(ctr[4:9])))
     print("hash after 250 steps: %016x" % int(out["hash250"][0]))
 
 
