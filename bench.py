@@ -22,6 +22,8 @@ cpu_baseline  the oracle port of the reference's CPU step (OpenMP, all host thre
 """
 import argparse
 import json
+
+import numpy as np
 import os
 import statistics
 import subprocess
@@ -106,6 +108,75 @@ def workload():
     return venues.hall_c1()
 
 
+def bench_batched(P, steps=10, warmup=3):
+    """The 256-instance batch (N log-uniform in [1 024, 65 536], 1-2 exits of U[1.5, 6] m, halls sized to 4 agents/m^2,
+    independent seeds) as one packed state, against the same instances launched one at a time. Both sides run the
+    same steps from the same states (the results are bit-identical), so agent-steps are the same: the speed-up is
+    the time ratio. The batch's working set (3.8 M agents, 2.1 GB of venue fields) is far larger than L2."""
+    import torch
+    import swarm_gb300
+    from swarm_gb300 import venues
+    vens, boids, r, v0, counts = venues.build_batch(256, 0)
+    n = int(counts.sum())
+    stream = torch.cuda.Stream()
+    batch = swarm_gb300.BatchSim(P, vens, counts)
+    batch.set_stream(stream.cuda_stream)
+    batch.set_state(boids)
+    batch.set_agent_params(r, v0)
+    tuning = batch.autotune(steps=2)
+    dev = torch.empty((n, 8), dtype=torch.float32, device="cuda")
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            batch.step(1)
+    torch.cuda.synchronize()
+    start = batch.state()
+    active, t_batch = 0, 0.0
+    for _ in range(steps):
+        batch.download_device(dev.data_ptr())
+        active += int((dev[:, 3] != 0).sum().item())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            batch.step(1)
+            e1.record(stream)
+        stream.synchronize()
+        t_batch += e0.elapsed_time(e1)
+    batch.close()
+    # one at a time: each instance its own handle, all on one stream, stepped in turn
+    solos = []
+    for i, v in enumerate(vens):
+        a, b = int(np.sum(counts[:i])), int(np.sum(counts[:i + 1]))
+        sim = swarm_gb300.CrowdSim(P, v, b - a)
+        sim.set_stream(stream.cuda_stream)
+        sim.set_state(start[a:b])
+        sim.set_agent_params(r[a:b], v0[a:b])
+        solos.append(sim)
+    for _ in range(2):
+        for sim in solos:
+            sim.step(1)
+    torch.cuda.synchronize()
+    for i, sim in enumerate(solos):   # back to the same start
+        a, b = int(np.sum(counts[:i])), int(np.sum(counts[:i + 1]))
+        sim.set_state(start[a:b])
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        for sim in solos:
+            sim.step(1)
+    e1.record(stream)
+    e1.synchronize()
+    t_solo = e0.elapsed_time(e1)
+    for sim in solos:
+        sim.close()
+    return {"workload": "256 halls, N log-uniform [1024, 65536] (total %d agents), 1-2 exits U[1.5, 6] m, seed 0" % n,
+            "value": active / (t_batch * 1e-3), "unit": UNIT, "ms_per_step": t_batch / steps,
+            "one_at_a_time": {"value": active / (t_solo * 1e-3), "ms_per_step": t_solo / steps,
+                              "launches_per_step": len(vens)},
+            "speedup_vs_one_at_a_time": t_solo / t_batch, "tuning": tuning,
+            "fraction_of_hbm_roofline": active / (t_batch * 1e-3) * B_STEP / (peaks()[0] * 1e9)}
+
+
 def cpu_baseline(budget_s=12.0, max_steps=400):
     """The oracle port (OpenMP, every host thread) on the same workload: 2 warm-up steps, then steps until the budget."""
     import numpy as np
@@ -152,6 +223,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--phase-kernels", action="store_true", help="one kernel per phase instead of the fused step")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 256-instance batched measurement")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -302,6 +374,11 @@ def main():
             "gpu_launches": launches,
         }
         line["clocks"] = clk.summary()
+        if not args.no_batch and world == 1:
+            try:
+                line["batched"] = bench_batched(P)
+            except Exception as e:  # reported, not fatal
+                line["batched"] = {"error": str(e)[:300]}
         if not args.no_cpu_baseline and world == 1:
             try:
                 line["cpu_baseline"] = cpu_baseline()

@@ -144,6 +144,12 @@ int swarm_params_si(SwarmParams* out);
  *   (src/cpu_crowd_sim.cpp:918-927). n_capacity: the agent buffer size (no power-of-two rule: the key sort has none). */
 int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capacity, SwarmHandle* out);
 int swarm_destroy(SwarmHandle h);
+/* Batched instances: m independent grid venues (no floor heights or speed factors) with counts[i] agents each, packed
+ * into one handle. The state is every instance's agents one after another (instance i's first agent follows the
+ * counts before it); each instance keeps its own hash grid, in one shared key space, so one sort and one step cover
+ * them all and no instance sees another's agents: each instance's result is bit-identical to running it alone.
+ * Every other entry point works on the batch as on one simulation (metrics excepted). */
+int swarm_batch_create(const SwarmParams* params, const SwarmVenue* venues, const int* counts, int m, SwarmHandle* out);
 /* Optional: run on the caller's stream (a cudaStream_t) instead of the handle's own. */
 int swarm_set_stream(SwarmHandle h, void* cuda_stream);
 int swarm_last_error(SwarmHandle h, char* buf, int len);
@@ -178,6 +184,14 @@ int swarm_set_graph(SwarmHandle h, int enabled);
  * grid is sized to stay resident); 0: one kernel per phase (hash, scan x2, scatter, rank + gather, predict, K - 1
  * sweeps, final), replayed from CUDA graphs when swarm_set_graph is on. Both give the same bits. */
 int swarm_set_fused(SwarmHandle h, int enabled);
+/* The launch configuration: the fused persistent kernel (fused = 1) with `threads` per block (0: the state size over
+ * the SMs, rounded up to a warp, 128..512) and at most `blocks_per_sm` blocks per SM (0: as many as fit; fewer blocks
+ * mean more agents per thread), or one kernel per phase (fused = 0: one Jacobi sweep per launch). */
+typedef struct SwarmTuning { int32_t fused, threads, blocks_per_sm; float ms_per_step; } SwarmTuning;
+int swarm_set_tuning(SwarmHandle h, const SwarmTuning* tuning);
+/* Times `steps` steps of each candidate configuration from the current state (restored after every trial and at the
+ * end), keeps the fastest in force and returns it. The results of every configuration are the same bits. */
+int swarm_autotune(SwarmHandle h, int steps, SwarmTuning* best);
 /* Failure-path test: the next fused step's first grid barrier waits for one block more than the launch has, runs
  * out its 1 s limit, records the timeout and ends the launch early; the next swarm_synchronize (or download)
  * returns SWARM_E_TIMEOUT and the handle stays usable. For tests only. */

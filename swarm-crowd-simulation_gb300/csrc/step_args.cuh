@@ -35,6 +35,7 @@ struct VenueArgs {
     float nox, noy, ninv;
     const float* floorH;
     const float* speedF;
+    uint32_t cellOffset;    // batched instances: this instance's first cell in the shared key space (0 otherwise)
 };
 
 struct StepArgs {
@@ -75,6 +76,12 @@ struct StepArgs {
     unsigned long long* stamps;   // timing on: the fused kernel's stage boundaries (%globaltimer, ns), else null
     int32_t hashed;         // fused step: the keys and counts of this step's input were counted by the last final pass
     int32_t hashNext;       // fused step: count the next step's keys in the final pass
+    int32_t fusedThreads;   // fused step: threads per block (0: n / SMs rounded up to a warp, 128..512)
+    int32_t fusedBlocksPerSm;   // fused step: at most this many blocks per SM (0: as many as fit)
+    // batched instances (null otherwise): each instance's venue, the instance of each agent and of each slot
+    const VenueArgs* venueTable;
+    const uint32_t* instAgent;
+    uint32_t* instSlot;
 };
 
 }  // namespace swarm_gpu

@@ -30,7 +30,17 @@ namespace swarm_gpu {
 __device__ __forceinline__ uint32_t cellID(const VenueArgs& V, float4 p) {
     const int x = sclamp(int((p.x - V.dminX) / V.dspanX * float(V.resX)), 0, V.resX - 1);
     const int y = sclamp(int((p.y - V.dminY) / V.dspanY * float(V.resY)), 0, V.resY - 1);
-    return uint32_t(x + y * V.resX);
+    return V.cellOffset + uint32_t(x + y * V.resX);
+}
+
+// The venue of an agent / a slot: the handle's one venue, or its instance's in a batch
+template <bool kB>
+__device__ __forceinline__ const VenueArgs& venueOfAgent(const StepArgs& A, uint32_t i) {
+    if constexpr (kB) return A.venueTable[A.instAgent[i]]; else return A.V;
+}
+template <bool kB>
+__device__ __forceinline__ const VenueArgs& venueOfSlot(const StepArgs& A, int s) {
+    if constexpr (kB) return A.venueTable[A.instSlot[s]]; else return A.V;
 }
 
 // Counts agent i's key in its cell's counter and records its arrival rank. Called by all 32 lanes of a warp together
@@ -50,18 +60,20 @@ __device__ __forceinline__ void countKey(const StepArgs& A, uint32_t i, uint32_t
 }
 
 // calc_grid.comp (CpuCrowdSim::hash, cpu_crowd_sim.cpp:983-993), with its NaN sanitiser. All lanes of a warp together.
+template <bool kB>
 __device__ __forceinline__ void hashItem(const StepArgs& A, int i) {
     const bool valid = i < A.n;
     uint32_t key = 0;
     if (valid) {
         float4 p = A.stateIn[2 * size_t(i)];
         if (isnan(p.x)) { p = make_float4(0.0f, 0.0f, 0.0f, 1.0f); A.stateIn[2 * size_t(i)] = p; }
-        key = p.w == 0.0f ? INACTIVE_CELL : cellID(A.V, p);
+        key = p.w == 0.0f ? INACTIVE_CELL : cellID(venueOfAgent<kB>(A, uint32_t(i)), p);
     }
     countKey(A, uint32_t(valid ? i : 0), key, valid);
 }
 
-__global__ void k_hash(StepArgs A) { hashItem(A, blockIdx.x * blockDim.x + threadIdx.x); }
+template <bool kB>
+__global__ void k_hash(StepArgs A) { hashItem<kB>(A, blockIdx.x * blockDim.x + threadIdx.x); }
 
 // The exclusive scan of the ncells + 1 counts, in tiles of SCAN_TILE: k_scan_reduce writes each tile's total,
 // k_scan_apply scans its tile on top of the totals of the tiles before it, writes the run starts and the cell table,
@@ -158,7 +170,7 @@ __global__ void k_scatter(StepArgs A) {
     if (i < A.n) scatterItem(A, i);
 }
 
-template <bool kPerAgent>
+template <bool kPerAgent, bool kB>
 __device__ __forceinline__ void rankGatherItem(const StepArgs& A, int s) {
     const int nActive = int(A.start[A.V.ncells]);
     const uint32_t me = A.sidTmp[s];
@@ -176,12 +188,13 @@ __device__ __forceinline__ void rankGatherItem(const StepArgs& A, int s) {
     A.pos0[t] = p;
     A.vel0[t] = A.stateIn[2 * size_t(me) + 1];
     if (kPerAgent) A.prm[t] = A.aparam[me];
+    if (kB) A.instSlot[t] = A.instAgent[me];
 }
 
-template <bool kPerAgent>
+template <bool kPerAgent, bool kB>
 __global__ void k_rank_gather(StepArgs A) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < A.n) rankGatherItem<kPerAgent>(A, s);
+    if (s < A.n) rankGatherItem<kPerAgent, kB>(A, s);
 }
 
 // ---- the physics passes ----
@@ -206,14 +219,15 @@ __device__ __forceinline__ f2 separationForce(const SwarmParams& P, f3 offset, u
     return magnitude * xy(offset) * (1.0f / sqrtf(dxy2));
 }
 
-template <class Venue>
+template <class Venue, bool kB>
 __device__ __forceinline__ void predictItem(const StepArgs& A, int s) {
     constexpr bool kUniform = Body<Venue>::kUniform;
     const int nActive = int(A.start[A.V.ncells]);
     if (s >= nActive) return;
     const SwarmParams& P = A.P;
-    const Venue ven{A.P, A.V};
-    const uint32_t self = A.sid[s], cid = A.skey[s];
+    const VenueArgs& V = venueOfSlot<kB>(A, s);
+    const Venue ven{A.P, V};
+    const uint32_t self = A.sid[s], cid = A.skey[s] - V.cellOffset;
     uint32_t contact = 0;
     const float4 p = A.pos0[s], v = A.vel0[s];
     if (ven.exits(p)) {
@@ -224,7 +238,7 @@ __device__ __forceinline__ void predictItem(const StepArgs& A, int s) {
     }
     const f2 eGoal = goalOf(A, ven, xyz(p), self);
     const float ri = kUniform ? P.body_radius : A.prm[s].x;
-    const int resX = A.V.resX, resY = A.V.resY;
+    const int resX = V.resX, resY = V.resY;
     const int cx = int(cid % uint32_t(resX)), cy = int(cid / uint32_t(resX));
     f2 sep{0.0f, 0.0f};
     float sAhead = 1e9f;
@@ -233,7 +247,7 @@ __device__ __forceinline__ void predictItem(const StepArgs& A, int s) {
     // walking it visits the reference's order (cells by x, agents by slot). Cells that cannot hold an agent within
     // R_PERC are left out of each row (every agent lies inside its cell, widened by `margin`): they contribute
     // nothing, and the nearest-agent-ahead minimum does not depend on the visiting order.
-    const float csx = A.V.dspanX / float(resX), csy = A.V.dspanY / float(resY);
+    const float csx = V.dspanX / float(resX), csy = V.dspanY / float(resY);
     const float margin = 0.01f * smax(csx, csy);
     // The search disk: R_PERC, or less where that cannot change the result. A neighbour farther than
     // (largest pair contact distance) + vFree * T_HEADWAY leaves a gap whose headway speed is above vFree, so it
@@ -251,31 +265,15 @@ __device__ __forceinline__ void predictItem(const StepArgs& A, int s) {
         const int y = j - R;
         const int ny = cy + y;
         if (y > R || ny < 0 || ny >= resY) continue;
-        const float ylo = A.V.dminY + float(ny) * csy - margin, yhi = A.V.dminY + float(ny + 1) * csy + margin;
+        const float ylo = V.dminY + float(ny) * csy - margin, yhi = V.dminY + float(ny + 1) * csy + margin;
         const float dy = fmaxf(0.0f, fmaxf(ylo - p.y, p.y - yhi));
         if (dy >= rPerc) continue;
         const float w = sqrtf(rPerc * rPerc - dy * dy) + margin;
-        const int xlo = max(max(cx - R, 0), int(floorf((p.x - w - A.V.dminX) / csx)));
-        const int xhi = min(min(cx + R, resX - 1), int(floorf((p.x + w - A.V.dminX) / csx)));
+        const int xlo = max(max(cx - R, 0), int(floorf((p.x - w - V.dminX) / csx)));
+        const int xhi = min(min(cx + R, resX - 1), int(floorf((p.x + w - V.dminX) / csx)));
         if (xlo > xhi) continue;
-        rk0[j] = A.start[xlo + ny * resX];
-        rk1[j] = A.start[xhi + 1 + ny * resX];
-    }
-#pragma unroll
-    for (int j = 0; j < MAXR; ++j) {
-        rk0[j] = rk1[j] = 0;
-        const int y = j - R;
-        const int ny = cy + y;
-        if (y > R || ny < 0 || ny >= resY) continue;
-        const float ylo = A.V.dminY + float(ny) * csy - margin, yhi = A.V.dminY + float(ny + 1) * csy + margin;
-        const float dy = fmaxf(0.0f, fmaxf(ylo - p.y, p.y - yhi));
-        if (dy >= rPerc) continue;
-        const float w = sqrtf(rPerc * rPerc - dy * dy) + margin;
-        const int xlo = max(max(cx - R, 0), int(floorf((p.x - w - A.V.dminX) / csx)));
-        const int xhi = min(min(cx + R, resX - 1), int(floorf((p.x + w - A.V.dminX) / csx)));
-        if (xlo > xhi) continue;
-        rk0[j] = A.start[xlo + ny * resX];
-        rk1[j] = A.start[xhi + 1 + ny * resX];
+        rk0[j] = A.start[V.cellOffset + xlo + ny * resX];
+        rk1[j] = A.start[V.cellOffset + xhi + 1 + ny * resX];
     }
 #pragma unroll
     for (int j = 0; j < MAXR; ++j) {
@@ -346,10 +344,10 @@ __device__ __forceinline__ void predictItem(const StepArgs& A, int s) {
     A.ctc[s] = uint8_t(contact);
 }
 
-template <class Venue>
+template <class Venue, bool kB>
 __global__ void __launch_bounds__(128) k_predict(StepArgs A) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < A.n) predictItem<Venue>(A, s);
+    if (s < A.n) predictItem<Venue, kB>(A, s);
 }
 
 // Where a sweep reads its neighbours: global memory, or a tile's window of slots staged in shared memory
@@ -368,16 +366,17 @@ struct WindowNbr {
 };
 
 // The 3 x 3 neighbour rows of slot s: slot ranges [rk0[j], rk1[j]) for the rows cy - 1 .. cy + 1
-__device__ __forceinline__ void sweepRows(const StepArgs& A, uint32_t cid, uint32_t* rk0, uint32_t* rk1) {
-    const int resX = A.V.resX, resY = A.V.resY;
+__device__ __forceinline__ void sweepRows(const StepArgs& A, const VenueArgs& V, uint32_t key, uint32_t* rk0, uint32_t* rk1) {
+    const int resX = V.resX, resY = V.resY;
+    const uint32_t cid = key - V.cellOffset;
     const int cx = int(cid % uint32_t(resX)), cy = int(cid / uint32_t(resX));
     const int xlo = max(cx - 1, 0), xhi = min(cx + 1, resX - 1);
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
         const int ny = cy + j - 1;
         const bool ok = ny >= 0 && ny < resY;
-        rk0[j] = ok ? A.start[xlo + ny * resX] : 0u;
-        rk1[j] = ok ? A.start[xhi + 1 + ny * resX] : 0u;
+        rk0[j] = ok ? A.start[V.cellOffset + xlo + ny * resX] : 0u;
+        rk1[j] = ok ? A.start[V.cellOffset + xhi + 1 + ny * resX] : 0u;
     }
 }
 
@@ -427,33 +426,34 @@ __device__ __forceinline__ float4 projectCore(const StepArgs& A, const Venue& ve
 
 // One Jacobi sweep for slot s reading `in` from global memory
 template <class Venue>
-__device__ __forceinline__ float4 projectSlot(const StepArgs& A, const Venue& ven, const float4* __restrict__ in, int s) {
+__device__ __forceinline__ float4 projectSlot(const StepArgs& A, const VenueArgs& V, const Venue& ven, const float4* __restrict__ in, int s) {
     constexpr bool kUniform = Body<Venue>::kUniform;
     const float4 b = in[s];
     if (b.w < 0.0f) return b;   // parked this step
     uint32_t rk0[3], rk1[3];
-    sweepRows(A, A.skey[s], rk0, rk1);
+    sweepRows(A, V, A.skey[s], rk0, rk1);
     const float ri = kUniform ? A.P.body_radius : A.prm[s].x;
     return projectCore(A, ven, b, s, ri, rk0, rk1, A.plane[s], GlobalNbr{in, A.prm});
 }
 
-template <class Venue>
+template <class Venue, bool kB>
 __device__ __forceinline__ void projectItem(const StepArgs& A, int s, int inBuf) {
     if (s >= int(A.start[A.V.ncells])) return;
-    const Venue ven{A.P, A.V};
-    A.proj[inBuf ^ 1][s] = projectSlot(A, ven, A.proj[inBuf], s);
+    const VenueArgs& V = venueOfSlot<kB>(A, s);
+    const Venue ven{A.P, V};
+    A.proj[inBuf ^ 1][s] = projectSlot(A, V, ven, A.proj[inBuf], s);
 }
 
-template <class Venue>
+template <class Venue, bool kB>
 __global__ void __launch_bounds__(128) k_project(StepArgs A, int inBuf) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < A.n) projectItem<Venue>(A, s, inBuf);
+    if (s < A.n) projectItem<Venue, kB>(A, s, inBuf);
 }
 
 // The final pass of an active slot whose last sweep gave b (cpu_crowd_sim.cpp:835-866)
 // Returns the agent's cell key for the next step (INACTIVE_CELL once parked; a NaN position hashes as (0, 0, 0, 1))
 template <class Venue>
-__device__ __forceinline__ uint32_t finalActive(const StepArgs& A, const Venue& ven, int s, float4 b) {
+__device__ __forceinline__ uint32_t finalActive(const StepArgs& A, const VenueArgs& V, const Venue& ven, int s, float4 b) {
     const SwarmParams& P = A.P;
     const uint32_t self = A.sid[s];
     if (b.w < 0.0f) {   // parked this step
@@ -478,7 +478,7 @@ __device__ __forceinline__ uint32_t finalActive(const StepArgs& A, const Venue& 
     A.stateOut[2 * size_t(self)] = out;
     A.stateOut[2 * size_t(self) + 1] = make_float4(nv.x, nv.y, nv.z, length(nv));
     A.contacts[self] = uint8_t(contact);
-    return cellID(A.V, isnan(out.x) ? make_float4(0.0f, 0.0f, 0.0f, 1.0f) : out);
+    return cellID(V, isnan(out.x) ? make_float4(0.0f, 0.0f, 0.0f, 1.0f) : out);
 }
 
 // An agent evacuated before this step: carried over (its next key: inactive)
@@ -489,18 +489,19 @@ __device__ __forceinline__ void finalInactive(const StepArgs& A, int s) {
     A.contacts[self] = 0;
 }
 
-template <class Venue>
+template <class Venue, bool kB>
 __device__ __forceinline__ void finalItem(const StepArgs& A, int s, int inBuf) {
     if (s >= int(A.start[A.V.ncells])) { finalInactive(A, s); return; }
-    const Venue ven{A.P, A.V};
-    const float4 b = A.projectInFinal ? projectSlot(A, ven, A.proj[inBuf], s) : A.proj[inBuf][s];
-    finalActive(A, ven, s, b);
+    const VenueArgs& V = venueOfSlot<kB>(A, s);
+    const Venue ven{A.P, V};
+    const float4 b = A.projectInFinal ? projectSlot(A, V, ven, A.proj[inBuf], s) : A.proj[inBuf][s];
+    finalActive(A, V, ven, s, b);
 }
 
-template <class Venue>
+template <class Venue, bool kB>
 __global__ void __launch_bounds__(128) k_final(StepArgs A, int inBuf) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < A.n) finalItem<Venue>(A, s, inBuf);
+    if (s < A.n) finalItem<Venue, kB>(A, s, inBuf);
 }
 
 // ---- the whole step as one persistent kernel ----
@@ -545,23 +546,27 @@ __device__ __forceinline__ void gridBarrier(const StepArgs& A, unsigned expected
 // The sweeps' neighbour data for the fused kernel, once per step: each active slot's 3 x 3 rows, and each tile of
 // FUSED_THREADS slots' window [lo, hi) -- every slot any of its slots can read (cells c - resX - 1 .. c + resX + 1 of
 // its first and last cells), a contiguous range in key order.
+template <bool kB>
 __device__ __forceinline__ void prepareSweepItem(const StepArgs& A, int s, int nActive, int tile) {
     const uint32_t cid = A.skey[s];
+    const VenueArgs& V = venueOfSlot<kB>(A, s);
     uint32_t rk0[3], rk1[3];
-    sweepRows(A, cid, rk0, rk1);
+    sweepRows(A, V, cid, rk0, rk1);
     A.rowsA[s] = make_uint4(rk0[0], rk1[0], rk0[1], rk1[1]);
     A.rowsB[s] = make_uint2(rk0[2], rk1[2]);
     if (s % tile == 0) {
+        // (a tile spanning instances: each slot's rows lie inside its own instance's cells, within these bounds)
         const int last = min(s + tile, nActive) - 1;
-        const int resX = A.V.resX, ncells = A.V.ncells;
+        const int ncells = A.V.ncells;
         const int c0 = int(cid), c1 = int(A.skey[last]);
-        A.tileWin[s / tile] = make_uint2(A.start[max(c0 - resX - 1, 0)], A.start[min(c1 + resX + 2, ncells)]);
+        const int res0 = V.resX, res1 = venueOfSlot<kB>(A, last).resX;
+        A.tileWin[s / tile] = make_uint2(A.start[max(c0 - res0 - 1, 0)], A.start[min(c1 + res1 + 2, ncells)]);
     }
 }
 
 constexpr int WIN_CAP = 2048;   // slots a tile window may hold in shared memory (40 KB); larger windows read global memory
 
-template <class Venue, bool kPerAgent>
+template <class Venue, bool kPerAgent, bool kB>
 __global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A) {
     constexpr bool kUniform = Body<Venue>::kUniform;
     __shared__ uint32_t warpSums[32];
@@ -573,7 +578,7 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A)
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
     stamp(A, 0);
     if (!A.hashed) {   // (the previous fused step's final pass counted the keys already)
-        for (int base = tid - int(threadIdx.x & 31u); base < n; base += stride) hashItem(A, base + int(threadIdx.x & 31u));
+        for (int base = tid - int(threadIdx.x & 31u); base < n; base += stride) hashItem<kB>(A, base + int(threadIdx.x & 31u));
         gridBarrier(A, gridDim.x);
     }
     const int tiles = (A.V.ncells + 1 + T * SCAN_ITEMS - 1) / (T * SCAN_ITEMS);
@@ -583,17 +588,16 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A)
     gridBarrier(A, gridDim.x);
     for (int i = tid; i < n; i += stride) scatterItem(A, i);
     gridBarrier(A, gridDim.x);
-    for (int s = tid; s < n; s += stride) rankGatherItem<kPerAgent>(A, s);
+    for (int s = tid; s < n; s += stride) rankGatherItem<kPerAgent, kB>(A, s);
     gridBarrier(A, gridDim.x);
     stamp(A, 1);
     const int nActive = int(A.start[A.V.ncells]);
     for (int s = tid; s < n; s += stride) {
-        predictItem<Venue>(A, s);
-        if (s < nActive) prepareSweepItem(A, s, nActive, T);
+        predictItem<Venue, kB>(A, s);
+        if (s < nActive) prepareSweepItem<kB>(A, s, nActive, T);
     }
     gridBarrier(A, gridDim.x);
     stamp(A, 2);
-    const Venue ven{A.P, A.V};
     const int K = A.P.proj_iterations;
     const int activeTiles = (nActive + T - 1) / T;
     // one sweep (or the final pass) over tile t: stage its window, then each slot reads its neighbours from it
@@ -621,6 +625,7 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A)
         }
         __syncthreads();
         if (own && b.w >= 0.0f) {
+            const Venue ven{A.P, venueOfSlot<kB>(A, s)};
             const uint32_t rk0[3] = {ra.x, ra.z, rb.x}, rk1[3] = {ra.y, ra.w, rb.y};
             b = useWin ? projectCore(A, ven, b, s, ri, rk0, rk1, plane, WindowNbr{smPos, smR, win.x})
                        : projectCore(A, ven, b, s, ri, rk0, rk1, plane, GlobalNbr{in, A.prm});
@@ -648,7 +653,10 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A)
         if (A.projectInFinal) sweepTile(t, A.proj[in], b, own);
         else { own = s < nActive; b = own ? A.proj[in][s] : make_float4(0.0f, 0.0f, 0.0f, 0.0f); }
         uint32_t nextKey = INACTIVE_CELL;
-        if (own) nextKey = finalActive(A, ven, s, b);
+        if (own) {
+            const VenueArgs& V = venueOfSlot<kB>(A, s);
+            nextKey = finalActive(A, V, Venue{A.P, V}, s, b);
+        }
         else if (s < n) finalInactive(A, s);
         // the next step's hash, counted here (all lanes of the warp together)
         if (A.hashNext) countKey(A, s < n ? A.sid[s] : 0u, nextKey, s < n);
@@ -671,33 +679,39 @@ namespace {
 inline int blocks(int n, int t) { return (n + t - 1) / t; }
 }
 
-void launch_sort(const StepArgs& A, cudaStream_t st, int64_t* launches) {
+template <bool kB>
+static void sortImpl(const StepArgs& A, cudaStream_t st, int64_t* launches) {
     const int n = A.n;
-    k_hash<<<blocks(n, 256), 256, 0, st>>>(A);
+    k_hash<kB><<<blocks(n, 256), 256, 0, st>>>(A);
     const int tiles = (A.V.ncells + 1 + SCAN_TILE - 1) / SCAN_TILE;
     k_scan_reduce<<<tiles, SCAN_THREADS, 0, st>>>(A);
     k_scan_apply<<<tiles, SCAN_THREADS, 0, st>>>(A);
     k_scatter<<<blocks(n, 256), 256, 0, st>>>(A);
-    if (A.P.uniform_body) k_rank_gather<false><<<blocks(n, 256), 256, 0, st>>>(A);
-    else k_rank_gather<true><<<blocks(n, 256), 256, 0, st>>>(A);
+    if (A.P.uniform_body) k_rank_gather<false, kB><<<blocks(n, 256), 256, 0, st>>>(A);
+    else k_rank_gather<true, kB><<<blocks(n, 256), 256, 0, st>>>(A);
     *launches += 5;
 }
 
-template <class Venue>
+void launch_sort(const StepArgs& A, cudaStream_t st, int64_t* launches) {
+    if (A.venueTable) sortImpl<true>(A, st, launches);
+    else sortImpl<false>(A, st, launches);
+}
+
+template <class Venue, bool kB>
 static void stageImpl(const StepArgs& A, int stage, cudaStream_t st, int64_t* launches) {
     const int n = A.n, K = A.P.proj_iterations;
     if (stage == 1) {
-        k_predict<Venue><<<blocks(n, 128), 128, 0, st>>>(A);
+        k_predict<Venue, kB><<<blocks(n, 128), 128, 0, st>>>(A);
         *launches += 1;
     } else if (stage == 2) {
         int in = 0;
         for (int it = 1; it < K; ++it) {
-            k_project<Venue><<<blocks(n, 128), 128, 0, st>>>(A, in);
+            k_project<Venue, kB><<<blocks(n, 128), 128, 0, st>>>(A, in);
             in ^= 1;
         }
         *launches += K > 1 ? K - 1 : 0;
     } else if (stage == 3) {
-        k_final<Venue><<<blocks(n, 128), 128, 0, st>>>(A, K > 1 ? (K - 1) & 1 : 0);
+        k_final<Venue, kB><<<blocks(n, 128), 128, 0, st>>>(A, K > 1 ? (K - 1) & 1 : 0);
         *launches += 1;
     }
 }
@@ -706,19 +720,21 @@ constexpr int FUSED_SMEM = WIN_CAP * (int(sizeof(float4)) + int(sizeof(float)));
 
 // The fused grid: one block per SM when the state fits (threads = n / SMs rounded up to a warp, 128..512), else as
 // many blocks as stay resident, each taking several tiles per phase
-template <class Venue, bool kPerAgent>
+template <class Venue, bool kPerAgent, bool kB>
 static cudaError_t fusedImpl(const StepArgs& A, cudaStream_t st) {
     static int sms = 0;
     if (!sms) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaFuncSetAttribute(k_step_fused<Venue, kPerAgent>, cudaFuncAttributeMaxDynamicSharedMemorySize, FUSED_SMEM);
+        cudaFuncSetAttribute(k_step_fused<Venue, kPerAgent, kB>, cudaFuncAttributeMaxDynamicSharedMemorySize, FUSED_SMEM);
     }
-    int threads = ((A.n + sms - 1) / sms + 31) / 32 * 32;
+    int threads = A.fusedThreads > 0 ? A.fusedThreads : ((A.n + sms - 1) / sms + 31) / 32 * 32;
     threads = threads < 128 ? 128 : (threads > FUSED_MAX_THREADS ? FUSED_MAX_THREADS : threads);
+    threads = (threads + 31) / 32 * 32;
     int perSm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_step_fused<Venue, kPerAgent>, threads, FUSED_SMEM);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_step_fused<Venue, kPerAgent, kB>, threads, FUSED_SMEM);
+    if (A.fusedBlocksPerSm > 0 && A.fusedBlocksPerSm < perSm) perSm = A.fusedBlocksPerSm;
     const int resident = perSm * sms;
     if (resident <= 0) return cudaErrorCooperativeLaunchTooLarge;
     const int want = blocks(A.n, threads);
@@ -732,18 +748,20 @@ static cudaError_t fusedImpl(const StepArgs& A, cudaStream_t st) {
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_step_fused<Venue, kPerAgent>, A);
+    return cudaLaunchKernelEx(&cfg, k_step_fused<Venue, kPerAgent, kB>, A);
 }
 
 cudaError_t launch_step_fused(const StepArgs& A, cudaStream_t st) {
-    if (A.V.kind == SWARM_VENUE_STADIUM) return fusedImpl<Stadium, false>(A, st);
-    return fusedImpl<GridVenue, true>(A, st);
+    if (A.V.kind == SWARM_VENUE_STADIUM) return fusedImpl<Stadium, false, false>(A, st);
+    if (A.venueTable) return fusedImpl<GridVenue, true, true>(A, st);
+    return fusedImpl<GridVenue, true, false>(A, st);
 }
 
 void launch_stage(const StepArgs& A, int stage, cudaStream_t st, int64_t* launches) {
     if (stage == 0) { launch_sort(A, st, launches); return; }
-    if (A.V.kind == SWARM_VENUE_STADIUM) stageImpl<Stadium>(A, stage, st, launches);
-    else stageImpl<GridVenue>(A, stage, st, launches);
+    if (A.V.kind == SWARM_VENUE_STADIUM) stageImpl<Stadium, false>(A, stage, st, launches);
+    else if (A.venueTable) stageImpl<GridVenue, true>(A, stage, st, launches);
+    else stageImpl<GridVenue, false>(A, stage, st, launches);
 }
 
 }  // namespace swarm_gpu

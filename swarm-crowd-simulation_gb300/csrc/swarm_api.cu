@@ -52,6 +52,7 @@ struct SwarmSim {
     unsigned long long* stamps = nullptr;
     bool fused = true;          // the whole step as one persistent kernel when the grid fits on the GPU
     int barrierExtra = 0;       // the timeout test's missing block (swarm_test_barrier_timeout)
+    SwarmTuning tuning{1, 0, 0, 0.0f};   // the launch configuration (swarm_autotune / swarm_set_tuning)
     bool counted = false;       // the counts hold the current state's keys (a fused step's final pass counted them)
     // safety metrics (swarm_metrics_enable)
     int metricRes = 0;
@@ -64,6 +65,12 @@ struct SwarmSim {
     float4* mBoxes = nullptr;
     std::vector<float> exitBoxesHost;
     int enqueueMetrics(int in);
+    // batched instances (swarm_batch_create)
+    int instances = 0;
+    swarm_gpu::VenueArgs* dVenueTable = nullptr;
+    uint32_t* dInstAgent = nullptr;
+    uint32_t* dInstSlot = nullptr;
+    std::vector<int> instStart;   // first agent of each instance, + the total
     float *dSdf = nullptr, *dWall = nullptr, *dNav = nullptr, *dFloor = nullptr, *dSpeed = nullptr;
     int ncells = 0;
     // execution
@@ -148,6 +155,11 @@ StepArgs SwarmSim::args(int in) const {
     A.pos0 = pos0; A.vel0 = vel0; A.prm = prm; A.proj[0] = proj0; A.proj[1] = proj1;
     A.vel1 = vel1; A.plane = plane; A.ctc = ctc; A.rowsA = rowsA; A.rowsB = rowsB; A.tileWin = tileWin; A.err = errFlag; A.barrier = barrier; A.barrierExtra = barrierExtra;
     A.stamps = timing ? stamps : nullptr;
+    A.fusedThreads = tuning.threads;
+    A.fusedBlocksPerSm = tuning.blocks_per_sm;
+    A.venueTable = dVenueTable;
+    A.instAgent = dInstAgent;
+    A.instSlot = dInstSlot;
     return A;
 }
 
@@ -263,6 +275,81 @@ int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capac
     return SWARM_OK;
 }
 
+int swarm_batch_create(const SwarmParams* params, const SwarmVenue* venues, const int* counts, int m, SwarmHandle* out) {
+    if (!params || !venues || !counts || !out || m <= 0) return SWARM_E_INVALID;
+    *out = nullptr;
+    if (params->proj_iterations < 0 || params->perc_ring < 1 || params->perc_ring > 4) return SWARM_E_INVALID;
+    size_t total = 0, cells = 0, nWall = 0, nNav = 0;
+    for (int i = 0; i < m; ++i) {
+        const SwarmVenue& V = venues[i];
+        if (V.kind != SWARM_VENUE_GRID || counts[i] <= 0 || !V.wall_sdf || !V.nav_dist || V.floor_height || V.speed_factor ||
+            V.grid_res_x <= 0 || V.grid_res_y <= 0 || V.wall_nx < 2 || V.wall_ny < 2 || V.nav_nx < 2 || V.nav_ny < 2 ||
+            !(V.wall_h > 0.0f) || !(V.nav_h > 0.0f) || !(V.domain_span_x > 0.0f) || !(V.domain_span_y > 0.0f))
+            return SWARM_E_INVALID;   // plain grid venues only (no floor heights or speed factors in a batch)
+        total += size_t(counts[i]);
+        cells += size_t(V.grid_res_x) * size_t(V.grid_res_y);
+        nWall += size_t(V.wall_nx) * size_t(V.wall_ny);
+        nNav += size_t(V.nav_nx) * size_t(V.nav_ny);
+    }
+    if (total > size_t(INT32_MAX) / 2 || cells > 2000000000u) return SWARM_E_INVALID;
+    // the handle: a grid venue whose key space is every instance's cells, one after another
+    SwarmVenue all = venues[0];
+    all.grid_res_x = int(cells);
+    all.grid_res_y = 1;
+    all.floor_height = all.speed_factor = nullptr;
+    all.n_exits = 0;
+    all.exit_boxes = nullptr;
+    SwarmHandle h = nullptr;
+    const int rc = swarm_create(params, &all, int(total), &h);
+    if (rc != SWARM_OK) return rc;
+    // every instance's fields in two device buffers, and its venue record
+    float *dWall = nullptr, *dNav = nullptr;
+    if (!devAlloc(h, &dWall, nWall) || !devAlloc(h, &dNav, nNav) || !devAlloc(h, &h->dVenueTable, size_t(m)) ||
+        !devAlloc(h, &h->dInstAgent, total) || !devAlloc(h, &h->dInstSlot, total)) {
+        swarm_destroy(h);
+        return SWARM_E_OOM;
+    }
+    std::vector<swarm_gpu::VenueArgs> table(static_cast<size_t>(m));
+    std::vector<uint32_t> inst(total);
+    size_t oWall = 0, oNav = 0, oAgent = 0;
+    uint32_t oCell = 0;
+    h->instStart.clear();
+    for (int i = 0; i < m; ++i) {
+        const SwarmVenue& V = venues[i];
+        const size_t w = size_t(V.wall_nx) * size_t(V.wall_ny), nv = size_t(V.nav_nx) * size_t(V.nav_ny);
+        if (cudaMemcpy(dWall + oWall, V.wall_sdf, w * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(dNav + oNav, V.nav_dist, nv * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+            swarm_destroy(h);
+            return SWARM_E_CUDA;
+        }
+        swarm_gpu::VenueArgs& a = table[size_t(i)];
+        a = swarm_gpu::VenueArgs{};
+        a.kind = SWARM_VENUE_GRID;
+        a.resX = V.grid_res_x; a.resY = V.grid_res_y; a.ncells = V.grid_res_x * V.grid_res_y;
+        a.dminX = V.domain_min_x; a.dminY = V.domain_min_y; a.dspanX = V.domain_span_x; a.dspanY = V.domain_span_y;
+        a.dmaxX = V.domain_min_x + V.domain_span_x; a.dmaxY = V.domain_min_y + V.domain_span_y;
+        a.exloX = V.exit_lo_x; a.exloY = V.exit_lo_y; a.exhiX = V.exit_hi_x; a.exhiY = V.exit_hi_y; a.exMaxZ = V.exit_max_z;
+        a.wall = dWall + oWall; a.wnx = V.wall_nx; a.wny = V.wall_ny; a.wox = V.wall_origin_x; a.woy = V.wall_origin_y;
+        a.winv = 1.0f / V.wall_h;
+        a.nav = dNav + oNav; a.nnx = V.nav_nx; a.nny = V.nav_ny; a.nox = V.nav_origin_x; a.noy = V.nav_origin_y;
+        a.ninv = 1.0f / V.nav_h;
+        a.cellOffset = oCell;
+        h->instStart.push_back(int(oAgent));
+        for (int k = 0; k < counts[i]; ++k) inst[oAgent + size_t(k)] = uint32_t(i);
+        oWall += w; oNav += nv; oAgent += size_t(counts[i]);
+        oCell += uint32_t(V.grid_res_x * V.grid_res_y);
+    }
+    h->instStart.push_back(int(total));
+    if (cudaMemcpy(h->dVenueTable, table.data(), table.size() * sizeof(table[0]), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(h->dInstAgent, inst.data(), total * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+        swarm_destroy(h);
+        return SWARM_E_CUDA;
+    }
+    h->instances = m;
+    *out = h;
+    return SWARM_OK;
+}
+
 int swarm_destroy(SwarmHandle h) {
     if (!h) return SWARM_E_INVALID;
     cudaStreamSynchronize(h->stream);
@@ -285,6 +372,7 @@ int swarm_last_error(SwarmHandle h, char* buf, int len) {
 
 static int uploadImpl(SwarmHandle h, const float* boids, int n, cudaMemcpyKind kind) {
     if (!h || !boids) return SWARM_E_INVALID;
+    if (h->instances && n != h->capacity) return h->fail(SWARM_E_INVALID, "a batch's state holds every instance's agents");
     if (n <= 0 || n > h->capacity) return h->fail(SWARM_E_INVALID, "agent count " + std::to_string(n) + " outside 1.." + std::to_string(h->capacity));
     if (n != h->n) h->dropGraphs();
     if (h->counted && !h->clearCounts()) return h->fail(SWARM_E_CUDA, "clearing the counts");
@@ -355,6 +443,7 @@ int swarm_set_graph(SwarmHandle h, int enabled) {
 
 int swarm_metrics_enable(SwarmHandle h, int res, const uint32_t* threshold_mass) {
     if (!h || !threshold_mass || res <= 0 || res % 16 != 0 || res > 4096) return SWARM_E_INVALID;
+    if (h->instances) return h->fail(SWARM_E_INVALID, "metrics are per venue; a batch has many");
     if (!h->metricRes) {
         const size_t cells = size_t(res) * size_t(res), N = size_t(h->capacity);
         const size_t boxes = std::max<size_t>(h->exitBoxesHost.size() / 4, 1);
@@ -396,6 +485,75 @@ int swarm_metrics_read(SwarmHandle h, SwarmMetricCounters* counters, SwarmMetric
         cudaMemcpy(evac_step, h->mEvac, size_t(n) * 4, cudaMemcpyDeviceToHost);
     }
     return cudaOk(h, cudaGetLastError(), "metrics read") ? SWARM_OK : SWARM_E_CUDA;
+}
+
+static int stepImpl(SwarmHandle h, int steps);
+
+int swarm_set_tuning(SwarmHandle h, const SwarmTuning* t) {
+    if (!h || !t || t->threads < 0 || t->threads > 512 || t->blocks_per_sm < 0) return SWARM_E_INVALID;
+    h->tuning = *t;
+    h->fused = t->fused != 0;
+    h->dropGraphs();
+    return SWARM_OK;
+}
+
+int swarm_autotune(SwarmHandle h, int steps, SwarmTuning* best) {
+    if (!h || steps <= 0) return SWARM_E_INVALID;
+    if (!h->hasState) return h->fail(SWARM_E_STATE, "autotune needs a state (upload one first)");
+    // the candidates: the fused step at several block shapes, and the per-phase kernels replayed from graphs
+    std::vector<SwarmTuning> cands;
+    for (int threads : {0, 128, 256, 512})
+        for (int bps : {0, 1, 2}) cands.push_back(SwarmTuning{1, threads, bps, 0.0f});
+    cands.push_back(SwarmTuning{0, 0, 0, 0.0f});
+    // snapshot of the state (and the metrics' running sums are not touched: the trials run with metrics off)
+    float4* snap = nullptr;
+    const size_t bytes = size_t(h->n) * 32;
+    if (cudaMalloc(&snap, bytes) != cudaSuccess) return h->fail(SWARM_E_OOM, "autotune snapshot");
+    cudaMemcpyAsync(snap, h->state[h->readIdx], bytes, cudaMemcpyDeviceToDevice, h->stream);
+    const int metricRes = h->metricRes;
+    const bool graph = h->useGraph, timing = h->timing;
+    const SwarmTuning keep = h->tuning;
+    h->metricRes = 0;
+    h->useGraph = true;
+    h->timing = false;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    SwarmTuning top{};
+    top.ms_per_step = 1e30f;
+    int rc = SWARM_OK;
+    for (SwarmTuning c : cands) {
+        h->tuning = c;
+        h->fused = c.fused != 0;
+        h->dropGraphs();
+        cudaMemcpyAsync(h->state[h->readIdx], snap, bytes, cudaMemcpyDeviceToDevice, h->stream);
+        if (h->counted && !h->clearCounts()) { rc = SWARM_E_CUDA; break; }
+        if ((rc = stepImpl(h, 1)) != SWARM_OK) break;   // warm-up (graph capture)
+        cudaEventRecord(e0, h->stream);
+        if ((rc = stepImpl(h, steps)) != SWARM_OK) break;
+        cudaEventRecord(e1, h->stream);
+        if (cudaEventSynchronize(e1) != cudaSuccess) { rc = SWARM_E_CUDA; break; }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        c.ms_per_step = ms / float(steps);
+        if (c.ms_per_step < top.ms_per_step) top = c;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    // the state as it was, the best configuration in force
+    cudaMemcpyAsync(h->state[h->readIdx], snap, bytes, cudaMemcpyDeviceToDevice, h->stream);
+    if (h->counted) h->clearCounts();
+    cudaStreamSynchronize(h->stream);
+    cudaFree(snap);
+    h->metricRes = metricRes;
+    h->useGraph = graph;
+    h->timing = timing;
+    h->dropGraphs();
+    if (rc != SWARM_OK) { h->tuning = keep; h->fused = keep.fused != 0; return rc; }
+    h->tuning = top;
+    h->fused = top.fused != 0;
+    if (best) *best = top;
+    return swarm_synchronize(h);
 }
 
 int swarm_test_barrier_timeout(SwarmHandle h) {

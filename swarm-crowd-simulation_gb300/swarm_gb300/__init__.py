@@ -13,7 +13,7 @@ import os
 import numpy as np
 
 from .abi import (METRIC_CELL_WORDS, SWARM_OK, SWARM_VENUE_GRID, SWARM_VENUE_STADIUM, SwarmMetricCounters, SwarmParams,
-                  SwarmStageTimes, SwarmVenue, fptr)
+                  SwarmStageTimes, SwarmTuning, SwarmVenue, fptr)
 
 PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG_DIR, "libswarm_gb300.so")
@@ -38,6 +38,7 @@ def lib():
             "swarm_params_si": [C.POINTER(SwarmParams)],
             "swarm_create": [C.POINTER(SwarmParams), C.POINTER(SwarmVenue), C.c_int, C.POINTER(H)],
             "swarm_destroy": [H],
+            "swarm_batch_create": [C.POINTER(SwarmParams), C.c_void_p, C.c_void_p, C.c_int, C.POINTER(H)],
             "swarm_set_stream": [H, C.c_void_p],
             "swarm_last_error": [H, C.c_char_p, C.c_int],
             "swarm_upload_state": [H, C.POINTER(C.c_float), C.c_int],
@@ -51,6 +52,8 @@ def lib():
             "swarm_set_drive_table": [H, C.POINTER(C.c_float), C.c_int],
             "swarm_set_graph": [H, C.c_int],
             "swarm_set_fused": [H, C.c_int],
+            "swarm_set_tuning": [H, C.POINTER(SwarmTuning)],
+            "swarm_autotune": [H, C.c_int, C.POINTER(SwarmTuning)],
             "swarm_test_barrier_timeout": [H],
             "swarm_synchronize": [H],
             "swarm_get_grid": [H, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_int],
@@ -181,6 +184,21 @@ class CrowdSim:
         """One persistent kernel per step (True, the default) or one kernel per phase (False)."""
         self._ck(lib().swarm_set_fused(self._h, int(bool(enabled))), "set_fused")
 
+    def set_tuning(self, fused=True, threads=0, blocks_per_sm=0):
+        t = SwarmTuning(int(bool(fused)), int(threads), int(blocks_per_sm), 0.0)
+        self._ck(lib().swarm_set_tuning(self._h, C.byref(t)), "set_tuning")
+
+    def autotune(self, steps=3):
+        """Times each launch configuration from the current state (restored), keeps the fastest; returns it."""
+        t = SwarmTuning()
+        self._ck(lib().swarm_autotune(self._h, int(steps), C.byref(t)), "autotune")
+        return {"fused": bool(t.fused), "threads": t.threads, "blocks_per_sm": t.blocks_per_sm,
+                "ms_per_step": t.ms_per_step}
+
+    def download_device(self, dst_ptr):
+        """The state into device memory at dst_ptr (n x 8 floats)."""
+        self._ck(lib().swarm_download_state_device(self._h, C.c_void_p(dst_ptr), self.n), "download_device")
+
     def set_timing(self, enabled=True):
         self._ck(lib().swarm_set_timing(self._h, int(bool(enabled))), "set_timing")
 
@@ -236,5 +254,25 @@ class CrowdSim:
         return out
 
 
-__all__ = ["CrowdSim", "Venue", "SwarmError", "lib", "params_reference", "params_si", "SwarmParams", "SwarmVenue",
+class BatchSim(CrowdSim):
+    """Many independent grid venues packed into one simulation (swarm_batch_create): the state is every instance's
+    agents one after another; instance i occupies [starts[i], starts[i + 1])."""
+
+    def __init__(self, params, venues, counts):
+        self.params = params
+        self.venue = None
+        self.venues = list(venues)
+        counts = np.ascontiguousarray(counts, dtype=np.int32)
+        arr = (SwarmVenue * len(self.venues))(*[v.struct for v in self.venues])
+        self._arr = arr
+        h = C.c_void_p()
+        _check(lib().swarm_batch_create(C.byref(params), C.cast(arr, C.c_void_p), counts.ctypes.data_as(C.c_void_p),
+                                        len(self.venues), C.byref(h)), "swarm_batch_create")
+        self._h = h
+        self.capacity = int(counts.sum())
+        self.starts = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+        self.n = 0
+
+
+__all__ = ["CrowdSim", "BatchSim", "Venue", "SwarmError", "lib", "params_reference", "params_si", "SwarmParams", "SwarmVenue",
            "SWARM_VENUE_GRID", "SWARM_VENUE_STADIUM"]

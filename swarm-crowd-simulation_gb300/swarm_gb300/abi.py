@@ -86,3 +86,7 @@ class SwarmMetricCounters(C.Structure):
 
 METRIC_CELL_WORDS = 16   # SwarmMetricCell: 16 uint32 (last_mass, last_speed_mass, peak_mass, occupied_steps,
                          # steps_above[4], mass_steps[2], speed_mass_steps[2], exposure_mass_steps[2], pad[2])
+
+
+class SwarmTuning(C.Structure):
+    _fields_ = [("fused", C.c_int32), ("threads", C.c_int32), ("blocks_per_sm", C.c_int32), ("ms_per_step", C.c_float)]

@@ -138,3 +138,29 @@ def batch_instances(count=256, seed=0, n_lo=1024, n_hi=65536):
         doors = [(int(w), 0.0, float(rng.uniform(1.5, 6.0))) for w in walls]
         out.append({"n": n, "side": side, "lattice": side_agents, "doors": doors, "seed": int(rng.integers(1, 2**62))})
     return out
+
+
+def build_instance(spec):
+    """One instance of batch_instances(): its hall and its lattice spawn (n agents, seeded)."""
+    venue = Venue.hall(spec["side"], spec["side"], spec["doors"], name=f"hall {spec['side']:.1f} m, {spec['n']} agents")
+    nx = spec["lattice"]
+    ny = (spec["n"] + nx - 1) // nx
+    return venue, spawn_lattice(nx, ny, n=spec["n"], seed=spec["seed"])
+
+
+def build_batch(count=256, seed=0, n_lo=1024, n_hi=65536, threads=None):
+    """The batched workload: (venues, boids, radius, v0, counts), agents of all instances one after another. The
+    instances are built on a thread pool (the native builders release the interpreter lock)."""
+    import concurrent.futures as cf
+    import os
+    specs = batch_instances(count, seed, n_lo, n_hi)
+    with cf.ThreadPoolExecutor(max_workers=threads or min(32, os.cpu_count() or 4)) as ex:
+        built = list(ex.map(build_instance, specs))
+    venues, bs, rs, vs, counts = [], [], [], [], []
+    for spec, (v, (b, r, v0)) in zip(specs, built):
+        venues.append(v)
+        bs.append(b)
+        rs.append(r)
+        vs.append(v0)
+        counts.append(spec["n"])
+    return venues, np.concatenate(bs), np.concatenate(rs), np.concatenate(vs), np.array(counts, np.int32)
