@@ -552,6 +552,7 @@ int swarm_autotune(SwarmHandle h, int steps, SwarmTuning* best) {
     if (rc != SWARM_OK) { h->tuning = keep; h->fused = keep.fused != 0; return rc; }
     h->tuning = top;
     h->fused = top.fused != 0;
+    if (!h->fused) h->useGraph = true;   // the per-phase candidate was timed replaying graphs
     if (best) *best = top;
     return swarm_synchronize(h);
 }
