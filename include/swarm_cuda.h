@@ -286,6 +286,36 @@ int swarm_metrics_read(SwarmHandle h, SwarmMetricCounters* counters, SwarmMetric
  * the wall SDF is positive, inside the exit line); cells under 0.1 m^2 never reach a threshold. */
 int swarm_metric_thresholds_grid(const SwarmVenue* venue, int res, uint32_t* threshold_mass);
 
+/* ---- the adjoint: gradients of an evacuation loss ----
+ * No counterpart in the reference, which has no differentiation. The loss of `steps` steps from the handle's state:
+ *   SWARM_LOSS_NAV_DISTANCE   L = dt * sum_{t = 1..steps} sum_{i active after step t} D(p_i(t)),
+ * D the bilinear sample of the venue's geodesic distance grid (the time-integrated distance to the exits). Its
+ * gradient with respect to each agent's radius r_i and desired speed v0_i and to the relaxation time tau (the model
+ * reads tau and relax_step = exp(-dt / tau)) comes from the hand-written adjoint of the step: branches frozen at the
+ * forward's choices (contact sets, the headway argmin, clamps, wall passes), the forward state checkpointed every
+ * ckpt_every steps and recomputed, with a tape, one segment at a time while the segments are reversed. */
+#define SWARM_LOSS_NAV_DISTANCE 0
+typedef struct SwarmLossSpec {
+    int32_t kind;                 /* SWARM_LOSS_NAV_DISTANCE */
+    int32_t pad;
+} SwarmLossSpec;
+typedef struct SwarmAdjointStats {
+    float ms_checkpoint;          /* the forward pass that stores the checkpoints */
+    float ms_recompute;           /* the segments' taped forward */
+    float ms_reverse;             /* the reverse steps */
+    float ms_total;
+    int64_t launches;             /* kernels launched */
+    int64_t tape_bytes;           /* device memory of the tape and checkpoints */
+} SwarmAdjointStats;
+/* Grid venues, one instance, no drive table, wall_passes <= 5. The handle's state is left as it was. loss_out gets L;
+ * dL_dv0 and dL_dr (n each, agent order) and dL_dtau (1) the gradient; stats (may be NULL) the pass times, measured
+ * with events on the handle's stream. */
+int swarm_adjoint_run(SwarmHandle h, const SwarmLossSpec* loss, int steps, int ckpt_every, double* loss_out,
+                      float* dL_dv0, float* dL_dr, float* dL_dtau, SwarmAdjointStats* stats);
+/* Sets the relaxation time: tau_relax = tau and relax_step = exp(-dt / tau) (rounded once from double), the
+ * parameterisation the adjoint differentiates. No reference counterpart (the reference fixes tau at build time). */
+int swarm_set_relaxation_time(SwarmHandle h, float tau);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif

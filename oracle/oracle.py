@@ -49,6 +49,9 @@ def lib():
         L.oracle_get_grid.argtypes = [V, V, V]
         L.oracle_get_cells.argtypes = [V, V, C.c_int]
         L.oracle_get_contacts.argtypes = [V, V]
+        L.grad_eval.restype = C.c_int
+        L.grad_eval.argtypes = [C.c_int, V, V, V, C.c_int, V, V, C.c_double, C.c_int, C.c_int, C.c_int, V, V, V, V, V, V, V]
+        L.grad_last_error.restype = C.c_char_p
         _o = L
     return _o
 
@@ -119,6 +122,38 @@ class OracleSim:
         out = np.empty(self.n, np.uint8)
         lib().oracle_get_contacts(self._h, _p(out))
         return out
+
+
+def grad_eval(prec, params, venue_struct, state, radius, v0, tau, steps, dirs=None, threads=0, want_state=False):
+    """The loss L = dt * sum_t sum_i D(p_i(t)) of `steps` steps from `state` (swarm_grad.cpp), its derivatives along
+    directions and the run's branch signature.
+
+    prec 32: float arithmetic (bit-exact with the step); prec 64: double. dirs: None, or (dr, dv0, dtau) with dr, dv0
+    of shape (k, n) and dtau of shape (k,), k <= 8 (tangents in double). Returns (loss, dloss (k,) or None, signature,
+    end state (n, 8) float32 or None).
+    """
+    b = np.ascontiguousarray(state, dtype=np.float32).reshape(-1, 8)
+    n = b.shape[0]
+    r = np.ascontiguousarray(radius, dtype=np.float64)
+    v = np.ascontiguousarray(v0, dtype=np.float64)
+    loss = np.zeros(1, np.float64)
+    sig = np.zeros(1, np.uint64)
+    out = np.empty((n, 8), np.float32) if want_state else None
+    nt = 0
+    dr = dv = dt = dl = None
+    if dirs is not None:
+        dr = np.ascontiguousarray(np.atleast_2d(dirs[0]), dtype=np.float64)
+        dv = np.ascontiguousarray(np.atleast_2d(dirs[1]), dtype=np.float64)
+        dt = np.ascontiguousarray(np.atleast_1d(dirs[2]), dtype=np.float64)
+        nt = dt.shape[0]
+        assert dr.shape == (nt, n) and dv.shape == (nt, n) and 1 <= nt <= 8
+        dl = np.zeros(nt, np.float64)
+    pp = lambda a: None if a is None else _p(a)
+    rc = lib().grad_eval(int(prec), C.byref(params), C.byref(venue_struct), _p(b), n, _p(r), _p(v), float(tau), int(steps),
+                         int(threads), nt, pp(dr), pp(dv), pp(dt), _p(loss), pp(dl), _p(sig), pp(out))
+    if rc != 0:
+        raise RuntimeError("grad_eval: " + lib().grad_last_error().decode())
+    return float(loss[0]), dl, int(sig[0]), out
 
 
 class OracleMetrics:

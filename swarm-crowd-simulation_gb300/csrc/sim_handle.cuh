@@ -1,0 +1,95 @@
+// The handle behind the C ABI of include/swarm_cuda.h (swarm_api.cu; the adjoint's entry, adjoint_api.cu).
+#pragma once
+
+#include "../../include/swarm_cuda.h"
+#include "step_args.cuh"
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+struct SwarmAdjoint;   // the adjoint's buffers (adjoint_api.cu), made on first use
+void swarm_adjoint_free(SwarmAdjoint* a);
+
+struct SwarmSim {
+    SwarmParams P{};
+    SwarmVenue V{};
+    int device = 0;
+    int capacity = 0;
+    int n = 0;
+    int readIdx = 0;
+    bool hasState = false;
+    cudaStream_t ownStream = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    // device buffers
+    float4* state[2] = {nullptr, nullptr};
+    float2* aparam = nullptr;
+    float2* drive = nullptr;
+    bool driveOn = false;
+    uint8_t* contacts = nullptr;
+    uint32_t *key = nullptr, *rank = nullptr, *count = nullptr, *start = nullptr, *sidTmp = nullptr, *sid = nullptr, *skey = nullptr;
+    uint2* cells = nullptr;
+    uint32_t* tileSums = nullptr;
+    float4 *pos0 = nullptr, *vel0 = nullptr, *proj0 = nullptr, *proj1 = nullptr, *vel1 = nullptr, *plane = nullptr;
+    float2* prm = nullptr;
+    uint8_t* ctc = nullptr;
+    uint4* rowsA = nullptr;
+    uint2* rowsB = nullptr;
+    uint2* tileWin = nullptr;
+    int* errFlag = nullptr;
+    unsigned* barrier = nullptr;
+    unsigned long long* stamps = nullptr;
+    bool fused = true;          // the whole step as one persistent kernel when the grid fits on the GPU
+    int barrierExtra = 0;       // the timeout test's missing block (swarm_test_barrier_timeout)
+    SwarmTuning tuning{1, 0, 0, 0.0f};   // the launch configuration (swarm_autotune / swarm_set_tuning)
+    bool counted = false;       // the counts hold the current state's keys (a fused step's final pass counted them)
+    // safety metrics (swarm_metrics_enable)
+    int metricRes = 0;
+    uint32_t metricStep = 0;
+    SwarmMetricCounters* mCounters = nullptr;
+    uint32_t* mEvac = nullptr;
+    uint2* mMass = nullptr;
+    uint4* mThr = nullptr;
+    SwarmMetricCell* mCells = nullptr;
+    float4* mBoxes = nullptr;
+    std::vector<float> exitBoxesHost;
+    int enqueueMetrics(int in);
+    // batched instances (swarm_batch_create)
+    int instances = 0;
+    swarm_gpu::VenueArgs* dVenueTable = nullptr;
+    uint32_t* dInstAgent = nullptr;
+    uint32_t* dInstSlot = nullptr;
+    std::vector<int> instStart;   // first agent of each instance, + the total
+    float *dSdf = nullptr, *dWall = nullptr, *dNav = nullptr, *dFloor = nullptr, *dSpeed = nullptr;
+    int ncells = 0;
+    // execution
+    bool useGraph = false;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};        // a whole step, per state half read
+    cudaGraphExec_t stageGraph[2][4] = {};                  // its four stages (timing on)
+    bool timing = false;
+    cudaEvent_t ev[6] = {};
+    SwarmStageTimes times{};
+    bool timesValid = false;
+    int64_t launches = 0;
+    std::vector<void*> allocs;
+    SwarmAdjoint* adjoint = nullptr;
+
+    swarm_gpu::StepArgs args(int in) const;
+    int fail(int code, const std::string& msg) { err = msg; return code; }
+    // The per-phase path hashes from zeroed counts: drop what a fused final pass counted ahead
+    bool clearCounts() {
+        counted = false;
+        return cudaMemsetAsync(count, 0, (size_t(ncells) + 1) * 4, stream) == cudaSuccess;
+    }
+    void dropGraphs() {
+        for (auto& g : graph) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+        for (auto& row : stageGraph) for (auto& g : row) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    }
+    int enqueueStages(int in, int s0, int s1);
+    int captureStages(int in, int s0, int s1, cudaGraphExec_t* out);
+    ~SwarmSim();
+};
+

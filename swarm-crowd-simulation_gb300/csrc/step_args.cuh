@@ -82,6 +82,11 @@ struct StepArgs {
     const VenueArgs* venueTable;
     const uint32_t* instAgent;
     uint32_t* instSlot;
+    // the adjoint's taped forward (null otherwise): predict's (sep.x, sep.y, sAhead, argmin slot as int bits, -1: none),
+    // one sweep's (relaxed correction before the cap .xy, contact count), the last sweep's result in the final pass
+    float4* tapePred;
+    float4* tapeCorr;
+    float4* tapeQK;
 };
 
 }  // namespace swarm_gpu

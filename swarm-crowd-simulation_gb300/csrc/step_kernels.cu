@@ -219,7 +219,7 @@ __device__ __forceinline__ f2 separationForce(const SwarmParams& P, f3 offset, u
     return magnitude * xy(offset) * (1.0f / sqrtf(dxy2));
 }
 
-template <class Venue, bool kB>
+template <class Venue, bool kB, bool kTape = false>
 __device__ __forceinline__ void predictItem(const StepArgs& A, int s) {
     constexpr bool kUniform = Body<Venue>::kUniform;
     const int nActive = int(A.start[A.V.ncells]);
@@ -234,6 +234,7 @@ __device__ __forceinline__ void predictItem(const StepArgs& A, int s) {
         A.proj[0][s] = make_float4(P.park_coord, P.park_coord, P.park_coord, -1.0f);
         A.vel1[s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         A.ctc[s] = C_EXIT;
+        if constexpr (kTape) A.tapePred[s] = make_float4(0.0f, 0.0f, 1e9f, __int_as_float(-1));
         return;
     }
     const f2 eGoal = goalOf(A, ven, xyz(p), self);
@@ -242,6 +243,7 @@ __device__ __forceinline__ void predictItem(const StepArgs& A, int s) {
     const int cx = int(cid % uint32_t(resX)), cy = int(cid / uint32_t(resX));
     f2 sep{0.0f, 0.0f};
     float sAhead = 1e9f;
+    int jstar = -1;   // the argmin's slot (taped forward only)
     const int R = P.perc_ring;
     // The neighbour rows: a row of cells is one contiguous run of slots, so each row is [start[a], start[b + 1]) and
     // walking it visits the reference's order (cells by x, agents by slot). Cells that cannot hold an agent within
@@ -297,11 +299,15 @@ __device__ __forceinline__ void predictItem(const StepArgs& A, int s) {
                     const f2 eOther = goalOf(A, ven, xyz(op), other);
                     const float aheadOther = dot(xy(offset), eOther);
                     const bool mutual = aheadOther > 0.0f && fabsf(offset.x * eOther.y - offset.y * eOther.x) < dc;
-                    if (!mutual || ahead > aheadOther || (ahead == aheadOther && self > other)) sAhead = key;
+                    if (!mutual || ahead > aheadOther || (ahead == aheadOther && self > other)) {
+                        sAhead = key;
+                        if constexpr (kTape) jstar = int(k);
+                    }
                 }
             }
         }
     }
+    if constexpr (kTape) A.tapePred[s] = make_float4(sep.x, sep.y, sAhead, __int_as_float(jstar));
     float vDes;
     if (kUniform) {
         vDes = sclamp((sAhead - P.body_diam) * P.headway_rate, 0.0f, P.v_max) * length(eGoal);
@@ -344,10 +350,10 @@ __device__ __forceinline__ void predictItem(const StepArgs& A, int s) {
     A.ctc[s] = uint8_t(contact);
 }
 
-template <class Venue, bool kB>
+template <class Venue, bool kB, bool kTape = false>
 __global__ void __launch_bounds__(128) k_predict(StepArgs A) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < A.n) predictItem<Venue, kB>(A, s);
+    if (s < A.n) predictItem<Venue, kB, kTape>(A, s);
 }
 
 // Where a sweep reads its neighbours: global memory, or a tile's window of slots staged in shared memory
@@ -381,9 +387,10 @@ __device__ __forceinline__ void sweepRows(const StepArgs& A, const VenueArgs& V,
 }
 
 // One Jacobi sweep of an unparked slot s at b (cpu_crowd_sim.cpp:781-822 projectSlot); w of the result: displacement
-template <class Venue, class Nbr>
+template <class Venue, class Nbr, bool kTape = false>
 __device__ __forceinline__ float4 projectCore(const StepArgs& A, const Venue& ven, float4 b, int s, float ri,
-                                             const uint32_t* rk0, const uint32_t* rk1, float4 plane, const Nbr& nb) {
+                                             const uint32_t* rk0, const uint32_t* rk1, float4 plane, const Nbr& nb,
+                                             float4* corrOut = nullptr) {
     constexpr bool kUniform = Body<Venue>::kUniform;
     const SwarmParams& P = A.P;
     f2 corr{0.0f, 0.0f};
@@ -411,6 +418,7 @@ __device__ __forceinline__ float4 projectCore(const StepArgs& A, const Venue& ve
         }
     }
     corr = corr * (P.proj_relax / float(smax(nContacts, 1)));
+    if constexpr (kTape) *corrOut = make_float4(corr.x, corr.y, float(nContacts), 0.0f);
     const float len = length(corr);
     if (len > P.proj_max_shift) corr = corr * (P.proj_max_shift / len);
     f3 q = xyz(b);
@@ -425,7 +433,7 @@ __device__ __forceinline__ float4 projectCore(const StepArgs& A, const Venue& ve
 }
 
 // One Jacobi sweep for slot s reading `in` from global memory
-template <class Venue>
+template <class Venue, bool kTape = false>
 __device__ __forceinline__ float4 projectSlot(const StepArgs& A, const VenueArgs& V, const Venue& ven, const float4* __restrict__ in, int s) {
     constexpr bool kUniform = Body<Venue>::kUniform;
     const float4 b = in[s];
@@ -433,21 +441,22 @@ __device__ __forceinline__ float4 projectSlot(const StepArgs& A, const VenueArgs
     uint32_t rk0[3], rk1[3];
     sweepRows(A, V, A.skey[s], rk0, rk1);
     const float ri = kUniform ? A.P.body_radius : A.prm[s].x;
-    return projectCore(A, ven, b, s, ri, rk0, rk1, A.plane[s], GlobalNbr{in, A.prm});
+    return projectCore<Venue, GlobalNbr, kTape>(A, ven, b, s, ri, rk0, rk1, A.plane[s], GlobalNbr{in, A.prm},
+                                                kTape ? A.tapeCorr + s : nullptr);
 }
 
-template <class Venue, bool kB>
+template <class Venue, bool kB, bool kTape = false>
 __device__ __forceinline__ void projectItem(const StepArgs& A, int s, int inBuf) {
     if (s >= int(A.start[A.V.ncells])) return;
     const VenueArgs& V = venueOfSlot<kB>(A, s);
     const Venue ven{A.P, V};
-    A.proj[inBuf ^ 1][s] = projectSlot(A, V, ven, A.proj[inBuf], s);
+    A.proj[inBuf ^ 1][s] = projectSlot<Venue, kTape>(A, V, ven, A.proj[inBuf], s);
 }
 
-template <class Venue, bool kB>
+template <class Venue, bool kB, bool kTape = false>
 __global__ void __launch_bounds__(128) k_project(StepArgs A, int inBuf) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < A.n) projectItem<Venue, kB>(A, s, inBuf);
+    if (s < A.n) projectItem<Venue, kB, kTape>(A, s, inBuf);
 }
 
 // The final pass of an active slot whose last sweep gave b (cpu_crowd_sim.cpp:835-866)
@@ -489,19 +498,20 @@ __device__ __forceinline__ void finalInactive(const StepArgs& A, int s) {
     A.contacts[self] = 0;
 }
 
-template <class Venue, bool kB>
+template <class Venue, bool kB, bool kTape = false>
 __device__ __forceinline__ void finalItem(const StepArgs& A, int s, int inBuf) {
     if (s >= int(A.start[A.V.ncells])) { finalInactive(A, s); return; }
     const VenueArgs& V = venueOfSlot<kB>(A, s);
     const Venue ven{A.P, V};
-    const float4 b = A.projectInFinal ? projectSlot(A, V, ven, A.proj[inBuf], s) : A.proj[inBuf][s];
+    const float4 b = A.projectInFinal ? projectSlot<Venue, kTape>(A, V, ven, A.proj[inBuf], s) : A.proj[inBuf][s];
+    if constexpr (kTape) A.tapeQK[s] = b;
     finalActive(A, V, ven, s, b);
 }
 
-template <class Venue, bool kB>
+template <class Venue, bool kB, bool kTape = false>
 __global__ void __launch_bounds__(128) k_final(StepArgs A, int inBuf) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < A.n) finalItem<Venue, kB>(A, s, inBuf);
+    if (s < A.n) finalItem<Venue, kB, kTape>(A, s, inBuf);
 }
 
 // ---- the whole step as one persistent kernel ----
@@ -755,6 +765,31 @@ cudaError_t launch_step_fused(const StepArgs& A, cudaStream_t st) {
     if (A.V.kind == SWARM_VENUE_STADIUM) return fusedImpl<Stadium, false, false>(A, st);
     if (A.venueTable) return fusedImpl<GridVenue, true, true>(A, st);
     return fusedImpl<GridVenue, true, false>(A, st);
+}
+
+// The adjoint's taped forward step (grid venue, one instance): the sort, then predict into q[0], sweep k from q[k - 1]
+// into q[k] (k = 1 .. K - 1) with its corrections in corr[k], the final pass from q[K - 1] (q[0] when K = 0) with the
+// last sweep's result in qK and its corrections in corr[K]
+void launch_step_taped(const StepArgs& A, float4* const* q, float4* const* corr, float4* qK, float4* pred, cudaStream_t st,
+                       int64_t* launches) {
+    const int n = A.n, K = A.P.proj_iterations;
+    launch_sort(A, st, launches);
+    StepArgs B = A;
+    B.proj[0] = q[0];
+    B.tapePred = pred;
+    k_predict<GridVenue, false, true><<<blocks(n, 128), 128, 0, st>>>(B);
+    for (int it = 1; it < K; ++it) {
+        B.proj[0] = q[it - 1];
+        B.proj[1] = q[it];
+        B.tapeCorr = corr[it];
+        k_project<GridVenue, false, true><<<blocks(n, 128), 128, 0, st>>>(B, 0);
+    }
+    B.proj[0] = q[K > 0 ? K - 1 : 0];
+    B.tapeCorr = K > 0 ? corr[K] : nullptr;
+    B.tapeQK = qK;
+    if (K > 0) k_final<GridVenue, false, true><<<blocks(n, 128), 128, 0, st>>>(B, 0);
+    else k_final<GridVenue, false, false><<<blocks(n, 128), 128, 0, st>>>(B, 0);
+    *launches += 2 + (K > 1 ? K - 1 : 0);
 }
 
 void launch_stage(const StepArgs& A, int stage, cudaStream_t st, int64_t* launches) {

@@ -11,6 +11,10 @@ namespace swarm_gpu {
 void launch_sort(const StepArgs& A, cudaStream_t st, int64_t* launches);
 // stage 0: the sort (hash, scan, scatter, rank + gather); 1: predict; 2: the K - 1 sweeps; 3: the final pass
 void launch_stage(const StepArgs& A, int stage, cudaStream_t st, int64_t* launches);
+// the adjoint's taped forward step (grid venue, one instance): q[0 .. K - 1] the sweeps' inputs, corr[1 .. K] their
+// corrections, qK the last sweep's result, pred predict's separation / headway record
+void launch_step_taped(const StepArgs& A, float4* const* q, float4* const* corr, float4* qK, float4* pred, cudaStream_t st,
+                       int64_t* launches);
 // the whole step as one cooperative persistent kernel (grid barriers between the phases)
 cudaError_t launch_step_fused(const StepArgs& A, cudaStream_t st);
 

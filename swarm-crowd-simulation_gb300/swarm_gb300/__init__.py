@@ -12,8 +12,9 @@ import os
 
 import numpy as np
 
-from .abi import (METRIC_CELL_WORDS, SWARM_OK, SWARM_VENUE_GRID, SWARM_VENUE_STADIUM, SwarmMetricCounters, SwarmParams,
-                  SwarmStageTimes, SwarmTuning, SwarmVenue, fptr)
+from .abi import (METRIC_CELL_WORDS, SWARM_LOSS_NAV_DISTANCE, SWARM_OK, SWARM_VENUE_GRID, SWARM_VENUE_STADIUM,
+                  SwarmAdjointStats, SwarmLossSpec, SwarmMetricCounters, SwarmParams, SwarmStageTimes, SwarmTuning,
+                  SwarmVenue, fptr)
 
 PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG_DIR, "libswarm_gb300.so")
@@ -69,6 +70,10 @@ def lib():
             "swarm_hall_layout": [C.c_void_p, C.POINTER(SwarmVenue)],
             "swarm_hall_fields": [C.c_void_p, C.POINTER(SwarmVenue), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                   C.POINTER(C.c_float)],
+            "swarm_adjoint_run": [H, C.POINTER(SwarmLossSpec), C.c_int, C.c_int, C.POINTER(C.c_double),
+                                  C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                  C.POINTER(SwarmAdjointStats)],
+            "swarm_set_relaxation_time": [H, C.c_float],
             "swarm_spawn_lattice": [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_uint64,
                                     C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
                                     C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)],
@@ -231,6 +236,27 @@ class CrowdSim:
         self._ck(lib().swarm_metrics_read(self._h, C.byref(ctr), cells.ctypes.data_as(C.c_void_p),
                                           evac.ctypes.data_as(C.c_void_p), self.n), "metrics_read")
         return ctr, cells, evac
+
+    # ---- the adjoint ----
+    def set_relaxation_time(self, tau):
+        """tau_relax = tau, relax_step = exp(-dt / tau)."""
+        self._ck(lib().swarm_set_relaxation_time(self._h, float(tau)), "set_relaxation_time")
+
+    def adjoint(self, steps, ckpt_every=20, stats=False):
+        """The evacuation loss L = dt * sum_t sum_i D(p_i(t)) of `steps` steps from the current state (left as it is)
+        and its gradient by the adjoint: (L, dL/dv0 (n,), dL/dr (n,), dL/dtau) [, stats dict]."""
+        spec = SwarmLossSpec(SWARM_LOSS_NAV_DISTANCE, 0)
+        loss = C.c_double()
+        gv = np.empty(self.n, np.float32)
+        gr = np.empty(self.n, np.float32)
+        gt = np.empty(1, np.float32)
+        st = SwarmAdjointStats()
+        self._ck(lib().swarm_adjoint_run(self._h, C.byref(spec), int(steps), int(ckpt_every), C.byref(loss), fptr(gv),
+                                         fptr(gr), fptr(gt), C.byref(st)), "adjoint_run")
+        out = (loss.value, gv, gr, float(gt[0]))
+        if stats:
+            return out + ({k: getattr(st, k) for k, _ in SwarmAdjointStats._fields_},)
+        return out
 
     # ---- inspection ----
     def grid(self):

@@ -70,6 +70,18 @@ class SwarmStageTimes(C.Structure):
                 ("final_pass", _f), ("total", _f)]
 
 
+SWARM_LOSS_NAV_DISTANCE = 0
+
+
+class SwarmLossSpec(C.Structure):
+    _fields_ = [("kind", _i), ("pad", _i)]
+
+
+class SwarmAdjointStats(C.Structure):
+    _fields_ = [("ms_checkpoint", _f), ("ms_recompute", _f), ("ms_reverse", _f), ("ms_total", _f),
+                ("launches", C.c_int64), ("tape_bytes", C.c_int64)]
+
+
 def fptr(a):
     """A float* into a C-contiguous float32 numpy array (None for None)."""
     if a is None:
