@@ -306,6 +306,9 @@ typedef struct SwarmAdjointStats {
     float ms_total;
     int64_t launches;             /* kernels launched */
     int64_t tape_bytes;           /* device memory of the tape and checkpoints */
+    /* the fused reverse's phases (block 0's clock, summed over the steps): final pass, sweeps, predict's own terms,
+     * predict's pair gather; 0 on the per-phase path */
+    float ms_rev_final, ms_rev_sweeps, ms_rev_predict, ms_rev_gather;
 } SwarmAdjointStats;
 /* Grid venues, one instance, no drive table, wall_passes <= 5. The handle's state is left as it was. loss_out gets L;
  * dL_dv0 and dL_dr (n each, agent order) and dL_dtau (1) the gradient; stats (may be NULL) the pass times, measured

@@ -20,7 +20,13 @@
 //                  direction, headway clamp, e_goal (the separation sum and sAhead come from the tape)
 //   k_adj_gather   predict's pair terms (separation, the headway argmin) gathered over the perception disk; writes the
 //                  state adjoint before the step and the radius gradient
+//   k_adj_step_fused  the four as one persistent cooperative launch (K + 2 grid barriers), the neighbour gathers
+//                  split over ADJ_LANES lanes per slot
 #include "adjoint.cuh"
+
+#include <algorithm>
+
+#include <cuda/atomic>
 
 #include "device_math.cuh"
 #include "venue_grid.cuh"
@@ -309,71 +315,87 @@ __device__ f2 sweepOwnBack(const AdjArgs& A, int s, int k, f2 lq, float2* lamCOu
     return l1;
 }
 
-__global__ void __launch_bounds__(ADJ_FINAL_THREADS) k_adj_final(AdjArgs A) {
-    __shared__ double warpSum[ADJ_FINAL_THREADS / 32];
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+// The final pass of slot s reversed; returns D of its result (0 unless it stays active)
+__device__ double adjFinalSlot(const AdjArgs& A, int s) {
     const SwarmParams& P = A.P;
     const VenueArgs& V = A.V;
     const TapeLayout& L = A.L;
-    double dsum = 0.0;
-    if (s < L.n) {
-        const uint32_t id = A.sid[s];
-        if (s >= activeCount(A)) {   // inactive at the step: carried over unchanged
-            A.lamOut[2 * size_t(id)] = A.lamIn[2 * size_t(id)];
-            A.lamOut[2 * size_t(id) + 1] = A.lamIn[2 * size_t(id) + 1];
-        } else {
-            const float4 q0 = A.f4[L.q(0) + size_t(s)];
-            const float4 zero = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (q0.w < 0.0f) {   // parked this step: its result is a constant
-                A.lamQ[s] = zero;
-                A.lamNv[s] = zero;
-                A.lamPOld[s] = zero;
-                A.lamPlane[s] = zero;
-                A.lamR[s] = 0.0f;
-            } else {
-                const GridVenue ven{P, V};
-                const int K = L.K;
-                const float4 b = K > 0 ? A.f4[L.qK() + size_t(s)] : q0;
-                f3 np = xyz(b), nv = xyz(A.f4[L.vel1() + size_t(s)]);
-                const f3 pOld = xyz(A.f4[L.pos0() + size_t(s)]);
-                const float ri = A.prm[s].x;
-                const float4 plane = A.f4[L.plane() + size_t(s)];
-                STape T;
-                T.nops = 0;
-                const bool moved = b.w > 0.0f;
-                if (moved) {
-                    f3 wl;
-                    recResolve(ven, T, pOld, np, nv, plane.w >= PLANE_GROUNDED, wl, ri);
-                }
-                // the loss term of the result, and its adjoint
-                const NavD nd = navD(P, V, xy(np));
-                dsum = double(nd.D);
-                const float4 lp = A.lamIn[2 * size_t(id)], lv = A.lamIn[2 * size_t(id) + 1];
-                f3 lnp{lp.x + P.dt * nd.g.x * nd.sx, lp.y + P.dt * nd.g.y * nd.sy, lp.z};
-                f3 lnv{lv.x, lv.y, lv.z};
-                float lr = 0.0f;
-                f3 lpOld{0.0f, 0.0f, 0.0f};
-                if (moved) revStatics(P, V, T, pOld, ri, f2{0.0f, 0.0f}, 0.0f, lnp, lnv, lr, lpOld);
-                float4 lplane = zero;
-                f2 lq = xy(lnp);
-                if (K > 0) lq = sweepOwnBack(A, s, K, lq, A.lamC[K & 1], plane, lplane);
-                A.lamQ[s] = make_float4(lq.x, lq.y, lnp.z, 0.0f);
-                A.lamNv[s] = make_float4(lnv.x, lnv.y, lnv.z, 0.0f);
-                A.lamPOld[s] = make_float4(lpOld.x, lpOld.y, lpOld.z, 0.0f);
-                A.lamPlane[s] = lplane;
-                A.lamR[s] = lr;
-            }
-        }
+    const uint32_t id = A.sid[s];
+    if (s >= activeCount(A)) {   // inactive at the step: carried over unchanged
+        A.lamOut[2 * size_t(id)] = A.lamIn[2 * size_t(id)];
+        A.lamOut[2 * size_t(id) + 1] = A.lamIn[2 * size_t(id) + 1];
+        return 0.0;
     }
-    // the block's sum of D (fixed order: warp tree, then warps in order)
-    for (int o = 16; o > 0; o >>= 1) dsum += __shfl_down_sync(0xffffffffu, dsum, o);
-    if ((threadIdx.x & 31u) == 0) warpSum[threadIdx.x >> 5] = dsum;
+    const float4 q0 = A.f4[L.q(0) + size_t(s)];
+    const float4 zero = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (q0.w < 0.0f) {   // parked this step: its result is a constant
+        A.lamQ[s] = zero;
+        A.lamNv[s] = zero;
+        A.lamPOld[s] = zero;
+        A.lamPlane[s] = zero;
+        A.lamR[s] = 0.0f;
+        return 0.0;
+    }
+    const GridVenue ven{P, V};
+    const int K = L.K;
+    const float4 b = K > 0 ? A.f4[L.qK() + size_t(s)] : q0;
+    f3 np = xyz(b), nv = xyz(A.f4[L.vel1() + size_t(s)]);
+    const f3 pOld = xyz(A.f4[L.pos0() + size_t(s)]);
+    const float ri = A.prm[s].x;
+    const float4 plane = A.f4[L.plane() + size_t(s)];
+    STape T;
+    T.nops = 0;
+    const bool moved = b.w > 0.0f;
+    if (moved) {
+        f3 wl;
+        recResolve(ven, T, pOld, np, nv, plane.w >= PLANE_GROUNDED, wl, ri);
+    }
+    // the loss term of the result, and its adjoint
+    const NavD nd = navD(P, V, xy(np));
+    const float4 lp = A.lamIn[2 * size_t(id)], lv = A.lamIn[2 * size_t(id) + 1];
+    f3 lnp{lp.x + P.dt * nd.g.x * nd.sx, lp.y + P.dt * nd.g.y * nd.sy, lp.z};
+    f3 lnv{lv.x, lv.y, lv.z};
+    float lr = 0.0f;
+    f3 lpOld{0.0f, 0.0f, 0.0f};
+    if (moved) revStatics(P, V, T, pOld, ri, f2{0.0f, 0.0f}, 0.0f, lnp, lnv, lr, lpOld);
+    float4 lplane = zero;
+    f2 lq = xy(lnp);
+    if (K > 0) lq = sweepOwnBack(A, s, K, lq, A.lamC[K & 1], plane, lplane);
+    A.lamQ[s] = make_float4(lq.x, lq.y, lnp.z, 0.0f);
+    A.lamNv[s] = make_float4(lnv.x, lnv.y, lnv.z, 0.0f);
+    A.lamPOld[s] = make_float4(lpOld.x, lpOld.y, lpOld.z, 0.0f);
+    A.lamPlane[s] = lplane;
+    A.lamR[s] = lr;
+    return double(nd.D);
+}
+
+// A block's sum of v in a fixed order (warp trees, then the warps in order); valid in thread 0
+template <int THREADS>
+__device__ __forceinline__ double blockSum(double v, double* warpSum) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31u) == 0) warpSum[threadIdx.x >> 5] = v;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int w = 0; w < ADJ_FINAL_THREADS / 32; ++w) t += warpSum[w];
-        A.lossPart[blockIdx.x] = t;
-    }
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < THREADS / 32; ++w) t += warpSum[w];
+    __syncthreads();
+    return t;
+}
+
+__global__ void __launch_bounds__(ADJ_FINAL_THREADS) k_adj_final(AdjArgs A) {
+    __shared__ double warpSum[ADJ_FINAL_THREADS / 32];
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const double d = s < A.L.n ? adjFinalSlot(A, s) : 0.0;
+    const double t = blockSum<ADJ_FINAL_THREADS>(d, warpSum);
+    if (threadIdx.x == 0) A.lossPart[blockIdx.x] = t;
+}
+
+// Sums v over the G consecutive lanes of a lane group (every lane of the warp calls it; all get the same bits)
+template <int G>
+__device__ __forceinline__ float groupSum(float v) {
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
 }
 
 // The 3 x 3 neighbour rows of a slot: slot ranges [rk0[j], rk1[j])
@@ -391,51 +413,67 @@ __device__ __forceinline__ void rows3(const AdjArgs& A, uint32_t cid, uint32_t* 
     }
 }
 
-__global__ void __launch_bounds__(128) k_adj_sweep(AdjArgs A) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= A.L.n || s >= activeCount(A)) return;
+// Sweep k of slot s reversed by a group of G lanes (lane = 0 .. G - 1; every lane of the warp takes part): the
+// neighbour gather split over the lanes, summed, then lane 0 adds the identity path and reverses the own part of
+// sweep k - 1. valid: s is active and not parked.
+// rows: the slot's 3 x 3 neighbour rows when the caller holds them (null: looked up)
+template <int G>
+__device__ void adjSweepSlot(const AdjArgs& A, int s, int lane, bool valid, int k, const uint32_t* rows = nullptr) {
     const SwarmParams& P = A.P;
     const TapeLayout& L = A.L;
-    const int k = A.sweep;
     const float4* q = A.f4 + L.q(k - 1);
-    const float4 b = q[s];
-    if (b.w < 0.0f) return;   // parked this step
     const float2* lc = A.lamC[k & 1];
-    const float2 lcs = lc[s];
-    const float4 lq4 = A.lamQ[s];
-    f2 lq{lq4.x, lq4.y};
-    float lr = 0.0f;
-    const float ri = A.prm[s].x;
-    uint32_t rk0[3], rk1[3];
-    rows3(A, A.skey[s], rk0, rk1);
+    float4 b = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+    float2 lcs = make_float2(0.0f, 0.0f);
+    float ri = 0.0f;
+    uint32_t rk0[3] = {0u, 0u, 0u}, rk1[3] = {0u, 0u, 0u};
+    if (valid) {
+        b = q[s];
+        lcs = lc[s];
+        ri = A.prm[s].x;
+        if (rows) {
 #pragma unroll
-    for (int j = 0; j < 3; ++j) {
-        for (uint32_t m = rk0[j]; m < rk1[j]; ++m) {
-            if (int(m) == s) continue;
-            const float4 op = q[m];
-            const float rj = A.prm[m].x;
-            const f3 offset = xyz(b) - xyz(op);
-            const float dc = ri + rj, dc2 = dc * dc;
-            const float dxy2 = dot(xy(offset), xy(offset));
-            if (op.w >= 0.0f && fabsf(offset.z) < dc && dxy2 < dc2) {
-                const float2 lcm = lc[m];
-                const f2 dl{lcs.x - lcm.x, lcs.y - lcm.y};
-                if (dxy2 <= P.stacked_xy2) {
-                    const f2 dir = pairDirection(A.sid[s], A.sid[m], P.hash_to_radians);
-                    lr += 0.5f * dot(dir, dl);
-                } else {
-                    // g = (dc / d - 1) o / 2: dg/do = ((dc / d - 1) I - (dc / d) oh oh^T) / 2, dg/ddc = oh / 2
-                    const float d = sqrtf(dxy2);
-                    const f2 oh = xy(offset) / d;
-                    const float ohl = dot(oh, dl);
-                    const float t = dc / d;
-                    lq.x += 0.5f * ((t - 1.0f) * dl.x - t * oh.x * ohl);
-                    lq.y += 0.5f * ((t - 1.0f) * dl.y - t * oh.y * ohl);
-                    lr += 0.5f * ohl;
-                }
+            for (int j = 0; j < 3; ++j) { rk0[j] = rows[j]; rk1[j] = rows[3 + j]; }
+        } else {
+            rows3(A, A.skey[s], rk0, rk1);
+        }
+    }
+    const uint32_t len0 = rk1[0] - rk0[0], len1 = rk1[1] - rk0[1], total = len0 + len1 + (rk1[2] - rk0[2]);
+    f2 lq{0.0f, 0.0f};
+    float lr = 0.0f;
+    for (uint32_t idx = uint32_t(lane); idx < total; idx += uint32_t(G)) {
+        const uint32_t m = idx < len0 ? rk0[0] + idx : (idx < len0 + len1 ? rk0[1] + (idx - len0) : rk0[2] + (idx - len0 - len1));
+        if (int(m) == s) continue;
+        const float4 op = q[m];
+        const float rj = A.prm[m].x;
+        const f3 offset = xyz(b) - xyz(op);
+        const float dc = ri + rj, dc2 = dc * dc;
+        const float dxy2 = dot(xy(offset), xy(offset));
+        if (op.w >= 0.0f && fabsf(offset.z) < dc && dxy2 < dc2) {
+            const float2 lcm = lc[m];
+            const f2 dl{lcs.x - lcm.x, lcs.y - lcm.y};
+            if (dxy2 <= P.stacked_xy2) {
+                const f2 dir = pairDirection(A.sid[s], A.sid[m], P.hash_to_radians);
+                lr += 0.5f * dot(dir, dl);
+            } else {
+                // g = (dc / d - 1) o / 2: dg/do = ((dc / d - 1) I - (dc / d) oh oh^T) / 2, dg/ddc = oh / 2
+                const float d = sqrtf(dxy2);
+                const f2 oh = xy(offset) / d;
+                const float ohl = dot(oh, dl);
+                const float t = dc / d;
+                lq.x += 0.5f * ((t - 1.0f) * dl.x - t * oh.x * ohl);
+                lq.y += 0.5f * ((t - 1.0f) * dl.y - t * oh.y * ohl);
+                lr += 0.5f * ohl;
             }
         }
     }
+    lq.x = groupSum<G>(lq.x);
+    lq.y = groupSum<G>(lq.y);
+    lr = groupSum<G>(lr);
+    if (!valid || lane != 0) return;
+    const float4 lq4 = A.lamQ[s];
+    lq.x += lq4.x;
+    lq.y += lq4.y;
     if (k > 1) {
         float4 lplane = A.lamPlane[s];
         lq = sweepOwnBack(A, s, k - 1, lq, A.lamC[(k - 1) & 1], A.f4[L.plane() + size_t(s)], lplane);
@@ -445,9 +483,17 @@ __global__ void __launch_bounds__(128) k_adj_sweep(AdjArgs A) {
     A.lamR[s] += lr;
 }
 
-__global__ void __launch_bounds__(128) k_adj_predict(AdjArgs A) {
+__device__ __forceinline__ bool sweepsSlot(const AdjArgs& A, int s) {   // active and not parked this step
+    return s < A.L.n && s < activeCount(A) && A.f4[A.L.q(0) + size_t(s)].w >= 0.0f;
+}
+
+__global__ void __launch_bounds__(128) k_adj_sweep(AdjArgs A) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= A.L.n || s >= activeCount(A)) return;
+    adjSweepSlot<1>(A, s, 0, sweepsSlot(A, s), A.sweep);
+}
+
+// Predict's own terms of slot s reversed (the separation sum and sAhead from the tape)
+__device__ void adjPredictSlot(const AdjArgs& A, int s) {
     const SwarmParams& P = A.P;
     const VenueArgs& V = A.V;
     const TapeLayout& L = A.L;
@@ -642,69 +688,210 @@ __global__ void __launch_bounds__(128) k_adj_predict(AdjArgs A) {
     A.gTau[id] += ltau;
 }
 
-__global__ void __launch_bounds__(128) k_adj_gather(AdjArgs A) {
+__global__ void __launch_bounds__(128) k_adj_predict(AdjArgs A) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= A.L.n || s >= activeCount(A)) return;
+    if (s < A.L.n && s < activeCount(A)) adjPredictSlot(A, s);
+}
+
+// Predict's pair terms of slot s gathered by a group of G lanes over the perception disk (every lane takes part);
+// lane 0 writes the state adjoint before the step and the radius gradient. valid: s is active at the step.
+template <int G>
+__device__ void adjGatherSlot(const AdjArgs& A, int s, int lane, bool valid) {
     const SwarmParams& P = A.P;
     const VenueArgs& V = A.V;
     const TapeLayout& L = A.L;
-    const uint32_t id = A.sid[s];
     const float4* pos = A.f4 + L.pos0();
     const float4* pred = A.f4 + L.pred();
-    const float4 p = pos[s];
-    const float ri = A.prm[s].x;
-    const float4 ls = A.lamSep[s];
-    const float4 lp4 = A.lamP[s];
-    f3 lp{lp4.x, lp4.y, lp4.z};
-    float lr = A.lamR[s];
-    const uint32_t cid = A.skey[s];
-    const int resX = V.resX, resY = V.resY, R = P.perc_ring;
-    const int cx = int(cid % uint32_t(resX)), cy = int(cid / uint32_t(resX));
-    const int xlo = max(cx - R, 0), xhi = min(cx + R, resX - 1);
-    for (int ny = max(cy - R, 0); ny <= min(cy + R, resY - 1); ++ny) {
-        const uint32_t k0 = A.start[xlo + ny * resX], k1 = A.start[xhi + 1 + ny * resX];
-        for (uint32_t k = k0; k < k1; ++k) {
-            if (int(k) == s) continue;
-            const float4 op = pos[k];
-            const f3 o = xyz(p) - xyz(op);
-            const float dxy2 = dot(xy(o), xy(o));
-            if (!(dxy2 < P.r_perc2)) continue;
-            const float4 lk = A.lamSep[k];
-            const float dc = ri + A.prm[k].x;
-            const float rs = dc + P.sep_margin, rs2 = rs * rs;
-            const float d2 = dot(o, o);
-            if (d2 < rs2) {   // separation f = k_sep w^2 dir, w = 1 - |o| / rs: F^T (lambda_s - lambda_k)
-                const f2 dl{ls.x - lk.x, ls.y - lk.y};
-                const float D = sqrtf(d2);
-                const float w = 1.0f - D / rs;
-                const bool stacked = dxy2 <= P.stacked_xy2;
-                float rxy = 0.0f;
-                f2 dir;
-                if (stacked) dir = pairDirection(id, A.sid[k], P.hash_to_radians);
-                else { rxy = sqrtf(dxy2); dir = xy(o) / rxy; }
-                const float kd = dot(dir, dl);
-                if (D > 0.0f) {
-                    const float c1 = -2.0f * P.k_sep * w / (D * rs) * kd;
-                    lp = lp + o * c1;
-                }
-                if (!stacked) {
-                    const float c2 = P.k_sep * w * w / rxy;
-                    lp.x += c2 * (dl.x - dir.x * kd);
-                    lp.y += c2 * (dl.y - dir.y * kd);
-                }
-                lr += 2.0f * P.k_sep * w * D / rs2 * kd;
+    constexpr int MAXR = 2 * 4 + 1;   // perc_ring <= 4
+    uint32_t rk0[MAXR], len[MAXR];
+    uint32_t total = 0;
+    float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f), ls = p;
+    float ri = 0.0f;
+    uint32_t id = 0;
+    const int R = P.perc_ring;
+#pragma unroll
+    for (int j = 0; j < MAXR; ++j) { rk0[j] = 0u; len[j] = 0u; }
+    if (valid) {
+        id = A.sid[s];
+        p = pos[s];
+        ri = A.prm[s].x;
+        ls = A.lamSep[s];
+        const uint32_t cid = A.skey[s];
+        const int resX = V.resX, resY = V.resY;
+        const int cx = int(cid % uint32_t(resX)), cy = int(cid / uint32_t(resX));
+        // each row's cells that can hold an agent within the reach (cells widened by margin, as predict trims)
+        const float csx = V.dspanX / float(resX), csy = V.dspanY / float(resY);
+        const float margin = 0.01f * smax(csx, csy);
+        const float rr = smin(sqrtf(P.r_perc2), A.gatherReach) + margin;
+#pragma unroll
+        for (int j = 0; j < MAXR; ++j) {
+            const int ny = cy - R + j;
+            if (j > 2 * R || ny < 0 || ny >= resY) continue;
+            const float ylo = V.dminY + float(ny) * csy - margin, yhi = V.dminY + float(ny + 1) * csy + margin;
+            const float dy = fmaxf(0.0f, fmaxf(ylo - p.y, p.y - yhi));
+            if (dy >= rr) continue;
+            const float w = sqrtf(rr * rr - dy * dy) + margin;
+            const int xlo = max(max(cx - R, 0), int(floorf((p.x - w - V.dminX) / csx)));
+            const int xhi = min(min(cx + R, resX - 1), int(floorf((p.x + w - V.dminX) / csx)));
+            if (xlo > xhi) continue;
+            rk0[j] = A.start[xlo + ny * resX];
+            len[j] = A.start[xhi + 1 + ny * resX] - rk0[j];
+            total += len[j];
+        }
+    }
+    f3 lp{0.0f, 0.0f, 0.0f};
+    float lr = 0.0f;
+    for (uint32_t idx = uint32_t(lane); idx < total; idx += uint32_t(G)) {
+        uint32_t k = idx, j = 0;
+        while (k >= len[j]) { k -= len[j]; ++j; }
+        k += rk0[j];
+        if (int(k) == s) continue;
+        const float4 op = pos[k];
+        const f3 o = xyz(p) - xyz(op);
+        const float dxy2 = dot(xy(o), xy(o));
+        if (!(dxy2 < P.r_perc2)) continue;
+        const float4 lk = A.lamSep[k];
+        const float dc = ri + A.prm[k].x;
+        const float rs = dc + P.sep_margin, rs2 = rs * rs;
+        const float d2 = dot(o, o);
+        if (d2 < rs2) {   // separation f = k_sep w^2 dir, w = 1 - |o| / rs: F^T (lambda_s - lambda_k)
+            const f2 dl{ls.x - lk.x, ls.y - lk.y};
+            const float D = sqrtf(d2);
+            const float w = 1.0f - D / rs;
+            const bool stacked = dxy2 <= P.stacked_xy2;
+            float rxy = 0.0f;
+            f2 dir;
+            if (stacked) dir = pairDirection(id, A.sid[k], P.hash_to_radians);
+            else { rxy = sqrtf(dxy2); dir = xy(o) / rxy; }
+            const float kd = dot(dir, dl);
+            if (D > 0.0f) {
+                const float c1 = -2.0f * P.k_sep * w / (D * rs) * kd;
+                lp = lp + o * c1;
             }
-            if (__float_as_int(pred[k].w) == s && lk.z != 0.0f) {   // this slot is k's nearest agent ahead
-                const float dxy = sqrtf(dxy2);
-                if (dxy > 0.0f) { lp.x += o.x / dxy * lk.z; lp.y += o.y / dxy * lk.z; }
-                lr -= lk.z;
+            if (!stacked) {
+                const float c2 = P.k_sep * w * w / rxy;
+                lp.x += c2 * (dl.x - dir.x * kd);
+                lp.y += c2 * (dl.y - dir.y * kd);
+            }
+            lr += 2.0f * P.k_sep * w * D / rs2 * kd;
+        }
+        if (__float_as_int(pred[k].w) == s && lk.z != 0.0f) {   // this slot is k's nearest agent ahead
+            const float dxy = sqrtf(dxy2);
+            if (dxy > 0.0f) { lp.x += o.x / dxy * lk.z; lp.y += o.y / dxy * lk.z; }
+            lr -= lk.z;
+        }
+    }
+    lp.x = groupSum<G>(lp.x);
+    lp.y = groupSum<G>(lp.y);
+    lp.z = groupSum<G>(lp.z);
+    lr = groupSum<G>(lr);
+    if (!valid || lane != 0) return;
+    const float4 lp4 = A.lamP[s];
+    const float4 lv = A.lamV[s];
+    A.lamOut[2 * size_t(id)] = make_float4(lp.x + lp4.x, lp.y + lp4.y, lp.z + lp4.z, 0.0f);
+    A.lamOut[2 * size_t(id) + 1] = make_float4(lv.x, lv.y, lv.z, 0.0f);
+    A.gR[id] += double(A.lamR[s] + lr);
+}
+
+__global__ void __launch_bounds__(128) k_adj_gather(AdjArgs A) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    adjGatherSlot<1>(A, s, 0, s < A.L.n && s < activeCount(A));
+}
+
+// ---- the whole reverse step as one persistent kernel ----
+// Every block stays resident (a cooperative launch); the phases are separated by a grid barrier on one word: block 0
+// adds 2^31 - (blocks - 1), every other block 1, so the word's top bit flips once all have arrived; a block waits for
+// the flip at most ADJ_BARRIER_WAIT_NS of %globaltimer, then records ERR_TIMEOUT and stops waiting for the rest of
+// the launch (the host reports SWARM_E_TIMEOUT).
+constexpr uint64_t ADJ_BARRIER_WAIT_NS = 1000000000ull;
+
+__device__ __forceinline__ uint64_t adjNs() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void adjBarrier(const AdjArgs& A) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        cuda::atomic_ref<int, cuda::thread_scope_device> err(*A.err);
+        if (!(err.load(cuda::memory_order_relaxed) & ERR_TIMEOUT)) {
+            cuda::atomic_ref<unsigned, cuda::thread_scope_device> word(*A.barrier);
+            const unsigned add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
+            const unsigned old = word.fetch_add(add, cuda::memory_order_release);
+            const uint64_t t0 = adjNs();
+            while (((word.load(cuda::memory_order_acquire) ^ old) & 0x80000000u) == 0u) {
+                if (adjNs() - t0 > ADJ_BARRIER_WAIT_NS) { err.fetch_or(ERR_TIMEOUT, cuda::memory_order_relaxed); break; }
             }
         }
     }
-    const float4 lv = A.lamV[s];
-    A.lamOut[2 * size_t(id)] = make_float4(lp.x, lp.y, lp.z, 0.0f);
-    A.lamOut[2 * size_t(id) + 1] = make_float4(lv.x, lv.y, lv.z, 0.0f);
-    A.gR[id] += double(lr);
+    __syncthreads();
+}
+
+// Timing on: block 0 adds the span since *t0 to stamps[i] and restarts the clock
+__device__ __forceinline__ void adjStamp(const AdjArgs& A, int i, uint64_t& t0) {
+    if (A.stamps && blockIdx.x == 0 && threadIdx.x == 0) {
+        const uint64_t t = adjNs();
+        A.stamps[i] += t - t0;
+        t0 = t;
+    }
+}
+
+template <int G>
+__global__ void __launch_bounds__(ADJ_FUSED_THREADS, 1) k_adj_step_fused(AdjArgs A) {
+    __shared__ double warpSum[ADJ_FUSED_THREADS / 32];
+    const int n = A.L.n, K = A.L.K;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    const int lane = int(threadIdx.x) % G;
+    uint64_t t0 = A.stamps ? adjNs() : 0;
+    // final pass (and the loss sum of the block's slots)
+    double d = 0.0;
+    for (int s = tid; s < n; s += stride) d += adjFinalSlot(A, s);
+    const double t = blockSum<ADJ_FUSED_THREADS>(d, warpSum);
+    if (threadIdx.x == 0) A.lossPart[blockIdx.x] = t;
+    adjBarrier(A);
+    adjStamp(A, 0, t0);
+    // the sweeps, last to first: G lanes per slot (warp-uniform loop)
+    const int groups = stride / G, g0 = tid / G;
+    const int nActive = activeCount(A);
+    if (nActive <= groups) {   // one slot per lane group: its rows and status once for all the sweeps
+        const int s = g0;
+        const bool valid = sweepsSlot(A, s);
+        uint32_t rows[6] = {0u, 0u, 0u, 0u, 0u, 0u};
+        if (valid) rows3(A, A.skey[s], rows, rows + 3);
+        for (int k = K; k >= 1; --k) {
+            if (g0 - (g0 % (32 / G)) < nActive) adjSweepSlot<G>(A, s, lane, valid, k, rows);
+            adjBarrier(A);
+        }
+    } else {
+        for (int k = K; k >= 1; --k) {
+            for (int base = g0 - (g0 % (32 / G)); base < nActive; base += groups) {
+                const int s = base + (g0 % (32 / G));
+                adjSweepSlot<G>(A, s, lane, sweepsSlot(A, s), k);
+            }
+            adjBarrier(A);
+        }
+    }
+    adjStamp(A, 1, t0);
+    for (int s = tid; s < nActive; s += stride) adjPredictSlot(A, s);
+    adjBarrier(A);
+    adjStamp(A, 2, t0);
+    if (A.stamps && blockIdx.x == 0 && threadIdx.x == 0) A.stamps[4] = t0;   // the gather's start
+    for (int base = g0 - (g0 % (32 / G)); base < nActive; base += groups) {
+        const int s = base + (g0 % (32 / G));
+        adjGatherSlot<G>(A, s, lane, s < nActive);
+    }
+    if (A.stamps) {   // the gather ends when the last block leaves
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            cuda::atomic_ref<unsigned, cuda::thread_scope_device> done(A.barrier[1]);
+            if (done.fetch_add(1u, cuda::memory_order_acq_rel) == gridDim.x - 1) {
+                A.stamps[3] += adjNs() - A.stamps[4];
+                done.store(0u, cuda::memory_order_relaxed);
+            }
+        }
+    }
 }
 
 inline int blocksOf(int n, int t) { return (n + t - 1) / t; }
@@ -721,6 +908,40 @@ void launch_adjoint_step(AdjArgs& A, cudaStream_t st, int64_t* launches) {
     k_adj_predict<<<blocksOf(n, 128), 128, 0, st>>>(A);
     k_adj_gather<<<blocksOf(n, 128), 128, 0, st>>>(A);
     *launches += 3 + A.L.K;
+}
+
+namespace {
+int g_sms = 0, g_perSm = 0;
+void fusedConfig() {
+    if (g_sms) return;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_perSm, k_adj_step_fused<ADJ_LANES>, ADJ_FUSED_THREADS, 0);
+}
+}  // namespace
+
+int adjFusedBlocks(int n) {
+    fusedConfig();
+    const int resident = g_sms * g_perSm;
+    const int want = int((int64_t(n) * ADJ_LANES + ADJ_FUSED_THREADS - 1) / ADJ_FUSED_THREADS);
+    return std::max(1, std::min(want, resident));
+}
+
+cudaError_t launch_adjoint_step_fused(AdjArgs& A, cudaStream_t st) {
+    fusedConfig();
+    if (g_sms * g_perSm <= 0) return cudaErrorCooperativeLaunchTooLarge;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(unsigned(adjFusedBlocks(A.L.n)));
+    cfg.blockDim = dim3(unsigned(ADJ_FUSED_THREADS));
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_adj_step_fused<ADJ_LANES>, A);
 }
 
 }  // namespace swarm_gpu

@@ -51,15 +51,28 @@ struct AdjArgs {
     double* gR;
     double* gV0;
     double* gTau;
-    double* lossPart;           // per block of the final kernel: sum of D over its active outputs
+    double* lossPart;           // per block of the final pass: sum of D over its active outputs
     int sweep;                  // the sweep a k_adj_sweep launch reverses
+    float gatherReach;          // the pair gather's disk: no pair farther apart has a separation force or is a
+                                // headway argmin whose gap moves v_des (2 r_pair_max + max(sep_margin,
+                                // v_max * largest speed factor / headway_rate), 1 % slack)
+    int* err;                   // device error flags (ERR_TIMEOUT)
+    unsigned* barrier;          // the fused reverse's grid barrier words (arrival word, exit counter)
+    unsigned long long* stamps; // timing on: the fused reverse adds each phase's %globaltimer span (ns): final, sweeps,
+                                // predict, gather (block 0's view; the gather ends when the last block leaves)
 };
 
 constexpr int ADJ_FINAL_THREADS = 128;
+constexpr int ADJ_FUSED_THREADS = 512;
+constexpr int ADJ_LANES = 4;    // lanes per slot in the fused reverse's neighbour gathers
 inline int adjFinalBlocks(int n) { return (n + ADJ_FINAL_THREADS - 1) / ADJ_FINAL_THREADS; }
 
 // Reverses one step: the final pass (and the last sweep's own terms, and the loss term of the step's result), the K
 // sweeps, predict's local terms, predict's neighbour terms. K + 3 launches.
 void launch_adjoint_step(AdjArgs& A, cudaStream_t st, int64_t* launches);
+// The same as one cooperative persistent launch with K + 2 grid barriers
+cudaError_t launch_adjoint_step_fused(AdjArgs& A, cudaStream_t st);
+// The fused reverse's grid size for n agents (the blocks that write loss partials)
+int adjFusedBlocks(int n);
 
 }  // namespace swarm_gpu

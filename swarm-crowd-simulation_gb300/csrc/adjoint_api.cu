@@ -1,10 +1,10 @@
 // swarm_adjoint_run (include/swarm_cuda.h): the loss and its gradient by the adjoint of the step.
 //
-// Schedule, for T steps with checkpoints every C: a forward pass stores the state at the start of each segment
-// (segments 0 .. S - 2; the last segment's start is where it ends); then, for each segment from the last to the
-// first, the segment is recomputed from its checkpoint with the tape on (launch_step_taped) and its steps are
-// reversed from the last to the first (launch_adjoint_step). Forward work 2T - C steps, reverse work T steps, device
-// memory C taped steps + S checkpoints. The handle's own state and buffers are not touched: the adjoint owns copies of
+// Schedule, for T steps with checkpoints every C: a forward pass stores the state at the start of each of the S
+// segments and tapes the last segment as it goes; then, for each segment from the last to the first, the segment is
+// recomputed from its checkpoint with the tape on (all but the last) and its steps are reversed from the last to the
+// first. Forward work 2T - C steps (T - C of them untaped), reverse work T steps, device memory C taped steps + S
+// checkpoints. With a fused handle each forward step and each reverse step is one persistent cooperative launch. The handle's own state and buffers are not touched: the adjoint owns copies of
 // every buffer a step writes.
 #include "adjoint.cuh"
 #include "sim_handle.cuh"
@@ -24,6 +24,7 @@ using swarm_gpu::TapeLayout;
 
 struct SwarmAdjoint {
     int n = 0, K = 0, ckpt = 0, nseg = 0, steps = 0, ncells = 0;
+    double speedMax = 1.0;           // the venue's largest speed factor
     TapeLayout L{};
     std::vector<void*> allocs;
     int64_t bytes = 0;
@@ -40,7 +41,8 @@ struct SwarmAdjoint {
     uint2* cells = nullptr;
     uint8_t* contacts = nullptr;
     int* err = nullptr;
-    unsigned* barrier = nullptr;
+    unsigned* barrier = nullptr;     // 8 words: the forward's (0 .. 3), the reverse's (4 .. 7)
+    unsigned long long* stamps = nullptr;   // the fused reverse's phase spans
     uint4* rowsA = nullptr;
     uint2* rowsB = nullptr;
     uint2* tileWin = nullptr;
@@ -83,16 +85,17 @@ SwarmAdjoint* makeAdjoint(SwarmSim* h, int n, int K, int ckpt, int nseg, int ste
     SwarmAdjoint* a = new (std::nothrow) SwarmAdjoint();
     if (!a) return nullptr;
     a->n = n; a->K = K; a->ckpt = ckpt; a->nseg = nseg; a->steps = steps; a->ncells = h->ncells;
+    a->speedMax = h->speedMax;
     a->L = TapeLayout{n, K, std::max(K, 1)};
     const size_t N = size_t(n), C = size_t(ckpt), NC = size_t(h->ncells) + 1;
-    a->lossBlocks = swarm_gpu::adjFinalBlocks(n);
+    a->lossBlocks = std::max(swarm_gpu::adjFinalBlocks(n), swarm_gpu::adjFusedBlocks(n));
     const bool good =
         a->alloc(&a->state[0], 2 * N) && a->alloc(&a->state[1], 2 * N) && a->alloc(&a->ckptState, size_t(nseg) * 2 * N) &&
         a->alloc(&a->tapeF4, C * a->f4Step()) && a->alloc(&a->tapePrm, C * N) && a->alloc(&a->tapeSid, C * N) &&
         a->alloc(&a->tapeSkey, C * N) && a->alloc(&a->tapeStart, C * NC) && a->alloc(&a->tapeCtc, C * N) &&
         a->alloc(&a->key, N) && a->alloc(&a->rank, N) && a->alloc(&a->count, NC) && a->alloc(&a->sidTmp, N) &&
         a->alloc(&a->tileSums, size_t(h->ncells) / 1024 + 2) && a->alloc(&a->cells, NC) && a->alloc(&a->contacts, N) &&
-        a->alloc(&a->err, 1) && a->alloc(&a->barrier, 4) && a->alloc(&a->rowsA, N) && a->alloc(&a->rowsB, N) &&
+        a->alloc(&a->err, 1) && a->alloc(&a->barrier, 8) && a->alloc(&a->stamps, 8) && a->alloc(&a->rowsA, N) && a->alloc(&a->rowsB, N) &&
         a->alloc(&a->tileWin, N / 64 + 2) && a->alloc(&a->proj[0], N) && a->alloc(&a->proj[1], N) &&
         a->alloc(&a->lamX[0], 2 * N) && a->alloc(&a->lamX[1], 2 * N) && a->alloc(&a->lamQ, N) && a->alloc(&a->lamPlane, N) &&
         a->alloc(&a->lamNv, N) && a->alloc(&a->lamPOld, N) && a->alloc(&a->lamSep, N) && a->alloc(&a->lamP, N) &&
@@ -100,7 +103,7 @@ SwarmAdjoint* makeAdjoint(SwarmSim* h, int n, int K, int ckpt, int nseg, int ste
         a->alloc(&a->gR, N) && a->alloc(&a->gV0, N) && a->alloc(&a->gTau, N) &&
         a->alloc(&a->lossPart, size_t(steps) * size_t(a->lossBlocks));
     if (!good || cudaMemset(a->count, 0, NC * 4) != cudaSuccess || cudaMemset(a->err, 0, 4) != cudaSuccess ||
-        cudaMemset(a->barrier, 0, 16) != cudaSuccess) {
+        cudaMemset(a->barrier, 0, 32) != cudaSuccess) {
         delete a;
         return nullptr;
     }
@@ -176,15 +179,52 @@ extern "C" int swarm_adjoint_run(SwarmHandle h, const SwarmLossSpec* loss, int s
                 ok(h, cudaMemsetAsync(a->gR, 0, N * 8, st), "adjoint clear") &&
                 ok(h, cudaMemsetAsync(a->gV0, 0, N * 8, st), "adjoint clear") &&
                 ok(h, cudaMemsetAsync(a->gTau, 0, N * 8, st), "adjoint clear") &&
-                ok(h, cudaMemsetAsync(a->err, 0, 4, st), "adjoint clear");
-    // the checkpoint pass
+                ok(h, cudaMemsetAsync(a->err, 0, 4, st), "adjoint clear") &&
+                ok(h, cudaMemsetAsync(a->lossPart, 0, size_t(steps) * size_t(a->lossBlocks) * 8, st), "adjoint clear") &&
+                ok(h, cudaMemsetAsync(a->stamps, 0, 8 * 8, st), "adjoint clear");
+    // the checkpoint pass; the last segment is taped here, not recomputed
     int in = 0;
+    std::vector<float4*> q(size_t(L.Kq)), corr(size_t(K) + 1, nullptr);
+    // Fused steps run in chains, as the handle's stepping does: each final pass counts the next state's keys
+    // (hashNext) for the next step of its chain (hashed); a chain's last step counts nothing, so the counts are clear
+    // whenever a checkpoint is restored.
+    bool counted = false;
+    auto chain = [&](StepArgs& A, bool last) {
+        A.hashed = counted ? 1 : 0;
+        A.hashNext = last ? 0 : 1;
+        counted = !last;
+    };
+    auto tapedStep = [&](int j, bool last) {
+        StepArgs A = forwardArgs(h, a, in, j);
+        float4* t = a->tape(j);
+        if (h->fused) {   // one persistent launch writing the tape
+            chain(A, last);
+            A.proj[0] = t + L.q(0);
+            A.tapeCorr = K > 0 ? t + L.corr(1) : nullptr;
+            A.tapeQK = t + L.qK();
+            A.tapePred = t + L.pred();
+            launches += 1;
+            return ok(h, swarm_gpu::launch_step_fused_taped(A, st), "adjoint recompute");
+        }
+        for (int k = 0; k < L.Kq; ++k) q[size_t(k)] = t + L.q(k);
+        for (int k = 1; k <= K; ++k) corr[size_t(k)] = t + L.corr(k);
+        swarm_gpu::launch_step_taped(A, q.data(), corr.data(), t + L.qK(), t + L.pred(), st, &launches);
+        return ok(h, cudaGetLastError(), "adjoint recompute");
+    };
     for (int seg = 0; good && seg < nseg; ++seg) {
         good = ok(h, cudaMemcpyAsync(a->ckptState + size_t(seg) * 2 * N, a->state[in], N * 32, cudaMemcpyDeviceToDevice, st), "checkpoint");
-        if (seg == nseg - 1) break;
+        if (seg == nseg - 1) {
+            const int cnt = steps - seg * C;
+            for (int j = 0; good && j < cnt; ++j) {
+                good = tapedStep(j, j == cnt - 1);
+                in ^= 1;
+            }
+            break;
+        }
         for (int j = 0; good && j < C; ++j) {
-            const StepArgs A = forwardArgs(h, a, in, 0);
+            StepArgs A = forwardArgs(h, a, in, 0);
             if (h->fused) {
+                chain(A, false);
                 good = ok(h, swarm_gpu::launch_step_fused(A, st), "adjoint forward");
                 launches += 1;
             } else {
@@ -196,21 +236,19 @@ extern "C" int swarm_adjoint_run(SwarmHandle h, const SwarmLossSpec* loss, int s
     }
     if (stats) cudaEventRecord(ev[1], st);
     // the segments, last to first: taped recompute, then the reverse steps
+    const float gatherReach = float((2.0 * h->P.r_pair_max + std::max(double(h->P.sep_margin),
+                                     double(h->P.v_max) * a->speedMax / double(h->P.headway_rate))) * 1.01);
     int lam = 0;
-    std::vector<float4*> q(size_t(L.Kq)), corr(size_t(K) + 1, nullptr);
     for (int seg = nseg - 1; good && seg >= 0; --seg) {
         const int t0 = seg * C, cnt = std::min(C, steps - t0);
         if (stats) cudaEventRecord(ev[2 + 3 * size_t(seg)], st);
-        good = ok(h, cudaMemcpyAsync(a->state[0], a->ckptState + size_t(seg) * 2 * N, N * 32, cudaMemcpyDeviceToDevice, st), "restore");
-        in = 0;
-        for (int j = 0; good && j < cnt; ++j) {
-            const StepArgs A = forwardArgs(h, a, in, j);
-            float4* t = a->tape(j);
-            for (int k = 0; k < L.Kq; ++k) q[size_t(k)] = t + L.q(k);
-            for (int k = 1; k <= K; ++k) corr[size_t(k)] = t + L.corr(k);
-            swarm_gpu::launch_step_taped(A, q.data(), corr.data(), t + L.qK(), t + L.pred(), st, &launches);
-            good = ok(h, cudaGetLastError(), "adjoint recompute");
-            in ^= 1;
+        if (seg < nseg - 1) {   // recompute the segment from its checkpoint, taped
+            good = ok(h, cudaMemcpyAsync(a->state[0], a->ckptState + size_t(seg) * 2 * N, N * 32, cudaMemcpyDeviceToDevice, st), "restore");
+            in = 0;
+            for (int j = 0; good && j < cnt; ++j) {
+                good = tapedStep(j, j == cnt - 1);
+                in ^= 1;
+            }
         }
         if (stats) cudaEventRecord(ev[3 + 3 * size_t(seg)], st);
         for (int j = cnt - 1; good && j >= 0; --j) {
@@ -230,8 +268,17 @@ extern "C" int swarm_adjoint_run(SwarmHandle h, const SwarmLossSpec* loss, int s
             R.lamPOld = a->lamPOld; R.lamSep = a->lamSep; R.lamP = a->lamP; R.lamV = a->lamV; R.lamR = a->lamR;
             R.gR = a->gR; R.gV0 = a->gV0; R.gTau = a->gTau;
             R.lossPart = a->lossPart + size_t(t0 + j) * size_t(a->lossBlocks);
-            swarm_gpu::launch_adjoint_step(R, st, &launches);
-            good = ok(h, cudaGetLastError(), "adjoint reverse");
+            R.gatherReach = gatherReach;
+            R.err = a->err;
+            R.barrier = a->barrier + 4;
+            R.stamps = stats ? a->stamps : nullptr;
+            if (h->fused) {
+                good = ok(h, swarm_gpu::launch_adjoint_step_fused(R, st), "adjoint reverse");
+                launches += 1;
+            } else {
+                swarm_gpu::launch_adjoint_step(R, st, &launches);
+                good = ok(h, cudaGetLastError(), "adjoint reverse");
+            }
             lam ^= 1;
         }
         if (stats) cudaEventRecord(ev[4 + 3 * size_t(seg)], st);
@@ -243,11 +290,13 @@ extern "C" int swarm_adjoint_run(SwarmHandle h, const SwarmLossSpec* loss, int s
     }
     std::vector<double> part(size_t(steps) * size_t(a->lossBlocks)), gr(N), gv(N), gt(N);
     int errFlag = 0;
+    unsigned long long stampNs[8] = {};
     good = ok(h, cudaMemcpyAsync(part.data(), a->lossPart, part.size() * 8, cudaMemcpyDeviceToHost, st), "loss") &&
            ok(h, cudaMemcpyAsync(gr.data(), a->gR, N * 8, cudaMemcpyDeviceToHost, st), "gradient") &&
            ok(h, cudaMemcpyAsync(gv.data(), a->gV0, N * 8, cudaMemcpyDeviceToHost, st), "gradient") &&
            ok(h, cudaMemcpyAsync(gt.data(), a->gTau, N * 8, cudaMemcpyDeviceToHost, st), "gradient") &&
            ok(h, cudaMemcpyAsync(&errFlag, a->err, 4, cudaMemcpyDeviceToHost, st), "error flag") &&
+           ok(h, cudaMemcpyAsync(stampNs, a->stamps, sizeof stampNs, cudaMemcpyDeviceToHost, st), "stamps") &&
            ok(h, cudaStreamSynchronize(st), "adjoint");
     if (good && stats) {
         float ms = 0.0f;
@@ -264,11 +313,15 @@ extern "C" int swarm_adjoint_run(SwarmHandle h, const SwarmLossSpec* loss, int s
         stats->ms_total = ms;
         stats->launches = launches;
         stats->tape_bytes = a->bytes;
+        stats->ms_rev_final = float(double(stampNs[0]) * 1e-6);
+        stats->ms_rev_sweeps = float(double(stampNs[1]) * 1e-6);
+        stats->ms_rev_predict = float(double(stampNs[2]) * 1e-6);
+        stats->ms_rev_gather = float(double(stampNs[3]) * 1e-6);
     }
     for (auto& e : ev) cudaEventDestroy(e);
     if (!good) return SWARM_E_CUDA;
     if (errFlag & swarm_gpu::ERR_TIMEOUT) {
-        cudaMemset(a->barrier, 0, 16);
+        cudaMemset(a->barrier, 0, 32);
         return h->fail(SWARM_E_TIMEOUT, "a grid barrier of the adjoint's forward timed out");
     }
     if (errFlag) return h->fail(SWARM_E_CUDA, "the adjoint's forward found its counts out of step with its keys");

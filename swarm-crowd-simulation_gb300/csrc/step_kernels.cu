@@ -576,7 +576,9 @@ __device__ __forceinline__ void prepareSweepItem(const StepArgs& A, int s, int n
 
 constexpr int WIN_CAP = 2048;   // slots a tile window may hold in shared memory (40 KB); larger windows read global memory
 
-template <class Venue, bool kPerAgent, bool kB>
+// kTape (the adjoint's recompute): sweep k reads q[k - 1] and writes q[k], q[k] = proj[0] + k n, with its relaxed
+// corrections at tapeCorr + (k - 1) n; the final pass records the last sweep's result in tapeQK; predict its record
+template <class Venue, bool kPerAgent, bool kB, bool kTape = false>
 __global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A) {
     constexpr bool kUniform = Body<Venue>::kUniform;
     __shared__ uint32_t warpSums[32];
@@ -603,7 +605,7 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A)
     stamp(A, 1);
     const int nActive = int(A.start[A.V.ncells]);
     for (int s = tid; s < n; s += stride) {
-        predictItem<Venue, kB>(A, s);
+        predictItem<Venue, kB, kTape>(A, s);
         if (s < nActive) prepareSweepItem<kB>(A, s, nActive, T);
     }
     gridBarrier(A, gridDim.x);
@@ -611,7 +613,7 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A)
     const int K = A.P.proj_iterations;
     const int activeTiles = (nActive + T - 1) / T;
     // one sweep (or the final pass) over tile t: stage its window, then each slot reads its neighbours from it
-    auto sweepTile = [&](int t, const float4* in, float4& result, bool& own) {
+    auto sweepTile = [&](int t, const float4* in, float4& result, bool& own, float4* corrOut) {
         const int s = t * T + int(threadIdx.x);
         own = s < nActive;
         const uint2 win = t < activeTiles ? A.tileWin[t] : make_uint2(0u, 0u);
@@ -637,19 +639,23 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A)
         if (own && b.w >= 0.0f) {
             const Venue ven{A.P, venueOfSlot<kB>(A, s)};
             const uint32_t rk0[3] = {ra.x, ra.z, rb.x}, rk1[3] = {ra.y, ra.w, rb.y};
-            b = useWin ? projectCore(A, ven, b, s, ri, rk0, rk1, plane, WindowNbr{smPos, smR, win.x})
-                       : projectCore(A, ven, b, s, ri, rk0, rk1, plane, GlobalNbr{in, A.prm});
+            float4* co = kTape ? corrOut + s : nullptr;
+            b = useWin ? projectCore<Venue, WindowNbr, kTape>(A, ven, b, s, ri, rk0, rk1, plane, WindowNbr{smPos, smR, win.x}, co)
+                       : projectCore<Venue, GlobalNbr, kTape>(A, ven, b, s, ri, rk0, rk1, plane, GlobalNbr{in, A.prm}, co);
         }
         result = b;
         __syncthreads();   // the window is reused by the next tile
     };
     int in = 0;
     for (int it = 1; it < K; ++it) {
+        const float4* src = kTape ? A.proj[0] + size_t(it - 1) * size_t(n) : A.proj[in];
+        float4* dst = kTape ? A.proj[0] + size_t(it) * size_t(n) : A.proj[in ^ 1];
+        float4* corr = kTape ? A.tapeCorr + size_t(it - 1) * size_t(n) : nullptr;
         for (int t = blockIdx.x; t < activeTiles; t += gridDim.x) {
             float4 r;
             bool own;
-            sweepTile(t, A.proj[in], r, own);
-            if (own) A.proj[in ^ 1][t * T + int(threadIdx.x)] = r;
+            sweepTile(t, src, r, own, corr);
+            if (own) dst[t * T + int(threadIdx.x)] = r;
         }
         in ^= 1;
         gridBarrier(A, gridDim.x);
@@ -660,9 +666,11 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A)
         const int s = t * T + int(threadIdx.x);
         float4 b;
         bool own;
-        if (A.projectInFinal) sweepTile(t, A.proj[in], b, own);
-        else { own = s < nActive; b = own ? A.proj[in][s] : make_float4(0.0f, 0.0f, 0.0f, 0.0f); }
+        const float4* src = kTape ? A.proj[0] + size_t(K > 0 ? K - 1 : 0) * size_t(n) : A.proj[in];
+        if (A.projectInFinal) sweepTile(t, src, b, own, kTape && K > 0 ? A.tapeCorr + size_t(K - 1) * size_t(n) : nullptr);
+        else { own = s < nActive; b = own ? src[s] : make_float4(0.0f, 0.0f, 0.0f, 0.0f); }
         uint32_t nextKey = INACTIVE_CELL;
+        if (kTape && own) A.tapeQK[s] = b;
         if (own) {
             const VenueArgs& V = venueOfSlot<kB>(A, s);
             nextKey = finalActive(A, V, Venue{A.P, V}, s, b);
@@ -730,20 +738,24 @@ constexpr int FUSED_SMEM = WIN_CAP * (int(sizeof(float4)) + int(sizeof(float)));
 
 // The fused grid: one block per SM when the state fits (threads = n / SMs rounded up to a warp, 128..512), else as
 // many blocks as stay resident, each taking several tiles per phase
-template <class Venue, bool kPerAgent, bool kB>
+template <class Venue, bool kPerAgent, bool kB, bool kTape = false>
 static cudaError_t fusedImpl(const StepArgs& A, cudaStream_t st) {
     static int sms = 0;
     if (!sms) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaFuncSetAttribute(k_step_fused<Venue, kPerAgent, kB>, cudaFuncAttributeMaxDynamicSharedMemorySize, FUSED_SMEM);
+        cudaFuncSetAttribute(k_step_fused<Venue, kPerAgent, kB, kTape>, cudaFuncAttributeMaxDynamicSharedMemorySize, FUSED_SMEM);
     }
     int threads = A.fusedThreads > 0 ? A.fusedThreads : ((A.n + sms - 1) / sms + 31) / 32 * 32;
     threads = threads < 128 ? 128 : (threads > FUSED_MAX_THREADS ? FUSED_MAX_THREADS : threads);
     threads = (threads + 31) / 32 * 32;
-    int perSm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_step_fused<Venue, kPerAgent, kB>, threads, FUSED_SMEM);
+    static int occThreads = -1, occPerSm = 0;   // the occupancy of the last block size asked for
+    if (occThreads != threads) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occPerSm, k_step_fused<Venue, kPerAgent, kB, kTape>, threads, FUSED_SMEM);
+        occThreads = threads;
+    }
+    int perSm = occPerSm;
     if (A.fusedBlocksPerSm > 0 && A.fusedBlocksPerSm < perSm) perSm = A.fusedBlocksPerSm;
     const int resident = perSm * sms;
     if (resident <= 0) return cudaErrorCooperativeLaunchTooLarge;
@@ -758,7 +770,7 @@ static cudaError_t fusedImpl(const StepArgs& A, cudaStream_t st) {
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_step_fused<Venue, kPerAgent, kB>, A);
+    return cudaLaunchKernelEx(&cfg, k_step_fused<Venue, kPerAgent, kB, kTape>, A);
 }
 
 cudaError_t launch_step_fused(const StepArgs& A, cudaStream_t st) {
@@ -790,6 +802,10 @@ void launch_step_taped(const StepArgs& A, float4* const* q, float4* const* corr,
     if (K > 0) k_final<GridVenue, false, true><<<blocks(n, 128), 128, 0, st>>>(B, 0);
     else k_final<GridVenue, false, false><<<blocks(n, 128), 128, 0, st>>>(B, 0);
     *launches += 2 + (K > 1 ? K - 1 : 0);
+}
+
+cudaError_t launch_step_fused_taped(const StepArgs& A, cudaStream_t st) {
+    return fusedImpl<GridVenue, true, false, true>(A, st);
 }
 
 void launch_stage(const StepArgs& A, int stage, cudaStream_t st, int64_t* launches) {

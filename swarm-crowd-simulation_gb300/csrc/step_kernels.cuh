@@ -15,6 +15,9 @@ void launch_stage(const StepArgs& A, int stage, cudaStream_t st, int64_t* launch
 // corrections, qK the last sweep's result, pred predict's separation / headway record
 void launch_step_taped(const StepArgs& A, float4* const* q, float4* const* corr, float4* qK, float4* pred, cudaStream_t st,
                        int64_t* launches);
+// the same as one fused launch (grid venue, one instance): proj[0] = q[0] with the sweeps' inputs n apart, tapeCorr =
+// corr[1] with the sweeps' corrections n apart, tapeQK, tapePred
+cudaError_t launch_step_fused_taped(const StepArgs& A, cudaStream_t st);
 // the whole step as one cooperative persistent kernel (grid barriers between the phases)
 cudaError_t launch_step_fused(const StepArgs& A, cudaStream_t st);
 

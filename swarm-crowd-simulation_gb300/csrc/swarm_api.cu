@@ -177,8 +177,10 @@ int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capac
              devAlloc(h, &h->dNav, nn) && cudaMemcpy(h->dNav, V.nav_dist, nn * 4, cudaMemcpyHostToDevice) == cudaSuccess;
         if (ok && V.floor_height)
             ok = devAlloc(h, &h->dFloor, nw) && cudaMemcpy(h->dFloor, V.floor_height, nw * 4, cudaMemcpyHostToDevice) == cudaSuccess;
-        if (ok && V.speed_factor)
+        if (ok && V.speed_factor) {
             ok = devAlloc(h, &h->dSpeed, nw) && cudaMemcpy(h->dSpeed, V.speed_factor, nw * 4, cudaMemcpyHostToDevice) == cudaSuccess;
+            for (size_t i = 0; i < nw; ++i) h->speedMax = std::max(h->speedMax, V.speed_factor[i]);
+        }
     }
     if (V.n_exits > 0 && V.exit_boxes) h->exitBoxesHost.assign(V.exit_boxes, V.exit_boxes + 4 * size_t(V.n_exits));
     // host pointers of the venue are not kept

@@ -37,9 +37,10 @@ def _with_k(P, k):
     return q
 
 
-def _gpu(P, venue, b, r, v0, steps, ckpt, stats=False):
+def _gpu(P, venue, b, r, v0, steps, ckpt, stats=False, fused=True):
     import swarm_gb300
     sim = swarm_gb300.CrowdSim(P, venue, b.shape[0])
+    sim.set_fused(fused)
     sim.set_state(b)
     sim.set_agent_params(r, v0)
     out = sim.adjoint(steps, ckpt, stats=stats)
@@ -57,9 +58,9 @@ def _directions(n, rng, singles):
     return dirs[:8]
 
 
-def _check_against_dual(P, venue, b, r, v0, steps, ckpt, singles=(3, 10, 27, 44), seed=0):
+def _check_against_dual(P, venue, b, r, v0, steps, ckpt, singles=(3, 10, 27, 44), seed=0, fused=True):
     n = b.shape[0]
-    _, (L, gv, gr, gt) = _gpu(P, venue, b, r, v0, steps, ckpt)
+    _, (L, gv, gr, gt) = _gpu(P, venue, b, r, v0, steps, ckpt, fused=fused)
     dirs = _directions(n, np.random.default_rng(seed), singles)
     dr = np.stack([d[0] for d in dirs]); dv = np.stack([d[1] for d in dirs]); dt = np.array([d[2] for d in dirs])
     L32, dl, _, _ = O.grad_eval(32, P, venue.struct, b, r, v0, P.tau_relax, steps, dirs=(dr, dv, dt))
@@ -72,10 +73,11 @@ def _check_against_dual(P, venue, b, r, v0, steps, ckpt, singles=(3, 10, 27, 44)
     return gv, gr, gt
 
 
+@pytest.mark.parametrize("fused", [True, False], ids=["fused", "per-phase"])
 @pytest.mark.parametrize("k", [8, 1, 0])
-def test_adjoint_small_hall_matches_dual(small, k):
+def test_adjoint_small_hall_matches_dual(small, k, fused):
     P, venue, b, r, v0 = small
-    _check_against_dual(_with_k(P, k), venue, b, r, v0, steps=40, ckpt=7)
+    _check_against_dual(_with_k(P, k), venue, b, r, v0, steps=40, ckpt=7, fused=fused)
 
 
 def test_adjoint_checkpoint_interval_and_repeatability(small):
@@ -96,7 +98,12 @@ def test_adjoint_terrace_4096(built):
     from swarm_gb300 import venues as V
     P = swarm_gb300.params_si()
     venue, (b, r, v0) = V.terrace_c0()
-    _check_against_dual(P, venue, b, r, v0, steps=60, ckpt=20, singles=(100, 2047, 3000, 4095))
+    gv, gr, gt = _check_against_dual(P, venue, b, r, v0, steps=60, ckpt=20, singles=(100, 2047, 3000, 4095))
+    # the per-phase reverse sums each gather in one order, the fused one over 4 lanes: the same gradient to rounding
+    _, (L2, gv2, gr2, gt2) = _gpu(P, venue, b, r, v0, 60, 20, fused=False)
+    for a, c in ((gv, gv2), (gr, gr2)):
+        assert np.abs(a - c).max() <= 1e-4 * np.abs(c).max()
+    assert abs(gt - gt2) <= 1e-4 * abs(gt2)
 
 
 def test_adjoint_vs_fp64_central_differences(small):
