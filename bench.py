@@ -17,6 +17,9 @@ roofline  the dominant kernel's algorithmic bytes per launch (bytes per agent x 
        HBM copy bandwidth (MEASURED_PEAKS.json).
 cpu_baseline  the oracle port of the reference's CPU step (OpenMP, all host threads) on a bounded sample of the same
        workload.
+batched  the 256-instance batch as one packed state against the same instances launched one at a time.
+adjoint  loss and gradient of 400 steps of the 16 384-agent hall (checkpoints every 20 steps, and the full tape)
+       against the plain forward of the same steps.
 --impl reference  the reference's CPU step (the oracle port: the reference's own build needs its source tree, which
        only exists where the oracle was pinned) on the host cores, same workload, metric and unit.
 """
@@ -177,6 +180,78 @@ def bench_batched(P, steps=10, warmup=3):
             "fraction_of_hbm_roofline": active / (t_batch * 1e-3) * B_STEP / (peaks()[0] * 1e9)}
 
 
+def adjoint_bytes(K, steps, ckpt):
+    """Algorithmic bytes per agent-step of the adjoint with checkpoints every `ckpt` steps: the forward work (2T - C
+    steps of B_step) plus the tape (written once, read once: per agent (2K + 6) float4 of positions, velocities,
+    planes, the predict record and the sweeps' corrections, and 17 B of params, ids and contact bits) plus the
+    reverse's own traffic (the state adjoint read and written, 64 B; each sweep's correction-sum adjoint written and
+    read, 16 B; the per-slot adjoints of the final pass, predict and gather, 7 x 16 + 4 B)."""
+    b_step = 336.0 + 48.0 * (K - 1)
+    forward = b_step * (2.0 * steps - min(ckpt, steps)) / steps
+    tape = 2.0 * ((2 * K + 6) * 16.0 + 17.0)
+    reverse = 64.0 + 16.0 * K + 7 * 16.0 + 4.0
+    return forward + tape + reverse
+
+
+def bench_adjoint(P, steps=400, ckpt=20):
+    """The adjoint on the 16 384-agent hall (80 m x 70 m, two 4 m exits, 128 x 128 lattice at 0.5 m, seed 0): the
+    loss L = dt * sum_t sum_i D(p_i(t)) of 400 steps from the spawn and its gradient with respect to every agent's
+    desired speed and radius and the relaxation time, checkpoints every 20 steps. Against the plain forward of the
+    same 400 steps. Both timed with CUDA events on the handle's stream (inputs larger than L2 are not at stake: the
+    working set, 16 384 agents, is L2-resident on both sides)."""
+    import torch
+    import swarm_gb300
+    from swarm_gb300 import venues
+    venue, (boids, r, v0) = venues.terrace_c4()
+    n = boids.shape[0]
+    stream = torch.cuda.Stream()
+    sim = swarm_gb300.CrowdSim(P, venue, n)
+    sim.set_stream(stream.cuda_stream)
+    sim.set_agent_params(r, v0)
+    # agent-steps: the agents active at the start of each of the 400 steps
+    sim.set_state(boids)
+    active = 0
+    for _ in range(steps):
+        active += int((sim.state()[:, 3] != 0).sum())
+        sim.step(1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sim.set_state(boids)
+    sim.step(3)
+    sim.set_state(boids)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    sim.step(steps)
+    e1.record(stream)
+    e1.synchronize()
+    fwd_ms = e0.elapsed_time(e1)
+    out = {"workload": "hall 80x70 m, 2 exits of 4 m, 16384 agents (128x128 lattice, 0.5 m), 400 steps from the "
+                       "spawn, loss dt*sum_t sum_i D(p_i(t)), gradient wrt v0_i, r_i, tau",
+           "steps": steps, "agent_steps": active, "forward_ms_per_step": fwd_ms / steps}
+    for c in (ckpt, steps):
+        sim.set_state(boids)
+        sim.adjoint(steps, c)   # allocation and warm-up
+        torch.cuda.synchronize()
+        e0.record(stream)
+        L, gv, gr, gt, st = sim.adjoint(steps, c, stats=True)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        value = active / (ms * 1e-3)
+        b = adjoint_bytes(P.proj_iterations, steps, c)
+        rec = {"ckpt_every": c, "value": value, "unit": UNIT, "ms_per_step": ms / steps,
+               "ratio_vs_forward": ms / fwd_ms, "loss": L, "dL_dtau": gt,
+               "bytes_per_agent_step": b, "fraction_of_hbm_roofline": value * b / (peaks()[0] * 1e9),
+               "tape_bytes": st["tape_bytes"], "launches": st["launches"],
+               "ms": {k: round(st[k], 3) for k in ("ms_checkpoint", "ms_recompute", "ms_reverse", "ms_rev_final",
+                                                   "ms_rev_sweeps", "ms_rev_predict", "ms_rev_gather")}}
+        if c == ckpt:
+            out.update(rec)
+        else:
+            out["full_tape"] = rec
+    sim.close()
+    return out
+
+
 def cpu_baseline(budget_s=12.0, max_steps=400):
     """The oracle port (OpenMP, every host thread) on the same workload: 2 warm-up steps, then steps until the budget."""
     import numpy as np
@@ -224,6 +299,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--phase-kernels", action="store_true", help="one kernel per phase instead of the fused step")
     ap.add_argument("--no-batch", action="store_true", help="skip the 256-instance batched measurement")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -379,6 +455,11 @@ def main():
                 line["batched"] = bench_batched(P)
             except Exception as e:  # reported, not fatal
                 line["batched"] = {"error": str(e)[:300]}
+        if not args.no_adjoint and world == 1:
+            try:
+                line["adjoint"] = bench_adjoint(P)
+            except Exception as e:  # reported, not fatal
+                line["adjoint"] = {"error": str(e)[:300]}
         if not args.no_cpu_baseline and world == 1:
             try:
                 line["cpu_baseline"] = cpu_baseline()

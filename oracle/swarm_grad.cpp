@@ -713,11 +713,13 @@ int grad_eval(int prec, const SwarmParams* p, const SwarmVenue* v, const float* 
     if (prec == 32) {
         if (nt == 0) return runT<float>(*p, *v, state, n, radius, v0, tau, steps, th, 0, nullptr, nullptr, nullptr, loss, nullptr, sig, stateOut);
         if (nt == 1) return runT<Dual<float, 1>>(*p, *v, state, n, radius, v0, tau, steps, th, nt, dr, dv0, dtau, loss, dloss, sig, stateOut);
+        if (nt <= 4) return runT<Dual<float, 4>>(*p, *v, state, n, radius, v0, tau, steps, th, nt, dr, dv0, dtau, loss, dloss, sig, stateOut);
         return runT<Dual<float, 8>>(*p, *v, state, n, radius, v0, tau, steps, th, nt, dr, dv0, dtau, loss, dloss, sig, stateOut);
     }
     if (prec == 64) {
         if (nt == 0) return runT<double>(*p, *v, state, n, radius, v0, tau, steps, th, 0, nullptr, nullptr, nullptr, loss, nullptr, sig, stateOut);
         if (nt == 1) return runT<Dual<double, 1>>(*p, *v, state, n, radius, v0, tau, steps, th, nt, dr, dv0, dtau, loss, dloss, sig, stateOut);
+        if (nt <= 4) return runT<Dual<double, 4>>(*p, *v, state, n, radius, v0, tau, steps, th, nt, dr, dv0, dtau, loss, dloss, sig, stateOut);
         return runT<Dual<double, 8>>(*p, *v, state, n, radius, v0, tau, steps, th, nt, dr, dv0, dtau, loss, dloss, sig, stateOut);
     }
     g_err = "prec must be 32 or 64";
