@@ -18,6 +18,7 @@ roofline  the dominant kernel's algorithmic bytes per launch (bytes per agent x 
 cpu_baseline  the oracle port of the reference's CPU step (OpenMP, all host threads) on a bounded sample of the same
        workload.
 batched  the 256-instance batch as one packed state against the same instances launched one at a time.
+bowl   the 63 488-agent seated bowl: the plain step (as value) and its evacuation run to completion.
 adjoint  loss and gradient of 400 steps of the 16 384-agent hall (checkpoints every 20 steps, and the full tape)
        against the plain forward of the same steps.
 --impl reference  the reference's CPU step (the oracle port: the reference's own build needs its source tree, which
@@ -180,6 +181,60 @@ def bench_batched(P, steps=10, warmup=3):
             "fraction_of_hbm_roofline": active / (t_batch * 1e-3) * B_STEP / (peaks()[0] * 1e9)}
 
 
+def bench_bowl(P, steps=50, warmup=5, cap=20000, chunk=100):
+    """The seated bowl (32 sectors x 32 rows x 62 seats = 63 488 agents; stairs, vomitories, perimeter exits): the
+    plain step timed as the main workload (CUDA events per step on the handle's stream, the L2 flushed by a 256 MiB
+    write before each), then the evacuation run from the seats (checked every `chunk` steps): the steps until 99.9 %
+    of the crowd is out, and how many are left after `cap` steps (a few agents end in symmetric standoffs at gangway
+    feet that the deterministic model never breaks)."""
+    import torch
+    import swarm_gb300
+    from swarm_gb300 import venues
+    venue, (boids, r, v0) = venues.bowl_c2()
+    n = boids.shape[0]
+    stream = torch.cuda.Stream()
+    sim = swarm_gb300.CrowdSim(P, venue, n)
+    sim.set_stream(stream.cuda_stream)
+    sim.set_state(boids)
+    sim.set_agent_params(r, v0)
+    sim.set_graph(True)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    with torch.cuda.stream(stream):
+        sim.step(warmup)
+    torch.cuda.synchronize()
+    active, total_ms = 0, 0.0
+    for k in range(steps):
+        active += int((sim.state()[:, 3] != 0).sum())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xFF)
+            e0.record(stream)
+            sim.step(1)
+            e1.record(stream)
+        stream.synchronize()
+        total_ms += e0.elapsed_time(e1)
+    value = active / (total_ms * 1e-3)
+    # the evacuation from the seats
+    sim.set_state(boids)
+    t999, left, t0 = None, n, time.perf_counter()
+    for s in range(chunk, cap + 1, chunk):
+        sim.step(chunk)
+        left = int((sim.state()[:, 3] != 0).sum())
+        if t999 is None and left <= n // 1000:
+            t999 = s
+        if left == 0:
+            break
+    wall_s = time.perf_counter() - t0
+    sim.close()
+    return {"workload": "seated bowl, 32 sectors x 32 rows x 62 seats (63488 agents), seat 0.5 m, row pitch 0.8 m, "
+                        "rise 0.4 m, 1.2 m gangway stairs (speed factor 0.6), 2.4 m vomitories at row 16, 8 perimeter "
+                        "exits of 4 m; wall SDF 0.05 m, nav 0.1 m",
+            "value": value, "unit": UNIT, "ms_per_step": total_ms / steps, "steps": steps, "warmup": warmup,
+            "fraction_of_hbm_roofline": value * B_STEP / (peaks()[0] * 1e9),
+            "evacuation": {"steps_to_99.9pct": t999, "seconds_to_99.9pct": None if t999 is None else t999 * float(P.dt),
+                           "left_after": {"steps": s, "agents": left}, "checked_every": chunk, "wall_s": wall_s}}
+
+
 def adjoint_bytes(K, steps, ckpt):
     """Algorithmic bytes per agent-step of the adjoint with checkpoints every `ckpt` steps: the forward work (2T - C
     steps of B_step) plus the tape (written once, read once: per agent (2K + 6) float4 of positions, velocities,
@@ -300,6 +355,7 @@ def main():
     ap.add_argument("--phase-kernels", action="store_true", help="one kernel per phase instead of the fused step")
     ap.add_argument("--no-batch", action="store_true", help="skip the 256-instance batched measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
+    ap.add_argument("--no-bowl", action="store_true", help="skip the seated-bowl measurement")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -455,6 +511,11 @@ def main():
                 line["batched"] = bench_batched(P)
             except Exception as e:  # reported, not fatal
                 line["batched"] = {"error": str(e)[:300]}
+        if not args.no_bowl and world == 1:
+            try:
+                line["bowl"] = bench_bowl(P)
+            except Exception as e:  # reported, not fatal
+                line["bowl"] = {"error": str(e)[:300]}
         if not args.no_adjoint and world == 1:
             try:
                 line["adjoint"] = bench_adjoint(P)

@@ -123,6 +123,10 @@ typedef struct SwarmVenue {
     /* metrics: the 1 m floor grid, metric_res^2 cells centred on metric_center */
     int32_t metric_res;
     float metric_center_x, metric_center_y;
+    /* grid venues, optional: nav_nx x nav_ny bytes, nonzero at the nodes beyond an exit. When set, an agent is
+     * parked when the nav node nearest to it is an exit node (or it leaves the domain) instead of by the exit
+     * rectangle: exits anywhere in the plan, such as vomitories inside a seating bowl. */
+    const uint8_t* exit_mask;
 } SwarmVenue;
 
 typedef struct SwarmSim* SwarmHandle;
@@ -234,6 +238,40 @@ typedef struct SwarmHallSpec {
 int swarm_hall_layout(const SwarmHallSpec* spec, SwarmVenue* venue);
 /* Fills the arrays of a layout made by swarm_hall_layout (caller-allocated). */
 int swarm_hall_fields(const SwarmHallSpec* spec, const SwarmVenue* venue, float* wall_sdf, float* nav_dist, float* exit_boxes);
+
+/* A seated bowl (the generated venue of the seated-bowl workload): `sectors` straight blocks of `rows` rows x `seats`
+ * seats around a regular polygon, rising `rise` per row of depth `row_pitch`; each row is a tread between thin walls
+ * (its front and back edges; the first row opens onto a flat cross-aisle along the pitch wall), so agents walk
+ * along their row to the gangways between blocks; gangways are stairs of rise / 2 steps (speed factor stair_speed)
+ * from the cross-aisle up to a flat concourse of depth concourse behind the top row; a vomitory (an exit portal vomitory_width wide) lies across every gangway at row vomitory_row;
+ * perimeter_exits gaps of perimeter_exit_width in the concourse's outer wall, evenly spaced, lead out. The floor
+ * heightfield and the speed factors are on the wall grid; the nav field is the speed-weighted travel distance to the
+ * nearest exit (one plan-view field: the levels never overlap in plan). All lengths in metres. */
+typedef struct SwarmBowlSpec {
+    int32_t sectors, rows, seats;       /* 32, 32, 62 */
+    float seat_width, row_pitch, rise;  /* 0.5, 0.8, 0.4 */
+    float gangway;                      /* width at the pitch wall (the gap between blocks widens upward): 1.2 */
+    float vomitory_width;               /* 2.4 */
+    int32_t vomitory_row;               /* 16 (0-based) */
+    int32_t perimeter_exits;            /* 8 */
+    float perimeter_exit_width;         /* 4 */
+    float concourse;                    /* 4 */
+    float aisle;                        /* the cross-aisle in front of the first row (the pitch wall beyond it): 1.2 */
+    float stair_speed;                  /* 0.6 */
+    float clearance;                    /* the nav field treats nodes this close to a wall as walls: 0.25 (the
+                                           largest body radius) */
+    float wall_h, nav_h, cell;          /* 0.05, 0.1, 0.5 */
+} SwarmBowlSpec;
+/* Fills every scalar of *venue; array sizes as swarm_hall_layout, plus the exit mask (nav_nx * nav_ny bytes) and the
+ * floor heights and speed factors (wall_nx * wall_ny floats each); n_exits = sectors + perimeter_exits. */
+int swarm_bowl_layout(const SwarmBowlSpec* spec, SwarmVenue* venue);
+/* Fills the arrays of a layout made by swarm_bowl_layout (caller-allocated); exit_boxes: each exit's bounding box. */
+int swarm_bowl_fields(const SwarmBowlSpec* spec, const SwarmVenue* venue, float* wall_sdf, float* nav_dist,
+                      float* floor_height, float* speed_factor, uint8_t* exit_mask, float* exit_boxes);
+/* One agent per seat (sectors x rows x seats, by sector, row, seat) at the seat centre jittered U(-jitter, jitter)
+ * per axis, on the floor (z = floor + radius), at rest; radius and desired speed as swarm_spawn_lattice. */
+int swarm_spawn_bowl(const SwarmBowlSpec* spec, float jitter, uint64_t seed, float r_lo, float r_hi, float v_mean,
+                     float v_sd, float v_lo, float v_hi, float* boids, float* radius, float* v0);
 
 /* A jittered lattice of nx x ny agents (row-major, the first n of them) at `spacing`, centred on (cx, cy), resting on
  * the floor (z = radius), at rest. Jitter U(-jitter, jitter) per axis, radius U[r_lo, r_hi], desired speed

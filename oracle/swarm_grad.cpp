@@ -262,10 +262,17 @@ struct GVen {
     V2<S> goal(V3<S> p, Sig* g) const { V2<S> e; navSample(xy(p), nullptr, &e, g); return e; }
 
     bool exits(V4<S> p) const {
+        using Pt = typename Prim<S>::type;
         const double x = val(p.x), y = val(p.y), z = val(p.z);
         const float dmaxX = V.domain_min_x + V.domain_span_x, dmaxY = V.domain_min_y + V.domain_span_y;
-        bool out = x < V.exit_lo_x || x > V.exit_hi_x || y < V.exit_lo_y || y > V.exit_hi_y;
         bool outDomain = x < V.domain_min_x || x > dmaxX || y < V.domain_min_y || y > dmaxY;
+        if (V.exit_mask) {   // the exit mask: the nav node nearest to p (in the primal type)
+            const Pt inv = Pt(1) / Pt(V.nav_h);
+            const Pt fx = (Pt(x) - Pt(V.nav_origin_x)) * inv + Pt(0.5f), fy = (Pt(y) - Pt(V.nav_origin_y)) * inv + Pt(0.5f);
+            const int ix = std::clamp(int(std::floor(fx)), 0, V.nav_nx - 1), iy = std::clamp(int(std::floor(fy)), 0, V.nav_ny - 1);
+            return outDomain || V.exit_mask[size_t(iy) * size_t(V.nav_nx) + size_t(ix)] != 0;
+        }
+        bool out = x < V.exit_lo_x || x > V.exit_hi_x || y < V.exit_lo_y || y > V.exit_hi_y;
         return (out && z < V.exit_max_z) || outDomain;
     }
 

@@ -640,8 +640,13 @@ struct GridVenue {
     }
 
     bool exits(F4 p) const {
-        bool out = p.x < V.exit_lo_x || p.x > V.exit_hi_x || p.y < V.exit_lo_y || p.y > V.exit_hi_y;
         bool outDomain = p.x < domMinX || p.x > domMaxX || p.y < domMinY || p.y > domMaxY;
+        if (V.exit_mask) {   // the exit mask: the nav node nearest to p
+            float fx = (p.x - V.nav_origin_x) * navInvH + 0.5f, fy = (p.y - V.nav_origin_y) * navInvH + 0.5f;
+            int ix = std::clamp(int(std::floor(fx)), 0, V.nav_nx - 1), iy = std::clamp(int(std::floor(fy)), 0, V.nav_ny - 1);
+            return outDomain || V.exit_mask[size_t(iy) * size_t(V.nav_nx) + size_t(ix)] != 0;
+        }
+        bool out = p.x < V.exit_lo_x || p.x > V.exit_hi_x || p.y < V.exit_lo_y || p.y > V.exit_hi_y;
         return (out && p.z < V.exit_max_z) || outDomain;
     }
 
@@ -745,6 +750,7 @@ struct Sim {
     SwarmParams P;
     SwarmVenue V;
     std::vector<float> sdf, wallSdf, navDist, floorH, speedF, exitBoxes;
+    std::vector<uint8_t> exitMask;
     int threads;
     int n = 0;
     std::vector<Boid> boids[2];
@@ -773,6 +779,7 @@ struct Sim {
             V.nav_dist = navDist.data();
             if (V.floor_height) { floorH.assign(V.floor_height, V.floor_height + wallSdf.size()); V.floor_height = floorH.data(); }
             if (V.speed_factor) { speedF.assign(V.speed_factor, V.speed_factor + wallSdf.size()); V.speed_factor = speedF.data(); }
+            if (V.exit_mask) { exitMask.assign(V.exit_mask, V.exit_mask + navDist.size()); V.exit_mask = exitMask.data(); }
         }
         if (V.n_exits > 0 && V.exit_boxes) { exitBoxes.assign(V.exit_boxes, V.exit_boxes + 4 * V.n_exits); V.exit_boxes = exitBoxes.data(); }
         cells.assign(size_t(resX) * size_t(resY), Cell{0, 0});

@@ -801,8 +801,8 @@ __global__ void __launch_bounds__(128) k_adj_gather(AdjArgs A) {
 // ---- the whole reverse step as one persistent kernel ----
 // Every block stays resident (a cooperative launch); the phases are separated by a grid barrier on one word: block 0
 // adds 2^31 - (blocks - 1), every other block 1, so the word's top bit flips once all have arrived; a block waits for
-// the flip at most ADJ_BARRIER_WAIT_NS of %globaltimer, then records ERR_TIMEOUT and stops waiting for the rest of
-// the launch (the host reports SWARM_E_TIMEOUT).
+// the flip at most ADJ_BARRIER_WAIT_NS of %globaltimer, then records ERR_TIMEOUT and leaves the kernel, as does every
+// block that finds ERR_TIMEOUT at a later barrier (the host reports SWARM_E_TIMEOUT).
 constexpr uint64_t ADJ_BARRIER_WAIT_NS = 1000000000ull;
 
 __device__ __forceinline__ uint64_t adjNs() {
@@ -811,21 +811,28 @@ __device__ __forceinline__ uint64_t adjNs() {
     return t;
 }
 
-__device__ __forceinline__ void adjBarrier(const AdjArgs& A) {
+// Returns false (the same in every thread of the block) when the block must leave the kernel: its wait ran out, or
+// another block's did (no phase runs on data another block has not finished)
+__device__ __forceinline__ bool adjBarrier(const AdjArgs& A) {
+    __shared__ int leave;
     __syncthreads();
     if (threadIdx.x == 0) {
         cuda::atomic_ref<int, cuda::thread_scope_device> err(*A.err);
+        int out = 1;
         if (!(err.load(cuda::memory_order_relaxed) & ERR_TIMEOUT)) {
             cuda::atomic_ref<unsigned, cuda::thread_scope_device> word(*A.barrier);
             const unsigned add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
             const unsigned old = word.fetch_add(add, cuda::memory_order_release);
             const uint64_t t0 = adjNs();
+            out = 0;
             while (((word.load(cuda::memory_order_acquire) ^ old) & 0x80000000u) == 0u) {
-                if (adjNs() - t0 > ADJ_BARRIER_WAIT_NS) { err.fetch_or(ERR_TIMEOUT, cuda::memory_order_relaxed); break; }
+                if (adjNs() - t0 > ADJ_BARRIER_WAIT_NS) { err.fetch_or(ERR_TIMEOUT, cuda::memory_order_relaxed); out = 1; break; }
             }
         }
+        leave = out;
     }
     __syncthreads();
+    return leave == 0;
 }
 
 // Timing on: block 0 adds the span since *t0 to stamps[i] and restarts the clock
@@ -849,7 +856,7 @@ __global__ void __launch_bounds__(ADJ_FUSED_THREADS, 1) k_adj_step_fused(AdjArgs
     for (int s = tid; s < n; s += stride) d += adjFinalSlot(A, s);
     const double t = blockSum<ADJ_FUSED_THREADS>(d, warpSum);
     if (threadIdx.x == 0) A.lossPart[blockIdx.x] = t;
-    adjBarrier(A);
+    if (!adjBarrier(A)) return;
     adjStamp(A, 0, t0);
     // the sweeps, last to first: G lanes per slot (warp-uniform loop)
     const int groups = stride / G, g0 = tid / G;
@@ -861,7 +868,7 @@ __global__ void __launch_bounds__(ADJ_FUSED_THREADS, 1) k_adj_step_fused(AdjArgs
         if (valid) rows3(A, A.skey[s], rows, rows + 3);
         for (int k = K; k >= 1; --k) {
             if (g0 - (g0 % (32 / G)) < nActive) adjSweepSlot<G>(A, s, lane, valid, k, rows);
-            adjBarrier(A);
+            if (!adjBarrier(A)) return;
         }
     } else {
         for (int k = K; k >= 1; --k) {
@@ -869,12 +876,12 @@ __global__ void __launch_bounds__(ADJ_FUSED_THREADS, 1) k_adj_step_fused(AdjArgs
                 const int s = base + (g0 % (32 / G));
                 adjSweepSlot<G>(A, s, lane, sweepsSlot(A, s), k);
             }
-            adjBarrier(A);
+            if (!adjBarrier(A)) return;
         }
     }
     adjStamp(A, 1, t0);
     for (int s = tid; s < nActive; s += stride) adjPredictSlot(A, s);
-    adjBarrier(A);
+    if (!adjBarrier(A)) return;
     adjStamp(A, 2, t0);
     if (A.stamps && blockIdx.x == 0 && threadIdx.x == 0) A.stamps[4] = t0;   // the gather's start
     for (int base = g0 - (g0 % (32 / G)); base < nActive; base += groups) {

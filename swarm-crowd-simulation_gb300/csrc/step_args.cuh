@@ -35,6 +35,7 @@ struct VenueArgs {
     float nox, noy, ninv;
     const float* floorH;
     const float* speedF;
+    const uint8_t* exitMask;    // optional: nonzero at the nav nodes beyond an exit
     uint32_t cellOffset;    // batched instances: this instance's first cell in the shared key space (0 otherwise)
 };
 

@@ -177,7 +177,9 @@ __device__ __forceinline__ void rankGatherItem(const StepArgs& A, int s) {
     if (me >= uint32_t(A.n)) { atomicOr(A.err, ERR_BOUNDS); return; }
     if (s >= nActive) { A.sid[s] = me; A.skey[s] = INACTIVE_CELL; return; }
     const uint32_t c = A.key[me];
+    if (c >= uint32_t(A.V.ncells)) { atomicOr(A.err, ERR_BOUNDS); return; }   // keys and counts out of step
     const uint2 cs = A.cells[c];
+    if (uint64_t(cs.x) + cs.y > uint64_t(A.n)) { atomicOr(A.err, ERR_BOUNDS); return; }
     uint32_t r = 0;
     for (uint32_t j = cs.x; j < cs.x + cs.y; ++j) r += A.sidTmp[j] < me ? 1u : 0u;
     const uint32_t t = cs.x + r;
@@ -518,8 +520,9 @@ __global__ void __launch_bounds__(128) k_final(StepArgs A, int inBuf) {
 // Every block stays resident (a cooperative launch) and the phases are separated by grid barriers. A barrier is a
 // counter and a generation word: the last block to arrive resets the counter and advances the generation (release);
 // the others wait for the generation to move (acquire) for at most BARRIER_WAIT_NS of wall-clock time (%globaltimer),
-// after which the kernel records ERR_TIMEOUT and stops waiting: every later barrier of the launch returns at once,
-// the launch ends, and the host reports SWARM_E_TIMEOUT and resets the barrier words.
+// after which the block records ERR_TIMEOUT and leaves the kernel; a block that finds ERR_TIMEOUT set at a barrier
+// leaves too, so no phase ever runs on data another block has not finished; the host reports SWARM_E_TIMEOUT and
+// resets the barrier words.
 constexpr uint64_t BARRIER_WAIT_NS = 1000000000ull;   // 1 s; a healthy barrier waits microseconds
 
 __device__ __forceinline__ uint64_t globalNs() {
@@ -536,21 +539,27 @@ __device__ __forceinline__ void stamp(const StepArgs& A, int i) {
 // One word per barrier: block 0 adds 2^31 - (expected - 1), every other block adds 1, so the word's top bit flips
 // exactly when all `expected` blocks have arrived; each block waits for the flip of the value it saw (the scheme of
 // CUDA's cooperative groups grid sync). Release before the add, acquire on the poll.
-__device__ __forceinline__ void gridBarrier(const StepArgs& A, unsigned expected) {
+// Returns false (the same in every thread of the block) when the block must leave the kernel.
+__device__ __forceinline__ bool gridBarrier(const StepArgs& A, unsigned expected) {
+    __shared__ int leave;
     __syncthreads();
     if (threadIdx.x == 0) {
         cuda::atomic_ref<int, cuda::thread_scope_device> err(*A.err);
+        int out = 1;
         if (!(err.load(cuda::memory_order_relaxed) & ERR_TIMEOUT)) {
             cuda::atomic_ref<unsigned, cuda::thread_scope_device> word(A.barrier[0]);
             const unsigned add = blockIdx.x == 0 ? 0x80000000u - (expected - 1u) : 1u;
             const unsigned old = word.fetch_add(add, cuda::memory_order_release);
             const uint64_t t0 = globalNs();
+            out = 0;
             while (((word.load(cuda::memory_order_acquire) ^ old) & 0x80000000u) == 0u) {
-                if (globalNs() - t0 > BARRIER_WAIT_NS) { err.fetch_or(ERR_TIMEOUT, cuda::memory_order_relaxed); break; }
+                if (globalNs() - t0 > BARRIER_WAIT_NS) { err.fetch_or(ERR_TIMEOUT, cuda::memory_order_relaxed); out = 1; break; }
             }
         }
+        leave = out;
     }
     __syncthreads();
+    return leave == 0;
 }
 
 // The sweeps' neighbour data for the fused kernel, once per step: each active slot's 3 x 3 rows, and each tile of
@@ -591,24 +600,24 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A)
     stamp(A, 0);
     if (!A.hashed) {   // (the previous fused step's final pass counted the keys already)
         for (int base = tid - int(threadIdx.x & 31u); base < n; base += stride) hashItem<kB>(A, base + int(threadIdx.x & 31u));
-        gridBarrier(A, gridDim.x);
+        if (!gridBarrier(A, gridDim.x)) return;
     }
     const int tiles = (A.V.ncells + 1 + T * SCAN_ITEMS - 1) / (T * SCAN_ITEMS);
     for (int t = blockIdx.x; t < tiles; t += gridDim.x) scanReduceTile(A, t, warpSums);
-    gridBarrier(A, gridDim.x + unsigned(A.barrierExtra));   // barrierExtra: the timeout test's block that never arrives
+    if (!gridBarrier(A, gridDim.x + unsigned(A.barrierExtra))) return;   // barrierExtra: the timeout test's block that never arrives
     for (int t = blockIdx.x; t < tiles; t += gridDim.x) scanApplyTile(A, t, warpSums, &prefix);
-    gridBarrier(A, gridDim.x);
+    if (!gridBarrier(A, gridDim.x)) return;
     for (int i = tid; i < n; i += stride) scatterItem(A, i);
-    gridBarrier(A, gridDim.x);
+    if (!gridBarrier(A, gridDim.x)) return;
     for (int s = tid; s < n; s += stride) rankGatherItem<kPerAgent, kB>(A, s);
-    gridBarrier(A, gridDim.x);
+    if (!gridBarrier(A, gridDim.x)) return;
     stamp(A, 1);
     const int nActive = int(A.start[A.V.ncells]);
     for (int s = tid; s < n; s += stride) {
         predictItem<Venue, kB, kTape>(A, s);
         if (s < nActive) prepareSweepItem<kB>(A, s, nActive, T);
     }
-    gridBarrier(A, gridDim.x);
+    if (!gridBarrier(A, gridDim.x)) return;
     stamp(A, 2);
     const int K = A.P.proj_iterations;
     const int activeTiles = (nActive + T - 1) / T;
@@ -658,7 +667,7 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A)
             if (own) dst[t * T + int(threadIdx.x)] = r;
         }
         in ^= 1;
-        gridBarrier(A, gridDim.x);
+        if (!gridBarrier(A, gridDim.x)) return;
     }
     stamp(A, 3);
     const int allTiles = (n + T - 1) / T;

@@ -66,7 +66,7 @@ StepArgs SwarmSim::args(int in) const {
     v.winv = V.wall_h > 0.0f ? 1.0f / V.wall_h : 0.0f;
     v.nav = dNav; v.nnx = V.nav_nx; v.nny = V.nav_ny; v.nox = V.nav_origin_x; v.noy = V.nav_origin_y;
     v.ninv = V.nav_h > 0.0f ? 1.0f / V.nav_h : 0.0f;
-    v.floorH = dFloor; v.speedF = dSpeed;
+    v.floorH = dFloor; v.speedF = dSpeed; v.exitMask = dMask;
     A.n = n;
     A.projectInFinal = P.proj_iterations > 0 ? 1 : 0;
     A.stateIn = state[in];
@@ -177,6 +177,8 @@ int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capac
              devAlloc(h, &h->dNav, nn) && cudaMemcpy(h->dNav, V.nav_dist, nn * 4, cudaMemcpyHostToDevice) == cudaSuccess;
         if (ok && V.floor_height)
             ok = devAlloc(h, &h->dFloor, nw) && cudaMemcpy(h->dFloor, V.floor_height, nw * 4, cudaMemcpyHostToDevice) == cudaSuccess;
+        if (ok && V.exit_mask)
+            ok = devAlloc(h, &h->dMask, nn) && cudaMemcpy(h->dMask, V.exit_mask, nn, cudaMemcpyHostToDevice) == cudaSuccess;
         if (ok && V.speed_factor) {
             ok = devAlloc(h, &h->dSpeed, nw) && cudaMemcpy(h->dSpeed, V.speed_factor, nw * 4, cudaMemcpyHostToDevice) == cudaSuccess;
             for (size_t i = 0; i < nw; ++i) h->speedMax = std::max(h->speedMax, V.speed_factor[i]);
@@ -185,7 +187,7 @@ int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capac
     if (V.n_exits > 0 && V.exit_boxes) h->exitBoxesHost.assign(V.exit_boxes, V.exit_boxes + 4 * size_t(V.n_exits));
     // host pointers of the venue are not kept
     h->V.sdf = nullptr; h->V.wall_sdf = nullptr; h->V.nav_dist = nullptr; h->V.floor_height = nullptr;
-    h->V.speed_factor = nullptr; h->V.exit_boxes = nullptr;
+    h->V.speed_factor = nullptr; h->V.exit_boxes = nullptr; h->V.exit_mask = nullptr;
     if (!ok) { delete h; return SWARM_E_OOM; }
     if (cudaMemset(h->count, 0, (size_t(h->ncells) + 1) * 4) != cudaSuccess || cudaMemset(h->errFlag, 0, 4) != cudaSuccess ||
         cudaMemset(h->barrier, 0, 16) != cudaSuccess ||
@@ -208,10 +210,10 @@ int swarm_batch_create(const SwarmParams* params, const SwarmVenue* venues, cons
     size_t total = 0, cells = 0, nWall = 0, nNav = 0;
     for (int i = 0; i < m; ++i) {
         const SwarmVenue& V = venues[i];
-        if (V.kind != SWARM_VENUE_GRID || counts[i] <= 0 || !V.wall_sdf || !V.nav_dist || V.floor_height || V.speed_factor ||
+        if (V.kind != SWARM_VENUE_GRID || counts[i] <= 0 || !V.wall_sdf || !V.nav_dist || V.floor_height || V.speed_factor || V.exit_mask ||
             V.grid_res_x <= 0 || V.grid_res_y <= 0 || V.wall_nx < 2 || V.wall_ny < 2 || V.nav_nx < 2 || V.nav_ny < 2 ||
             !(V.wall_h > 0.0f) || !(V.nav_h > 0.0f) || !(V.domain_span_x > 0.0f) || !(V.domain_span_y > 0.0f))
-            return SWARM_E_INVALID;   // plain grid venues only (no floor heights or speed factors in a batch)
+            return SWARM_E_INVALID;   // plain grid venues only (no floor heights, speed factors or exit masks in a batch)
         total += size_t(counts[i]);
         cells += size_t(V.grid_res_x) * size_t(V.grid_res_y);
         nWall += size_t(V.wall_nx) * size_t(V.wall_ny);
@@ -223,6 +225,7 @@ int swarm_batch_create(const SwarmParams* params, const SwarmVenue* venues, cons
     all.grid_res_x = int(cells);
     all.grid_res_y = 1;
     all.floor_height = all.speed_factor = nullptr;
+    all.exit_mask = nullptr;
     all.n_exits = 0;
     all.exit_boxes = nullptr;
     SwarmHandle h = nullptr;

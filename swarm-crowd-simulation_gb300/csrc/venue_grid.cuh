@@ -52,8 +52,13 @@ struct GridVenue {
     }
 
     __device__ __forceinline__ bool exits(float4 p) const {
-        const bool out = p.x < V.exloX || p.x > V.exhiX || p.y < V.exloY || p.y > V.exhiY;
         const bool outDomain = p.x < V.dminX || p.x > V.dmaxX || p.y < V.dminY || p.y > V.dmaxY;
+        if (V.exitMask) {   // the exit mask: the nav node nearest to p
+            const float fx = (p.x - V.nox) * V.ninv + 0.5f, fy = (p.y - V.noy) * V.ninv + 0.5f;
+            const int ix = sclamp(int(floorf(fx)), 0, V.nnx - 1), iy = sclamp(int(floorf(fy)), 0, V.nny - 1);
+            return outDomain || __ldg(V.exitMask + size_t(iy) * size_t(V.nnx) + size_t(ix)) != 0;
+        }
+        const bool out = p.x < V.exloX || p.x > V.exhiX || p.y < V.exloY || p.y > V.exhiY;
         return (out && p.z < V.exMaxZ) || outDomain;
     }
 

@@ -15,6 +15,7 @@
 #include <cstdint>
 #include <limits>
 #include <queue>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -78,6 +79,49 @@ uint64_t splitmix64(uint64_t& s) {
 }
 double uniform01(uint64_t& s) { return double(splitmix64(s) >> 11) * 0x1.0p-53; }   // [0, 1)
 
+// First-order fast marching (Sethian 1996) on an nx x ny grid of spacing h. kind per node: 0 free, 1 source (0),
+// 3 wall (never entered). The local step is h / speed (speed: per node, null = 1): the travel distance in
+// flat-floor metres. Nodes never reached and walls get the largest reached value + 10 m, so the normalised negative
+// gradient never points into a wall.
+void fastMarch(int nx, int ny, double h, std::vector<uint8_t> state, const float* speed, float* out) {
+    const size_t M = size_t(nx) * size_t(ny);
+    const double INF = std::numeric_limits<double>::infinity();
+    std::vector<double> D(M, INF);
+    using Item = std::pair<double, size_t>;
+    std::priority_queue<Item, std::vector<Item>, std::greater<Item>> heap;
+    for (size_t k = 0; k < M; ++k) {   // state: 0 far, 1 trial, 2 known, 3 wall
+        if (state[k] == 1) { D[k] = 0.0; heap.push({0.0, k}); }
+    }
+    auto val = [&](int i, int j) -> double {
+        if (i < 0 || j < 0 || i >= nx || j >= ny) return INF;
+        const size_t k = size_t(j) * size_t(nx) + size_t(i);
+        return state[k] == 2 ? D[k] : INF;
+    };
+    while (!heap.empty()) {
+        const auto [d, k] = heap.top();
+        heap.pop();
+        if (state[k] == 2 || d > D[k]) continue;
+        state[k] = 2;
+        const int i = int(k % size_t(nx)), j = int(k / size_t(nx));
+        const int ni[4] = {i - 1, i + 1, i, i}, nj[4] = {j, j, j - 1, j + 1};
+        for (int q = 0; q < 4; ++q) {
+            if (ni[q] < 0 || nj[q] < 0 || ni[q] >= nx || nj[q] >= ny) continue;
+            const size_t kk = size_t(nj[q]) * size_t(nx) + size_t(ni[q]);
+            if (state[kk] >= 2) continue;
+            const double hs = speed ? h / double(speed[kk]) : h;
+            const double a = std::min(val(ni[q] - 1, nj[q]), val(ni[q] + 1, nj[q]));
+            const double b = std::min(val(ni[q], nj[q] - 1), val(ni[q], nj[q] + 1));
+            double T;
+            if (std::isinf(a) || std::isinf(b) || std::fabs(a - b) >= hs) T = std::min(a, b) + hs;
+            else T = 0.5 * (a + b + std::sqrt(2.0 * hs * hs - (a - b) * (a - b)));
+            if (T < D[kk]) { D[kk] = T; state[kk] = 1; heap.push({T, kk}); }
+        }
+    }
+    double maxFree = 0.0;
+    for (size_t k = 0; k < M; ++k) if (state[k] == 2) maxFree = std::max(maxFree, D[k]);
+    for (size_t k = 0; k < M; ++k) out[k] = float(state[k] == 2 ? D[k] : maxFree + 10.0);
+}
+
 }  // namespace
 
 extern "C" int swarm_hall_layout(const SwarmHallSpec* s, SwarmVenue* v) {
@@ -119,49 +163,18 @@ extern "C" int swarm_hall_fields(const SwarmHallSpec* s, const SwarmVenue* v, fl
         for (int i = 0; i < v->wall_nx; ++i)
             wall[size_t(j) * size_t(v->wall_nx) + size_t(i)] =
                 float(wallSdf(boxes, double(v->wall_origin_x) + i * double(v->wall_h), double(v->wall_origin_y) + j * double(v->wall_h)));
-    // fast marching on the nav grid
+    // fast marching on the nav grid: sources beyond the exit line, walls where the wall SDF is <= 0
     const int nx = v->nav_nx, ny = v->nav_ny;
-    const size_t M = size_t(nx) * size_t(ny);
-    const double h = v->nav_h, INF = std::numeric_limits<double>::infinity();
-    std::vector<double> D(M, INF);
-    std::vector<uint8_t> state(M, 0);   // 0 far, 1 trial, 2 known, 3 wall
-    using Item = std::pair<double, size_t>;
-    std::priority_queue<Item, std::vector<Item>, std::greater<Item>> heap;
+    std::vector<uint8_t> kind(size_t(nx) * size_t(ny), 0);
     for (int j = 0; j < ny; ++j) {
         for (int i = 0; i < nx; ++i) {
             const size_t k = size_t(j) * size_t(nx) + size_t(i);
-            const double x = double(v->nav_origin_x) + i * h, y = double(v->nav_origin_y) + j * h;
-            if (wallSdf(boxes, x, y) <= 0.0) { state[k] = 3; continue; }
-            if (x < v->exit_lo_x || x > v->exit_hi_x || y < v->exit_lo_y || y > v->exit_hi_y) { D[k] = 0.0; state[k] = 1; heap.push({0.0, k}); }
+            const double x = double(v->nav_origin_x) + i * double(v->nav_h), y = double(v->nav_origin_y) + j * double(v->nav_h);
+            if (wallSdf(boxes, x, y) <= 0.0) kind[k] = 3;
+            else if (x < v->exit_lo_x || x > v->exit_hi_x || y < v->exit_lo_y || y > v->exit_hi_y) kind[k] = 1;
         }
     }
-    auto val = [&](int i, int j) -> double {
-        if (i < 0 || j < 0 || i >= nx || j >= ny) return INF;
-        const size_t k = size_t(j) * size_t(nx) + size_t(i);
-        return state[k] == 2 ? D[k] : INF;
-    };
-    while (!heap.empty()) {
-        const auto [d, k] = heap.top();
-        heap.pop();
-        if (state[k] == 2 || d > D[k]) continue;
-        state[k] = 2;
-        const int i = int(k % size_t(nx)), j = int(k / size_t(nx));
-        const int ni[4] = {i - 1, i + 1, i, i}, nj[4] = {j, j, j - 1, j + 1};
-        for (int q = 0; q < 4; ++q) {
-            if (ni[q] < 0 || nj[q] < 0 || ni[q] >= nx || nj[q] >= ny) continue;
-            const size_t kk = size_t(nj[q]) * size_t(nx) + size_t(ni[q]);
-            if (state[kk] >= 2) continue;
-            const double a = std::min(val(ni[q] - 1, nj[q]), val(ni[q] + 1, nj[q]));
-            const double b = std::min(val(ni[q], nj[q] - 1), val(ni[q], nj[q] + 1));
-            double T;
-            if (std::isinf(a) || std::isinf(b) || std::fabs(a - b) >= h) T = std::min(a, b) + h;
-            else T = 0.5 * (a + b + std::sqrt(2.0 * h * h - (a - b) * (a - b)));
-            if (T < D[kk]) { D[kk] = T; state[kk] = 1; heap.push({T, kk}); }
-        }
-    }
-    double maxFree = 0.0;
-    for (size_t k = 0; k < M; ++k) if (state[k] == 2) maxFree = std::max(maxFree, D[k]);
-    for (size_t k = 0; k < M; ++k) nav[k] = float(state[k] == 2 ? D[k] : maxFree + 10.0);
+    fastMarch(nx, ny, v->nav_h, kind, nullptr, nav);
     // exit boxes: each door's opening, from the interior face out to the domain edge
     if (exitBoxes) {
         for (int d = 0; d < s->n_doors; ++d) {
@@ -178,6 +191,238 @@ extern "C" int swarm_hall_fields(const SwarmHallSpec* s, const SwarmVenue* v, fl
         }
     }
     (void)t;
+    return SWARM_OK;
+}
+
+// ---- the seated bowl ----
+namespace {
+
+bool validBowl(const SwarmBowlSpec* s) {
+    return s && s->sectors >= 3 && s->rows >= 1 && s->seats >= 1 && s->seat_width > 0 && s->row_pitch > 0 && s->rise >= 0 &&
+           s->gangway > 0 && s->vomitory_width > 0 && s->vomitory_row >= 0 && s->vomitory_row < s->rows &&
+           s->perimeter_exits >= 0 && s->perimeter_exits <= s->sectors && s->perimeter_exit_width > 0 && s->concourse > 0 &&
+           s->aisle >= 0 && s->clearance >= 0 &&
+           s->stair_speed > 0 && s->wall_h > 0 && s->nav_h > 0 && s->cell > 0 && s->sectors + s->perimeter_exits <= 56;
+}
+
+// The bowl in each sector's frame: u along its rows, w outward from the pitch wall (the polygon's inner edge)
+struct Bowl {
+    const SwarmBowlSpec& s;
+    double dphi, halfRow, rin, depth, outerW;
+    const double wallT = 0.3, rowWallT = 0.1;
+    std::vector<double> c, sn;
+    std::vector<uint8_t> exitSector;
+    explicit Bowl(const SwarmBowlSpec& sp) : s(sp) {
+        dphi = 2.0 * 3.141592653589793 / s.sectors;
+        halfRow = 0.5 * s.seats * double(s.seat_width);
+        rin = (2.0 * halfRow + s.gangway) / (2.0 * std::tan(0.5 * dphi));   // blocks gangway apart at the pitch wall
+        depth = s.rows * double(s.row_pitch);
+        outerW = depth + s.concourse;
+        c.resize(size_t(s.sectors)); sn.resize(size_t(s.sectors)); exitSector.assign(size_t(s.sectors), 0);
+        for (int k = 0; k < s.sectors; ++k) { c[size_t(k)] = std::cos(k * dphi); sn[size_t(k)] = std::sin(k * dphi); }
+        for (int e = 0; e < s.perimeter_exits; ++e) exitSector[size_t((long(e) * s.sectors) / s.perimeter_exits)] = 1;
+    }
+    double outerRadius() const { return (rin + outerW + wallT) / std::cos(0.5 * dphi); }
+    int sector(double x, double y) const {
+        int k = int(std::lround(std::atan2(y, x) / dphi)) % s.sectors;
+        return k < 0 ? k + s.sectors : k;
+    }
+    void local(int k, double x, double y, double& u, double& w) const {
+        k = ((k % s.sectors) + s.sectors) % s.sectors;
+        w = x * c[size_t(k)] + y * sn[size_t(k)] - rin;
+        u = -x * sn[size_t(k)] + y * c[size_t(k)];
+    }
+    static double box(double u, double w, double u0, double u1, double w0, double w1) {
+        return sdBox(u, w, Box{u0, w0, u1, w1});
+    }
+    // the walls of sector k near (u, w): the pitch wall (beyond the cross-aisle), the nearest row edges (the back edge
+    // of every row), the outer wall (with its exit gap)
+    double sectorSdf(int k, double u, double w) const {
+        const double half = std::tan(0.5 * dphi), a = s.aisle;
+        const double lf = (rin - a) * half + wallT, lo = (rin + outerW + wallT) * half + wallT;
+        double d = box(u, w, -lf, lf, -a - wallT, -a);
+        const int j0 = int(std::lround(w / s.row_pitch));
+        for (int j = j0 - 1; j <= j0 + 1; ++j) {
+            if (j < 1 || j > s.rows) continue;
+            const double wj = j * double(s.row_pitch);
+            d = std::min(d, box(u, w, -halfRow, halfRow, wj - 0.5 * rowWallT, wj + 0.5 * rowWallT));
+        }
+        const int kk = ((k % s.sectors) + s.sectors) % s.sectors;
+        if (exitSector[size_t(kk)]) {
+            const double g = 0.5 * s.perimeter_exit_width;
+            d = std::min(d, box(u, w, -lo, -g, outerW, outerW + wallT));
+            d = std::min(d, box(u, w, g, lo, outerW, outerW + wallT));
+        } else {
+            d = std::min(d, box(u, w, -lo, lo, outerW, outerW + wallT));
+        }
+        return d;
+    }
+    double sdf(double x, double y) const {
+        const int k = sector(x, y);
+        double d = 1e9;
+        for (int q = k - 1; q <= k + 1; ++q) {
+            double u, w;
+            local(q, x, y, u, w);
+            d = std::min(d, sectorSdf(q, u, w));
+        }
+        return d;
+    }
+    // floor height and speed factor: row treads, gangway stairs of half-rise steps, the concourse
+    void floorAt(double x, double y, double& h, double& speed) const {
+        double u, w;
+        local(sector(x, y), x, y, u, w);
+        speed = 1.0;
+        if (w < 0.0) { h = 0.0; return; }
+        if (w >= depth) { h = s.rows * double(s.rise); return; }
+        if (std::fabs(u) <= halfRow) { h = std::floor(w / s.row_pitch) * s.rise; return; }
+        h = std::floor(w / (0.5 * s.row_pitch)) * (0.5 * s.rise);
+        speed = s.stair_speed;
+    }
+    // beyond an exit: a vomitory across a gangway at the vomitory row, or past a perimeter gap
+    bool isExit(double x, double y) const {
+        const int k = sector(x, y);
+        double u, w;
+        local(k, x, y, u, w);
+        const double vw0 = s.vomitory_row * double(s.row_pitch);
+        if (std::fabs(u) > halfRow && w >= vw0 && w < vw0 + s.row_pitch) {
+            for (int side = -1; side <= 1; side += 2) {   // the bisectors with the neighbouring sectors
+                const double b = (k + 0.5 * side) * dphi;
+                if (std::fabs(-x * std::sin(b) + y * std::cos(b)) <= 0.5 * s.vomitory_width) return true;
+            }
+        }
+        return exitSector[size_t(k)] && w >= outerW + wallT && std::fabs(u) < 0.5 * s.perimeter_exit_width;
+    }
+};
+
+// Runs f(j) for j in [0, n) over the host's threads
+template <class F>
+void parallelRows(int n, F f) {
+    const int t = std::max(1, std::min(int(std::thread::hardware_concurrency()), 32));
+    std::vector<std::thread> pool;
+    for (int i = 0; i < t; ++i)
+        pool.emplace_back([&, i] { for (int j = i; j < n; j += t) f(j); });
+    for (auto& th : pool) th.join();
+}
+
+}  // namespace
+
+extern "C" int swarm_bowl_layout(const SwarmBowlSpec* s, SwarmVenue* v) {
+    if (!validBowl(s) || !v) return SWARM_E_INVALID;
+    const Bowl B(*s);
+    *v = SwarmVenue{};
+    const double half = std::ceil((B.outerRadius() + 2.0) / s->cell) * s->cell;
+    v->kind = SWARM_VENUE_GRID;
+    v->grid_res_x = v->grid_res_y = int(std::lround(2.0 * half / s->cell));
+    v->domain_span_x = v->domain_span_y = float(v->grid_res_x * double(s->cell));
+    v->domain_min_x = v->domain_min_y = -0.5f * v->domain_span_x;
+    v->exit_lo_x = v->exit_lo_y = v->domain_min_x;   // (the exit mask decides)
+    v->exit_hi_x = v->exit_hi_y = -v->domain_min_x;
+    v->exit_max_z = 1e30f;
+    v->wall_h = s->wall_h;
+    v->wall_origin_x = v->wall_origin_y = v->domain_min_x;
+    v->wall_nx = v->wall_ny = int(std::lround(double(v->domain_span_x) / s->wall_h)) + 1;
+    v->nav_h = s->nav_h;
+    v->nav_origin_x = v->nav_origin_y = v->domain_min_x;
+    v->nav_nx = v->nav_ny = int(std::lround(double(v->domain_span_x) / s->nav_h)) + 1;
+    v->n_exits = s->sectors + s->perimeter_exits;
+    v->metric_res = int(std::ceil(double(v->domain_span_x) / 16.0)) * 16;
+    return SWARM_OK;
+}
+
+extern "C" int swarm_bowl_fields(const SwarmBowlSpec* s, const SwarmVenue* v, float* wall, float* nav, float* floorH,
+                                 float* speedF, uint8_t* mask, float* exitBoxes) {
+    if (!validBowl(s) || !v || !wall || !nav || !floorH || !speedF || !mask) return SWARM_E_INVALID;
+    const Bowl B(*s);
+    const int wn = v->wall_nx, nn = v->nav_nx;
+    parallelRows(v->wall_ny, [&](int j) {
+        for (int i = 0; i < wn; ++i) {
+            const double x = double(v->wall_origin_x) + i * double(v->wall_h), y = double(v->wall_origin_y) + j * double(v->wall_h);
+            const size_t k = size_t(j) * size_t(wn) + size_t(i);
+            double h, sp;
+            B.floorAt(x, y, h, sp);
+            wall[k] = float(B.sdf(x, y));
+            floorH[k] = float(h);
+            speedF[k] = float(sp);
+        }
+    });
+    std::vector<uint8_t> kind(size_t(nn) * size_t(v->nav_ny), 0);
+    std::vector<float> speed(kind.size());
+    parallelRows(v->nav_ny, [&](int j) {
+        for (int i = 0; i < nn; ++i) {
+            const double x = double(v->nav_origin_x) + i * double(v->nav_h), y = double(v->nav_origin_y) + j * double(v->nav_h);
+            const size_t k = size_t(j) * size_t(nn) + size_t(i);
+            double h, sp;
+            B.floorAt(x, y, h, sp);
+            speed[k] = float(sp);
+            const bool ex = B.isExit(x, y);
+            mask[k] = ex ? 1 : 0;
+            // blocked within the clearance of a wall (the largest body radius): a thin row wall between nodes still
+            // cuts the field, and the paths round every wall end at a distance a body can keep, so e_goal never
+            // points into the wall an agent touches
+            kind[k] = B.sdf(x, y) <= double(s->clearance) ? 3 : (ex ? 1 : 0);
+        }
+    });
+    fastMarch(nn, v->nav_ny, v->nav_h, kind, speed.data(), nav);
+    if (exitBoxes) {   // each exit's bounding box (the metrics' exit attribution)
+        auto bound = [&](int e, int k, double u0, double u1, double w0, double w1) {
+            double lo[2] = {1e30, 1e30}, hi[2] = {-1e30, -1e30};
+            for (int q = 0; q < 4; ++q) {
+                const double u = (q & 1) ? u1 : u0, w = (q & 2) ? w1 : w0;
+                const double x = (B.rin + w) * B.c[size_t(k)] - u * B.sn[size_t(k)], y = (B.rin + w) * B.sn[size_t(k)] + u * B.c[size_t(k)];
+                lo[0] = std::min(lo[0], x); lo[1] = std::min(lo[1], y); hi[0] = std::max(hi[0], x); hi[1] = std::max(hi[1], y);
+            }
+            exitBoxes[4 * e] = float(lo[0]); exitBoxes[4 * e + 1] = float(lo[1]);
+            exitBoxes[4 * e + 2] = float(hi[0]); exitBoxes[4 * e + 3] = float(hi[1]);
+        };
+        const double vw0 = s->vomitory_row * double(s->row_pitch);
+        for (int k = 0; k < s->sectors; ++k) {   // the vomitory between sector k and k + 1, in the bisector's frame
+            const double b = (k + 0.5) * B.dphi, cb = std::cos(b), sb = std::sin(b), cw = std::cos(0.5 * B.dphi);
+            const double r0 = (B.rin + vw0) / cw, r1 = (B.rin + vw0 + s->row_pitch) / cw, hw = 0.5 * s->vomitory_width;
+            double lo[2] = {1e30, 1e30}, hi[2] = {-1e30, -1e30};
+            for (int q = 0; q < 4; ++q) {
+                const double r = (q & 1) ? r1 : r0, t = (q & 2) ? hw : -hw;
+                const double x = r * cb - t * sb, y = r * sb + t * cb;
+                lo[0] = std::min(lo[0], x); lo[1] = std::min(lo[1], y); hi[0] = std::max(hi[0], x); hi[1] = std::max(hi[1], y);
+            }
+            exitBoxes[4 * k] = float(lo[0]); exitBoxes[4 * k + 1] = float(lo[1]);
+            exitBoxes[4 * k + 2] = float(hi[0]); exitBoxes[4 * k + 3] = float(hi[1]);
+        }
+        int e = s->sectors;
+        for (int k = 0; k < s->sectors; ++k)
+            if (B.exitSector[size_t(k)])
+                bound(e++, k, -0.5 * s->perimeter_exit_width, 0.5 * s->perimeter_exit_width, B.outerW + B.wallT,
+                      B.outerW + B.wallT + 3.0);
+    }
+    return SWARM_OK;
+}
+
+extern "C" int swarm_spawn_bowl(const SwarmBowlSpec* sp, float jitter, uint64_t seed, float r_lo, float r_hi, float v_mean,
+                                float v_sd, float v_lo, float v_hi, float* boids, float* radius, float* v0) {
+    if (!validBowl(sp) || !boids || !radius || !v0) return SWARM_E_INVALID;
+    const Bowl B(*sp);
+    uint64_t s = seed;
+    const double pi2 = 6.283185307179586;
+    size_t i = 0;
+    for (int k = 0; k < sp->sectors; ++k) {
+        for (int row = 0; row < sp->rows; ++row) {
+            for (int seat = 0; seat < sp->seats; ++seat, ++i) {
+                const double u = -B.halfRow + (seat + 0.5) * sp->seat_width, w = (row + 0.5) * sp->row_pitch;
+                const double jx = (2.0 * uniform01(s) - 1.0) * jitter, jy = (2.0 * uniform01(s) - 1.0) * jitter;
+                const double rad = r_lo + (r_hi - r_lo) * uniform01(s);
+                const double u1 = 1.0 - uniform01(s), u2 = uniform01(s);
+                const double z = std::sqrt(-2.0 * std::log(u1)) * std::cos(pi2 * u2);
+                const double v = std::min(std::max(v_mean + v_sd * z, double(v_lo)), double(v_hi));
+                float* b = boids + i * 8;
+                b[0] = float((B.rin + w) * B.c[size_t(k)] - u * B.sn[size_t(k)] + jx);
+                b[1] = float((B.rin + w) * B.sn[size_t(k)] + u * B.c[size_t(k)] + jy);
+                b[2] = float(row * double(sp->rise) + rad);
+                b[3] = 1.0f;
+                b[4] = b[5] = b[6] = b[7] = 0.0f;
+                radius[i] = float(rad);
+                v0[i] = float(v);
+            }
+        }
+    }
     return SWARM_OK;
 }
 

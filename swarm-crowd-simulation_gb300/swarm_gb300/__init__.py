@@ -74,6 +74,11 @@ def lib():
                                   C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                   C.POINTER(SwarmAdjointStats)],
             "swarm_set_relaxation_time": [H, C.c_float],
+            "swarm_bowl_layout": [C.c_void_p, C.POINTER(SwarmVenue)],
+            "swarm_bowl_fields": [C.c_void_p, C.POINTER(SwarmVenue), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                  C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_void_p, C.POINTER(C.c_float)],
+            "swarm_spawn_bowl": [C.c_void_p, C.c_float, C.c_uint64, C.c_float, C.c_float, C.c_float, C.c_float,
+                                 C.c_float, C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)],
             "swarm_spawn_lattice": [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_uint64,
                                     C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
                                     C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)],

@@ -62,6 +62,7 @@ class SwarmVenue(C.Structure):
         ("nav_origin_x", _f), ("nav_origin_y", _f), ("nav_h", _f),
         ("floor_height", C.POINTER(_f)), ("speed_factor", C.POINTER(_f)), ("exit_boxes", C.POINTER(_f)),
         ("metric_res", _i), ("metric_center_x", _f), ("metric_center_y", _f),
+        ("exit_mask", C.POINTER(C.c_uint8)),
     ]
 
 

@@ -23,6 +23,22 @@ class HallSpec(C.Structure):
                 ("door_width", C.c_float * 8)]
 
 
+class BowlSpec(C.Structure):
+    _fields_ = [("sectors", C.c_int32), ("rows", C.c_int32), ("seats", C.c_int32), ("seat_width", C.c_float),
+                ("row_pitch", C.c_float), ("rise", C.c_float), ("gangway", C.c_float), ("vomitory_width", C.c_float),
+                ("vomitory_row", C.c_int32), ("perimeter_exits", C.c_int32), ("perimeter_exit_width", C.c_float),
+                ("concourse", C.c_float), ("aisle", C.c_float), ("stair_speed", C.c_float), ("clearance", C.c_float),
+                ("wall_h", C.c_float), ("nav_h", C.c_float),
+                ("cell", C.c_float)]
+
+
+def bowl_spec(sectors=32, rows=32, seats=62, seat_width=0.5, row_pitch=0.8, rise=0.4, gangway=1.2, vomitory_width=2.4,
+              vomitory_row=16, perimeter_exits=8, perimeter_exit_width=4.0, concourse=4.0, aisle=1.2, stair_speed=0.6,
+              clearance=0.2, wall_h=0.05, nav_h=0.1, cell=0.5):
+    return BowlSpec(sectors, rows, seats, seat_width, row_pitch, rise, gangway, vomitory_width, vomitory_row,
+                    perimeter_exits, perimeter_exit_width, concourse, aisle, stair_speed, clearance, wall_h, nav_h, cell)
+
+
 class Venue:
     """A SwarmVenue plus the host arrays it points to (kept alive with it)."""
 
@@ -88,6 +104,36 @@ class Venue:
         return Venue(v, {"wall": wall, "nav": nav, "exit_boxes": boxes}, name, meta)
 
 
+def _bowl(spec, name):
+    v = SwarmVenue()
+    _check(lib().swarm_bowl_layout(C.byref(spec), C.byref(v)), "swarm_bowl_layout")
+    nw, nn = v.wall_nx * v.wall_ny, v.nav_nx * v.nav_ny
+    wall, floor, speed = np.empty(nw, np.float32), np.empty(nw, np.float32), np.empty(nw, np.float32)
+    nav, mask = np.empty(nn, np.float32), np.empty(nn, np.uint8)
+    boxes = np.empty(4 * v.n_exits, np.float32)
+    _check(lib().swarm_bowl_fields(C.byref(spec), C.byref(v), fptr(wall), fptr(nav), fptr(floor), fptr(speed),
+                                   mask.ctypes.data_as(C.c_void_p), fptr(boxes)), "swarm_bowl_fields")
+    v.wall_sdf, v.nav_dist, v.floor_height, v.speed_factor = fptr(wall), fptr(nav), fptr(floor), fptr(speed)
+    v.exit_mask = mask.ctypes.data_as(C.POINTER(C.c_uint8))
+    v.exit_boxes = fptr(boxes)
+    arrays = {"wall": wall, "nav": nav, "floor": floor, "speed": speed, "exit_mask": mask, "exit_boxes": boxes}
+    return Venue(v, arrays, name, {"spec": spec})
+
+
+Venue.bowl = staticmethod(_bowl)
+
+
+def spawn_bowl(spec, jitter=0.03, seed=0, r=(0.20, 0.25), v=(1.34, 0.26, 0.6, 2.0)):
+    """One agent per seat at the seat centre, jittered: (boids (n, 8), radius (n,), v0 (n,))."""
+    n = spec.sectors * spec.rows * spec.seats
+    boids = np.empty((n, 8), np.float32)
+    rad = np.empty(n, np.float32)
+    v0 = np.empty(n, np.float32)
+    _check(lib().swarm_spawn_bowl(C.byref(spec), jitter, seed, r[0], r[1], v[0], v[1], v[2], v[3], fptr(boids), fptr(rad),
+                                  fptr(v0)), "swarm_spawn_bowl")
+    return boids, rad, v0
+
+
 def spawn_lattice(nx, ny, n=None, spacing=0.5, center=(0.0, 0.0), jitter=0.05, seed=0, r=(0.20, 0.25),
                   v=(1.34, 0.26, 0.6, 2.0)):
     """A jittered lattice spawn: (boids (n, 8), radius (n,), v0 (n,))."""
@@ -116,6 +162,14 @@ def hall_c1():
     venue = Venue.hall(140.0, 140.0, [(0, 0.0, 4.0), (1, 0.0, 4.0), (2, 0.0, 4.0), (3, 0.0, 4.0)],
                        name="hall 140x140 m, 4 exits")
     return venue, spawn_lattice(256, 256, seed=0)
+
+
+def bowl_c2(**kw):
+    """The seated bowl: 32 sectors x 32 rows x 62 seats (63 488 agents), seat 0.5 m, row pitch 0.8 m, rise 0.4 m per
+    row, 1.2 m gangways (stairs, speed factor 0.6), a 2.4 m vomitory per gangway at row 16, 8 perimeter exits of 4 m;
+    agents at the seat centres jittered U(+-0.03 m), radius and desired speed as the lattice workloads (seed 0)."""
+    spec = bowl_spec(**kw)
+    return Venue.bowl(spec, "seated bowl %dx%dx%d" % (spec.sectors, spec.rows, spec.seats)), spawn_bowl(spec, seed=0)
 
 
 def terrace_c4():

@@ -70,3 +70,46 @@ def test_cpp_host_class_compiles_and_links(built, tmp_path):
                     "-L", PKG, "-lswarm_gb300", "-Wl,-rpath," + PKG], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
     assert out == ["32", "0.0064"]
+
+
+@pytest.fixture(scope="module")
+def bowl_small(built):
+    from swarm_gb300 import venues
+    spec = venues.bowl_spec(sectors=8, rows=8, seats=12, vomitory_row=4, perimeter_exits=2)
+    return spec, venues.Venue.bowl(spec, "small bowl"), venues.spawn_bowl(spec, seed=1)
+
+
+def _node(v, arr, x, y, h, nx):
+    return arr[int(round((y - v.wall_origin_y) / h)) * nx + int(round((x - v.wall_origin_x) / h))]
+
+
+def test_bowl_fields_and_seats(bowl_small):
+    """Seats: clear of every wall by more than the largest radius, standing on their row's tread (rise per row), on
+    free nav nodes with a finite distance, outside the exits. Stairs are slower; exits exist."""
+    spec, venue, (b, r, v0) = bowl_small
+    v = venue.struct
+    A = venue.arrays
+    n = spec.sectors * spec.rows * spec.seats
+    assert b.shape == (n, 8) and v.n_exits == spec.sectors + spec.perimeter_exits
+    wall = np.array([_node(v, A["wall"], x, y, v.wall_h, v.wall_nx) for x, y in b[:, :2]])
+    floor = np.array([_node(v, A["floor"], x, y, v.wall_h, v.wall_nx) for x, y in b[:, :2]])
+    nav = np.array([_node(v, A["nav"], x, y, v.nav_h, v.nav_nx) for x, y in b[:, :2]])
+    mask = np.array([_node(v, A["exit_mask"], x, y, v.nav_h, v.nav_nx) for x, y in b[:, :2]])
+    assert wall.min() > 0.25
+    rows = np.repeat(np.tile(np.arange(spec.rows), spec.sectors), spec.seats)
+    assert np.allclose(floor, rows * spec.rise) and np.allclose(b[:, 2], floor + r, atol=1e-6)
+    assert (mask == 0).all() and np.isfinite(nav).all() and nav.max() < A["nav"].max()
+    assert sorted(float(x) for x in np.unique(A["speed"])) == [float(np.float32(spec.stair_speed)), 1.0]
+    assert A["exit_mask"].sum() > 0
+
+
+def test_small_bowl_evacuates_on_the_oracle(bowl_small):
+    """The whole crowd finds the gangways, the stairs and an exit (the oracle, 768 agents)."""
+    import swarm_gb300
+    from oracle import oracle as O
+    spec, venue, (b, r, v0) = bowl_small
+    sim = O.OracleSim(swarm_gb300.params_si(), venue.struct)
+    sim.set_state(b)
+    sim.set_agent_params(r, v0)
+    sim.step(600)
+    assert (sim.state()[:, 3] == 0).all()
