@@ -356,8 +356,23 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the 256-instance batched measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
     ap.add_argument("--no-bowl", action="store_true", help="skip the seated-bowl measurement")
+    ap.add_argument("--adjoint-steps", type=int, default=400, help="steps of the adjoint measurement (400: the workload)")
+    ap.add_argument("--only", choices=["adjoint", "bowl", "batched"], default=None,
+                    help="run only this sub-measurement and print its object (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+
+    if args.only:   # one sub-measurement alone (a profiling run; not the benchmark line)
+        import torch
+        import __graft_entry__
+        __graft_entry__._pkg_build().build()
+        import swarm_gb300
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        P = swarm_gb300.params_si()
+        fn = {"adjoint": lambda: bench_adjoint(P, steps=args.adjoint_steps), "bowl": lambda: bench_bowl(P),
+              "batched": lambda: bench_batched(P)}[args.only]
+        print(json.dumps({args.only: fn()}))
+        return 0
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -518,7 +533,7 @@ def main():
                 line["bowl"] = {"error": str(e)[:300]}
         if not args.no_adjoint and world == 1:
             try:
-                line["adjoint"] = bench_adjoint(P)
+                line["adjoint"] = bench_adjoint(P, steps=args.adjoint_steps)
             except Exception as e:  # reported, not fatal
                 line["adjoint"] = {"error": str(e)[:300]}
         if not args.no_cpu_baseline and world == 1:

@@ -221,8 +221,25 @@ __device__ __forceinline__ f2 separationForce(const SwarmParams& P, f3 offset, u
     return magnitude * xy(offset) * (1.0f / sqrtf(dxy2));
 }
 
-template <class Venue, bool kB, bool kTape = false>
-__device__ __forceinline__ void predictItem(const StepArgs& A, int s) {
+// Where predict reads its neighbours: the slot buffers, or a tile's perception window staged in shared memory
+struct PredGlobal {
+    const StepArgs& A;
+    __device__ __forceinline__ float4 pos(uint32_t k) const { return A.pos0[k]; }
+    __device__ __forceinline__ uint32_t sid(uint32_t k) const { return A.sid[k]; }
+    __device__ __forceinline__ float r(uint32_t k) const { return A.prm[k].x; }
+};
+struct PredWindow {
+    const float4* pos_;
+    const float* r_;
+    const uint32_t* sid_;
+    uint32_t lo;
+    __device__ __forceinline__ float4 pos(uint32_t k) const { return pos_[k - lo]; }
+    __device__ __forceinline__ uint32_t sid(uint32_t k) const { return sid_[k - lo]; }
+    __device__ __forceinline__ float r(uint32_t k) const { return r_[k - lo]; }
+};
+
+template <class Venue, bool kB, bool kTape = false, class Nbr = PredGlobal>
+__device__ __forceinline__ void predictCore(const StepArgs& A, int s, const Nbr& nb) {
     constexpr bool kUniform = Body<Venue>::kUniform;
     const int nActive = int(A.start[A.V.ncells]);
     if (s >= nActive) return;
@@ -283,9 +300,9 @@ __device__ __forceinline__ void predictItem(const StepArgs& A, int s) {
     for (int j = 0; j < MAXR; ++j) {
         for (uint32_t k = rk0[j]; k < rk1[j]; k++) {
             if (int(k) == s) continue;
-            const float4 op = A.pos0[k];
-            const uint32_t other = A.sid[k];
-            const float rj = kUniform ? 0.0f : A.prm[k].x;
+            const float4 op = nb.pos(k);
+            const uint32_t other = nb.sid(k);
+            const float rj = kUniform ? 0.0f : nb.r(k);
             const f3 offset = xyz(p) - xyz(op);
             const float dxy2 = dot(xy(offset), xy(offset));
             if (dxy2 < P.r_perc2) {
@@ -350,6 +367,11 @@ __device__ __forceinline__ void predictItem(const StepArgs& A, int s) {
     A.plane[s] = make_float4(wn.x, wn.y, dot(xy(np), wn) - wall.z,
                              (nonzero(wn) ? PLANE_WALL : 0.0f) + (grounded ? PLANE_GROUNDED : 0.0f));
     A.ctc[s] = uint8_t(contact);
+}
+
+template <class Venue, bool kB, bool kTape = false>
+__device__ __forceinline__ void predictItem(const StepArgs& A, int s) {
+    predictCore<Venue, kB, kTape>(A, s, PredGlobal{A});
 }
 
 template <class Venue, bool kB, bool kTape = false>
@@ -583,7 +605,21 @@ __device__ __forceinline__ void prepareSweepItem(const StepArgs& A, int s, int n
     }
 }
 
-constexpr int WIN_CAP = 2048;   // slots a tile window may hold in shared memory (40 KB); larger windows read global memory
+constexpr int WIN_CAP = 4096;   // slots a tile window may hold in shared memory (96 KB); larger windows read global memory
+
+// The perception window of tile t (its active slots [t T, min((t + 1) T, nActive))): every slot within perc_ring cell
+// rows and columns of its first and last cells, a contiguous range in key order; (0, 0) for a tile with no active slot.
+// (A tile spanning batched instances: each slot's cells lie inside its own instance, within these bounds.)
+template <bool kB>
+__device__ __forceinline__ uint2 predWindow(const StepArgs& A, int t, int T, int nActive) {
+    const int s0 = t * T;
+    if (s0 >= nActive) return make_uint2(0u, 0u);
+    const int s1 = min(s0 + T, nActive) - 1;
+    const int R = A.P.perc_ring;
+    const int c0 = int(A.skey[s0]), c1 = int(A.skey[s1]);
+    const int res0 = venueOfSlot<kB>(A, s0).resX, res1 = venueOfSlot<kB>(A, s1).resX;
+    return make_uint2(A.start[max(c0 - R * res0 - R, 0)], A.start[min(c1 + R * res1 + R + 1, A.V.ncells)]);
+}
 
 // kTape (the adjoint's recompute): sweep k reads q[k - 1] and writes q[k], q[k] = proj[0] + k n, with its relaxed
 // corrections at tapeCorr + (k - 1) n; the final pass records the last sweep's result in tapeQK; predict its record
@@ -592,8 +628,9 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A)
     constexpr bool kUniform = Body<Venue>::kUniform;
     __shared__ uint32_t warpSums[32];
     __shared__ uint32_t prefix;
-    extern __shared__ float4 smPos[];                    // WIN_CAP positions, then WIN_CAP radii
+    extern __shared__ float4 smPos[];                    // WIN_CAP positions, then WIN_CAP radii, then WIN_CAP ids
     float* smR = reinterpret_cast<float*>(smPos + WIN_CAP);
+    uint32_t* smSid = reinterpret_cast<uint32_t*>(smR + WIN_CAP);
     const int n = A.n;
     const int T = int(blockDim.x);   // the tile of slots a block handles at a time
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
@@ -613,9 +650,26 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A)
     if (!gridBarrier(A, gridDim.x)) return;
     stamp(A, 1);
     const int nActive = int(A.start[A.V.ncells]);
-    for (int s = tid; s < n; s += stride) {
-        predictItem<Venue, kB, kTape>(A, s);
-        if (s < nActive) prepareSweepItem<kB>(A, s, nActive, T);
+    // predict, tile by tile: the tile's perception window staged in shared memory (global reads when it is larger)
+    const int allTilesP = (n + T - 1) / T;
+    for (int t = blockIdx.x; t < allTilesP; t += gridDim.x) {
+        const int s = t * T + int(threadIdx.x);
+        const uint2 win = predWindow<kB>(A, t, T, nActive);
+        const bool useWin = win.y > win.x && win.y - win.x <= uint32_t(WIN_CAP);
+        if (useWin) {
+            for (uint32_t k = win.x + threadIdx.x; k < win.y; k += blockDim.x) {
+                smPos[k - win.x] = A.pos0[k];
+                smR[k - win.x] = kUniform ? 0.0f : A.prm[k].x;
+                smSid[k - win.x] = A.sid[k];
+            }
+        }
+        __syncthreads();
+        if (s < n) {
+            if (useWin) predictCore<Venue, kB, kTape>(A, s, PredWindow{smPos, smR, smSid, win.x});
+            else predictCore<Venue, kB, kTape>(A, s, PredGlobal{A});
+            if (s < nActive) prepareSweepItem<kB>(A, s, nActive, T);
+        }
+        __syncthreads();   // the window is reused by the next tile
     }
     if (!gridBarrier(A, gridDim.x)) return;
     stamp(A, 2);
@@ -743,7 +797,7 @@ static void stageImpl(const StepArgs& A, int stage, cudaStream_t st, int64_t* la
     }
 }
 
-constexpr int FUSED_SMEM = WIN_CAP * (int(sizeof(float4)) + int(sizeof(float)));
+constexpr int FUSED_SMEM = WIN_CAP * (int(sizeof(float4)) + int(sizeof(float)) + int(sizeof(uint32_t)));
 
 // The fused grid: one block per SM when the state fits (threads = n / SMs rounded up to a warp, 128..512), else as
 // many blocks as stay resident, each taking several tiles per phase

@@ -13,6 +13,8 @@ Writes
   terrace_metrics_ref.npz  the terrace's metric cell table (computeMetricVenue: threshold masses, walkable area) and
                      MetricsReference (src/metrics.cpp:429-476) after recording the first 250 steps from the spawn:
                      counters, per-cell accumulators, evacuation step per agent.
+  terrace_evac_ref.npz  the same spawn run by the reference to full evacuation: the active agents after every step,
+                     and the evacuation time (the first step after which none is active).
 """
 import os
 import sys
@@ -63,6 +65,18 @@ def main():
     np.savez_compressed(os.path.join(HERE, "terrace_metrics_ref.npz"), threshold_mass=thr, walkable_m2=area,
                         counters=ctr, cells=cells, evac_step=evac)
     print("metrics: %d evacuated, exits %s" % (ctr[2], list(ctr[4:9])))
+
+    sim = O.RefSim("terrace")
+    sim.set_state(spawn)
+    active = []
+    while not active or active[-1] > 0:
+        sim.step(1)
+        active.append(int((sim.state()[:, 3] != 0).sum()))
+        if len(active) > 20000:
+            raise RuntimeError("the terrace did not evacuate in 20 000 steps")
+    np.savez_compressed(os.path.join(HERE, "terrace_evac_ref.npz"), active=np.array(active, np.int32),
+                        evacuation_steps=np.array([len(active)], np.int32))
+    print("terrace evacuated after %d steps" % len(active))
     print("hash after 250 steps: %016x" % int(out["hash250"][0]))
 
 

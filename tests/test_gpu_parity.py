@@ -133,6 +133,24 @@ def test_terrace_ragged_sizes(terrace, terrace_golden, n):
     assert np.array_equal(_bits(sim.state()), _bits(ora.state()))
 
 
+def test_terrace_evacuation_time_matches_the_reference(terrace, terrace_golden):
+    """The reference terrace run to full evacuation on the GPU: the active count after every step equals the
+    reference's own run (tests/golden/terrace_evac_ref.npz), so the evacuation time is the reference's exactly
+    (2 696 steps; the required tolerance is 1 %)."""
+    import os
+    P, venue = terrace
+    ref = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "terrace_evac_ref.npz"))
+    sim = _sim(P, venue, terrace_golden["spawn"])
+    active = []
+    for _ in range(int(ref["evacuation_steps"][0])):
+        sim.step(1)
+        active.append(int((sim.state()[:, 3] != 0).sum()))
+    active = np.array(active)
+    assert np.array_equal(active, ref["active"])
+    t_gpu = int(np.argmax(active == 0)) + 1
+    assert abs(t_gpu - int(ref["evacuation_steps"][0])) <= 0.01 * int(ref["evacuation_steps"][0])
+
+
 def test_terrace_all_evacuated(terrace, terrace_golden):
     P, venue = terrace
     st = terrace_golden["spawn"][:64].copy()

@@ -51,6 +51,19 @@ def test_250_steps_reproduce_the_reference_state_hash(terrace, terrace_golden):
     assert np.array_equal(_bits(sim.state()), _bits(g["state251"]))
 
 
+def test_full_evacuation_matches_the_reference(terrace, terrace_golden):
+    """The spawn run to full evacuation: the active count after every step equals the reference's (2 696 steps)."""
+    P, venue = terrace
+    ref = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "terrace_evac_ref.npz"))
+    sim = O.OracleSim(P, venue.struct)
+    sim.set_state(terrace_golden["spawn"])
+    active = []
+    for _ in range(int(ref["evacuation_steps"][0])):
+        sim.step(1)
+        active.append(int((sim.state()[:, 3] != 0).sum()))
+    assert np.array_equal(np.array(active), ref["active"])
+
+
 def test_thread_invariance(terrace, terrace_golden):
     """parity.thread_invariance (tools/test_gpu.cpp:2035): bit-identical for any thread count."""
     P, venue = terrace
