@@ -277,6 +277,7 @@ __device__ __forceinline__ void predictCore(const StepArgs& A, int s, const Nbr&
     const float dcMax = kUniform ? P.body_diam : ri + P.r_pair_max;
     const float reach = smax(dcMax + vFreeSelf / P.headway_rate, kUniform ? P.r_sep : dcMax + P.sep_margin) * 1.01f + margin;
     const float rPerc = smin(sqrtf(P.r_perc2) + margin, reach);
+    const float reach2 = reach * reach;
     // every row's slot range first (independent loads, issued together), then the rows in order
     constexpr int MAXR = 2 * 4 + 1;   // PERC_RING <= 4
     uint32_t rk0[MAXR], rk1[MAXR];
@@ -301,10 +302,14 @@ __device__ __forceinline__ void predictCore(const StepArgs& A, int s, const Nbr&
         for (uint32_t k = rk0[j]; k < rk1[j]; k++) {
             if (int(k) == s) continue;
             const float4 op = nb.pos(k);
-            const uint32_t other = nb.sid(k);
-            const float rj = kUniform ? 0.0f : nb.r(k);
             const f3 offset = xyz(p) - xyz(op);
             const float dxy2 = dot(xy(offset), xy(offset));
+            // beyond the search disk a neighbour adds a zero separation and no headway gap below vFree T (the rows'
+            // argument, per agent): skipping it changes no bit (separation terms are +0, and +0 additions never
+            // change a sum that starts at +0)
+            if (dxy2 >= reach2) continue;
+            const uint32_t other = nb.sid(k);
+            const float rj = kUniform ? 0.0f : nb.r(k);
             if (dxy2 < P.r_perc2) {
                 float dc, rs, rs2;
                 if (kUniform) { dc = P.body_diam; rs = P.r_sep; rs2 = P.r_sep2; }

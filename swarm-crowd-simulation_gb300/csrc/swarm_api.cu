@@ -425,7 +425,7 @@ int swarm_metrics_read(SwarmHandle h, SwarmMetricCounters* counters, SwarmMetric
     return cudaOk(h, cudaGetLastError(), "metrics read") ? SWARM_OK : SWARM_E_CUDA;
 }
 
-static int stepImpl(SwarmHandle h, int steps);
+static int stepImpl(SwarmHandle h, int steps, bool countLast = true);
 
 int swarm_set_tuning(SwarmHandle h, const SwarmTuning* t) {
     if (!h || !t || t->threads < 0 || t->threads > 512 || t->blocks_per_sm < 0) return SWARM_E_INVALID;
@@ -516,7 +516,9 @@ int swarm_set_timing(SwarmHandle h, int enabled) {
 
 // One step = 4 stages. Timing on: an event before each stage and after the last, recorded on the stream between
 // stage launches (or stage graphs), never inside a capture.
-static int stepImpl(SwarmHandle h, int steps) {
+// countLast: the last fused step counts the next state's keys for the next call (false when the next call uploads a
+// new state: the counts are then left clear, and nothing has to clear them)
+static int stepImpl(SwarmHandle h, int steps, bool countLast) {
     h->launches = 0;
     const int perStep = 7 + std::max(h->P.proj_iterations - 1, 0);
     for (int s = 0; s < steps; ++s) {
@@ -525,10 +527,10 @@ static int stepImpl(SwarmHandle h, int steps) {
             if (h->timing && !cudaOk(h, cudaEventRecord(h->ev[0], h->stream), "event")) return SWARM_E_CUDA;
             StepArgs A = h->args(in);
             A.hashed = h->counted ? 1 : 0;
-            A.hashNext = 1;
+            A.hashNext = (countLast || s + 1 < steps) ? 1 : 0;
             if (!cudaOk(h, swarm_gpu::launch_step_fused(A, h->stream), "fused step launch")) return SWARM_E_CUDA;
             h->barrierExtra = 0;
-            h->counted = true;
+            h->counted = A.hashNext != 0;
             if (h->timing && !cudaOk(h, cudaEventRecord(h->ev[4], h->stream), "event")) return SWARM_E_CUDA;
             h->launches += 1;
         } else if (h->counted && !h->clearCounts()) {
@@ -577,7 +579,7 @@ int swarm_step_host(SwarmHandle h, const float* in_boids, float* out_boids, int 
     const size_t bytes = size_t(n) * 32;
     // the read half only: the final pass writes every agent of the other half
     if (!cudaOk(h, cudaMemcpyAsync(h->state[h->readIdx], in_boids, bytes, cudaMemcpyHostToDevice, h->stream), "upload")) return SWARM_E_CUDA;
-    const int rc = stepImpl(h, steps);
+    const int rc = stepImpl(h, steps, false);
     if (rc != SWARM_OK) return rc;
     if (!cudaOk(h, cudaMemcpyAsync(out_boids, h->state[h->readIdx], bytes, cudaMemcpyDeviceToHost, h->stream), "download")) return SWARM_E_CUDA;
     return cudaOk(h, cudaStreamSynchronize(h->stream), "step sync") ? SWARM_OK : SWARM_E_CUDA;
