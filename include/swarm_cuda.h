@@ -324,6 +324,31 @@ int swarm_metrics_read(SwarmHandle h, SwarmMetricCounters* counters, SwarmMetric
  * the wall SDF is positive, inside the exit line); cells under 0.1 m^2 never reach a threshold. */
 int swarm_metric_thresholds_grid(const SwarmVenue* venue, int res, uint32_t* threshold_mass);
 
+/* ---- headless evacuation runs and the on-disk formats ---- */
+/* The evacuation statistics of a run (the reference's run_experiment summary: t50 / t90 / t100). */
+typedef struct SwarmEvacuation {
+    int32_t steps;                /* steps run */
+    int32_t initial_active;       /* agents active before the first step */
+    int32_t remaining;            /* agents active after the last step */
+    int32_t t50_step, t90_step, t100_step;   /* the first step after which at least 50 / 90 / 100 % of the initially
+                                                active agents have left; -1: not within the steps run */
+    float t50_s, t90_s, t100_s;   /* the same in seconds (step x dt); -1: not reached */
+} SwarmEvacuation;
+/* run_experiment's headless evacuation (DedovSergei/swarm-crowd-simulation tools/experiment/run_experiment.cpp): steps
+ * until no agent is active or max_steps, counting the active agents after every step on the device (the metrics,
+ * when enabled, record every step as usual). active_out (may be NULL): max_steps entries, the active count after each
+ * step run. The state is left after the last step. */
+int swarm_run_evacuation(SwarmHandle h, int max_steps, int32_t* active_out, SwarmEvacuation* out);
+
+/* Workload snapshots (tools/benchmark/bench_common.hpp:109-134 saveSnapshot / loadSnapshot): a raw GpuBoid array, n x
+ * 32 bytes, nothing else. read: the file must hold exactly n agents. count: the agents a file holds (-1: not a
+ * whole number of GpuBoids or unreadable). */
+int swarm_snapshot_write(const char* path, const float* boids, int n);
+int swarm_snapshot_read(const char* path, float* boids, int n);
+int swarm_snapshot_count(const char* path);
+/* The baked terrace volume (src/sdf.cpp:84-107 loadSDFVolume): res^3 float32, exactly (stadium.sdf: res 130). */
+int swarm_sdf_read(const char* path, float* sdf, int res);
+
 /* ---- the adjoint: gradients of an evacuation loss ----
  * No counterpart in the reference, which has no differentiation. The loss of `steps` steps from the handle's state:
  *   SWARM_LOSS_NAV_DISTANCE   L = dt * sum_{t = 1..steps} sum_{i active after step t} D(p_i(t)),

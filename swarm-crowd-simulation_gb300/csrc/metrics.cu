@@ -98,6 +98,24 @@ __global__ void k_metrics_finalize(MetricArgs M) {
     M.cells[c] = s;
 }
 
+__global__ void k_count_active(const float4* __restrict__ state, int n, uint32_t* out) {
+    __shared__ uint32_t blockCount;
+    if (threadIdx.x == 0) blockCount = 0;
+    __syncthreads();
+    uint32_t c = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        c += state[2 * size_t(i)].w != 0.0f ? 1u : 0u;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31u) == 0 && c) atomicAdd(&blockCount, c);
+    __syncthreads();
+    if (threadIdx.x == 0 && blockCount) atomicAdd(out, blockCount);
+}
+
+void launch_count_active(const float4* state, int n, uint32_t* out, cudaStream_t st) {
+    const int blocks = (n + 255) / 256 < 256 ? (n + 255) / 256 : 256;
+    k_count_active<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(state, n, out);
+}
+
 void launch_metrics(const MetricArgs& M, cudaStream_t st) {
     k_metrics_deposit<<<(M.n + 255) / 256, 256, 0, st>>>(M);
     const int cells = M.res * M.res;

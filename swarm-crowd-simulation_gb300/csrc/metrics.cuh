@@ -28,5 +28,7 @@ struct MetricArgs {
 };
 
 void launch_metrics(const MetricArgs& M, cudaStream_t st);
+// The active agents of a state (position.w != 0) into *out (an integer sum: exact, order-independent); *out must be 0
+void launch_count_active(const float4* state, int n, uint32_t* out, cudaStream_t st);
 
 }  // namespace swarm_gpu

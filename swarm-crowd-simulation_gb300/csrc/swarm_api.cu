@@ -561,6 +561,63 @@ static int stepImpl(SwarmHandle h, int steps, bool countLast) {
     return SWARM_OK;
 }
 
+int swarm_run_evacuation(SwarmHandle h, int max_steps, int32_t* active_out, SwarmEvacuation* out) {
+    if (!h || !out || max_steps < 0) return SWARM_E_INVALID;
+    if (!h->hasState) return h->fail(SWARM_E_STATE, "no state (upload one first)");
+    constexpr int CHUNK = 256;   // steps between host checks; every step is counted on the device
+    uint32_t* dCounts = nullptr;
+    if (!cudaOk(h, cudaMalloc(&dCounts, (CHUNK + 1) * sizeof(uint32_t)), "evacuation counters")) return SWARM_E_OOM;
+    std::vector<uint32_t> counts(CHUNK + 1);
+    std::vector<int32_t> series;
+    int rc = SWARM_OK;
+    auto fail = [&](int code) { cudaFree(dCounts); return code; };
+    // the active agents before the first step
+    if (!cudaOk(h, cudaMemsetAsync(dCounts, 0, sizeof(uint32_t), h->stream), "evacuation counters")) return fail(SWARM_E_CUDA);
+    swarm_gpu::launch_count_active(h->state[h->readIdx], h->n, dCounts, h->stream);
+    if (!cudaOk(h, cudaMemcpyAsync(counts.data(), dCounts, sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream), "count") ||
+        (rc = swarm_synchronize(h)) != SWARM_OK)
+        return fail(rc != SWARM_OK ? rc : SWARM_E_CUDA);
+    const int64_t initial = counts[0];
+    int64_t launches = 1;
+    int steps = 0;
+    int64_t active = initial;
+    while (steps < max_steps && active > 0) {
+        const int c = std::min(CHUNK, max_steps - steps);
+        if (!cudaOk(h, cudaMemsetAsync(dCounts, 0, size_t(c) * sizeof(uint32_t), h->stream), "evacuation counters"))
+            return fail(SWARM_E_CUDA);
+        for (int j = 0; j < c; ++j) {
+            if ((rc = stepImpl(h, 1)) != SWARM_OK) return fail(rc);
+            swarm_gpu::launch_count_active(h->state[h->readIdx], h->n, dCounts + j, h->stream);
+            launches += h->launches + 1;
+        }
+        if (!cudaOk(h, cudaMemcpyAsync(counts.data(), dCounts, size_t(c) * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream), "count"))
+            return fail(SWARM_E_CUDA);
+        if ((rc = swarm_synchronize(h)) != SWARM_OK) return fail(rc);
+        for (int j = 0; j < c; ++j) series.push_back(int32_t(counts[size_t(j)]));
+        steps += c;
+        active = counts[size_t(c - 1)];
+    }
+    cudaFree(dCounts);
+    SwarmEvacuation e{};
+    e.steps = steps;
+    e.initial_active = int32_t(initial);
+    e.remaining = int32_t(active);
+    int32_t* ts[3] = {&e.t50_step, &e.t90_step, &e.t100_step};
+    const int pct[3] = {50, 90, 100};
+    for (int q = 0; q < 3; ++q) {
+        *ts[q] = -1;
+        for (size_t t = 0; t < series.size(); ++t)
+            if ((initial - series[t]) * 100 >= pct[q] * initial) { *ts[q] = int32_t(t + 1); break; }
+    }
+    e.t50_s = e.t50_step < 0 ? -1.0f : float(double(e.t50_step) * double(h->P.dt));
+    e.t90_s = e.t90_step < 0 ? -1.0f : float(double(e.t90_step) * double(h->P.dt));
+    e.t100_s = e.t100_step < 0 ? -1.0f : float(double(e.t100_step) * double(h->P.dt));
+    *out = e;
+    if (active_out) std::copy(series.begin(), series.end(), active_out);
+    h->launches = launches;
+    return SWARM_OK;
+}
+
 int swarm_step(SwarmHandle h, int steps) {
     if (!h) return SWARM_E_INVALID;
     if (!h->hasState) return h->fail(SWARM_E_STATE, "no state (upload one first)");

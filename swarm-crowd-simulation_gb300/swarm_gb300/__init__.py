@@ -13,8 +13,8 @@ import os
 import numpy as np
 
 from .abi import (METRIC_CELL_WORDS, SWARM_LOSS_NAV_DISTANCE, SWARM_OK, SWARM_VENUE_GRID, SWARM_VENUE_STADIUM,
-                  SwarmAdjointStats, SwarmLossSpec, SwarmMetricCounters, SwarmParams, SwarmStageTimes, SwarmTuning,
-                  SwarmVenue, fptr)
+                  SwarmAdjointStats, SwarmEvacuation, SwarmLossSpec, SwarmMetricCounters, SwarmParams, SwarmStageTimes,
+                  SwarmTuning, SwarmVenue, fptr)
 
 PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG_DIR, "libswarm_gb300.so")
@@ -74,6 +74,11 @@ def lib():
                                   C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                   C.POINTER(SwarmAdjointStats)],
             "swarm_set_relaxation_time": [H, C.c_float],
+            "swarm_run_evacuation": [H, C.c_int, C.c_void_p, C.POINTER(SwarmEvacuation)],
+            "swarm_snapshot_write": [C.c_char_p, C.POINTER(C.c_float), C.c_int],
+            "swarm_snapshot_read": [C.c_char_p, C.POINTER(C.c_float), C.c_int],
+            "swarm_snapshot_count": [C.c_char_p],
+            "swarm_sdf_read": [C.c_char_p, C.POINTER(C.c_float), C.c_int],
             "swarm_bowl_layout": [C.c_void_p, C.POINTER(SwarmVenue)],
             "swarm_bowl_fields": [C.c_void_p, C.POINTER(SwarmVenue), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                   C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_void_p, C.POINTER(C.c_float)],
@@ -103,6 +108,28 @@ def params_si():
     p = SwarmParams()
     _check(lib().swarm_params_si(C.byref(p)), "swarm_params_si")
     return p
+
+
+def snapshot_write(path, boids):
+    """A workload snapshot: the raw GpuBoid array (the reference's bench_common saveSnapshot format)."""
+    b = np.ascontiguousarray(boids, dtype=np.float32).reshape(-1, 8)
+    _check(lib().swarm_snapshot_write(os.fsencode(path), fptr(b), b.shape[0]), "swarm_snapshot_write")
+
+
+def snapshot_read(path):
+    n = lib().swarm_snapshot_count(os.fsencode(path))
+    if n <= 0:
+        raise SwarmError(f"{path}: not a GpuBoid snapshot")
+    out = np.empty((n, 8), np.float32)
+    _check(lib().swarm_snapshot_read(os.fsencode(path), fptr(out), n), "swarm_snapshot_read")
+    return out
+
+
+def sdf_read(path, res=130):
+    """The reference's stadium.sdf: res^3 float32 ([x][y][z], z fastest)."""
+    out = np.empty(res ** 3, np.float32)
+    _check(lib().swarm_sdf_read(os.fsencode(path), fptr(out), int(res)), "swarm_sdf_read")
+    return out
 
 
 def _check(rc, what, h=None):
@@ -241,6 +268,16 @@ class CrowdSim:
         self._ck(lib().swarm_metrics_read(self._h, C.byref(ctr), cells.ctypes.data_as(C.c_void_p),
                                           evac.ctypes.data_as(C.c_void_p), self.n), "metrics_read")
         return ctr, cells, evac
+
+    # ---- headless evacuation ----
+    def run_evacuation(self, max_steps):
+        """Steps until no agent is active or max_steps: (stats dict: steps, initial_active, remaining, t50/t90/t100 in
+        steps and seconds), active count after every step run (int32 array))."""
+        e = SwarmEvacuation()
+        active = np.zeros(int(max_steps), np.int32)
+        self._ck(lib().swarm_run_evacuation(self._h, int(max_steps), active.ctypes.data_as(C.c_void_p), C.byref(e)),
+                 "run_evacuation")
+        return {k: getattr(e, k) for k, _ in SwarmEvacuation._fields_}, active[:e.steps]
 
     # ---- the adjoint ----
     def set_relaxation_time(self, tau):

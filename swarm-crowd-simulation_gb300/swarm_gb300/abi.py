@@ -71,6 +71,11 @@ class SwarmStageTimes(C.Structure):
                 ("final_pass", _f), ("total", _f)]
 
 
+class SwarmEvacuation(C.Structure):
+    _fields_ = [("steps", _i), ("initial_active", _i), ("remaining", _i), ("t50_step", _i), ("t90_step", _i),
+                ("t100_step", _i), ("t50_s", _f), ("t90_s", _f), ("t100_s", _f)]
+
+
 SWARM_LOSS_NAV_DISTANCE = 0
 
 

@@ -295,3 +295,35 @@ def test_barrier_timeout_is_reported_and_the_handle_recovers(terrace, terrace_go
     sim.step(1)
     sim.synchronize()
     assert np.array_equal(_bits(sim.state()), _bits(terrace_golden["state1"]))
+
+
+def test_evacuation_runner_matches_the_reference(terrace, terrace_golden):
+    """swarm_run_evacuation on the reference terrace: the active count it keeps on the device after every step is
+    the reference's own run, and its t100 is the reference's evacuation time (2 696 steps)."""
+    import os
+    P, venue = terrace
+    ref = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "terrace_evac_ref.npz"))
+    t_ref = int(ref["evacuation_steps"][0])
+    sim = _sim(P, venue, terrace_golden["spawn"])
+    stats, active = sim.run_evacuation(t_ref + 500)
+    assert stats["steps"] == t_ref and stats["remaining"] == 0
+    assert np.array_equal(active, ref["active"])
+    n0 = int((terrace_golden["spawn"][:, 3] != 0).sum())
+    assert stats["initial_active"] == n0
+    assert stats["t100_step"] == t_ref
+    assert stats["t50_step"] == int(np.argmax((n0 - ref["active"]) * 100 >= 50 * n0)) + 1
+    assert stats["t90_step"] == int(np.argmax((n0 - ref["active"]) * 100 >= 90 * n0)) + 1
+    assert stats["t100_s"] == pytest.approx(t_ref * P.dt, rel=1e-6)
+    # the state it leaves is the state after t_ref steps: nobody active
+    assert (sim.state()[:, 3] == 0).all()
+
+
+def test_evacuation_runner_stops_at_max_steps(terrace, terrace_golden):
+    import os
+    P, venue = terrace
+    ref = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "terrace_evac_ref.npz"))
+    sim = _sim(P, venue, terrace_golden["spawn"])
+    stats, active = sim.run_evacuation(300)
+    assert stats["steps"] == 300 and active.shape == (300,)
+    assert np.array_equal(active, ref["active"][:300])
+    assert stats["remaining"] == int(ref["active"][299]) and stats["t100_step"] == -1
