@@ -337,7 +337,8 @@ typedef struct SwarmEvacuation {
 /* run_experiment's headless evacuation (DedovSergei/swarm-crowd-simulation tools/experiment/run_experiment.cpp): steps
  * until no agent is active or max_steps, counting the active agents after every step on the device (the metrics,
  * when enabled, record every step as usual). active_out (may be NULL): max_steps entries, the active count after each
- * step run. The state is left after the last step. */
+ * step run. The state (and the metrics) are left after the last step run: the step at which the crowd emptied, or
+ * max_steps. */
 int swarm_run_evacuation(SwarmHandle h, int max_steps, int32_t* active_out, SwarmEvacuation* out);
 
 /* Workload snapshots (tools/benchmark/bench_common.hpp:109-134 saveSnapshot / loadSnapshot): a raw GpuBoid array, n x

@@ -565,39 +565,86 @@ int swarm_run_evacuation(SwarmHandle h, int max_steps, int32_t* active_out, Swar
     if (!h || !out || max_steps < 0) return SWARM_E_INVALID;
     if (!h->hasState) return h->fail(SWARM_E_STATE, "no state (upload one first)");
     constexpr int CHUNK = 256;   // steps between host checks; every step is counted on the device
+    // What a step changes, saved at the start of every chunk: both state halves and, when on, the metrics'
+    // accumulators. A chunk in which the crowd empties is rolled back and replayed up to that step, so the run stops
+    // exactly there (the step is deterministic: the replay gives the same bits).
+    std::vector<std::pair<void*, size_t>> live = {{h->state[0], size_t(h->n) * 32}, {h->state[1], size_t(h->n) * 32}};
+    if (h->metricRes) {
+        const size_t cells = size_t(h->metricRes) * size_t(h->metricRes);
+        live.push_back({h->mCounters, sizeof(SwarmMetricCounters)});
+        live.push_back({h->mEvac, size_t(h->capacity) * 4});
+        live.push_back({h->mMass, cells * 8});
+        live.push_back({h->mCells, cells * sizeof(SwarmMetricCell)});
+    }
+    size_t saveBytes = 0;
+    for (auto& l : live) saveBytes += (l.second + 255) / 256 * 256;
     uint32_t* dCounts = nullptr;
+    char* dSave = nullptr;
     if (!cudaOk(h, cudaMalloc(&dCounts, (CHUNK + 1) * sizeof(uint32_t)), "evacuation counters")) return SWARM_E_OOM;
+    if (!cudaOk(h, cudaMalloc(&dSave, saveBytes), "evacuation rollback copy")) { cudaFree(dCounts); return SWARM_E_OOM; }
+    auto release = [&] { cudaFree(dCounts); cudaFree(dSave); };
+    auto fail = [&](int code) { release(); return code; };
+    auto copyLive = [&](bool save) {
+        size_t off = 0;
+        for (auto& l : live) {
+            void* dst = save ? static_cast<void*>(dSave + off) : l.first;
+            const void* src = save ? l.first : static_cast<const void*>(dSave + off);
+            if (cudaMemcpyAsync(dst, src, l.second, cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess) return false;
+            off += (l.second + 255) / 256 * 256;
+        }
+        return true;
+    };
     std::vector<uint32_t> counts(CHUNK + 1);
     std::vector<int32_t> series;
     int rc = SWARM_OK;
-    auto fail = [&](int code) { cudaFree(dCounts); return code; };
+    int64_t launches = 0;
+    // steps j = 0 .. c - 1 of a chunk, the active count after step j into dCounts[j]
+    auto runChunk = [&](int c) -> int {
+        if (!cudaOk(h, cudaMemsetAsync(dCounts, 0, size_t(c) * sizeof(uint32_t), h->stream), "evacuation counters"))
+            return SWARM_E_CUDA;
+        for (int j = 0; j < c; ++j) {
+            const int r = stepImpl(h, 1);
+            if (r != SWARM_OK) return r;
+            swarm_gpu::launch_count_active(h->state[h->readIdx], h->n, dCounts + j, h->stream);
+            launches += h->launches + 1;
+        }
+        if (!cudaOk(h, cudaMemcpyAsync(counts.data(), dCounts, size_t(c) * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                       h->stream), "count"))
+            return SWARM_E_CUDA;
+        return swarm_synchronize(h);
+    };
     // the active agents before the first step
     if (!cudaOk(h, cudaMemsetAsync(dCounts, 0, sizeof(uint32_t), h->stream), "evacuation counters")) return fail(SWARM_E_CUDA);
     swarm_gpu::launch_count_active(h->state[h->readIdx], h->n, dCounts, h->stream);
+    launches += 1;
     if (!cudaOk(h, cudaMemcpyAsync(counts.data(), dCounts, sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream), "count") ||
         (rc = swarm_synchronize(h)) != SWARM_OK)
         return fail(rc != SWARM_OK ? rc : SWARM_E_CUDA);
     const int64_t initial = counts[0];
-    int64_t launches = 1;
     int steps = 0;
     int64_t active = initial;
     while (steps < max_steps && active > 0) {
         const int c = std::min(CHUNK, max_steps - steps);
-        if (!cudaOk(h, cudaMemsetAsync(dCounts, 0, size_t(c) * sizeof(uint32_t), h->stream), "evacuation counters"))
-            return fail(SWARM_E_CUDA);
-        for (int j = 0; j < c; ++j) {
-            if ((rc = stepImpl(h, 1)) != SWARM_OK) return fail(rc);
-            swarm_gpu::launch_count_active(h->state[h->readIdx], h->n, dCounts + j, h->stream);
-            launches += h->launches + 1;
+        const int readIdx = h->readIdx;
+        const uint32_t metricStep = h->metricStep;
+        if (!copyLive(true)) return fail(h->fail(SWARM_E_CUDA, "evacuation rollback copy"));
+        if ((rc = runChunk(c)) != SWARM_OK) return fail(rc);
+        int run = c;
+        for (int j = 0; j < c; ++j)
+            if (counts[size_t(j)] == 0) { run = j + 1; break; }
+        if (run < c) {
+            // the crowd emptied at step run of this chunk: back to the chunk's start, then exactly run steps
+            if (!copyLive(false)) return fail(h->fail(SWARM_E_CUDA, "evacuation rollback copy"));
+            h->readIdx = readIdx;
+            h->metricStep = metricStep;
+            if (!h->clearCounts()) return fail(h->fail(SWARM_E_CUDA, "clearing the counts"));
+            if ((rc = runChunk(run)) != SWARM_OK) return fail(rc);
         }
-        if (!cudaOk(h, cudaMemcpyAsync(counts.data(), dCounts, size_t(c) * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream), "count"))
-            return fail(SWARM_E_CUDA);
-        if ((rc = swarm_synchronize(h)) != SWARM_OK) return fail(rc);
-        for (int j = 0; j < c; ++j) series.push_back(int32_t(counts[size_t(j)]));
-        steps += c;
-        active = counts[size_t(c - 1)];
+        for (int j = 0; j < run; ++j) series.push_back(int32_t(counts[size_t(j)]));
+        steps += run;
+        active = counts[size_t(run - 1)];
     }
-    cudaFree(dCounts);
+    release();
     SwarmEvacuation e{};
     e.steps = steps;
     e.initial_active = int32_t(initial);

@@ -95,3 +95,36 @@ def test_gpu_metrics_grid_terrace_vs_oracle(built, fused):
     assert np.array_equal(np.frombuffer(bytes(ctr), np.uint32), octr) and octr[2] > 0
     assert np.array_equal(cells, ocells)
     assert np.array_equal(evac, oevac)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fused", [True, False])
+def test_evacuation_runner_leaves_the_metrics_of_its_exact_run(built, stadium_sdf, terrace_golden, metrics_golden, fused):
+    """swarm_run_evacuation checks the count every 256 steps and rolls the chunk in which the crowd empties back to
+    that step: the state and the metrics it leaves are those of exactly t100 steps (2 696 on the reference terrace),
+    bit for bit."""
+    import swarm_gb300
+    P, venue = _terrace(stadium_sdf)
+    g = metrics_golden
+
+    def fresh():
+        sim = swarm_gb300.CrowdSim(P, venue, 4096)
+        sim.set_fused(fused)
+        sim.set_state(terrace_golden["spawn"])
+        sim.metrics_enable(64, g["threshold_mass"])
+        return sim
+
+    a = fresh()
+    stats, active = a.run_evacuation(4000)
+    assert stats["steps"] == 2696 and stats["t100_step"] == 2696 and active[-1] == 0 and (active[:-1] > 0).all()
+    b = fresh()
+    b.step(2696)
+    assert np.array_equal(a.state().view(np.uint32), b.state().view(np.uint32))
+    (actr, acells, aevac), (bctr, bcells, bevac) = a.metrics(), b.metrics()
+    assert bytes(actr) == bytes(bctr)
+    assert np.array_equal(acells, bcells) and np.array_equal(aevac, bevac)
+    # and the run goes on from there as the stepped one does
+    a.step(3)
+    b.step(3)
+    assert np.array_equal(a.state().view(np.uint32), b.state().view(np.uint32))
+    assert np.array_equal(a.metrics()[1], b.metrics()[1])
