@@ -268,6 +268,26 @@ int swarm_bowl_layout(const SwarmBowlSpec* spec, SwarmVenue* venue);
 /* Fills the arrays of a layout made by swarm_bowl_layout (caller-allocated); exit_boxes: each exit's bounding box. */
 int swarm_bowl_fields(const SwarmBowlSpec* spec, const SwarmVenue* venue, float* wall_sdf, float* nav_dist,
                       float* floor_height, float* speed_factor, uint8_t* exit_mask, float* exit_boxes);
+/* ---- the navigation field solver ----
+ * The first-order fast-marching travel distance (the nav_dist of every grid venue above) on an nx x ny grid of spacing
+ * h: kind per node 0 free, 1 source (distance 0), 3 wall; speed per node (NULL: 1) divides the local step h. Walls and
+ * unreached nodes get the largest reached distance + 10 m. The host builders use fast marching on the CPU unless
+ * swarm_set_nav_solver(SWARM_NAV_GPU) selected the GPU solver, which gives the same floats node for node (the fixed
+ * point of the same FP64 update). No counterpart in the reference (its seated venues build Lazy Theta* fields on the
+ * CPU, src/nav_field.cpp:268-344). */
+typedef struct SwarmNavFieldStats {
+    int32_t passes;       /* tile passes run (launched in groups of 8) */
+    int32_t tiles;        /* 32 x 32-node tiles of the grid */
+    int64_t tile_runs;    /* tile relaxations over all passes */
+    float ms;             /* wall-clock time of the call, uploads and downloads included */
+} SwarmNavFieldStats;
+enum { SWARM_NAV_CPU = 0, SWARM_NAV_GPU = 1 };
+int swarm_nav_field_gpu(int nx, int ny, double h, const uint8_t* kind, const float* speed, float* out,
+                        SwarmNavFieldStats* stats);
+int swarm_nav_field_cpu(int nx, int ny, double h, const uint8_t* kind, const float* speed, float* out);
+/* The solver the venue builders use from now on (process-wide); returns the previous one, or SWARM_E_INVALID. */
+int swarm_set_nav_solver(int solver);
+
 /* One agent per seat (sectors x rows x seats, by sector, row, seat) at the seat centre jittered U(-jitter, jitter)
  * per axis, on the floor (z = floor + radius), at rest; radius and desired speed as swarm_spawn_lattice. */
 int swarm_spawn_bowl(const SwarmBowlSpec* spec, float jitter, uint64_t seed, float r_lo, float r_hi, float v_mean,

@@ -11,6 +11,7 @@
 #include "../../include/swarm_cuda.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <limits>
@@ -83,7 +84,7 @@ double uniform01(uint64_t& s) { return double(splitmix64(s) >> 11) * 0x1.0p-53; 
 // 3 wall (never entered). The local step is h / speed (speed: per node, null = 1): the travel distance in
 // flat-floor metres. Nodes never reached and walls get the largest reached value + 10 m, so the normalised negative
 // gradient never points into a wall.
-void fastMarch(int nx, int ny, double h, std::vector<uint8_t> state, const float* speed, float* out) {
+void fastMarchCpu(int nx, int ny, double h, std::vector<uint8_t> state, const float* speed, float* out) {
     const size_t M = size_t(nx) * size_t(ny);
     const double INF = std::numeric_limits<double>::infinity();
     std::vector<double> D(M, INF);
@@ -122,7 +123,31 @@ void fastMarch(int nx, int ny, double h, std::vector<uint8_t> state, const float
     for (size_t k = 0; k < M; ++k) out[k] = float(state[k] == 2 ? D[k] : maxFree + 10.0);
 }
 
+std::atomic<int> navSolver{SWARM_NAV_CPU};
+
+// The builders' solver: fast marching here, or the GPU solver (the same floats) when selected
+int fastMarch(int nx, int ny, double h, std::vector<uint8_t> state, const float* speed, float* out) {
+    if (navSolver.load() == SWARM_NAV_GPU) return swarm_nav_field_gpu(nx, ny, h, state.data(), speed, out, nullptr);
+    fastMarchCpu(nx, ny, h, std::move(state), speed, out);
+    return SWARM_OK;
+}
+
 }  // namespace
+
+extern "C" int swarm_set_nav_solver(int solver) {
+    if (solver != SWARM_NAV_CPU && solver != SWARM_NAV_GPU) return SWARM_E_INVALID;
+    return navSolver.exchange(solver);
+}
+
+extern "C" int swarm_nav_field_cpu(int nx, int ny, double h, const uint8_t* kind, const float* speed, float* out) {
+    if (nx < 2 || ny < 2 || !(h > 0.0) || !kind || !out) return SWARM_E_INVALID;
+    const size_t m = size_t(nx) * size_t(ny);
+    if (speed)
+        for (size_t k = 0; k < m; ++k)
+            if (kind[k] == 0 && !(speed[k] > 0.0f)) return SWARM_E_INVALID;
+    fastMarchCpu(nx, ny, h, std::vector<uint8_t>(kind, kind + m), speed, out);
+    return SWARM_OK;
+}
 
 extern "C" int swarm_hall_layout(const SwarmHallSpec* s, SwarmVenue* v) {
     if (!validSpec(s) || !v) return SWARM_E_INVALID;
@@ -174,7 +199,7 @@ extern "C" int swarm_hall_fields(const SwarmHallSpec* s, const SwarmVenue* v, fl
             else if (x < v->exit_lo_x || x > v->exit_hi_x || y < v->exit_lo_y || y > v->exit_hi_y) kind[k] = 1;
         }
     }
-    fastMarch(nx, ny, v->nav_h, kind, nullptr, nav);
+    if (const int rc = fastMarch(nx, ny, v->nav_h, kind, nullptr, nav); rc != SWARM_OK) return rc;
     // exit boxes: each door's opening, from the interior face out to the domain edge
     if (exitBoxes) {
         for (int d = 0; d < s->n_doors; ++d) {
@@ -362,7 +387,7 @@ extern "C" int swarm_bowl_fields(const SwarmBowlSpec* s, const SwarmVenue* v, fl
             kind[k] = B.sdf(x, y) <= double(s->clearance) ? 3 : (ex ? 1 : 0);
         }
     });
-    fastMarch(nn, v->nav_ny, v->nav_h, kind, speed.data(), nav);
+    if (const int rc = fastMarch(nn, v->nav_ny, v->nav_h, kind, speed.data(), nav); rc != SWARM_OK) return rc;
     if (exitBoxes) {   // each exit's bounding box (the metrics' exit attribution)
         auto bound = [&](int e, int k, double u0, double u1, double w0, double w1) {
             double lo[2] = {1e30, 1e30}, hi[2] = {-1e30, -1e30};

@@ -13,8 +13,8 @@ import os
 import numpy as np
 
 from .abi import (METRIC_CELL_WORDS, SWARM_LOSS_NAV_DISTANCE, SWARM_OK, SWARM_VENUE_GRID, SWARM_VENUE_STADIUM,
-                  SwarmAdjointStats, SwarmEvacuation, SwarmLossSpec, SwarmMetricCounters, SwarmParams, SwarmStageTimes,
-                  SwarmTuning, SwarmVenue, fptr)
+                  SwarmAdjointStats, SwarmEvacuation, SwarmLossSpec, SwarmMetricCounters, SwarmNavFieldStats, SwarmParams,
+                  SwarmStageTimes, SwarmTuning, SwarmVenue, fptr)
 
 PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG_DIR, "libswarm_gb300.so")
@@ -79,6 +79,10 @@ def lib():
             "swarm_snapshot_read": [C.c_char_p, C.POINTER(C.c_float), C.c_int],
             "swarm_snapshot_count": [C.c_char_p],
             "swarm_sdf_read": [C.c_char_p, C.POINTER(C.c_float), C.c_int],
+            "swarm_nav_field_gpu": [C.c_int, C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.POINTER(C.c_float),
+                                    C.POINTER(SwarmNavFieldStats)],
+            "swarm_nav_field_cpu": [C.c_int, C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.POINTER(C.c_float)],
+            "swarm_set_nav_solver": [C.c_int],
             "swarm_bowl_layout": [C.c_void_p, C.POINTER(SwarmVenue)],
             "swarm_bowl_fields": [C.c_void_p, C.POINTER(SwarmVenue), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                   C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_void_p, C.POINTER(C.c_float)],
@@ -130,6 +134,36 @@ def sdf_read(path, res=130):
     out = np.empty(res ** 3, np.float32)
     _check(lib().swarm_sdf_read(os.fsencode(path), fptr(out), int(res)), "swarm_sdf_read")
     return out
+
+
+def nav_field(kind, h, speed=None, solver="gpu"):
+    """The fast-marching travel distance on a grid (kind: (ny, nx) uint8, 0 free, 1 source, 3 wall; speed: (ny, nx)
+    float32 or None): (field (ny, nx) float32, stats dict or None). solver "gpu" or "cpu": the same floats."""
+    kind = np.ascontiguousarray(kind, dtype=np.uint8)
+    ny, nx = kind.shape
+    sp = None if speed is None else np.ascontiguousarray(speed, dtype=np.float32).reshape(ny, nx)
+    out = np.empty((ny, nx), np.float32)
+    kp = kind.ctypes.data_as(C.c_void_p)
+    spp = None if sp is None else sp.ctypes.data_as(C.c_void_p)
+    if solver == "gpu":
+        st = SwarmNavFieldStats()
+        _check(lib().swarm_nav_field_gpu(nx, ny, float(h), kp, spp, fptr(out), C.byref(st)), "swarm_nav_field_gpu")
+        return out, {k: getattr(st, k) for k, _ in SwarmNavFieldStats._fields_}
+    if solver != "cpu":
+        raise ValueError("solver: 'gpu' or 'cpu'")
+    _check(lib().swarm_nav_field_cpu(nx, ny, float(h), kp, spp, fptr(out)), "swarm_nav_field_cpu")
+    return out, None
+
+
+def set_nav_solver(solver):
+    """The solver the venue builders use from now on ("cpu" or "gpu"); returns the previous one."""
+    if solver not in ("cpu", "gpu"):
+        raise ValueError("solver: 'gpu' or 'cpu'")
+    code = 1 if solver == "gpu" else 0
+    prev = lib().swarm_set_nav_solver(code)
+    if prev < 0:
+        raise SwarmError("swarm_set_nav_solver failed")
+    return "gpu" if prev == 1 else "cpu"
 
 
 def _check(rc, what, h=None):

@@ -71,6 +71,13 @@ class SwarmStageTimes(C.Structure):
                 ("final_pass", _f), ("total", _f)]
 
 
+class SwarmNavFieldStats(C.Structure):
+    _fields_ = [("passes", _i), ("tiles", _i), ("tile_runs", C.c_int64), ("ms", _f)]
+
+
+SWARM_NAV_CPU, SWARM_NAV_GPU = 0, 1
+
+
 class SwarmEvacuation(C.Structure):
     _fields_ = [("steps", _i), ("initial_active", _i), ("remaining", _i), ("t50_step", _i), ("t90_step", _i),
                 ("t100_step", _i), ("t50_s", _f), ("t90_s", _f), ("t100_s", _f)]
