@@ -214,25 +214,47 @@ def bench_bowl(P, steps=50, warmup=5, cap=20000, chunk=100):
         stream.synchronize()
         total_ms += e0.elapsed_time(e1)
     value = active / (total_ms * 1e-3)
-    # the evacuation from the seats
+    # the evacuation from the seats, through the headless runner (active counts kept on the device every step)
     sim.set_state(boids)
-    t999, left, t0 = None, n, time.perf_counter()
-    for s in range(chunk, cap + 1, chunk):
-        sim.step(chunk)
-        left = int((sim.state()[:, 3] != 0).sum())
-        if t999 is None and left <= n // 1000:
-            t999 = s
-        if left == 0:
-            break
+    t0 = time.perf_counter()
+    ev, active = sim.run_evacuation(cap)
     wall_s = time.perf_counter() - t0
+    out999 = np.nonzero(active <= n // 1000)[0]
+    t999 = int(out999[0]) + 1 if out999.size else None
     sim.close()
     return {"workload": "seated bowl, 32 sectors x 32 rows x 62 seats (63488 agents), seat 0.5 m, row pitch 0.8 m, "
                         "rise 0.4 m, 1.2 m gangway stairs (speed factor 0.6), 2.4 m vomitories at row 16, 8 perimeter "
                         "exits of 4 m; wall SDF 0.05 m, nav 0.1 m",
             "value": value, "unit": UNIT, "ms_per_step": total_ms / steps, "steps": steps, "warmup": warmup,
             "fraction_of_hbm_roofline": value * B_STEP / (peaks()[0] * 1e9),
-            "evacuation": {"steps_to_99.9pct": t999, "seconds_to_99.9pct": None if t999 is None else t999 * float(P.dt),
-                           "left_after": {"steps": s, "agents": left}, "checked_every": chunk, "wall_s": wall_s}}
+            "evacuation": {"t50_s": ev["t50_s"], "t90_s": ev["t90_s"], "t100_s": ev["t100_s"],
+                           "steps_to_99.9pct": t999, "seconds_to_99.9pct": None if t999 is None else t999 * float(P.dt),
+                           "left_after": {"steps": ev["steps"], "agents": ev["remaining"]}, "wall_s": wall_s,
+                           "path": "swarm_run_evacuation (C ABI)"},
+            "nav_field": bench_nav_field(venue)}
+
+
+def bench_nav_field(venue, clearance=0.2):
+    """The navigation-field solver on the bowl's nav grid (3931 x 3931 nodes at 0.1 m; walls where the wall SDF is
+    within the clearance, sources at the exit mask, the stair speed factors): host fast marching against the GPU
+    solver (wall-clock per call, uploads and downloads included; the GPU's second call), and whether the floats agree."""
+    import swarm_gb300
+    v = venue.struct
+    step = int(round(v.nav_h / v.wall_h))
+    wall = venue.arrays["wall"].reshape(v.wall_ny, v.wall_nx)[::step, ::step][:v.nav_ny, :v.nav_nx]
+    speed = venue.arrays["speed"].reshape(v.wall_ny, v.wall_nx)[::step, ::step][:v.nav_ny, :v.nav_nx]
+    mask = venue.arrays["exit_mask"].reshape(v.nav_ny, v.nav_nx)
+    kind = np.where(wall <= clearance, 3, np.where(mask != 0, 1, 0)).astype(np.uint8)
+    t0 = time.perf_counter()
+    cpu, _ = swarm_gb300.nav_field(kind, v.nav_h, speed=speed, solver="cpu")
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    swarm_gb300.nav_field(kind, v.nav_h, speed=speed, solver="gpu")
+    t0 = time.perf_counter()
+    gpu, st = swarm_gb300.nav_field(kind, v.nav_h, speed=speed, solver="gpu")
+    gpu_ms = (time.perf_counter() - t0) * 1e3
+    return {"grid": f"{v.nav_nx}x{v.nav_ny}", "cpu_fast_marching_ms": cpu_ms, "gpu_ms": gpu_ms,
+            "speedup": cpu_ms / gpu_ms, "gpu_solve_ms": st["ms_solve"], "passes": st["passes"], "tile_runs": st["tile_runs"], "tiles": st["tiles"],
+            "equal_to_fast_marching": bool(np.array_equal(cpu.view(np.uint32), gpu.view(np.uint32)))}
 
 
 def adjoint_bytes(K, steps, ckpt):

@@ -279,7 +279,8 @@ typedef struct SwarmNavFieldStats {
     int32_t passes;       /* tile passes run (launched in groups of 8) */
     int32_t tiles;        /* 32 x 32-node tiles of the grid */
     int64_t tile_runs;    /* tile relaxations over all passes */
-    float ms;             /* wall-clock time of the call, uploads and downloads included */
+    float ms;             /* wall-clock time of the call, allocation, uploads and downloads included */
+    float ms_solve;       /* the passes alone (CUDA events) */
 } SwarmNavFieldStats;
 enum { SWARM_NAV_CPU = 0, SWARM_NAV_GPU = 1 };
 int swarm_nav_field_gpu(int nx, int ny, double h, const uint8_t* kind, const float* speed, float* out,

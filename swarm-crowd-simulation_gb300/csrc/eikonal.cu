@@ -83,22 +83,34 @@ __global__ void __launch_bounds__(EIK_THREADS) k_eik_pass(EikArgs A) {
         }
         sH[ly][lx] = hs;
     }
+    // which nodes changed in the last sweep, one bit per node per parity (the ring never changes within a run): a
+    // node is updated again only when a neighbour changed, since its update reads nothing else
+    __shared__ uint32_t sChg[2][EIK_TILE];   // [parity][row], bit x
+    if (threadIdx.x < 2 * EIK_TILE) (&sChg[0][0])[threadIdx.x] = 0u;
     __syncthreads();
     bool eL = false, eR = false, eB = false, eT = false, changed = false;
     int it = 0;
     for (; it < EIK_LOCAL_ITERS; ++it) {
+        const uint32_t* prev = sChg[(it + 1) & 1];
+        uint32_t* cur = sChg[it & 1];
         bool ch = false;
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
             const int ly = ly0 + 8 * r;
             const double hs = sH[ly][lx];
             if (hs < 0.0) continue;
+            if (it > 0) {
+                const uint32_t row = prev[ly], below = ly > 0 ? prev[ly - 1] : 0u, above = ly + 1 < EIK_TILE ? prev[ly + 1] : 0u;
+                const uint32_t side = (lx > 0 ? row >> (lx - 1) : 0u) | (lx + 1 < EIK_TILE ? row >> (lx + 1) : 0u);
+                if (!(((side | (below >> lx) | (above >> lx)) & 1u))) continue;
+            }
             const double a = fmin(sD[ly + 1][lx], sD[ly + 1][lx + 2]);
             const double b = fmin(sD[ly][lx + 1], sD[ly + 2][lx + 1]);
             const double T = eikUpdate(a, b, hs);
             if (T < sD[ly + 1][lx + 1]) {
                 sD[ly + 1][lx + 1] = T;
                 ch = true;
+                atomicOr(&cur[ly], 1u << lx);
                 eL |= lx == 0;
                 eR |= lx == EIK_TILE - 1;
                 eB |= ly == 0;
@@ -107,6 +119,8 @@ __global__ void __launch_bounds__(EIK_THREADS) k_eik_pass(EikArgs A) {
         }
         changed |= ch;
         if (!__syncthreads_or(ch)) break;
+        if (threadIdx.x < EIK_TILE) sChg[(it + 1) & 1][threadIdx.x] = 0u;   // the next sweep's bits (prev is done)
+        __syncthreads();
     }
     const bool again = it == EIK_LOCAL_ITERS;   // (the same in every thread: the loop ends on a block-wide vote)
     if (__syncthreads_or(changed)) {
@@ -170,6 +184,7 @@ extern "C" int swarm_nav_field_gpu(int nx, int ny, double h, const uint8_t* kind
     unsigned* dActivated = nullptr;
     unsigned long long *dRuns = nullptr, *dMax = nullptr;
     cudaStream_t st = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
     int rc = SWARM_OK;
     auto ok = [&](cudaError_t e) {
         if (e != cudaSuccess && rc == SWARM_OK) rc = e == cudaErrorMemoryAllocation ? SWARM_E_OOM : SWARM_E_CUDA;
@@ -190,6 +205,9 @@ extern "C" int swarm_nav_field_gpu(int nx, int ny, double h, const uint8_t* kind
         k_eik_init<<<unsigned((m + 255) / 256), 256, 0, st>>>(dKind, dD, m);
         ok(cudaGetLastError());
         EikArgs A{nx, ny, tilesX, tilesY, h, dKind, dSpeed, dD, dAct, dAct + tiles, nullptr, dRuns};
+        cudaEventCreate(&ev[0]);
+        cudaEventCreate(&ev[1]);
+        cudaEventRecord(ev[0], st);
         unsigned last = 1;
         while (rc == SWARM_OK && last != 0) {
             if (passes >= EIK_MAX_PASSES) { rc = SWARM_E_TIMEOUT; break; }
@@ -205,6 +223,7 @@ extern "C" int swarm_nav_field_gpu(int nx, int ny, double h, const uint8_t* kind
                 !ok(cudaStreamSynchronize(st)))
                 break;
         }
+        cudaEventRecord(ev[1], st);
         if (rc == SWARM_OK) {
             k_eik_max<<<1024, 256, 0, st>>>(dD, m, dMax);
             k_eik_out<<<unsigned((m + 255) / 256), 256, 0, st>>>(dD, m, dMax, dOut);
@@ -222,8 +241,13 @@ extern "C" int swarm_nav_field_gpu(int nx, int ny, double h, const uint8_t* kind
     cudaFree(dAct);
     cudaFree(dActivated);
     cudaFree(dRuns);
+    float solveMs = 0.0f;
+    if (ev[0] && ev[1] && rc == SWARM_OK) cudaEventElapsedTime(&solveMs, ev[0], ev[1]);
+    for (cudaEvent_t e : ev)
+        if (e) cudaEventDestroy(e);
     if (st) cudaStreamDestroy(st);
     if (stats) {
+        stats->ms_solve = solveMs;
         stats->passes = passes;
         stats->tiles = tiles;
         stats->tile_runs = int64_t(runs);

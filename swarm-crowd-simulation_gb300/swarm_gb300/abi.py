@@ -72,7 +72,7 @@ class SwarmStageTimes(C.Structure):
 
 
 class SwarmNavFieldStats(C.Structure):
-    _fields_ = [("passes", _i), ("tiles", _i), ("tile_runs", C.c_int64), ("ms", _f)]
+    _fields_ = [("passes", _i), ("tiles", _i), ("tile_runs", C.c_int64), ("ms", _f), ("ms_solve", _f)]
 
 
 SWARM_NAV_CPU, SWARM_NAV_GPU = 0, 1
