@@ -39,6 +39,7 @@ struct SwarmSim {
     uint4* rowsA = nullptr;
     uint2* rowsB = nullptr;
     uint2* tileWin = nullptr;
+    float2* goal = nullptr;
     int* errFlag = nullptr;
     unsigned* barrier = nullptr;
     unsigned long long* stamps = nullptr;

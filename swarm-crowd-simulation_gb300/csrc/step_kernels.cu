@@ -170,7 +170,11 @@ __global__ void k_scatter(StepArgs A) {
     if (i < A.n) scatterItem(A, i);
 }
 
-template <bool kPerAgent, bool kB>
+template <class Venue>
+__device__ __forceinline__ f2 goalOf(const StepArgs& A, const Venue& ven, f3 p, uint32_t id);
+
+// Venue (not void): also each slot's e_goal, for the fused step's predict window
+template <bool kPerAgent, bool kB, class Venue = void>
 __device__ __forceinline__ void rankGatherItem(const StepArgs& A, int s) {
     const int nActive = int(A.start[A.V.ncells]);
     const uint32_t me = A.sidTmp[s];
@@ -191,6 +195,11 @@ __device__ __forceinline__ void rankGatherItem(const StepArgs& A, int s) {
     A.vel0[t] = A.stateIn[2 * size_t(me) + 1];
     if (kPerAgent) A.prm[t] = A.aparam[me];
     if (kB) A.instSlot[t] = A.instAgent[me];
+    if constexpr (!std::is_void<Venue>::value) {
+        const VenueArgs& V = kB ? A.venueTable[A.instAgent[me]] : A.V;
+        const f2 g = goalOf(A, Venue{A.P, V}, xyz(p), me);
+        A.goal[t] = make_float2(g.x, g.y);
+    }
 }
 
 template <bool kPerAgent, bool kB>
@@ -224,6 +233,8 @@ __device__ __forceinline__ f2 separationForce(const SwarmParams& P, f3 offset, u
 // Where predict reads its neighbours: the slot buffers, or a tile's perception window staged in shared memory
 struct PredGlobal {
     const StepArgs& A;
+    template <class Venue>
+    __device__ __forceinline__ f2 goal(uint32_t, const Venue& ven, f3 p, uint32_t id) const { return goalOf(A, ven, p, id); }
     __device__ __forceinline__ float4 pos(uint32_t k) const { return A.pos0[k]; }
     __device__ __forceinline__ uint32_t sid(uint32_t k) const { return A.sid[k]; }
     __device__ __forceinline__ float r(uint32_t k) const { return A.prm[k].x; }
@@ -232,7 +243,13 @@ struct PredWindow {
     const float4* pos_;
     const float* r_;
     const uint32_t* sid_;
+    const float2* goal_;    // the gather phase's e_goal of each window slot
     uint32_t lo;
+    template <class Venue>
+    __device__ __forceinline__ f2 goal(uint32_t k, const Venue&, f3, uint32_t) const {
+        const float2 g = goal_[k - lo];
+        return f2{g.x, g.y};
+    }
     __device__ __forceinline__ float4 pos(uint32_t k) const { return pos_[k - lo]; }
     __device__ __forceinline__ uint32_t sid(uint32_t k) const { return sid_[k - lo]; }
     __device__ __forceinline__ float r(uint32_t k) const { return r_[k - lo]; }
@@ -256,7 +273,7 @@ __device__ __forceinline__ void predictCore(const StepArgs& A, int s, const Nbr&
         if constexpr (kTape) A.tapePred[s] = make_float4(0.0f, 0.0f, 1e9f, __int_as_float(-1));
         return;
     }
-    const f2 eGoal = goalOf(A, ven, xyz(p), self);
+    const f2 eGoal = nb.goal(uint32_t(s), ven, xyz(p), self);
     const float ri = kUniform ? P.body_radius : A.prm[s].x;
     const int resX = V.resX, resY = V.resY;
     const int cx = int(cid % uint32_t(resX)), cy = int(cid / uint32_t(resX));
@@ -320,7 +337,7 @@ __device__ __forceinline__ void predictCore(const StepArgs& A, int s, const Nbr&
                 const float dxy = sqrtf(dxy2);
                 const float key = kUniform ? dxy : dxy - dc;
                 if (ahead > 0.0f && lateral < dc && key < sAhead) {
-                    const f2 eOther = goalOf(A, ven, xyz(op), other);
+                    const f2 eOther = nb.goal(k, ven, xyz(op), other);
                     const float aheadOther = dot(xy(offset), eOther);
                     const bool mutual = aheadOther > 0.0f && fabsf(offset.x * eOther.y - offset.y * eOther.x) < dc;
                     if (!mutual || ahead > aheadOther || (ahead == aheadOther && self > other)) {
@@ -633,8 +650,9 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A)
     constexpr bool kUniform = Body<Venue>::kUniform;
     __shared__ uint32_t warpSums[32];
     __shared__ uint32_t prefix;
-    extern __shared__ float4 smPos[];                    // WIN_CAP positions, then WIN_CAP radii, then WIN_CAP ids
-    float* smR = reinterpret_cast<float*>(smPos + WIN_CAP);
+    extern __shared__ float4 smPos[];   // WIN_CAP positions, then WIN_CAP e_goals, WIN_CAP radii, WIN_CAP ids
+    float2* smGoal = reinterpret_cast<float2*>(smPos + WIN_CAP);
+    float* smR = reinterpret_cast<float*>(smGoal + WIN_CAP);
     uint32_t* smSid = reinterpret_cast<uint32_t*>(smR + WIN_CAP);
     const int n = A.n;
     const int T = int(blockDim.x);   // the tile of slots a block handles at a time
@@ -651,7 +669,7 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A)
     if (!gridBarrier(A, gridDim.x)) return;
     for (int i = tid; i < n; i += stride) scatterItem(A, i);
     if (!gridBarrier(A, gridDim.x)) return;
-    for (int s = tid; s < n; s += stride) rankGatherItem<kPerAgent, kB>(A, s);
+    for (int s = tid; s < n; s += stride) rankGatherItem<kPerAgent, kB, Venue>(A, s);
     if (!gridBarrier(A, gridDim.x)) return;
     stamp(A, 1);
     const int nActive = int(A.start[A.V.ncells]);
@@ -664,13 +682,14 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A)
         if (useWin) {
             for (uint32_t k = win.x + threadIdx.x; k < win.y; k += blockDim.x) {
                 smPos[k - win.x] = A.pos0[k];
+                smGoal[k - win.x] = A.goal[k];
                 smR[k - win.x] = kUniform ? 0.0f : A.prm[k].x;
                 smSid[k - win.x] = A.sid[k];
             }
         }
         __syncthreads();
         if (s < n) {
-            if (useWin) predictCore<Venue, kB, kTape>(A, s, PredWindow{smPos, smR, smSid, win.x});
+            if (useWin) predictCore<Venue, kB, kTape>(A, s, PredWindow{smPos, smR, smSid, smGoal, win.x});
             else predictCore<Venue, kB, kTape>(A, s, PredGlobal{A});
             if (s < nActive) prepareSweepItem<kB>(A, s, nActive, T);
         }
@@ -802,7 +821,7 @@ static void stageImpl(const StepArgs& A, int stage, cudaStream_t st, int64_t* la
     }
 }
 
-constexpr int FUSED_SMEM = WIN_CAP * (int(sizeof(float4)) + int(sizeof(float)) + int(sizeof(uint32_t)));
+constexpr int FUSED_SMEM = WIN_CAP * (int(sizeof(float4)) + int(sizeof(float2)) + int(sizeof(float)) + int(sizeof(uint32_t)));
 
 // The fused grid: one block per SM when the state fits (threads = n / SMs rounded up to a warp, 128..512), else as
 // many blocks as stay resident, each taking several tiles per phase
