@@ -50,6 +50,7 @@ WORKLOAD = ("hall 140x140 m, 4 exits of 4 m, 65536 agents (256x256 lattice, 0.5 
 # the final pass reads 64 and writes the 32-byte agent record; the sort stage: hash 24 + sort 16 + ranges 4 + gather 100
 BYTES = {"predict": 96.0, "sweep": 48.0, "final": 96.0, "sort": 144.0}
 B_STEP = 336.0 + 48.0 * (8 - 1)   # 672 B per agent-step at K = 8
+CONGESTED_STEPS = 250             # the reference benchmark's congested state (tools/benchmark/bench_common.hpp)
 
 
 def peaks():
@@ -503,6 +504,29 @@ def main():
             if len(parts) == 2 and not line.startswith("#") and parts[0] == dom:
                 traffic = int(parts[1])
 
+    # the same workload congested: stepped on (untimed) to 250 steps from the spawn -- the reference's own benchmark
+    # states are the spawn and CONGESTED_STEPS = 250 -- then timed the same way
+    congested = None
+    if rank == 0 and world == 1:
+        done = args.warmup + args.steps
+        with torch.cuda.stream(stream):
+            sim.step(max(0, CONGESTED_STEPS - done))
+        torch.cuda.synchronize()
+        c_ms, c_active = [], []
+        for k in range(min(args.steps, 20)):
+            c_active.append(int((sim.state()[:, 3] != 0).sum()))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xFF)
+                e0.record(stream)
+                sim.step(1)
+                e1.record(stream)
+            stream.synchronize()
+            c_ms.append(e0.elapsed_time(e1))
+        congested = {"after_steps": max(CONGESTED_STEPS, done), "steps": len(c_ms),
+                     "value": sum(c_active) / (sum(c_ms) * 1e-3), "ms_per_step": statistics.mean(c_ms),
+                     "active_per_step": statistics.mean(c_active)}
+
     # e2e through swarm_step_host with pinned host buffers
     e2e_sim = swarm_gb300.CrowdSim(P, venue, n)
     e2e_sim.set_agent_params(r, v0)
@@ -542,6 +566,8 @@ def main():
                     "path": "swarm_step_host (C ABI), pinned host buffers"},
             "gpu_launches": launches,
         }
+        if congested:
+            line["config"]["congested"] = congested
         line["clocks"] = clk.summary()
         if not args.no_batch and world == 1:
             try:

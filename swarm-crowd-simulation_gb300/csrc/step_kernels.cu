@@ -104,13 +104,32 @@ __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* war
     return inc - v + (warp > 0 ? warpSums[warp - 1] : 0u);
 }
 
-// Block-level: the total of tile `tile` (blockDim.x * SCAN_ITEMS counts) into A.tileSums
+// A thread's ITEMS consecutive counts of the scan (16-byte loads when the run lies inside the array: its start is a
+// multiple of ITEMS >= 4 words, so 16-byte aligned)
+template <int ITEMS>
+__device__ __forceinline__ void loadCounts(const StepArgs& A, int base, int nb, uint32_t* c) {
+    if (base + ITEMS <= nb) {
+#pragma unroll
+        for (int j = 0; j < ITEMS; j += 4) {
+            const uint4 q = *reinterpret_cast<const uint4*>(A.count + base + j);
+            c[j] = q.x; c[j + 1] = q.y; c[j + 2] = q.z; c[j + 3] = q.w;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) c[j] = base + j < nb ? A.count[base + j] : 0u;
+    }
+}
+
+// Block-level: the total of tile `tile` (blockDim.x * ITEMS counts) into A.tileSums
+template <int ITEMS = SCAN_ITEMS>
 __device__ __forceinline__ void scanReduceTile(const StepArgs& A, int tile, uint32_t* warpSums) {
     const int nb = A.V.ncells + 1;
-    const int base = tile * int(blockDim.x * SCAN_ITEMS) + int(threadIdx.x) * SCAN_ITEMS;
+    const int base = tile * int(blockDim.x * ITEMS) + int(threadIdx.x) * ITEMS;
+    uint32_t c[ITEMS];
+    loadCounts<ITEMS>(A, base, nb, c);
     uint32_t sum = 0;
 #pragma unroll
-    for (int j = 0; j < SCAN_ITEMS; ++j) sum += base + j < nb ? A.count[base + j] : 0u;
+    for (int j = 0; j < ITEMS; ++j) sum += c[j];
     uint32_t total;
     blockExclusiveScan(sum, warpSums, total);
     if (threadIdx.x == 0) A.tileSums[tile] = total;
@@ -118,6 +137,7 @@ __device__ __forceinline__ void scanReduceTile(const StepArgs& A, int tile, uint
 }
 
 // Block-level: scan tile `tile` on top of the totals of the tiles before it; run starts, cell table, counts cleared
+template <int ITEMS = SCAN_ITEMS>
 __device__ __forceinline__ void scanApplyTile(const StepArgs& A, int tile, uint32_t* warpSums, uint32_t* prefix) {
     const int nb = A.V.ncells + 1;
     uint32_t p = 0;
@@ -126,22 +146,41 @@ __device__ __forceinline__ void scanApplyTile(const StepArgs& A, int tile, uint3
     if (threadIdx.x == 0) *prefix = 0;
     __syncthreads();
     if ((threadIdx.x & 31u) == 0 && p) atomicAdd(prefix, p);
-    const int base = tile * int(blockDim.x * SCAN_ITEMS) + int(threadIdx.x) * SCAN_ITEMS;
-    uint32_t c[SCAN_ITEMS];
+    const int base = tile * int(blockDim.x * ITEMS) + int(threadIdx.x) * ITEMS;
+    uint32_t c[ITEMS];
+    loadCounts<ITEMS>(A, base, nb, c);
     uint32_t sum = 0;
 #pragma unroll
-    for (int j = 0; j < SCAN_ITEMS; ++j) { c[j] = base + j < nb ? A.count[base + j] : 0u; sum += c[j]; }
+    for (int j = 0; j < ITEMS; ++j) sum += c[j];
     uint32_t total;
     uint32_t run = blockExclusiveScan(sum, warpSums, total);   // its barriers also order the prefix atomics
     run += *prefix;
+    if (base + ITEMS < nb) {   // the whole run inside the cell table: 16-byte stores
 #pragma unroll
-    for (int j = 0; j < SCAN_ITEMS; ++j) {
-        const int b = base + j;
-        if (b >= nb) break;
-        A.start[b] = run;
-        if (b < A.V.ncells) A.cells[b] = c[j] ? make_uint2(run, c[j]) : make_uint2(0u, 0u);
-        A.count[b] = 0u;   // ready for the next step's hash
-        run += c[j];
+        for (int j = 0; j < ITEMS; j += 4) {
+            uint32_t r[4];
+            uint2 cl[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                r[q] = run;
+                cl[q] = c[j + q] ? make_uint2(run, c[j + q]) : make_uint2(0u, 0u);
+                run += c[j + q];
+            }
+            *reinterpret_cast<uint4*>(A.start + base + j) = make_uint4(r[0], r[1], r[2], r[3]);
+            *reinterpret_cast<uint4*>(A.cells + base + j) = make_uint4(cl[0].x, cl[0].y, cl[1].x, cl[1].y);
+            *reinterpret_cast<uint4*>(A.cells + base + j + 2) = make_uint4(cl[2].x, cl[2].y, cl[3].x, cl[3].y);
+            *reinterpret_cast<uint4*>(A.count + base + j) = make_uint4(0u, 0u, 0u, 0u);   // ready for the next step's hash
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) {
+            const int b = base + j;
+            if (b >= nb) break;
+            A.start[b] = run;
+            if (b < A.V.ncells) A.cells[b] = c[j] ? make_uint2(run, c[j]) : make_uint2(0u, 0u);
+            A.count[b] = 0u;   // ready for the next step's hash
+            run += c[j];
+        }
     }
     __syncthreads();   // prefix and warpSums are reused by the next tile
 }
@@ -662,10 +701,19 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A)
         for (int base = tid - int(threadIdx.x & 31u); base < n; base += stride) hashItem<kB>(A, base + int(threadIdx.x & 31u));
         if (!gridBarrier(A, gridDim.x)) return;
     }
-    const int tiles = (A.V.ncells + 1 + T * SCAN_ITEMS - 1) / (T * SCAN_ITEMS);
-    for (int t = blockIdx.x; t < tiles; t += gridDim.x) scanReduceTile(A, t, warpSums);
+    // the scan in one tile per block where 8 counts a thread would need more tiles than blocks (sparse venues), else 8
+    const bool wide = (A.V.ncells + 1 + T * SCAN_ITEMS - 1) / (T * SCAN_ITEMS) > int(gridDim.x);
+    const int items = wide ? 2 * SCAN_ITEMS : SCAN_ITEMS;
+    const int tiles = (A.V.ncells + 1 + T * items - 1) / (T * items);
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
+        if (wide) scanReduceTile<2 * SCAN_ITEMS>(A, t, warpSums);
+        else scanReduceTile<SCAN_ITEMS>(A, t, warpSums);
+    }
     if (!gridBarrier(A, gridDim.x + unsigned(A.barrierExtra))) return;   // barrierExtra: the timeout test's block that never arrives
-    for (int t = blockIdx.x; t < tiles; t += gridDim.x) scanApplyTile(A, t, warpSums, &prefix);
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
+        if (wide) scanApplyTile<2 * SCAN_ITEMS>(A, t, warpSums, &prefix);
+        else scanApplyTile<SCAN_ITEMS>(A, t, warpSums, &prefix);
+    }
     if (!gridBarrier(A, gridDim.x)) return;
     for (int i = tid; i < n; i += stride) scatterItem(A, i);
     if (!gridBarrier(A, gridDim.x)) return;
