@@ -22,6 +22,10 @@ using swarm_gpu::AdjArgs;
 using swarm_gpu::StepArgs;
 using swarm_gpu::TapeLayout;
 
+// Words between consecutive steps' run starts on the tape: ncells + 1, rounded up to 4 so that each step's array
+// starts 16-byte aligned (the scan writes it with 16-byte stores)
+inline size_t startStride(int ncells) { return (size_t(ncells) + 1 + 3) / 4 * 4; }
+
 struct SwarmAdjoint {
     int n = 0, K = 0, ckpt = 0, nseg = 0, steps = 0, ncells = 0;
     double speedMax = 1.0;           // the venue's largest speed factor
@@ -35,7 +39,7 @@ struct SwarmAdjoint {
     float2* tapePrm = nullptr;       // ckpt x n
     uint32_t* tapeSid = nullptr;     // ckpt x n
     uint32_t* tapeSkey = nullptr;    // ckpt x n
-    uint32_t* tapeStart = nullptr;   // ckpt x (ncells + 1)
+    uint32_t* tapeStart = nullptr;   // ckpt x startStride (ncells + 1 run starts, padded to 16 bytes)
     uint8_t* tapeCtc = nullptr;      // ckpt x n
     uint32_t *key = nullptr, *rank = nullptr, *count = nullptr, *sidTmp = nullptr, *tileSums = nullptr;
     uint2* cells = nullptr;
@@ -92,7 +96,7 @@ SwarmAdjoint* makeAdjoint(SwarmSim* h, int n, int K, int ckpt, int nseg, int ste
     const bool good =
         a->alloc(&a->state[0], 2 * N) && a->alloc(&a->state[1], 2 * N) && a->alloc(&a->ckptState, size_t(nseg) * 2 * N) &&
         a->alloc(&a->tapeF4, C * a->f4Step()) && a->alloc(&a->tapePrm, C * N) && a->alloc(&a->tapeSid, C * N) &&
-        a->alloc(&a->tapeSkey, C * N) && a->alloc(&a->tapeStart, C * NC) && a->alloc(&a->tapeCtc, C * N) &&
+        a->alloc(&a->tapeSkey, C * N) && a->alloc(&a->tapeStart, C * startStride(h->ncells)) && a->alloc(&a->tapeCtc, C * N) &&
         a->alloc(&a->key, N) && a->alloc(&a->rank, N) && a->alloc(&a->count, NC) && a->alloc(&a->sidTmp, N) &&
         a->alloc(&a->tileSums, size_t(h->ncells) / 1024 + 2) && a->alloc(&a->cells, NC) && a->alloc(&a->contacts, N) &&
         a->alloc(&a->err, 1) && a->alloc(&a->barrier, 8) && a->alloc(&a->stamps, 8) && a->alloc(&a->rowsA, N) && a->alloc(&a->rowsB, N) &&
@@ -123,7 +127,7 @@ StepArgs forwardArgs(const SwarmSim* h, const SwarmAdjoint* a, int in, int j) {
     A.key = a->key; A.rank = a->rank; A.count = a->count; A.cells = a->cells; A.tileSums = a->tileSums; A.sidTmp = a->sidTmp;
     A.sid = a->tapeSid + size_t(j) * N;
     A.skey = a->tapeSkey + size_t(j) * N;
-    A.start = a->tapeStart + size_t(j) * (size_t(a->ncells) + 1);
+    A.start = a->tapeStart + size_t(j) * startStride(a->ncells);
     float4* t = a->tape(j);
     A.pos0 = t + L.pos0();
     A.vel0 = t + L.vel0();

@@ -104,11 +104,13 @@ __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* war
     return inc - v + (warp > 0 ? warpSums[warp - 1] : 0u);
 }
 
-// A thread's ITEMS consecutive counts of the scan (16-byte loads when the run lies inside the array: its start is a
-// multiple of ITEMS >= 4 words, so 16-byte aligned)
+// A thread's ITEMS consecutive counts of the scan (16-byte loads when the run lies inside the array and the array is
+// 16-byte aligned: the run's start is a multiple of ITEMS >= 4 words)
+__device__ __forceinline__ bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0u; }
+
 template <int ITEMS>
 __device__ __forceinline__ void loadCounts(const StepArgs& A, int base, int nb, uint32_t* c) {
-    if (base + ITEMS <= nb) {
+    if (base + ITEMS <= nb && aligned16(A.count)) {
 #pragma unroll
         for (int j = 0; j < ITEMS; j += 4) {
             const uint4 q = *reinterpret_cast<const uint4*>(A.count + base + j);
@@ -155,7 +157,8 @@ __device__ __forceinline__ void scanApplyTile(const StepArgs& A, int tile, uint3
     uint32_t total;
     uint32_t run = blockExclusiveScan(sum, warpSums, total);   // its barriers also order the prefix atomics
     run += *prefix;
-    if (base + ITEMS < nb) {   // the whole run inside the cell table: 16-byte stores
+    if (base + ITEMS < nb && aligned16(A.start) && aligned16(A.cells) && aligned16(A.count)) {
+        // the whole run inside the cell table, every array 16-byte aligned: 16-byte stores
 #pragma unroll
         for (int j = 0; j < ITEMS; j += 4) {
             uint32_t r[4];
@@ -211,6 +214,22 @@ __global__ void k_scatter(StepArgs A) {
 
 template <class Venue>
 __device__ __forceinline__ f2 goalOf(const StepArgs& A, const Venue& ven, f3 p, uint32_t id);
+
+// The obstacle avoidance term at torso height (physics.comp:1315-1325 sceneDist / sceneNormal / calcGradient): a
+// function of the start position alone
+template <class Venue>
+__device__ __forceinline__ f2 obstacleTerm(const SwarmParams& P, const Venue& ven, float4 p) {
+    f2 aObs{0.0f, 0.0f};
+    const f3 torso{p.x + 0.0f, p.y + 0.0f, p.z + P.torso_height};
+    bool onFence = false;
+    const float dTorso = ven.sceneDist(torso, onFence);
+    if (dTorso < P.obstacle_range) {
+        const f2 norm = ven.sceneNormal(torso, onFence);
+        if (length(norm) > P.obstacle_min_normal)
+            aObs = safeNormalize(norm, P.safe_eps) * (P.obstacle_range - dTorso) * P.w_obs * P.obstacle_gain;
+    }
+    return aObs;
+}
 
 // Venue (not void): also each slot's e_goal, for the fused step's predict window
 template <bool kPerAgent, bool kB, class Venue = void>
@@ -274,6 +293,8 @@ struct PredGlobal {
     const StepArgs& A;
     template <class Venue>
     __device__ __forceinline__ f2 goal(uint32_t, const Venue& ven, f3 p, uint32_t id) const { return goalOf(A, ven, p, id); }
+    template <class Venue>
+    __device__ __forceinline__ f2 obstacle(uint32_t, const Venue& ven, float4 p) const { return obstacleTerm(A.P, ven, p); }
     __device__ __forceinline__ float4 pos(uint32_t k) const { return A.pos0[k]; }
     __device__ __forceinline__ uint32_t sid(uint32_t k) const { return A.sid[k]; }
     __device__ __forceinline__ float r(uint32_t k) const { return A.prm[k].x; }
@@ -283,12 +304,15 @@ struct PredWindow {
     const float* r_;
     const uint32_t* sid_;
     const float2* goal_;    // the gather phase's e_goal of each window slot
+    const SwarmParams& P;
     uint32_t lo;
     template <class Venue>
     __device__ __forceinline__ f2 goal(uint32_t k, const Venue&, f3, uint32_t) const {
         const float2 g = goal_[k - lo];
         return f2{g.x, g.y};
     }
+    template <class Venue>
+    __device__ __forceinline__ f2 obstacle(uint32_t, const Venue& ven, float4 p) const { return obstacleTerm(P, ven, p); }
     __device__ __forceinline__ float4 pos(uint32_t k) const { return pos_[k - lo]; }
     __device__ __forceinline__ uint32_t sid(uint32_t k) const { return sid_[k - lo]; }
     __device__ __forceinline__ float r(uint32_t k) const { return r_[k - lo]; }
@@ -398,15 +422,7 @@ __device__ __forceinline__ void predictCore(const StepArgs& A, int s, const Nbr&
     const f2 eDir = safeNormalize(eGoal + sep, P.safe_eps);
 
     // obstacle avoidance at torso height
-    f2 aObs{0.0f, 0.0f};
-    const f3 torso{p.x + 0.0f, p.y + 0.0f, p.z + P.torso_height};
-    bool onFence = false;
-    const float dTorso = ven.sceneDist(torso, onFence);
-    if (dTorso < P.obstacle_range) {
-        const f2 norm = ven.sceneNormal(torso, onFence);
-        if (length(norm) > P.obstacle_min_normal)
-            aObs = safeNormalize(norm, P.safe_eps) * (P.obstacle_range - dTorso) * P.w_obs * P.obstacle_gain;
-    }
+    const f2 aObs = nb.obstacle(uint32_t(s), ven, p);
 
     // kinematics
     const f2 vEq = eDir * vDes + aObs * P.tau_relax;
@@ -737,7 +753,7 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A)
         }
         __syncthreads();
         if (s < n) {
-            if (useWin) predictCore<Venue, kB, kTape>(A, s, PredWindow{smPos, smR, smSid, smGoal, win.x});
+            if (useWin) predictCore<Venue, kB, kTape>(A, s, PredWindow{smPos, smR, smSid, smGoal, A.P, win.x});
             else predictCore<Venue, kB, kTape>(A, s, PredGlobal{A});
             if (s < nActive) prepareSweepItem<kB>(A, s, nActive, T);
         }
