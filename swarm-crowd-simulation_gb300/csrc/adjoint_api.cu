@@ -194,6 +194,9 @@ extern "C" int swarm_adjoint_run(SwarmHandle h, const SwarmLossSpec* loss, int s
     // whenever a checkpoint is restored.
     bool counted = false;
     auto chain = [&](StepArgs& A, bool last) {
+        // a chain's first step hashes from zero counts and zero scan-tile sums (the tile is the same along a chain:
+        // the agent count, cell count and tuning do not change within the run)
+        if (!counted) cudaMemsetAsync(a->tileSums, 0, (size_t(a->ncells) / 1024 + 2) * 4, st);
         A.hashed = counted ? 1 : 0;
         A.hashNext = last ? 0 : 1;
         counted = !last;

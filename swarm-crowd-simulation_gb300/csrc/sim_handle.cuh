@@ -47,6 +47,7 @@ struct SwarmSim {
     int barrierExtra = 0;       // the timeout test's missing block (swarm_test_barrier_timeout)
     SwarmTuning tuning{1, 0, 0, 0.0f};   // the launch configuration (swarm_autotune / swarm_set_tuning)
     bool counted = false;       // the counts hold the current state's keys (a fused step's final pass counted them)
+    int countedTile = 0;        // the scan tile (cells) of the tile sums that counting left
     // safety metrics (swarm_metrics_enable)
     int metricRes = 0;
     uint32_t metricStep = 0;
@@ -82,10 +83,11 @@ struct SwarmSim {
 
     swarm_gpu::StepArgs args(int in) const;
     int fail(int code, const std::string& msg) { err = msg; return code; }
-    // The per-phase path hashes from zeroed counts: drop what a fused final pass counted ahead
+    // The per-phase path hashes from zeroed counts: drop what a fused final pass counted ahead (and its scan-tile sums)
     bool clearCounts() {
         counted = false;
-        return cudaMemsetAsync(count, 0, (size_t(ncells) + 1) * 4, stream) == cudaSuccess;
+        return cudaMemsetAsync(count, 0, (size_t(ncells) + 1) * 4, stream) == cudaSuccess &&
+               cudaMemsetAsync(tileSums, 0, (size_t(ncells) / 1024 + 2) * 4, stream) == cudaSuccess;
     }
     void dropGraphs() {
         for (auto& g : graph) if (g) { cudaGraphExecDestroy(g); g = nullptr; }

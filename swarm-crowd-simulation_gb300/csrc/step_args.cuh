@@ -80,6 +80,8 @@ struct StepArgs {
     int32_t hashNext;       // fused step: count the next step's keys in the final pass
     int32_t fusedThreads;   // fused step: threads per block (0: n / SMs rounded up to a warp, 128..512)
     int32_t fusedBlocksPerSm;   // fused step: at most this many blocks per SM (0: as many as fit)
+    int32_t scanTile;       // fused step: cells per scan tile (set by the launcher: blockDim x 8, or x 16 on sparse
+                            // venues); a fused pass that counts keys also sums them per tile into tileSums
     // batched instances (null otherwise): each instance's venue, the instance of each agent and of each slot
     const VenueArgs* venueTable;
     const uint32_t* instAgent;

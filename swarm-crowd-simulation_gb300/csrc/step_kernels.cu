@@ -45,6 +45,8 @@ __device__ __forceinline__ const VenueArgs& venueOfSlot(const StepArgs& A, int s
 
 // Counts agent i's key in its cell's counter and records its arrival rank. Called by all 32 lanes of a warp together
 // (warp-aggregated atomics: one atomic per distinct cell per warp); lanes with valid == false take no part.
+// kTiles (the fused step): also the count of each scan tile of A.scanTile cells, into tileSums
+template <bool kTiles = false>
 __device__ __forceinline__ void countKey(const StepArgs& A, uint32_t i, uint32_t key, bool valid) {
     const unsigned lane = threadIdx.x & 31u;
     const unsigned mask = __ballot_sync(0xffffffffu, valid);
@@ -54,13 +56,18 @@ __device__ __forceinline__ void countKey(const StepArgs& A, uint32_t i, uint32_t
     const int leader = __ffs(peers) - 1;
     uint32_t base = 0;
     if (int(lane) == leader) base = atomicAdd(A.count + bucket, uint32_t(__popc(peers)));
+    if constexpr (kTiles) {
+        const uint32_t tile = bucket / uint32_t(A.scanTile);
+        const unsigned tp = __match_any_sync(mask, tile);
+        if (int(lane) == __ffs(tp) - 1) atomicAdd(A.tileSums + tile, uint32_t(__popc(tp)));
+    }
     base = __shfl_sync(peers, base, leader);
     A.key[i] = key;
     A.rank[i] = base + uint32_t(__popc(peers & ((1u << lane) - 1u)));
 }
 
 // calc_grid.comp (CpuCrowdSim::hash, cpu_crowd_sim.cpp:983-993), with its NaN sanitiser. All lanes of a warp together.
-template <bool kB>
+template <bool kB, bool kTiles = false>
 __device__ __forceinline__ void hashItem(const StepArgs& A, int i) {
     const bool valid = i < A.n;
     uint32_t key = 0;
@@ -69,7 +76,7 @@ __device__ __forceinline__ void hashItem(const StepArgs& A, int i) {
         if (isnan(p.x)) { p = make_float4(0.0f, 0.0f, 0.0f, 1.0f); A.stateIn[2 * size_t(i)] = p; }
         key = p.w == 0.0f ? INACTIVE_CELL : cellID(venueOfAgent<kB>(A, uint32_t(i)), p);
     }
-    countKey(A, uint32_t(valid ? i : 0), key, valid);
+    countKey<kTiles>(A, uint32_t(valid ? i : 0), key, valid);
 }
 
 template <bool kB>
@@ -713,24 +720,22 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A)
     const int T = int(blockDim.x);   // the tile of slots a block handles at a time
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
     stamp(A, 0);
-    if (!A.hashed) {   // (the previous fused step's final pass counted the keys already)
-        for (int base = tid - int(threadIdx.x & 31u); base < n; base += stride) hashItem<kB>(A, base + int(threadIdx.x & 31u));
+    // The scan runs in tiles of A.scanTile cells (8 counts a thread, or 16 on sparse venues). Whoever counted the
+    // keys -- the previous fused step's final pass, or the hash here -- also summed them per tile, so the scan starts
+    // at its apply phase (the tile sums were zero before that counting: cleared below, or by the host).
+    if (!A.hashed) {
+        for (int base = tid - int(threadIdx.x & 31u); base < n; base += stride)
+            hashItem<kB, true>(A, base + int(threadIdx.x & 31u));
         if (!gridBarrier(A, gridDim.x)) return;
     }
-    // the scan in one tile per block where 8 counts a thread would need more tiles than blocks (sparse venues), else 8
-    const bool wide = (A.V.ncells + 1 + T * SCAN_ITEMS - 1) / (T * SCAN_ITEMS) > int(gridDim.x);
-    const int items = wide ? 2 * SCAN_ITEMS : SCAN_ITEMS;
-    const int tiles = (A.V.ncells + 1 + T * items - 1) / (T * items);
-    for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
-        if (wide) scanReduceTile<2 * SCAN_ITEMS>(A, t, warpSums);
-        else scanReduceTile<SCAN_ITEMS>(A, t, warpSums);
-    }
-    if (!gridBarrier(A, gridDim.x + unsigned(A.barrierExtra))) return;   // barrierExtra: the timeout test's block that never arrives
+    const bool wide = A.scanTile > T * SCAN_ITEMS;
+    const int tiles = (A.V.ncells + 1 + A.scanTile - 1) / A.scanTile;
     for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
         if (wide) scanApplyTile<2 * SCAN_ITEMS>(A, t, warpSums, &prefix);
         else scanApplyTile<SCAN_ITEMS>(A, t, warpSums, &prefix);
     }
-    if (!gridBarrier(A, gridDim.x)) return;
+    if (!gridBarrier(A, gridDim.x + unsigned(A.barrierExtra))) return;   // barrierExtra: the timeout test's block that never arrives
+    for (int t = tid; t < tiles; t += stride) A.tileSums[t] = 0u;   // read by every apply tile above; summed again below
     for (int i = tid; i < n; i += stride) scatterItem(A, i);
     if (!gridBarrier(A, gridDim.x)) return;
     for (int s = tid; s < n; s += stride) rankGatherItem<kPerAgent, kB, Venue>(A, s);
@@ -828,7 +833,7 @@ __global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A)
         }
         else if (s < n) finalInactive(A, s);
         // the next step's hash, counted here (all lanes of the warp together)
-        if (A.hashNext) countKey(A, s < n ? A.sid[s] : 0u, nextKey, s < n);
+        if (A.hashNext) countKey<true>(A, s < n ? A.sid[s] : 0u, nextKey, s < n);
     }
     if (A.stamps) {   // the end: the last block out records it
         __syncthreads();
@@ -889,18 +894,41 @@ constexpr int FUSED_SMEM = WIN_CAP * (int(sizeof(float4)) + int(sizeof(float2)) 
 
 // The fused grid: one block per SM when the state fits (threads = n / SMs rounded up to a warp, 128..512), else as
 // many blocks as stay resident, each taking several tiles per phase
-template <class Venue, bool kPerAgent, bool kB, bool kTape = false>
-static cudaError_t fusedImpl(const StepArgs& A, cudaStream_t st) {
+static int smCount() {
     static int sms = 0;
     if (!sms) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaFuncSetAttribute(k_step_fused<Venue, kPerAgent, kB, kTape>, cudaFuncAttributeMaxDynamicSharedMemorySize, FUSED_SMEM);
     }
+    return sms;
+}
+
+static int fusedThreads(const StepArgs& A) {
+    const int sms = smCount();
     int threads = A.fusedThreads > 0 ? A.fusedThreads : ((A.n + sms - 1) / sms + 31) / 32 * 32;
     threads = threads < 128 ? 128 : (threads > FUSED_MAX_THREADS ? FUSED_MAX_THREADS : threads);
-    threads = (threads + 31) / 32 * 32;
+    return (threads + 31) / 32 * 32;
+}
+
+// 8 counts a thread, or 16 where that would take more tiles than there are SMs (sparse venues)
+int fusedScanTile(const StepArgs& A) {
+    const int T = fusedThreads(A);
+    const int tiles8 = (A.V.ncells + 1 + T * SCAN_ITEMS - 1) / (T * SCAN_ITEMS);
+    return tiles8 > smCount() ? T * 2 * SCAN_ITEMS : T * SCAN_ITEMS;
+}
+
+template <class Venue, bool kPerAgent, bool kB, bool kTape = false>
+static cudaError_t fusedImpl(const StepArgs& A0, cudaStream_t st) {
+    static bool smemSet = false;
+    if (!smemSet) {
+        cudaFuncSetAttribute(k_step_fused<Venue, kPerAgent, kB, kTape>, cudaFuncAttributeMaxDynamicSharedMemorySize, FUSED_SMEM);
+        smemSet = true;
+    }
+    const int sms = smCount();
+    StepArgs A = A0;
+    const int threads = fusedThreads(A);
+    A.scanTile = fusedScanTile(A);
     static int occThreads = -1, occPerSm = 0;   // the occupancy of the last block size asked for
     if (occThreads != threads) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occPerSm, k_step_fused<Venue, kPerAgent, kB, kTape>, threads, FUSED_SMEM);

@@ -20,5 +20,8 @@ void launch_step_taped(const StepArgs& A, float4* const* q, float4* const* corr,
 cudaError_t launch_step_fused_taped(const StepArgs& A, cudaStream_t st);
 // the whole step as one cooperative persistent kernel (grid barriers between the phases)
 cudaError_t launch_step_fused(const StepArgs& A, cudaStream_t st);
+// the fused step's scan tile (cells) for A's agent count, cell count and tuning: a fused step that counts the next
+// step's keys leaves their per-tile sums in tileSums for a next step with the same tile (else clear both first)
+int fusedScanTile(const StepArgs& A);
 
 }  // namespace swarm_gpu

@@ -526,11 +526,17 @@ static int stepImpl(SwarmHandle h, int steps, bool countLast) {
         if (h->fused) {
             if (h->timing && !cudaOk(h, cudaEventRecord(h->ev[0], h->stream), "event")) return SWARM_E_CUDA;
             StepArgs A = h->args(in);
+            // the counts (and their scan-tile sums) carried from the last fused step, if its tile matches this one's
+            const int tile = swarm_gpu::fusedScanTile(A);
+            if (h->counted && tile != h->countedTile && !h->clearCounts()) return SWARM_E_CUDA;
+            if (!h->counted && !cudaOk(h, cudaMemsetAsync(h->tileSums, 0, (size_t(h->ncells) / 1024 + 2) * 4, h->stream), "tile sums"))
+                return SWARM_E_CUDA;
             A.hashed = h->counted ? 1 : 0;
             A.hashNext = (countLast || s + 1 < steps) ? 1 : 0;
             if (!cudaOk(h, swarm_gpu::launch_step_fused(A, h->stream), "fused step launch")) return SWARM_E_CUDA;
             h->barrierExtra = 0;
             h->counted = A.hashNext != 0;
+            h->countedTile = tile;
             if (h->timing && !cudaOk(h, cudaEventRecord(h->ev[4], h->stream), "event")) return SWARM_E_CUDA;
             h->launches += 1;
         } else if (h->counted && !h->clearCounts()) {
