@@ -235,6 +235,12 @@ def bench_bowl(P, steps=50, warmup=5, cap=20000, chunk=100):
             "nav_field": bench_nav_field(venue)}
 
 
+def bowl_venue():
+    """The seated bowl's venue alone (its nav grid is the solver's workload)."""
+    from swarm_gb300 import venues
+    return venues.bowl_c2()[0]
+
+
 def bench_nav_field(venue, clearance=0.2):
     """The navigation-field solver on the bowl's nav grid (3931 x 3931 nodes at 0.1 m; walls where the wall SDF is
     within the clearance, sources at the exit mask, the stair speed factors): host fast marching against the GPU
@@ -380,7 +386,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
     ap.add_argument("--no-bowl", action="store_true", help="skip the seated-bowl measurement")
     ap.add_argument("--adjoint-steps", type=int, default=400, help="steps of the adjoint measurement (400: the workload)")
-    ap.add_argument("--only", choices=["adjoint", "bowl", "batched"], default=None,
+    ap.add_argument("--only", choices=["adjoint", "bowl", "batched", "navfield"], default=None,
                     help="run only this sub-measurement and print its object (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -393,7 +399,8 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         P = swarm_gb300.params_si()
         fn = {"adjoint": lambda: bench_adjoint(P, steps=args.adjoint_steps), "bowl": lambda: bench_bowl(P),
-              "batched": lambda: bench_batched(P)}[args.only]
+              "batched": lambda: bench_batched(P),
+              "navfield": lambda: bench_nav_field(bowl_venue())}[args.only]
         print(json.dumps({args.only: fn()}))
         return 0
 

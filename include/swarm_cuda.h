@@ -189,7 +189,7 @@ int swarm_set_graph(SwarmHandle h, int enabled);
  * sweeps, final), replayed from CUDA graphs when swarm_set_graph is on. Both give the same bits. */
 int swarm_set_fused(SwarmHandle h, int enabled);
 /* The launch configuration: the fused persistent kernel (fused = 1) with `threads` per block (0: the state size over
- * the SMs, rounded up to a warp, 128..512) and at most `blocks_per_sm` blocks per SM (0: as many as fit; fewer blocks
+ * the SMs, rounded up to a warp, 128..512, or 128..1024 for a batch) and at most `blocks_per_sm` blocks per SM (0: as many as fit; fewer blocks
  * mean more agents per thread), or one kernel per phase (fused = 0: one Jacobi sweep per launch). */
 typedef struct SwarmTuning { int32_t fused, threads, blocks_per_sm; float ms_per_step; } SwarmTuning;
 int swarm_set_tuning(SwarmHandle h, const SwarmTuning* tuning);

@@ -87,6 +87,9 @@ __global__ void k_hash(StepArgs A) { hashItem<kB>(A, blockIdx.x * blockDim.x + t
 // and clears the counts for the next step. No block waits on another.
 constexpr int SCAN_THREADS = 256, SCAN_ITEMS = 8, SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 constexpr int FUSED_MAX_THREADS = 512;   // the fused kernel's largest block (one block per SM, sized to the state)
+// the batched instantiation's largest block: a batch has many tiles per block and phase, and its phases are bound by
+// the latency of the window loads and the neighbour loops, which more warps per SM hide (64 registers a thread)
+constexpr int FUSED_MAX_THREADS_BATCH = 1024;
 
 // Block-wide exclusive scan of one value per thread (any block size that is a multiple of 32, up to 1024)
 __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* warpSums, uint32_t& total) {
@@ -708,7 +711,7 @@ __device__ __forceinline__ uint2 predWindow(const StepArgs& A, int t, int T, int
 // kTape (the adjoint's recompute): sweep k reads q[k - 1] and writes q[k], q[k] = proj[0] + k n, with its relaxed
 // corrections at tapeCorr + (k - 1) n; the final pass records the last sweep's result in tapeQK; predict its record
 template <class Venue, bool kPerAgent, bool kB, bool kTape = false>
-__global__ void __launch_bounds__(FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A) {
+__global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A) {
     constexpr bool kUniform = Body<Venue>::kUniform;
     __shared__ uint32_t warpSums[32];
     __shared__ uint32_t prefix;
@@ -892,8 +895,8 @@ static void stageImpl(const StepArgs& A, int stage, cudaStream_t st, int64_t* la
 
 constexpr int FUSED_SMEM = WIN_CAP * (int(sizeof(float4)) + int(sizeof(float2)) + int(sizeof(float)) + int(sizeof(uint32_t)));
 
-// The fused grid: one block per SM when the state fits (threads = n / SMs rounded up to a warp, 128..512), else as
-// many blocks as stay resident, each taking several tiles per phase
+// The fused grid: one block per SM when the state fits (threads = n / SMs rounded up to a warp, 128..512; 128..1024
+// for a batch), else as many blocks as stay resident, each taking several tiles per phase
 static int smCount() {
     static int sms = 0;
     if (!sms) {
@@ -907,7 +910,8 @@ static int smCount() {
 static int fusedThreads(const StepArgs& A) {
     const int sms = smCount();
     int threads = A.fusedThreads > 0 ? A.fusedThreads : ((A.n + sms - 1) / sms + 31) / 32 * 32;
-    threads = threads < 128 ? 128 : (threads > FUSED_MAX_THREADS ? FUSED_MAX_THREADS : threads);
+    const int cap = A.venueTable ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREADS;
+    threads = threads < 128 ? 128 : (threads > cap ? cap : threads);
     return (threads + 31) / 32 * 32;
 }
 

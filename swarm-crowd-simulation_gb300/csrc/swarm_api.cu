@@ -428,7 +428,9 @@ int swarm_metrics_read(SwarmHandle h, SwarmMetricCounters* counters, SwarmMetric
 static int stepImpl(SwarmHandle h, int steps, bool countLast = true);
 
 int swarm_set_tuning(SwarmHandle h, const SwarmTuning* t) {
-    if (!h || !t || t->threads < 0 || t->threads > 512 || t->blocks_per_sm < 0) return SWARM_E_INVALID;
+    if (!h || !t || t->threads < 0 || t->blocks_per_sm < 0) return SWARM_E_INVALID;
+    if (t->threads > (h->instances ? 1024 : 512))
+        return h->fail(SWARM_E_INVALID, "threads above " + std::to_string(h->instances ? 1024 : 512) + " per block");
     h->tuning = *t;
     h->fused = t->fused != 0;
     h->dropGraphs();
@@ -440,8 +442,10 @@ int swarm_autotune(SwarmHandle h, int steps, SwarmTuning* best) {
     if (!h->hasState) return h->fail(SWARM_E_STATE, "autotune needs a state (upload one first)");
     // the candidates: the fused step at several block shapes, and the per-phase kernels replayed from graphs
     std::vector<SwarmTuning> cands;
-    for (int threads : {0, 128, 256, 512})
+    for (int threads : {0, 128, 256, 512, 768, 1024}) {
+        if (threads > 512 && !h->instances) continue;   // wider blocks: the batched kernel only
         for (int bps : {0, 1, 2}) cands.push_back(SwarmTuning{1, threads, bps, 0.0f});
+    }
     cands.push_back(SwarmTuning{0, 0, 0, 0.0f});
     // snapshot of the state (and the metrics' running sums are not touched: the trials run with metrics off)
     float4* snap = nullptr;
