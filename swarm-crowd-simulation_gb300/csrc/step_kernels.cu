@@ -248,7 +248,23 @@ __device__ __forceinline__ void rankGatherItem(const StepArgs& A, int s) {
     const uint32_t me = A.sidTmp[s];
     if (me >= uint32_t(A.n)) { atomicOr(A.err, ERR_BOUNDS); return; }
     if (s >= nActive) { A.sid[s] = me; A.skey[s] = INACTIVE_CELL; return; }
+    // The agent's own records (and its e_goal lookup) do not depend on its rank: every load comes before the first
+    // store, so these overlap the cell lookup and the rank loop instead of following them
+    float4 p = A.stateIn[2 * size_t(me)];
+    const float4 v = A.stateIn[2 * size_t(me) + 1];
     const uint32_t c = A.key[me];
+    float2 prm = make_float2(0.0f, 0.0f);
+    if (kPerAgent) prm = A.aparam[me];
+    uint32_t inst = 0;
+    if (kB) inst = A.instAgent[me];
+    const bool bad = isnan(p.x);
+    if (bad) p = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+    float2 goal = make_float2(0.0f, 0.0f);
+    if constexpr (!std::is_void<Venue>::value) {
+        const VenueArgs& V = kB ? A.venueTable[inst] : A.V;
+        const f2 g = goalOf(A, Venue{A.P, V}, xyz(p), me);
+        goal = make_float2(g.x, g.y);
+    }
     if (c >= uint32_t(A.V.ncells)) { atomicOr(A.err, ERR_BOUNDS); return; }   // keys and counts out of step
     const uint2 cs = A.cells[c];
     if (uint64_t(cs.x) + cs.y > uint64_t(A.n)) { atomicOr(A.err, ERR_BOUNDS); return; }
@@ -257,17 +273,12 @@ __device__ __forceinline__ void rankGatherItem(const StepArgs& A, int s) {
     const uint32_t t = cs.x + r;
     A.sid[t] = me;
     A.skey[t] = c;
-    float4 p = A.stateIn[2 * size_t(me)];
-    if (isnan(p.x)) { p = make_float4(0.0f, 0.0f, 0.0f, 1.0f); A.stateIn[2 * size_t(me)] = p; }
+    if (bad) A.stateIn[2 * size_t(me)] = p;
     A.pos0[t] = p;
-    A.vel0[t] = A.stateIn[2 * size_t(me) + 1];
-    if (kPerAgent) A.prm[t] = A.aparam[me];
-    if (kB) A.instSlot[t] = A.instAgent[me];
-    if constexpr (!std::is_void<Venue>::value) {
-        const VenueArgs& V = kB ? A.venueTable[A.instAgent[me]] : A.V;
-        const f2 g = goalOf(A, Venue{A.P, V}, xyz(p), me);
-        A.goal[t] = make_float2(g.x, g.y);
-    }
+    A.vel0[t] = v;
+    if (kPerAgent) A.prm[t] = prm;
+    if (kB) A.instSlot[t] = inst;
+    if constexpr (!std::is_void<Venue>::value) A.goal[t] = goal;
 }
 
 template <bool kPerAgent, bool kB>
@@ -649,6 +660,25 @@ __device__ __forceinline__ void stamp(const StepArgs& A, int i) {
 // exactly when all `expected` blocks have arrived; each block waits for the flip of the value it saw (the scheme of
 // CUDA's cooperative groups grid sync). Release before the add, acquire on the poll.
 // Returns false (the same in every thread of the block) when the block must leave the kernel.
+// This block's share of an array of `bytes` bytes, prefetched into L2 by the copy engine (cp.async.bulk.prefetch: no
+// registers, no wait). The shares are whole 16-byte units of the array, the last one ends at the array's last full
+// 16-byte unit: every prefetched byte lies inside the array. A base that is not 16-byte aligned is skipped (a hint).
+constexpr size_t PREFETCH_STATE_MAX = size_t(16) << 20;
+constexpr uint32_t PREFETCH_CHUNK = 64u << 10;
+
+__device__ __forceinline__ void bulkPrefetchShare(const void* base, size_t bytes) {
+    if (!base || (reinterpret_cast<uintptr_t>(base) & 15u) != 0u) return;
+    const size_t units = bytes / 16u;
+    const size_t per = (units + gridDim.x - 1) / gridDim.x;
+    const size_t u0 = size_t(blockIdx.x) * per, u1 = u0 + per < units ? u0 + per : units;
+    const char* p = static_cast<const char*>(base);
+    for (size_t u = u0; u < u1;) {
+        const size_t take = u1 - u < PREFETCH_CHUNK / 16u ? u1 - u : PREFETCH_CHUNK / 16u;
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p + u * 16u), "r"(uint32_t(take * 16u)) : "memory");
+        u += take;
+    }
+}
+
 __device__ __forceinline__ bool gridBarrier(const StepArgs& A, unsigned expected) {
     __shared__ int leave;
     __syncthreads();
@@ -723,6 +753,15 @@ __global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREA
     const int T = int(blockDim.x);   // the tile of slots a block handles at a time
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
     stamp(A, 0);
+    // The per-agent records the gather phase reads in id order (state, keys, arrival ranks, radius and v0), prefetched
+    // into L2 by the copy engine while the scan and the scatter run: one bulk prefetch per array and block, each block
+    // a contiguous share. Only when the state is small beside L2 (a batch's state would evict its own working set).
+    if (threadIdx.x == 0 && size_t(n) * 32u <= PREFETCH_STATE_MAX) {
+        bulkPrefetchShare(A.stateIn, size_t(n) * 32u);
+        bulkPrefetchShare(A.key, size_t(n) * 4u);
+        bulkPrefetchShare(A.rank, size_t(n) * 4u);
+        if (kPerAgent) bulkPrefetchShare(A.aparam, size_t(n) * 8u);
+    }
     // The scan runs in tiles of A.scanTile cells (8 counts a thread, or 16 on sparse venues). Whoever counted the
     // keys -- the previous fused step's final pass, or the hash here -- also summed them per tile, so the scan starts
     // at its apply phase (the tile sums were zero before that counting: cleared below, or by the host).
