@@ -395,7 +395,8 @@ typedef struct SwarmAdjointStats {
      * predict's pair gather; 0 on the per-phase path */
     float ms_rev_final, ms_rev_sweeps, ms_rev_predict, ms_rev_gather;
 } SwarmAdjointStats;
-/* Grid venues, one instance, no drive table, wall_passes <= 5. The handle's state is left as it was. loss_out gets L;
+/* Grid venues without a floor grid (a floor grid brings in the step-up limit, whose blocked moves have no reverse),
+ * one instance, no drive table, wall_passes <= 5. The handle's state is left as it was. loss_out gets L;
  * dL_dv0 and dL_dr (n each, agent order) and dL_dtau (1) the gradient; stats (may be NULL) the pass times, measured
  * with events on the handle's stream. */
 int swarm_adjoint_run(SwarmHandle h, const SwarmLossSpec* loss, int steps, int ckpt_every, double* loss_out,

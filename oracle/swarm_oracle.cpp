@@ -733,8 +733,79 @@ struct GridVenue {
         }
         return grounded;
     }
-    // The step-up limit: a flat floor never blocks a move
-    bool limitStepUp(F3, F3&, F3&, float) const { return false; }
+    // The step-up limit over the floor heightfield (cpu_crowd_sim.cpp:566-591 limitStepUp, baked branch, with the
+    // floor grid in place of the baked column scan). The nearest-node floor is level treads with vertical risers, the
+    // reference's "exact venue": a floor in the window (f0 + tol, f0 + max] is never wall-steep, so only rule (a)
+    // blocks (stepUpBlocked :531-533): the floor under the move's end more than max_step_up above f0. No floor grid:
+    // flat, never blocked.
+    int stepUpWindow(F2 p, float f0) const {   // 0 level or lower, 1 in the window, 2 above it
+        const float h = floorHeight(p);
+        if (h > f0 + P.max_step_up) return 2;
+        return h > f0 + P.step_up_tol ? 1 : 0;
+    }
+    // the riser's normal: central differences of the floor over the neighbouring nodes, out of the higher column
+    F2 stepUpFace(F2 p) const {
+        const float fx = (p.x - V.wall_origin_x) * wallInvH + 0.5f, fy = (p.y - V.wall_origin_y) * wallInvH + 0.5f;
+        const int ix = std::clamp(int(std::floor(fx)), 0, V.wall_nx - 1), iy = std::clamp(int(std::floor(fy)), 0, V.wall_ny - 1);
+        const int x0 = std::max(ix - 1, 0), x1 = std::min(ix + 1, V.wall_nx - 1);
+        const int y0 = std::max(iy - 1, 0), y1 = std::min(iy + 1, V.wall_ny - 1);
+        const size_t row = size_t(iy) * size_t(V.wall_nx);
+        const float* H = V.floor_height;
+        const F2 g{H[row + size_t(x0)] - H[row + size_t(x1)],
+                   H[size_t(y0) * size_t(V.wall_nx) + size_t(ix)] - H[size_t(y1) * size_t(V.wall_nx) + size_t(ix)]};
+        return safeNormalize(g, P.safe_eps);
+    }
+    // cpu_crowd_sim.cpp:539-563 stepUpScan: only the end can block; the last allowed sample starts the bisection
+    float stepUpScan(F2 p0, F2 p1, float f0, F2& n) const {
+        n = {0.0f, 0.0f};
+        const float len = length(p1 - p0);
+        const int ns = std::clamp(int(std::ceil(len / P.step_up_sample)), 1, P.step_up_max_samples);
+        const F2 pe = mix(p0, p1, float(ns) / float(ns));
+        if (stepUpWindow(pe, f0) != 2) return 1.0f;
+        n = stepUpFace(pe);
+        int lastOk = 0;
+        for (int i = 1; i < ns; ++i)
+            if (stepUpWindow(mix(p0, p1, float(i) / float(ns)), f0) != 2) lastOk = i;
+        float lo = float(lastOk) / float(ns), hi = float(lastOk + 1) / float(ns);
+        for (int i = 0; i < P.step_up_bisections; ++i) {
+            const float t = 0.5f * (lo + hi);
+            const F2 q = mix(p0, p1, t);
+            if (stepUpWindow(q, f0) == 2) { hi = t; n = stepUpFace(q); }
+            else lo = t;
+        }
+        return lo;
+    }
+    // cpu_crowd_sim.cpp:566-591 limitStepUp: back to the riser, the rest along it (veering by the slide angles until
+    // one is allowed), the velocity into it removed, settled from the start-of-step height; radius r the agent's own
+    bool limitStepUp(F3 pOld, F3& np, F3& nv, float r) const {
+        if (!V.floor_height) return false;
+        float f0;
+        if (!floorUnderReach(pOld, pOld.z, P.step_up_floor_reach, r, f0)) f0 = pOld.z - P.step_up_floor_reach;
+        F2 n;
+        const float t = stepUpScan(xy(pOld), xy(np), f0, n);
+        if (t >= 1.0f) return false;
+        F2 q = mix(xy(pOld), xy(np), t);
+        const F2 rest = xy(np) - q;
+        const F2 tangent = rest - n * dot(rest, n);
+        const float lt = length(tangent);
+        if (lt > 0.0f) {
+            for (int k = 0; k < P.step_up_slide_tries; ++k) {
+                const F2 slide = q + tangent * P.step_up_slide[k][0] + n * (lt * P.step_up_slide[k][1]);
+                F2 n2;
+                if (stepUpScan(q, slide, f0, n2) >= 1.0f) { q = slide; break; }
+            }
+        }
+        const float vn = dot(xy(nv), n);
+        if (vn < 0.0f) setXY(nv, xy(nv) - n * vn);
+        float zFloor;
+        if (floorUnderReach(F3{q.x, q.y, pOld.z}, pOld.z, P.floor_settle_reach, r, zFloor)) {
+            np = F3{q.x, q.y, zFloor + r};
+            nv.z = 0.0f;
+        } else {
+            np = F3{q.x, q.y, std::min(np.z, pOld.z)};
+        }
+        return true;
+    }
     F3 calcGradient(F3 p) const {   // cpu_crowd_sim.cpp:312-318 over the grid's map
         const F3 kxyy{1.0f, -1.0f, -1.0f}, kyyx{-1.0f, -1.0f, 1.0f}, kyxy{-1.0f, 1.0f, -1.0f}, kxxx{1.0f, 1.0f, 1.0f};
         const float h = P.obstacle_grad_h;

@@ -156,6 +156,8 @@ extern "C" int swarm_adjoint_run(SwarmHandle h, const SwarmLossSpec* loss, int s
     if (!h || !loss || !loss_out || !dL_dv0 || !dL_dr || !dL_dtau) return SWARM_E_INVALID;
     if (loss->kind != SWARM_LOSS_NAV_DISTANCE) return h->fail(SWARM_E_INVALID, "unknown loss kind");
     if (h->V.kind != SWARM_VENUE_GRID || h->instances) return h->fail(SWARM_E_INVALID, "the adjoint runs on one grid venue");
+    // a floor grid brings the step-up limit into the forward step, whose blocked moves have no reverse here
+    if (h->dFloor) return h->fail(SWARM_E_INVALID, "the adjoint runs on flat venues (no floor grid: no step-up limit)");
     if (h->driveOn) return h->fail(SWARM_E_INVALID, "the adjoint follows e_goal: clear the drive table");
     if (!h->hasState) return h->fail(SWARM_E_STATE, "no state (upload one first)");
     if (steps < 1 || ckpt_every < 1) return h->fail(SWARM_E_INVALID, "steps and ckpt_every must be >= 1");

@@ -140,7 +140,80 @@ struct GridVenue {
         }
         return grounded;
     }
-    __device__ __forceinline__ bool limitStepUp(f3, f3&, f3&, float) const { return false; }   // flat floors never block
+    // The step-up limit over the floor heightfield (the reference's limitStepUp, cpu_crowd_sim.cpp:566-591, baked
+    // branch, with the floor grid in place of the baked column scan). The floor is the nearest node's height: level
+    // treads with vertical risers, the reference's "exact venue", where a floor in the window (f0 + tol, f0 + max]
+    // is never wall-steep and the window's top decides (rule (a), stepUpBlocked :531-533): a move is blocked when
+    // the floor under its end lies more than max_step_up above f0. No floor grid: a flat floor, never blocked.
+    __device__ __forceinline__ int stepUpWindow(f2 p, float f0) const {   // 0 level or lower, 1 in the window, 2 above
+        const float h = floorHeight(p);
+        if (h > f0 + P.max_step_up) return 2;
+        return h > f0 + P.step_up_tol ? 1 : 0;
+    }
+    // The riser's normal at p: the floor's central differences over the neighbouring nodes, pointing out of the
+    // higher column (the reference's face normal, the solid's gradient)
+    __device__ f2 stepUpFace(f2 p) const {
+        const float fx = (p.x - V.wox) * V.winv + 0.5f, fy = (p.y - V.woy) * V.winv + 0.5f;
+        const int ix = sclamp(int(floorf(fx)), 0, V.wnx - 1), iy = sclamp(int(floorf(fy)), 0, V.wny - 1);
+        const int x0 = smax(ix - 1, 0), x1 = smin(ix + 1, V.wnx - 1), y0 = smax(iy - 1, 0), y1 = smin(iy + 1, V.wny - 1);
+        const size_t row = size_t(iy) * size_t(V.wnx);
+        const f2 g{__ldg(V.floorH + row + size_t(x0)) - __ldg(V.floorH + row + size_t(x1)),
+                   __ldg(V.floorH + size_t(y0) * size_t(V.wnx) + size_t(ix)) - __ldg(V.floorH + size_t(y1) * size_t(V.wnx) + size_t(ix))};
+        return safeNormalize(g, P.safe_eps);
+    }
+    // stepUpScan (cpu_crowd_sim.cpp:539-563): only the end can block (rule (a)); the last allowed sample before it
+    // starts the bisection
+    __device__ float stepUpScan(f2 p0, f2 p1, float f0, f2& n) const {
+        n = f2{0.0f, 0.0f};
+        const float len = length(p1 - p0);
+        const int ns = sclamp(int(ceilf(len / P.step_up_sample)), 1, P.step_up_max_samples);
+        const f2 pe = mix(p0, p1, float(ns) / float(ns));
+        if (stepUpWindow(pe, f0) != 2) return 1.0f;
+        n = stepUpFace(pe);
+        int lastOk = 0;
+        for (int i = 1; i < ns; ++i)
+            if (stepUpWindow(mix(p0, p1, float(i) / float(ns)), f0) != 2) lastOk = i;
+        float lo = float(lastOk) / float(ns), hi = float(lastOk + 1) / float(ns);
+        for (int i = 0; i < P.step_up_bisections; ++i) {
+            const float t = 0.5f * (lo + hi);
+            const f2 q = mix(p0, p1, t);
+            if (stepUpWindow(q, f0) == 2) { hi = t; n = stepUpFace(q); }
+            else lo = t;
+        }
+        return lo;
+    }
+    // limitStepUp (cpu_crowd_sim.cpp:566-591): back to the riser, the rest of the move along it (veering off by the
+    // slide angles until a slide is allowed), the velocity into it removed, settled from the start-of-step height.
+    // Radius r: the agent's own (the floor contact of every grid-venue query).
+    __device__ bool limitStepUp(f3 pOld, f3& np, f3& nv, float r) const {
+        if (!V.floorH) return false;
+        float f0;
+        if (!floorUnderReach(pOld, pOld.z, P.step_up_floor_reach, r, f0)) f0 = pOld.z - P.step_up_floor_reach;
+        f2 n;
+        const float t = stepUpScan(xy(pOld), xy(np), f0, n);
+        if (t >= 1.0f) return false;
+        f2 q = mix(xy(pOld), xy(np), t);
+        const f2 rest = xy(np) - q;
+        const f2 tangent = rest - n * dot(rest, n);
+        const float lt = length(tangent);
+        if (lt > 0.0f) {
+            for (int k = 0; k < P.step_up_slide_tries; ++k) {
+                const f2 slide = q + tangent * P.step_up_slide[k][0] + n * (lt * P.step_up_slide[k][1]);
+                f2 n2;
+                if (stepUpScan(q, slide, f0, n2) >= 1.0f) { q = slide; break; }
+            }
+        }
+        const float vn = dot(xy(nv), n);
+        if (vn < 0.0f) setXY(nv, xy(nv) - n * vn);
+        float zFloor;
+        if (floorUnderReach(f3{q.x, q.y, pOld.z}, pOld.z, P.floor_settle_reach, r, zFloor)) {
+            np = f3{q.x, q.y, zFloor + r};
+            nv.z = 0.0f;
+        } else {
+            np = f3{q.x, q.y, smin(np.z, pOld.z)};
+        }
+        return true;
+    }
     __device__ f3 calcGradient(f3 p) const {
         const f3 kxyy{1.0f, -1.0f, -1.0f}, kyyx{-1.0f, -1.0f, 1.0f}, kyxy{-1.0f, 1.0f, -1.0f}, kxxx{1.0f, 1.0f, 1.0f};
         const float h = P.obstacle_grad_h;
