@@ -264,14 +264,14 @@ def bench_nav_field(venue, clearance=0.2):
             "equal_to_fast_marching": bool(np.array_equal(cpu.view(np.uint32), gpu.view(np.uint32)))}
 
 
-def adjoint_bytes(K, steps, ckpt):
-    """Algorithmic bytes per agent-step of the adjoint with checkpoints every `ckpt` steps: the forward work (2T - C
-    steps of B_step) plus the tape (written once, read once: per agent (2K + 6) float4 of positions, velocities,
+def adjoint_bytes(K, steps, ckpt, kept=1):
+    """Algorithmic bytes per agent-step of the adjoint with checkpoints every `ckpt` steps, the last `kept` segments
+    taped in the checkpoint pass: the forward work (2T - kept x C steps of B_step) plus the tape (written once, read once: per agent (2K + 6) float4 of positions, velocities,
     planes, the predict record and the sweeps' corrections, and 17 B of params, ids and contact bits) plus the
     reverse's own traffic (the state adjoint read and written, 64 B; each sweep's correction-sum adjoint written and
     read, 16 B; the per-slot adjoints of the final pass, predict and gather, 7 x 16 + 4 B)."""
     b_step = 336.0 + 48.0 * (K - 1)
-    forward = b_step * (2.0 * steps - min(ckpt, steps)) / steps
+    forward = b_step * (2.0 * steps - min(kept * ckpt, steps)) / steps
     tape = 2.0 * ((2 * K + 6) * 16.0 + 17.0)
     reverse = 64.0 + 16.0 * K + 7 * 16.0 + 4.0
     return forward + tape + reverse
@@ -280,8 +280,9 @@ def adjoint_bytes(K, steps, ckpt):
 def bench_adjoint(P, steps=400, ckpt=20):
     """The adjoint on the 16 384-agent hall (80 m x 70 m, two 4 m exits, 128 x 128 lattice at 0.5 m, seed 0): the
     loss L = dt * sum_t sum_i D(p_i(t)) of 400 steps from the spawn and its gradient with respect to every agent's
-    desired speed and radius and the relaxation time, checkpoints every 20 steps. Against the plain forward of the
-    same 400 steps. Both timed with CUDA events on the handle's stream (inputs larger than L2 are not at stake: the
+    desired speed and radius and the relaxation time, checkpoints every 20 steps (the default tape budget keeps the
+    last segments' tapes from the checkpoint pass; `pure_recompute`: budget 0, every other segment recomputed). Against
+    the plain forward of the same 400 steps. Both timed with CUDA events on the handle's stream (inputs larger than L2 are not at stake: the
     working set, 16 384 agents, is L2-resident on both sides)."""
     import torch
     import swarm_gb300
@@ -311,7 +312,8 @@ def bench_adjoint(P, steps=400, ckpt=20):
     out = {"workload": "hall 80x70 m, 2 exits of 4 m, 16384 agents (128x128 lattice, 0.5 m), 400 steps from the "
                        "spawn, loss dt*sum_t sum_i D(p_i(t)), gradient wrt v0_i, r_i, tau",
            "steps": steps, "agent_steps": active, "forward_ms_per_step": fwd_ms / steps}
-    for c in (ckpt, steps):
+    for c, budget in ((ckpt, None), (ckpt, 0), (steps, None)):
+        sim.set_adjoint_tape_budget(1 << 30 if budget is None else budget)
         sim.set_state(boids)
         sim.adjoint(steps, c)   # allocation and warm-up
         torch.cuda.synchronize()
@@ -321,15 +323,19 @@ def bench_adjoint(P, steps=400, ckpt=20):
         e1.synchronize()
         ms = e0.elapsed_time(e1)
         value = active / (ms * 1e-3)
-        b = adjoint_bytes(P.proj_iterations, steps, c)
-        rec = {"ckpt_every": c, "value": value, "unit": UNIT, "ms_per_step": ms / steps,
+        b = adjoint_bytes(P.proj_iterations, steps, c, st["kept_segments"])
+        rec = {"ckpt_every": c, "segments": st["segments"], "kept_segments": st["kept_segments"],
+               "tape_budget_bytes": 1 << 30 if budget is None else budget,
+               "value": value, "unit": UNIT, "ms_per_step": ms / steps,
                "ratio_vs_forward": ms / fwd_ms, "loss": L, "dL_dtau": gt,
                "bytes_per_agent_step": b, "fraction_of_hbm_roofline": value * b / (peaks()[0] * 1e9),
                "tape_bytes": st["tape_bytes"], "launches": st["launches"],
                "ms": {k: round(st[k], 3) for k in ("ms_checkpoint", "ms_recompute", "ms_reverse", "ms_rev_final",
                                                    "ms_rev_sweeps", "ms_rev_predict", "ms_rev_gather")}}
-        if c == ckpt:
+        if c == ckpt and budget is None:
             out.update(rec)
+        elif c == ckpt:
+            out["pure_recompute"] = rec
         else:
             out["full_tape"] = rec
     sim.close()

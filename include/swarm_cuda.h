@@ -174,8 +174,11 @@ int swarm_download_state_device(SwarmHandle h, float* d_boids, int n);
  * swarm_step: `steps` x CrowdSim::step (src/crowd_sim.cpp:316-412) = hash, key sort, cell ranges + gather,
  *   predict, K - 1 Jacobi sweeps, final pass; asynchronous on the handle's stream. */
 int swarm_step(SwarmHandle h, int steps);
-/* One call for callers holding the state in host memory: copies in_boids (n x 8 floats) into the device state,
- * runs `steps` steps, copies the result into out_boids and waits for it. Host buffers (pinned ones copy fastest). */
+/* One call for callers holding the state in host memory: in_boids (n x 8 floats) into the device state, `steps`
+ * steps, the result into out_boids, and waits for it. With pinned (page-locked, device-mapped) buffers and the fused
+ * step there are no copy operations: the first step's hash phase reads in_boids over the coherent host link, and the
+ * last step's kernel ends by writing its result into out_boids (the device state holds it too); otherwise one copy
+ * each way. in_boids may equal out_boids. */
 int swarm_step_host(SwarmHandle h, const float* in_boids, float* out_boids, int n, int steps);
 /* CpuCrowdSim::setProjectionIterations / CrowdSim::setProjectionIterations (src/crowd_sim.cpp:480-483). */
 int swarm_set_iterations(SwarmHandle h, int k);
@@ -394,6 +397,8 @@ typedef struct SwarmAdjointStats {
     /* the fused reverse's phases (block 0's clock, summed over the steps): final pass, sweeps, predict's own terms,
      * predict's pair gather; 0 on the per-phase path */
     float ms_rev_final, ms_rev_sweeps, ms_rev_predict, ms_rev_gather;
+    int32_t segments;             /* checkpointed segments */
+    int32_t kept_segments;        /* of them taped in the checkpoint pass (the others recomputed) */
 } SwarmAdjointStats;
 /* Grid venues without a floor grid (a floor grid brings in the step-up limit, whose blocked moves have no reverse),
  * one instance, no drive table, wall_passes <= 5. The handle's state is left as it was. loss_out gets L;
@@ -401,6 +406,11 @@ typedef struct SwarmAdjointStats {
  * with events on the handle's stream. */
 int swarm_adjoint_run(SwarmHandle h, const SwarmLossSpec* loss, int steps, int ckpt_every, double* loss_out,
                       float* dL_dv0, float* dL_dr, float* dL_dtau, SwarmAdjointStats* stats);
+/* Two-level checkpointing: the state is checkpointed every ckpt_every steps, and the checkpoint pass also keeps the
+ * full tapes of the last segments, as many as `bytes` of device memory hold beyond the one segment always kept; only
+ * the other segments are recomputed in the reverse sweep (the gradients are the same bits either way). Default 1 GiB;
+ * 0: every segment but the last is recomputed. No reference counterpart. */
+int swarm_adjoint_set_tape_budget(SwarmHandle h, int64_t bytes);
 /* Sets the relaxation time: tau_relax = tau and relax_step = exp(-dt / tau) (rounded once from double), the
  * parameterisation the adjoint differentiates. No reference counterpart (the reference fixes tau at build time). */
 int swarm_set_relaxation_time(SwarmHandle h, float tau);

@@ -376,8 +376,8 @@ __device__ __forceinline__ double blockSum(double v, double* warpSum) {
     if ((threadIdx.x & 31u) == 0) warpSum[threadIdx.x >> 5] = v;
     __syncthreads();
     double t = 0.0;
-    if (threadIdx.x == 0)
-        for (int w = 0; w < THREADS / 32; ++w) t += warpSum[w];
+    if (threadIdx.x == 0)   // the block's warps (THREADS: the most a block of this kernel has)
+        for (int w = 0; w < int(blockDim.x >> 5) && w < THREADS / 32; ++w) t += warpSum[w];
     __syncthreads();
     return t;
 }
@@ -928,10 +928,21 @@ void fusedConfig() {
 }
 }  // namespace
 
+// The fused reverse's block: the state's lane groups spread over every SM (threads = n x lanes / SMs rounded up to a
+// warp, 128..512), one block per SM; larger states take several slots per lane group
+int adjFusedThreads(int n) {
+    fusedConfig();
+    const int64_t lanes = int64_t(n) * ADJ_LANES;
+    int t = int((lanes + g_sms - 1) / g_sms);
+    t = (t + 31) / 32 * 32;
+    return std::max(128, std::min(t, ADJ_FUSED_THREADS));
+}
+
 int adjFusedBlocks(int n) {
     fusedConfig();
     const int resident = g_sms * g_perSm;
-    const int want = int((int64_t(n) * ADJ_LANES + ADJ_FUSED_THREADS - 1) / ADJ_FUSED_THREADS);
+    const int threads = adjFusedThreads(n);
+    const int want = int((int64_t(n) * ADJ_LANES + threads - 1) / threads);
     return std::max(1, std::min(want, resident));
 }
 
@@ -940,7 +951,7 @@ cudaError_t launch_adjoint_step_fused(AdjArgs& A, cudaStream_t st) {
     if (g_sms * g_perSm <= 0) return cudaErrorCooperativeLaunchTooLarge;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(unsigned(adjFusedBlocks(A.L.n)));
-    cfg.blockDim = dim3(unsigned(ADJ_FUSED_THREADS));
+    cfg.blockDim = dim3(unsigned(adjFusedThreads(A.L.n)));
     cfg.dynamicSmemBytes = 0;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];

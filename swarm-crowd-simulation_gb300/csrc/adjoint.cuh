@@ -74,5 +74,6 @@ void launch_adjoint_step(AdjArgs& A, cudaStream_t st, int64_t* launches);
 cudaError_t launch_adjoint_step_fused(AdjArgs& A, cudaStream_t st);
 // The fused reverse's grid size for n agents (the blocks that write loss partials)
 int adjFusedBlocks(int n);
+int adjFusedThreads(int n);
 
 }  // namespace swarm_gpu

@@ -28,6 +28,7 @@ inline size_t startStride(int ncells) { return (size_t(ncells) + 1 + 3) / 4 * 4;
 
 struct SwarmAdjoint {
     int n = 0, K = 0, ckpt = 0, nseg = 0, steps = 0, ncells = 0;
+    int keep = 1;                    // segments whose tapes the checkpoint pass keeps (the last ones): not recomputed
     double speedMax = 1.0;           // the venue's largest speed factor
     TapeLayout L{};
     std::vector<void*> allocs;
@@ -35,7 +36,7 @@ struct SwarmAdjoint {
     // forward
     float4* state[2] = {nullptr, nullptr};
     float4* ckptState = nullptr;     // nseg x 2n
-    float4* tapeF4 = nullptr;        // ckpt x L.f4PerStep()
+    float4* tapeF4 = nullptr;        // keep x ckpt x L.f4PerStep() (the tape arrays hold keep x ckpt steps)
     float2* tapePrm = nullptr;       // ckpt x n
     uint32_t* tapeSid = nullptr;     // ckpt x n
     uint32_t* tapeSkey = nullptr;    // ckpt x n
@@ -73,6 +74,9 @@ struct SwarmAdjoint {
     }
     size_t f4Step() const { return L.f4PerStep(); }
     float4* tape(int j) const { return tapeF4 + size_t(j) * f4Step(); }
+    // the first tape slot of segment seg: a kept segment its own run of slots, a recomputed one the first run (the
+    // kept segments are the last ones, reversed before any recomputed segment reuses their slots)
+    int tapeBase(int seg) const { return seg >= nseg - keep ? (seg - (nseg - keep)) * ckpt : 0; }
 };
 
 void swarm_adjoint_free(SwarmAdjoint* a) { delete a; }
@@ -85,13 +89,19 @@ bool ok(SwarmSim* h, cudaError_t e, const char* what) {
     return false;
 }
 
-SwarmAdjoint* makeAdjoint(SwarmSim* h, int n, int K, int ckpt, int nseg, int steps) {
+// Device bytes of one taped step: the float4 records, (r, v0), sorted ids and keys, run starts, contact bits
+size_t tapeStepBytes(int n, int K, int ncells) {
+    const TapeLayout L{n, K, std::max(K, 1)};
+    return L.f4PerStep() * 16 + size_t(n) * (8 + 4 + 4 + 1) + startStride(ncells) * 4;
+}
+
+SwarmAdjoint* makeAdjoint(SwarmSim* h, int n, int K, int ckpt, int nseg, int steps, int keep) {
     SwarmAdjoint* a = new (std::nothrow) SwarmAdjoint();
     if (!a) return nullptr;
-    a->n = n; a->K = K; a->ckpt = ckpt; a->nseg = nseg; a->steps = steps; a->ncells = h->ncells;
+    a->n = n; a->K = K; a->ckpt = ckpt; a->nseg = nseg; a->steps = steps; a->ncells = h->ncells; a->keep = keep;
     a->speedMax = h->speedMax;
     a->L = TapeLayout{n, K, std::max(K, 1)};
-    const size_t N = size_t(n), C = size_t(ckpt), NC = size_t(h->ncells) + 1;
+    const size_t N = size_t(n), C = size_t(ckpt) * size_t(keep), NC = size_t(h->ncells) + 1;
     a->lossBlocks = std::max(swarm_gpu::adjFinalBlocks(n), swarm_gpu::adjFusedBlocks(n));
     const bool good =
         a->alloc(&a->state[0], 2 * N) && a->alloc(&a->state[1], 2 * N) && a->alloc(&a->ckptState, size_t(nseg) * 2 * N) &&
@@ -151,6 +161,12 @@ StepArgs forwardArgs(const SwarmSim* h, const SwarmAdjoint* a, int in, int j) {
 
 }  // namespace
 
+extern "C" int swarm_adjoint_set_tape_budget(SwarmHandle h, int64_t bytes) {
+    if (!h || bytes < 0) return SWARM_E_INVALID;
+    h->adjTapeBudget = bytes;
+    return SWARM_OK;
+}
+
 extern "C" int swarm_adjoint_run(SwarmHandle h, const SwarmLossSpec* loss, int steps, int ckpt_every, double* loss_out,
                                  float* dL_dv0, float* dL_dr, float* dL_dtau, SwarmAdjointStats* stats) {
     if (!h || !loss || !loss_out || !dL_dv0 || !dL_dr || !dL_dtau) return SWARM_E_INVALID;
@@ -164,10 +180,14 @@ extern "C" int swarm_adjoint_run(SwarmHandle h, const SwarmLossSpec* loss, int s
     const int K = h->P.proj_iterations;
     if (h->P.wall_passes < 0 || h->P.wall_passes > 5 || K > 64) return h->fail(SWARM_E_INVALID, "wall_passes <= 5 and K <= 64");
     const int n = h->n, C = std::min(ckpt_every, steps), nseg = (steps + C - 1) / C;
+    // the last segment's tape always, and as many earlier segments' tapes as the tape budget holds
+    const int64_t segBytes = int64_t(tapeStepBytes(n, K, h->ncells)) * C;
+    const int keep = 1 + int(std::min<int64_t>(nseg - 1, h->adjTapeBudget / std::max<int64_t>(segBytes, 1)));
     SwarmAdjoint*& a = h->adjoint;
-    if (!a || a->n != n || a->K != K || a->ckpt != C || a->nseg != nseg || a->steps != steps || a->ncells != h->ncells) {
+    if (!a || a->n != n || a->K != K || a->ckpt != C || a->nseg != nseg || a->steps != steps || a->ncells != h->ncells ||
+        a->keep != keep) {
         delete a;
-        a = makeAdjoint(h, n, K, C, nseg, steps);
+        a = makeAdjoint(h, n, K, C, nseg, steps, keep);
         if (!a) return h->fail(SWARM_E_OOM, "adjoint buffers (tape of " + std::to_string(C) + " steps)");
     }
     cudaStream_t st = h->stream;
@@ -188,7 +208,7 @@ extern "C" int swarm_adjoint_run(SwarmHandle h, const SwarmLossSpec* loss, int s
                 ok(h, cudaMemsetAsync(a->err, 0, 4, st), "adjoint clear") &&
                 ok(h, cudaMemsetAsync(a->lossPart, 0, size_t(steps) * size_t(a->lossBlocks) * 8, st), "adjoint clear") &&
                 ok(h, cudaMemsetAsync(a->stamps, 0, 8 * 8, st), "adjoint clear");
-    // the checkpoint pass; the last segment is taped here, not recomputed
+    // the checkpoint pass; the kept segments (the last `keep`) are taped here, not recomputed
     int in = 0;
     std::vector<float4*> q(size_t(L.Kq)), corr(size_t(K) + 1, nullptr);
     // Fused steps run in chains, as the handle's stepping does: each final pass counts the next state's keys
@@ -222,13 +242,13 @@ extern "C" int swarm_adjoint_run(SwarmHandle h, const SwarmLossSpec* loss, int s
     };
     for (int seg = 0; good && seg < nseg; ++seg) {
         good = ok(h, cudaMemcpyAsync(a->ckptState + size_t(seg) * 2 * N, a->state[in], N * 32, cudaMemcpyDeviceToDevice, st), "checkpoint");
-        if (seg == nseg - 1) {
-            const int cnt = steps - seg * C;
+        if (seg >= nseg - a->keep) {   // a kept segment: taped now (one chain through the kept segments)
+            const int cnt = std::min(C, steps - seg * C), base = a->tapeBase(seg);
             for (int j = 0; good && j < cnt; ++j) {
-                good = tapedStep(j, j == cnt - 1);
+                good = tapedStep(base + j, seg == nseg - 1 && j == cnt - 1);
                 in ^= 1;
             }
-            break;
+            continue;
         }
         for (int j = 0; good && j < C; ++j) {
             StepArgs A = forwardArgs(h, a, in, 0);
@@ -251,7 +271,7 @@ extern "C" int swarm_adjoint_run(SwarmHandle h, const SwarmLossSpec* loss, int s
     for (int seg = nseg - 1; good && seg >= 0; --seg) {
         const int t0 = seg * C, cnt = std::min(C, steps - t0);
         if (stats) cudaEventRecord(ev[2 + 3 * size_t(seg)], st);
-        if (seg < nseg - 1) {   // recompute the segment from its checkpoint, taped
+        if (seg < nseg - a->keep) {   // recompute the segment from its checkpoint, taped (tape slots from 0)
             good = ok(h, cudaMemcpyAsync(a->state[0], a->ckptState + size_t(seg) * 2 * N, N * 32, cudaMemcpyDeviceToDevice, st), "restore");
             in = 0;
             for (int j = 0; good && j < cnt; ++j) {
@@ -260,13 +280,14 @@ extern "C" int swarm_adjoint_run(SwarmHandle h, const SwarmLossSpec* loss, int s
             }
         }
         if (stats) cudaEventRecord(ev[3 + 3 * size_t(seg)], st);
+        const int base = a->tapeBase(seg);
         for (int j = cnt - 1; good && j >= 0; --j) {
             AdjArgs R{};
-            const StepArgs A = forwardArgs(h, a, 0, j);
+            const StepArgs A = forwardArgs(h, a, 0, base + j);
             R.P = A.P;
             R.V = A.V;
             R.L = L;
-            R.f4 = a->tape(j);
+            R.f4 = a->tape(base + j);
             R.prm = A.prm;
             R.sid = A.sid;
             R.skey = A.skey;
@@ -322,6 +343,8 @@ extern "C" int swarm_adjoint_run(SwarmHandle h, const SwarmLossSpec* loss, int s
         stats->ms_total = ms;
         stats->launches = launches;
         stats->tape_bytes = a->bytes;
+        stats->segments = nseg;
+        stats->kept_segments = a->keep;
         stats->ms_rev_final = float(double(stampNs[0]) * 1e-6);
         stats->ms_rev_sweeps = float(double(stampNs[1]) * 1e-6);
         stats->ms_rev_predict = float(double(stampNs[2]) * 1e-6);

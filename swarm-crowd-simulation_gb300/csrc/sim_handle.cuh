@@ -48,6 +48,10 @@ struct SwarmSim {
     SwarmTuning tuning{1, 0, 0, 0.0f};   // the launch configuration (swarm_autotune / swarm_set_tuning)
     bool counted = false;       // the counts hold the current state's keys (a fused step's final pass counted them)
     int countedTile = 0;        // the scan tile (cells) of the tile sums that counting left
+    // swarm_step_host on the fused path with pinned buffers: the caller's input and output as the device sees them
+    // (the first step reads hostIn, the last step copies its result to hostOut; null outside that call)
+    const float4* hostIn = nullptr;
+    float4* hostOut = nullptr;
     // safety metrics (swarm_metrics_enable)
     int metricRes = 0;
     uint32_t metricStep = 0;
@@ -80,6 +84,7 @@ struct SwarmSim {
     int64_t launches = 0;
     std::vector<void*> allocs;
     SwarmAdjoint* adjoint = nullptr;
+    int64_t adjTapeBudget = int64_t(1) << 30;   // device bytes the adjoint may spend on kept segment tapes
 
     swarm_gpu::StepArgs args(int in) const;
     int fail(int code, const std::string& msg) { err = msg; return code; }

@@ -47,6 +47,11 @@ struct StepArgs {
     // agent order: the GpuBoid state (position, velocity interleaved: 2 float4 per agent); ping-pong by step
     float4* stateIn;
     float4* stateOut;
+    // Host buffers the fused step reads and writes in place of copies (the caller's pinned GpuBoid arrays, as the
+    // device sees them over the coherent host link; null otherwise): the hash phase loads the state from hostIn into
+    // stateIn; after the final pass (one more grid barrier) the blocks copy stateOut to hostOut in order
+    const float4* hostIn;
+    float4* hostOut;
     const float2* aparam;   // (radius, v0) per agent
     const float2* drive;    // forced e_goal per agent, or null
     uint8_t* contacts;      // ContactBits per agent (the last step's)

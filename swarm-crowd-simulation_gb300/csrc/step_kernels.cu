@@ -72,8 +72,16 @@ __device__ __forceinline__ void hashItem(const StepArgs& A, int i) {
     const bool valid = i < A.n;
     uint32_t key = 0;
     if (valid) {
-        float4 p = A.stateIn[2 * size_t(i)];
-        if (isnan(p.x)) { p = make_float4(0.0f, 0.0f, 0.0f, 1.0f); A.stateIn[2 * size_t(i)] = p; }
+        float4 p;
+        if (A.hostIn) {   // the state straight from the caller's host buffer: into the device half this step reads
+            p = A.hostIn[2 * size_t(i)];
+            A.stateIn[2 * size_t(i) + 1] = A.hostIn[2 * size_t(i) + 1];
+            if (isnan(p.x)) p = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+            A.stateIn[2 * size_t(i)] = p;
+        } else {
+            p = A.stateIn[2 * size_t(i)];
+            if (isnan(p.x)) { p = make_float4(0.0f, 0.0f, 0.0f, 1.0f); A.stateIn[2 * size_t(i)] = p; }
+        }
         key = p.w == 0.0f ? INACTIVE_CELL : cellID(venueOfAgent<kB>(A, uint32_t(i)), p);
     }
     countKey<kTiles>(A, uint32_t(valid ? i : 0), key, valid);
@@ -757,7 +765,7 @@ __global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREA
     // into L2 by the copy engine while the scan and the scatter run: one bulk prefetch per array and block, each block
     // a contiguous share. Only when the state is small beside L2 (a batch's state would evict its own working set).
     if (threadIdx.x == 0 && size_t(n) * 32u <= PREFETCH_STATE_MAX) {
-        bulkPrefetchShare(A.stateIn, size_t(n) * 32u);
+        if (!A.hostIn) bulkPrefetchShare(A.stateIn, size_t(n) * 32u);   // (else the hash phase writes it)
         bulkPrefetchShare(A.key, size_t(n) * 4u);
         bulkPrefetchShare(A.rank, size_t(n) * 4u);
         if (kPerAgent) bulkPrefetchShare(A.aparam, size_t(n) * 8u);
@@ -876,6 +884,12 @@ __global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREA
         else if (s < n) finalInactive(A, s);
         // the next step's hash, counted here (all lanes of the warp together)
         if (A.hashNext) countKey<true>(A, s < n ? A.sid[s] : 0u, nextKey, s < n);
+    }
+    // The caller's host buffer: the finished state in agent order, copied in order after the last barrier (coalesced
+    // 16-byte stores over the host link; the final pass's own writes go to agents in slot order, scattered)
+    if (A.hostOut) {
+        if (!gridBarrier(A, gridDim.x)) return;
+        for (size_t k = size_t(tid); k < 2 * size_t(n); k += size_t(stride)) A.hostOut[k] = A.stateOut[k];
     }
     if (A.stamps) {   // the end: the last block out records it
         __syncthreads();

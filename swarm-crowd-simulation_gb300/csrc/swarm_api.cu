@@ -537,6 +537,9 @@ static int stepImpl(SwarmHandle h, int steps, bool countLast) {
                 return SWARM_E_CUDA;
             A.hashed = h->counted ? 1 : 0;
             A.hashNext = (countLast || s + 1 < steps) ? 1 : 0;
+            A.hostIn = s == 0 ? h->hostIn : nullptr;
+            A.hostOut = s + 1 == steps ? h->hostOut : nullptr;
+            if (A.hostIn && A.hashed) return h->fail(SWARM_E_STATE, "a host input needs the hash phase (counts left over)");
             if (!cudaOk(h, swarm_gpu::launch_step_fused(A, h->stream), "fused step launch")) return SWARM_E_CUDA;
             h->barrierExtra = 0;
             h->counted = A.hashNext != 0;
@@ -691,6 +694,29 @@ int swarm_step_host(SwarmHandle h, const float* in_boids, float* out_boids, int 
     h->n = n;
     h->hasState = true;
     const size_t bytes = size_t(n) * 32;
+    // Pinned host buffers on the fused path: no copy operations. The first step's hash phase reads the input over the
+    // coherent host link (into the device half it steps from), and the last step ends with its blocks copying the
+    // result, in order, into the output. Pageable buffers, or the per-phase path: a copy each way.
+    const float4* dIn = nullptr;
+    float4* dOut = nullptr;
+    if (h->fused && steps > 0) {
+        cudaPointerAttributes ai{}, ao{};
+        if (cudaPointerGetAttributes(&ai, in_boids) == cudaSuccess && ai.type == cudaMemoryTypeHost && ai.devicePointer &&
+            cudaPointerGetAttributes(&ao, out_boids) == cudaSuccess && ao.type == cudaMemoryTypeHost && ao.devicePointer) {
+            dIn = static_cast<const float4*>(ai.devicePointer);
+            dOut = static_cast<float4*>(ao.devicePointer);
+        }
+        cudaGetLastError();   // (an unregistered pointer is not an error of this handle)
+    }
+    if (dIn && dOut) {
+        h->hostIn = dIn;
+        h->hostOut = dOut;
+        const int rc = stepImpl(h, steps, false);
+        h->hostIn = nullptr;
+        h->hostOut = nullptr;
+        if (rc != SWARM_OK) return rc;
+        return cudaOk(h, cudaStreamSynchronize(h->stream), "step sync") ? SWARM_OK : SWARM_E_CUDA;
+    }
     // the read half only: the final pass writes every agent of the other half
     if (!cudaOk(h, cudaMemcpyAsync(h->state[h->readIdx], in_boids, bytes, cudaMemcpyHostToDevice, h->stream), "upload")) return SWARM_E_CUDA;
     const int rc = stepImpl(h, steps, false);

@@ -73,6 +73,7 @@ def lib():
             "swarm_adjoint_run": [H, C.POINTER(SwarmLossSpec), C.c_int, C.c_int, C.POINTER(C.c_double),
                                   C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                   C.POINTER(SwarmAdjointStats)],
+            "swarm_adjoint_set_tape_budget": [H, C.c_int64],
             "swarm_set_relaxation_time": [H, C.c_float],
             "swarm_run_evacuation": [H, C.c_int, C.c_void_p, C.POINTER(SwarmEvacuation)],
             "swarm_snapshot_write": [C.c_char_p, C.POINTER(C.c_float), C.c_int],
@@ -317,6 +318,11 @@ class CrowdSim:
     def set_relaxation_time(self, tau):
         """tau_relax = tau, relax_step = exp(-dt / tau)."""
         self._ck(lib().swarm_set_relaxation_time(self._h, float(tau)), "set_relaxation_time")
+
+    def set_adjoint_tape_budget(self, nbytes):
+        """Device bytes the adjoint may keep as segment tapes beyond the last segment's (default 1 GiB; 0: recompute
+        every other segment); the gradients are the same either way."""
+        self._ck(lib().swarm_adjoint_set_tape_budget(self._h, int(nbytes)), "adjoint_set_tape_budget")
 
     def adjoint(self, steps, ckpt_every=20, stats=False):
         """The evacuation loss L = dt * sum_t sum_i D(p_i(t)) of `steps` steps from the current state (left as it is)

@@ -93,7 +93,8 @@ class SwarmLossSpec(C.Structure):
 class SwarmAdjointStats(C.Structure):
     _fields_ = [("ms_checkpoint", _f), ("ms_recompute", _f), ("ms_reverse", _f), ("ms_total", _f),
                 ("launches", C.c_int64), ("tape_bytes", C.c_int64),
-                ("ms_rev_final", _f), ("ms_rev_sweeps", _f), ("ms_rev_predict", _f), ("ms_rev_gather", _f)]
+                ("ms_rev_final", _f), ("ms_rev_sweeps", _f), ("ms_rev_predict", _f), ("ms_rev_gather", _f),
+                ("segments", C.c_int32), ("kept_segments", C.c_int32)]
 
 
 def fptr(a):

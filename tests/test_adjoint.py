@@ -93,6 +93,25 @@ def test_adjoint_checkpoint_interval_and_repeatability(small):
         assert np.array_equal(gv, gv1) and np.array_equal(gr, gr1)
 
 
+def test_adjoint_kept_tapes_give_the_same_gradient(small):
+    """Two-level checkpointing: the checkpoint pass keeps the tapes of the last segments that the tape budget holds;
+    every budget gives the same bits as recomputing every segment but the last."""
+    P, venue, b, r, v0 = small
+    sim, _ = _gpu(P, venue, b, r, v0, 40, 7)
+    K = P.proj_iterations
+    ncells = venue.struct.grid_res_x * venue.struct.grid_res_y
+    step_bytes = (6 + max(K, 1) + K) * sim.n * 16 + sim.n * 17 + (ncells + 1 + 3) // 4 * 4 * 4
+    runs = []
+    for budget in (0, 2 * 7 * step_bytes, 1 << 30):
+        sim.set_adjoint_tape_budget(budget)
+        runs.append(sim.adjoint(40, 7, stats=True))
+    assert [st["kept_segments"] for *_, st in runs] == [1, 3, 6] and runs[0][4]["segments"] == 6
+    L0, gv0, gr0, gt0, _ = runs[0]
+    for L, gv, gr, gt, _ in runs[1:]:
+        assert L == L0 and gt == gt0
+        assert np.array_equal(gv, gv0) and np.array_equal(gr, gr0)
+
+
 def test_adjoint_terrace_4096(built):
     import swarm_gb300
     from swarm_gb300 import venues as V
