@@ -367,6 +367,19 @@ def cpu_baseline(budget_s=12.0, max_steps=400):
                       f"{t_total:.1f} s of wall clock on {threads} OpenMP threads"}
 
 
+def replica_totals(dist, device, ms, agent_steps):
+    """The whole job over the ranks (replicas): the slowest rank's time and every rank's agent-steps. `dist` is
+    torch.distributed (None: one process); `device` holds the reduction tensors ("cuda" for NCCL, "cpu" for gloo)."""
+    if dist is None:
+        return float(ms), float(agent_steps)
+    import torch
+    t = torch.tensor([float(ms)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    a = torch.tensor([float(agent_steps)], device=device, dtype=torch.float64)
+    dist.all_reduce(a)
+    return float(t.item()), float(a.item())
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -480,16 +493,7 @@ def main():
         rep.step(1)
     rep.close()
 
-    t_max = total_ms
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-        a = torch.tensor([agent_steps], device="cuda", dtype=torch.float64)
-        dist.all_reduce(a)
-        agent_steps_all = float(a.item())
-    else:
-        agent_steps_all = float(agent_steps)
+    t_max, agent_steps_all = replica_totals(dist, "cuda", total_ms, agent_steps)
     value = agent_steps_all / (t_max * 1e-3)
 
     # roofline of the dominant kernel, from the library's events over the timed steps. The default path runs each
@@ -554,8 +558,8 @@ def main():
     for _ in range(args.steps):
         e2e_sim.step_host(cur_in.data_ptr(), cur_out.data_ptr(), n, 1)
         cur_in, cur_out = cur_out, cur_in
-    e2e_s = time.perf_counter() - t0
-    e2e_value = agent_steps_all / (e2e_s * (world if False else 1)) if world == 1 else agent_steps_all / e2e_s
+    e2e_ms, _ = replica_totals(dist, "cuda", (time.perf_counter() - t0) * 1e3, 0)   # the slowest rank's wall clock
+    e2e_value = agent_steps_all / (e2e_ms * 1e-3)
 
     line = None
     if rank == 0:
