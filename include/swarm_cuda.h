@@ -292,6 +292,44 @@ int swarm_nav_field_cpu(int nx, int ny, double h, const uint8_t* kind, const flo
 /* The solver the venue builders use from now on (process-wide); returns the previous one, or SWARM_E_INVALID. */
 int swarm_set_nav_solver(int solver);
 
+/* ---- queue-aware exit choice (the reference's ExitChoice::QueueAware: physics.comp PHYSICS_PASS 0,
+ * nav::choiceStep, src/exit_choice.cpp:580-790; constants include/swarm/sim_params.hpp:395-427) ----
+ * Every agent holds an assigned exit and steers on that exit's own distance field; it estimates its time to leave
+ * through each candidate exit e of its cell, E_e = d_e / V_FREE + A_e x 60 / (w_e J) seconds (d_e the cell's walking
+ * distance to e, A_e the agents assigned to e in nearer 0.5 m distance bins, w_e the clear width, J = 83.6 persons per
+ * metre per minute). Every 3 s of simulated time all agents re-evaluate on the same counts: an agent may switch to its
+ * best candidate if that gains more than max(10 % of E_current, 5 s), and per exit at most max(1, 10 % of its
+ * assigned agents) switch, the largest gains first (1 s gain bins). An agent whose exit is no candidate of its cell
+ * takes the best candidate at once. Integer histograms and counts throughout: deterministic.
+ * Exit types of the candidate rule: every cell's candidates hold its 2 nearest exits of type 0 (avenues: a bowl's
+ * vomitories) and its nearest of type 1 (doors: a bowl's perimeter exits, a hall's doors), then the nearest others. */
+#define SWARM_CHOICE_MAX_EXITS 63
+#define SWARM_CHOICE_MAX_CANDIDATES 24
+#define SWARM_CHOICE_EMPTY 0xFF          /* an empty candidate slot */
+#define SWARM_CHOICE_NONE 0xFFFFFFFFu    /* an agent with no exit assigned yet */
+typedef struct SwarmExitChoiceSpec {
+    int32_t n_exits;              /* 1 .. SWARM_CHOICE_MAX_EXITS */
+    int32_t candidates;           /* per cell, 1 .. SWARM_CHOICE_MAX_CANDIDATES */
+    const float* fields;          /* n_exits x nav_nx x nav_ny: each exit's walking distance on the venue's nav grid */
+    const float* width_m;         /* n_exits: clear widths, metres */
+    const uint8_t* type;          /* n_exits: 0 avenue, 1 door */
+} SwarmExitChoiceSpec;
+/* Per-exit distance fields of the generated venues, solved as their nav_dist (same walls, speeds, solver) with one
+ * exit's sources each (the other exits' sources blocked); fields: n_exits x nav_nx x nav_ny floats, width_m and type:
+ * n_exits each (halls: n_doors doors of type 1; bowls: the sectors' vomitories, type 0, then the perimeter exits). */
+int swarm_hall_exit_fields(const SwarmHallSpec* spec, const SwarmVenue* venue, float* fields, float* width_m, uint8_t* type);
+int swarm_bowl_exit_fields(const SwarmBowlSpec* spec, const SwarmVenue* venue, float* fields, float* width_m, uint8_t* type);
+/* The candidate table on the venue's hash cells (grid_res_x x grid_res_y cells, `candidates` slots each): per cell the
+ * reachable nav node nearest its centre stands for it; the slots hold exits (SWARM_CHOICE_EMPTY: none) and their
+ * distances there, ascending (ties: the lower exit id). Host code; swarm_set_exit_choice builds the same table. */
+int swarm_exit_choice_table(const SwarmVenue* venue, const SwarmExitChoiceSpec* spec, uint8_t* exits, float* dists);
+/* Queue-aware exit choice on (spec) or off (NULL: e_goal from the venue's nearest-exit field, the default). Grid venues,
+ * one instance; the handle's choice restarts (no exit assigned, step 0) here and at every state upload. */
+int swarm_set_exit_choice(SwarmHandle h, const SwarmExitChoiceSpec* spec);
+/* The assigned exit of each agent (SWARM_CHOICE_NONE: none yet) and the counters since the choice restarted:
+ * evaluations, eligible agents, switches, forced choices (4 values; either pointer may be NULL). */
+int swarm_get_exit_choice(SwarmHandle h, uint32_t* assigned, int n, uint32_t* counters);
+
 /* One agent per seat (sectors x rows x seats, by sector, row, seat) at the seat centre jittered U(-jitter, jitter)
  * per axis, on the floor (z = floor + radius), at rest; radius and desired speed as swarm_spawn_lattice. */
 int swarm_spawn_bowl(const SwarmBowlSpec* spec, float jitter, uint64_t seed, float r_lo, float r_hi, float v_mean,

@@ -36,7 +36,8 @@ def lib():
         L.oracle_last_error.restype = C.c_char_p
         for name in ["oracle_destroy", "oracle_set_state", "oracle_set_agent_params", "oracle_set_iterations",
                      "oracle_set_threads", "oracle_set_drive_table", "oracle_step", "oracle_get_state",
-                     "oracle_get_grid", "oracle_get_cells", "oracle_get_contacts"]:
+                     "oracle_get_grid", "oracle_get_cells", "oracle_get_contacts", "oracle_set_exit_choice",
+                     "oracle_get_exit_choice"]:
             getattr(L, name).restype = C.c_int
         L.oracle_destroy.argtypes = [V]
         L.oracle_set_state.argtypes = [V, V, C.c_int]
@@ -49,6 +50,8 @@ def lib():
         L.oracle_get_grid.argtypes = [V, V, V]
         L.oracle_get_cells.argtypes = [V, V, C.c_int]
         L.oracle_get_contacts.argtypes = [V, V]
+        L.oracle_set_exit_choice.argtypes = [V, C.c_int, C.c_int, V, V, V, V]
+        L.oracle_get_exit_choice.argtypes = [V, V, V]
         L.grad_eval.restype = C.c_int
         L.grad_eval.argtypes = [C.c_int, V, V, V, C.c_int, V, V, C.c_double, C.c_int, C.c_int, C.c_int, V, V, V, V, V, V, V]
         L.grad_last_error.restype = C.c_char_p
@@ -98,6 +101,26 @@ class OracleSim:
             return
         d = np.ascontiguousarray(dirs, dtype=np.float32).reshape(-1, 2)
         lib().oracle_set_drive_table(self._h, _p(d), d.shape[0])
+
+    def set_exit_choice(self, fields, inv_cap, table_exits, table_dists):
+        """The queue-aware exit choice: per-exit fields (n_exits, nav nodes), seconds per queued agent per exit, and
+        the candidate table (cells, K) of exits and distances (as the library builds it); fields None: off."""
+        if fields is None:
+            lib().oracle_set_exit_choice(self._h, 0, 0, None, None, None, None)
+            return
+        f = np.ascontiguousarray(fields, dtype=np.float32)
+        ic = np.ascontiguousarray(inv_cap, dtype=np.float32)
+        te = np.ascontiguousarray(table_exits, dtype=np.uint8)
+        td = np.ascontiguousarray(table_dists, dtype=np.float32)
+        self._choice = (f, ic, te, td)
+        lib().oracle_set_exit_choice(self._h, int(ic.shape[0]), int(te.shape[1]), _p(f), _p(ic), _p(te), _p(td))
+
+    def exit_choice(self):
+        """(assigned exit per agent, counters: evaluations, eligible, switches, forced)"""
+        a = np.empty(self.n, np.uint32)
+        c = np.empty(4, np.uint32)
+        lib().oracle_get_exit_choice(self._h, _p(a), _p(c))
+        return a, c
 
     def step(self, steps=1):
         assert lib().oracle_step(self._h, int(steps)) == 0, lib().oracle_last_error().decode()

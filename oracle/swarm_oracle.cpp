@@ -37,6 +37,13 @@ namespace {
 constexpr uint32_t INACTIVE_CELL = 0xFFFFFFFFu;
 constexpr float PLANE_WALL = 1.0f, PLANE_GROUNDED = 2.0f;
 constexpr float WALL_NONE = 1e9f;
+// the queue-aware exit choice's constants (include/swarm/sim_params.hpp:412-427, include/swarm/exit_choice.hpp:121-137;
+// the queue-ahead bins 0.5 m on SI venues)
+constexpr double CHOICE_T_S = 3.0;
+constexpr float CHOICE_REL_MARGIN = 0.10f, CHOICE_ABS_MARGIN_S = 5.0f, CHOICE_SWITCH_SHARE = 0.10f;
+constexpr uint32_t CHOICE_MIN_SWITCHES = 1;
+constexpr int CHOICE_GAIN_BINS = 256, CHOICE_AHEAD_BINS = 1024, CHOICE_STRIDE = 64;
+constexpr float CHOICE_S_PER_M = float(1.0 / double(1.34f));   // 1 / V_FREE_M_S
 
 // ContactBits (include/swarm/cpu_crowd_sim.hpp:52-61)
 enum : uint8_t { C_EXIT = 1, C_FENCE_CCD = 2, C_FENCE = 4, C_FLOOR = 8, C_WALL = 16, C_AGENT = 32, C_SWEEP = 64, C_STEP_UP = 128 };
@@ -625,14 +632,15 @@ struct GridVenue {
     // The 3D distance of the obstacle avoidance and the static sweep: the walls and the floor
     float map(F3 p) const { return std::min(wallDist(xy(p)), p.z - floorHeight(xy(p))); }
 
-    // e_goal: -grad D / |grad D| of the bilinear interpolant of the distance field
-    F2 goal(F3 p) const {
+    // e_goal: -grad D / |grad D| of the bilinear interpolant of the distance field (the nearest exit's, or D = one
+    // exit's own field on the same grid: the queue-aware exit choice)
+    F2 goal(F3 p) const { return goalIn(V.nav_dist, p); }
+    F2 goalIn(const float* D, F3 p) const {
         float fx = (p.x - V.nav_origin_x) * navInvH, fy = (p.y - V.nav_origin_y) * navInvH;
         fx = std::clamp(fx, 0.0f, float(V.nav_nx - 1));
         fy = std::clamp(fy, 0.0f, float(V.nav_ny - 1));
         int ix = std::min(int(std::floor(fx)), V.nav_nx - 2), iy = std::min(int(std::floor(fy)), V.nav_ny - 2);
         float wx = fx - float(ix), wy = fy - float(iy);
-        const float* D = V.nav_dist;
         size_t r0 = size_t(iy) * size_t(V.nav_nx) + size_t(ix), r1 = r0 + size_t(V.nav_nx);
         float d00 = D[r0], d10 = D[r0 + 1], d01 = D[r1], d11 = D[r1 + 1];
         F2 g{mix(d10 - d00, d11 - d01, wy), mix(d01 - d00, d11 - d10, wx)};
@@ -836,6 +844,26 @@ struct Sim {
     std::vector<F2> drive;
     bool hasDrive = false;
     int resX, resY;
+    // queue-aware exit choice (nav::choiceStep, src/exit_choice.cpp:671-790, restated on the hash cells' candidate
+    // table): off while choiceExits == 0
+    int choiceExits = 0, choiceK = 0;
+    uint32_t choiceStep = 0;
+    std::vector<float> exitFields, cDist, invCap;
+    std::vector<uint8_t> cExit;
+    std::vector<uint32_t> assign, pendExit, pendBin, hist, threshold, queue, ahead;
+    uint32_t choiceCounters[4] = {0, 0, 0, 0};
+    void resetChoice() {
+        choiceStep = 0;
+        assign.assign(size_t(n), SWARM_CHOICE_NONE);
+        pendExit.assign(size_t(n), SWARM_CHOICE_NONE);
+        pendBin.assign(size_t(n), 0u);
+        hist.assign(size_t(choiceExits) * CHOICE_GAIN_BINS, 0u);
+        threshold.assign(CHOICE_STRIDE, 0u);
+        queue.assign(2 * CHOICE_STRIDE, 0u);
+        ahead.assign(size_t(2) * CHOICE_STRIDE * CHOICE_AHEAD_BINS, 0u);
+        for (auto& c : choiceCounters) c = 0;
+    }
+    void choicePass();
 
     Sim(const SwarmParams& p, const SwarmVenue& v, int nThreads) : P(p), V(v), threads(nThreads > 0 ? nThreads : omp_get_max_threads()) {
         resX = V.grid_res_x; resY = V.grid_res_y;
@@ -869,6 +897,7 @@ struct Sim {
         planes.assign(size_t(n), F4{0, 0, 0, 0});
         contacts.assign(size_t(n), 0);
         if (radius.size() != size_t(n)) { radius.assign(size_t(n), P.body_radius); v0.assign(size_t(n), P.v_max); }
+        resetChoice();
     }
 
     // cpu_crowd_sim.cpp:82-86 cellID, generalised to a rectangular grid
@@ -911,6 +940,7 @@ struct Sim {
 
     template <class Venue> void physics(const Venue& ven);
     void step() {
+        if (choiceExits) choicePass();
         hash();
         sortCounting();
         buildCells();
@@ -928,11 +958,130 @@ struct Sim {
     }
 };
 
+// nav::choiceStep (src/exit_choice.cpp:671-790): the prefix stage, evaluate and thresholds on evaluation steps, apply;
+// sequential in agent order (every count an integer: the GPU's atomics give the same)
+void Sim::choicePass() {
+    const uint32_t par = choiceStep & 1u;
+    uint32_t* aRead = ahead.data() + size_t(par) * CHOICE_STRIDE * CHOICE_AHEAD_BINS;
+    uint32_t* aWrite = ahead.data() + size_t(1u - par) * CHOICE_STRIDE * CHOICE_AHEAD_BINS;
+    const int steps = std::max(1, int(CHOICE_T_S / double(P.dt) + 0.5));
+    const bool evalStep = choiceStep > 0u && choiceStep % uint32_t(steps) == 0u;
+    const int K = choiceK;
+    for (int e = 0; e < choiceExits; ++e) {
+        uint32_t run = 0;
+        for (int b = 0; b < CHOICE_AHEAD_BINS; ++b) {
+            const size_t i = size_t(e) * CHOICE_AHEAD_BINS + size_t(b);
+            const uint32_t h = aRead[i];
+            aRead[i] = run;
+            run += h;
+            aWrite[i] = 0u;
+        }
+    }
+    for (int e = 0; e < CHOICE_STRIDE; ++e) queue[(1u - par) * CHOICE_STRIDE + uint32_t(e)] = 0u;
+    auto bin = [](float d) { return std::min(uint32_t(d * 2.0f), uint32_t(CHOICE_AHEAD_BINS - 1)); };
+    auto est = [&](float d, uint32_t e, uint32_t q) {
+        const float walk = d * CHOICE_S_PER_M;
+        const float wait = float(q) * invCap[e];
+        return walk + wait;
+    };
+    auto slotOf = [&](size_t row, uint32_t e) {
+        int k = -1;
+        for (int i = 0; i < K; ++i) if (uint32_t(cExit[row + size_t(i)]) == e) k = i;
+        return k;
+    };
+    auto bestOf = [&](size_t row, float& eBest) {
+        int best = -1;
+        eBest = 0.0f;
+        for (int k = 0; k < K; ++k) {
+            const uint32_t ex = cExit[row + size_t(k)];
+            if (ex == SWARM_CHOICE_EMPTY) break;
+            const float d = cDist[row + size_t(k)];
+            const float e = est(d, ex, aRead[size_t(ex) * CHOICE_AHEAD_BINS + bin(d)]);
+            if (best < 0 || e < eBest) { best = k; eBest = e; }
+        }
+        return best;
+    };
+    auto rowOf = [&](int i, size_t& row) {
+        F4 p = boids[readIdx][size_t(i)].pos;
+        if (std::isnan(p.x)) p = F4{0.0f, 0.0f, 0.0f, 1.0f};
+        if (p.w == 0.0f) return false;
+        row = size_t(cellID(xy(p))) * size_t(K);
+        return true;
+    };
+    if (evalStep) {
+        for (int i = 0; i < n; ++i) {
+            pendExit[size_t(i)] = SWARM_CHOICE_NONE;
+            pendBin[size_t(i)] = 0u;
+            size_t row;
+            if (!rowOf(i, row) || cExit[row] == SWARM_CHOICE_EMPTY) continue;
+            const uint32_t cur = assign[size_t(i)];
+            const int curK = slotOf(row, cur);
+            if (curK < 0) continue;
+            ++choiceCounters[0];
+            float eBest;
+            const int best = bestOf(row, eBest);
+            const float dCur = cDist[row + size_t(curK)];
+            const float eCur = est(dCur, cur, aRead[size_t(cur) * CHOICE_AHEAD_BINS + bin(dCur)]);
+            const float gain = eCur - eBest;
+            if (best != curK && gain > std::max(CHOICE_REL_MARGIN * eCur, CHOICE_ABS_MARGIN_S)) {
+                const uint32_t b = std::min(uint32_t(gain), uint32_t(CHOICE_GAIN_BINS - 1));
+                pendExit[size_t(i)] = cExit[row + size_t(best)];
+                pendBin[size_t(i)] = b;
+                ++hist[size_t(cur) * CHOICE_GAIN_BINS + b];
+                ++choiceCounters[1];
+            }
+        }
+        for (int e = 0; e < choiceExits; ++e) {   // nav::switchThreshold (src/exit_choice.cpp:625-640)
+            uint32_t* h = hist.data() + size_t(e) * CHOICE_GAIN_BINS;
+            const uint32_t queued = queue[par * CHOICE_STRIDE + uint32_t(e)];
+            const uint32_t cap = std::max(CHOICE_MIN_SWITCHES, uint32_t(float(queued) * CHOICE_SWITCH_SHARE));
+            uint32_t cum = 0, thr = uint32_t(CHOICE_GAIN_BINS);
+            for (int b = CHOICE_GAIN_BINS - 1; b >= 0; --b) {
+                const uint32_t c = h[b];
+                if (c == 0) continue;
+                if (cum + c > cap) {
+                    if (cum == 0) thr = uint32_t(b);
+                    break;
+                }
+                cum += c;
+                thr = uint32_t(b);
+            }
+            threshold[size_t(e)] = thr;
+            std::fill(h, h + CHOICE_GAIN_BINS, 0u);
+        }
+    }
+    for (int i = 0; i < n; ++i) {   // nav::apply (src/exit_choice.cpp:642-658) and the counts for the next step
+        size_t row;
+        if (!rowOf(i, row)) continue;
+        const uint32_t cur = assign[size_t(i)];
+        uint32_t ex = cur;
+        const bool hasPath = cExit[row] != SWARM_CHOICE_EMPTY;
+        const int curK = hasPath ? slotOf(row, cur) : -1;
+        if (hasPath && curK < 0) {
+            float eBest;
+            ex = cExit[row + size_t(bestOf(row, eBest))];
+            if (cur != SWARM_CHOICE_NONE) ++choiceCounters[3];
+        } else if (evalStep && curK >= 0 && pendExit[size_t(i)] != SWARM_CHOICE_NONE && pendBin[size_t(i)] >= threshold[cur]) {
+            ex = pendExit[size_t(i)];
+            ++choiceCounters[2];
+        }
+        assign[size_t(i)] = ex;
+        if (ex != SWARM_CHOICE_NONE) {
+            ++queue[(1u - par) * CHOICE_STRIDE + ex];
+            const int k = slotOf(row, ex);
+            if (k >= 0) ++aWrite[size_t(ex) * CHOICE_AHEAD_BINS + bin(cDist[row + size_t(k)])];
+        }
+    }
+    ++choiceStep;
+}
+
 // The per-venue hooks the skeleton calls
 inline bool venueExits(const Stadium& s, F4 p) { return s.exits(p); }
 inline bool venueExits(const GridVenue& g, F4 p) { return g.exits(p); }
 inline F2 venueGoal(const Stadium& s, F3 p) { return s.goal(p); }
 inline F2 venueGoal(const GridVenue& g, F3 p) { return g.goal(p); }
+inline F2 venueGoalIn(const Stadium& s, const float*, F3 p) { return s.goal(p); }
+inline F2 venueGoalIn(const GridVenue& g, const float* D, F3 p) { return g.goalIn(D, p); }
 
 template <class Venue>
 struct Physics {
@@ -949,6 +1098,8 @@ struct Physics {
 
     F2 goalDirection(F3 p, uint32_t id) const {   // cpu_crowd_sim.cpp:213-218
         if (S.hasDrive) return S.drive[id];
+        if (S.choiceExits && S.assign[id] != SWARM_CHOICE_NONE)   // the assigned exit's own field
+            return venueGoalIn(ven, S.exitFields.data() + size_t(S.assign[id]) * size_t(S.V.nav_nx) * size_t(S.V.nav_ny), p);
         return venueGoal(ven, p);
     }
 
@@ -1201,6 +1352,29 @@ int oracle_set_drive_table(void* h, const float* dirs, int n) {
     s->drive.resize(size_t(n));
     std::memcpy(s->drive.data(), dirs, size_t(n) * 2 * sizeof(float));
     s->hasDrive = true;
+    return 0;
+}
+// The queue-aware exit choice: the per-exit fields (n_exits x nav nodes), seconds per queued agent per exit, and the
+// candidate table (ncells x K exits and distances, as swarm_exit_choice_table builds it); n_exits 0: off
+int oracle_set_exit_choice(void* h, int nExits, int K, const float* fields, const float* invCap, const uint8_t* cExit,
+                           const float* cDist) {
+    Sim* s = static_cast<Sim*>(h);
+    s->choiceExits = 0;
+    if (nExits <= 0) { s->resetChoice(); return 0; }
+    const size_t m = size_t(s->V.nav_nx) * size_t(s->V.nav_ny), rows = size_t(s->resX) * size_t(s->resY) * size_t(K);
+    s->exitFields.assign(fields, fields + size_t(nExits) * m);
+    s->invCap.assign(invCap, invCap + nExits);
+    s->cExit.assign(cExit, cExit + rows);
+    s->cDist.assign(cDist, cDist + rows);
+    s->choiceExits = nExits;
+    s->choiceK = K;
+    s->resetChoice();
+    return 0;
+}
+int oracle_get_exit_choice(void* h, uint32_t* assigned, uint32_t* counters) {
+    Sim* s = static_cast<Sim*>(h);
+    if (assigned) std::memcpy(assigned, s->assign.data(), size_t(s->n) * 4);
+    if (counters) std::memcpy(counters, s->choiceCounters, 16);
     return 0;
 }
 int oracle_step(void* h, int steps) {

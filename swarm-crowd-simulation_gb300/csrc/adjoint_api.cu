@@ -175,6 +175,7 @@ extern "C" int swarm_adjoint_run(SwarmHandle h, const SwarmLossSpec* loss, int s
     // a floor grid brings the step-up limit into the forward step, whose blocked moves have no reverse here
     if (h->dFloor) return h->fail(SWARM_E_INVALID, "the adjoint runs on flat venues (no floor grid: no step-up limit)");
     if (h->driveOn) return h->fail(SWARM_E_INVALID, "the adjoint follows e_goal: clear the drive table");
+    if (h->choiceExits) return h->fail(SWARM_E_INVALID, "the adjoint follows the nearest-exit field: turn the exit choice off");
     if (!h->hasState) return h->fail(SWARM_E_STATE, "no state (upload one first)");
     if (steps < 1 || ckpt_every < 1) return h->fail(SWARM_E_INVALID, "steps and ckpt_every must be >= 1");
     const int K = h->P.proj_iterations;

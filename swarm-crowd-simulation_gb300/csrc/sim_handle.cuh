@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <utility>
 #include <string>
 #include <vector>
 
@@ -84,6 +85,22 @@ struct SwarmSim {
     int64_t launches = 0;
     std::vector<void*> allocs;
     SwarmAdjoint* adjoint = nullptr;
+    // queue-aware exit choice (swarm_set_exit_choice, choice.cu): off while choiceExits == 0
+    int choiceExits = 0, choiceK = 0;
+    uint32_t choiceStep = 0;                // steps since the choice restarted (state upload or set)
+    float* dExitFields = nullptr;           // choiceExits x nav nodes
+    uint8_t* dChoiceExit = nullptr;         // ncells x choiceK candidate exits
+    float* dChoiceDist = nullptr;           // ncells x choiceK candidate distances
+    float* dChoiceInvCap = nullptr;         // per exit: seconds per queued agent
+    uint32_t* dAssign = nullptr;            // per agent
+    uint2* dPending = nullptr;              // per agent
+    uint32_t *dChoiceHist = nullptr, *dChoiceThr = nullptr, *dChoiceQueue = nullptr, *dChoiceAhead = nullptr,
+             *dChoiceCounters = nullptr;
+    std::vector<void*> choiceAllocs;
+    bool resetChoice();                     // no exit assigned, counts clear, step 0
+    void freeChoice();                      // off, buffers freed
+    int enqueueChoice(int in);              // the choice pass on state half `in`, before that step
+    std::vector<std::pair<void*, size_t>> choiceLive() const;   // what a step changes (the evacuation runner's rollback)
     int64_t adjTapeBudget = int64_t(1) << 30;   // device bytes the adjoint may spend on kept segment tapes
 
     swarm_gpu::StepArgs args(int in) const;

@@ -52,6 +52,11 @@ struct StepArgs {
     // stateIn; after the final pass (one more grid barrier) the blocks copy stateOut to hostOut in order
     const float4* hostIn;
     float4* hostOut;
+    // queue-aware exit choice (null: off): each agent's assigned exit, whose own distance field (exitFields + exit x
+    // navNodes, on the nav grid) gives its e_goal
+    const uint32_t* choiceAssign;
+    const float* exitFields;
+    uint32_t navNodes;
     const float2* aparam;   // (radius, v0) per agent
     const float2* drive;    // forced e_goal per agent, or null
     uint8_t* contacts;      // ContactBits per agent (the last step's)

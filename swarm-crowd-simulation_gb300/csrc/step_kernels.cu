@@ -304,6 +304,12 @@ struct Body {
 template <class Venue>
 __device__ __forceinline__ f2 goalOf(const StepArgs& A, const Venue& ven, f3 p, uint32_t id) {
     if (A.drive) { const float2 d = A.drive[id]; return f2{d.x, d.y}; }
+    if constexpr (std::is_same<Venue, GridVenue>::value) {
+        if (A.choiceAssign) {   // the queue-aware exit choice: the assigned exit's own field
+            const uint32_t e = A.choiceAssign[id];
+            if (e != SWARM_CHOICE_NONE) return ven.goalIn(A.exitFields + size_t(e) * A.navNodes, p);
+        }
+    }
     return ven.goal(p);
 }
 

@@ -47,6 +47,7 @@ SwarmSim::~SwarmSim() {
     swarm_adjoint_free(adjoint);
     for (auto& e : ev) if (e) cudaEventDestroy(e);
     for (void* p : allocs) cudaFree(p);
+    for (void* p : choiceAllocs) cudaFree(p);
     if (ownStream) cudaStreamDestroy(ownStream);
 }
 
@@ -79,6 +80,9 @@ StepArgs SwarmSim::args(int in) const {
     A.pos0 = pos0; A.vel0 = vel0; A.prm = prm; A.proj[0] = proj0; A.proj[1] = proj1;
     A.vel1 = vel1; A.plane = plane; A.ctc = ctc; A.rowsA = rowsA; A.rowsB = rowsB; A.tileWin = tileWin; A.goal = goal; A.err = errFlag; A.barrier = barrier; A.barrierExtra = barrierExtra;
     A.stamps = timing ? stamps : nullptr;
+    A.choiceAssign = choiceExits ? dAssign : nullptr;
+    A.exitFields = dExitFields;
+    A.navNodes = uint32_t(size_t(V.nav_nx) * size_t(V.nav_ny));
     A.fusedThreads = tuning.threads;
     A.fusedBlocksPerSm = tuning.blocks_per_sm;
     A.venueTable = dVenueTable;
@@ -313,6 +317,7 @@ static int uploadImpl(SwarmHandle h, const float* boids, int n, cudaMemcpyKind k
         !cudaOk(h, cudaMemcpyAsync(h->state[1], boids, bytes, kind, h->stream), "upload"))
         return SWARM_E_CUDA;
     h->hasState = true;
+    if (!h->resetChoice()) return h->fail(SWARM_E_CUDA, "exit choice reset");
     return SWARM_OK;
 }
 
@@ -452,10 +457,11 @@ int swarm_autotune(SwarmHandle h, int steps, SwarmTuning* best) {
     const size_t bytes = size_t(h->n) * 32;
     if (cudaMalloc(&snap, bytes) != cudaSuccess) return h->fail(SWARM_E_OOM, "autotune snapshot");
     cudaMemcpyAsync(snap, h->state[h->readIdx], bytes, cudaMemcpyDeviceToDevice, h->stream);
-    const int metricRes = h->metricRes;
+    const int metricRes = h->metricRes, choiceExits = h->choiceExits;
     const bool graph = h->useGraph, timing = h->timing;
     const SwarmTuning keep = h->tuning;
     h->metricRes = 0;
+    h->choiceExits = 0;   // (the trials step without the exit choice: its state is not touched)
     h->useGraph = true;
     h->timing = false;
     cudaEvent_t e0, e1;
@@ -488,6 +494,7 @@ int swarm_autotune(SwarmHandle h, int steps, SwarmTuning* best) {
     cudaStreamSynchronize(h->stream);
     cudaFree(snap);
     h->metricRes = metricRes;
+    h->choiceExits = choiceExits;
     h->useGraph = graph;
     h->timing = timing;
     h->dropGraphs();
@@ -527,6 +534,7 @@ static int stepImpl(SwarmHandle h, int steps, bool countLast) {
     const int perStep = 7 + std::max(h->P.proj_iterations - 1, 0);
     for (int s = 0; s < steps; ++s) {
         const int in = h->readIdx;
+        if (h->choiceExits && h->enqueueChoice(in) != SWARM_OK) return SWARM_E_CUDA;
         if (h->fused) {
             if (h->timing && !cudaOk(h, cudaEventRecord(h->ev[0], h->stream), "event")) return SWARM_E_CUDA;
             StepArgs A = h->args(in);
@@ -589,6 +597,7 @@ int swarm_run_evacuation(SwarmHandle h, int max_steps, int32_t* active_out, Swar
         live.push_back({h->mMass, cells * 8});
         live.push_back({h->mCells, cells * sizeof(SwarmMetricCell)});
     }
+    for (const auto& l : h->choiceLive()) live.push_back(l);   // the exit choice's assignments and counts
     size_t saveBytes = 0;
     for (auto& l : live) saveBytes += (l.second + 255) / 256 * 256;
     uint32_t* dCounts = nullptr;
@@ -639,7 +648,7 @@ int swarm_run_evacuation(SwarmHandle h, int max_steps, int32_t* active_out, Swar
     while (steps < max_steps && active > 0) {
         const int c = std::min(CHUNK, max_steps - steps);
         const int readIdx = h->readIdx;
-        const uint32_t metricStep = h->metricStep;
+        const uint32_t metricStep = h->metricStep, choiceStep = h->choiceStep;
         if (!copyLive(true)) return fail(h->fail(SWARM_E_CUDA, "evacuation rollback copy"));
         if ((rc = runChunk(c)) != SWARM_OK) return fail(rc);
         int run = c;
@@ -650,6 +659,7 @@ int swarm_run_evacuation(SwarmHandle h, int max_steps, int32_t* active_out, Swar
             if (!copyLive(false)) return fail(h->fail(SWARM_E_CUDA, "evacuation rollback copy"));
             h->readIdx = readIdx;
             h->metricStep = metricStep;
+            h->choiceStep = choiceStep;
             if (!h->clearCounts()) return fail(h->fail(SWARM_E_CUDA, "clearing the counts"));
             if ((rc = runChunk(run)) != SWARM_OK) return fail(rc);
         }
@@ -693,6 +703,7 @@ int swarm_step_host(SwarmHandle h, const float* in_boids, float* out_boids, int 
     if (h->counted && !h->clearCounts()) return h->fail(SWARM_E_CUDA, "clearing the counts");
     h->n = n;
     h->hasState = true;
+    if (!h->resetChoice()) return h->fail(SWARM_E_CUDA, "exit choice reset");
     const size_t bytes = size_t(n) * 32;
     // Pinned host buffers on the fused path: no copy operations. The first step's hash phase reads the input over the
     // coherent host link (into the device half it steps from), and the last step ends with its blocks copying the

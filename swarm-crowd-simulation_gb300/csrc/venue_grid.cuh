@@ -38,15 +38,17 @@ struct GridVenue {
     __device__ __forceinline__ float speedFactor(f3 p) const { return V.speedF ? __ldg(V.speedF + floorNode(xy(p))) : 1.0f; }
     __device__ __forceinline__ float map(f3 p) const { return smin(wallDist(xy(p)), p.z - floorHeight(xy(p))); }
 
-    // e_goal = -grad D / |grad D| of the bilinear interpolant of the distance grid
-    __device__ f2 goal(f3 p) const {
+    // e_goal = -grad D / |grad D| of the bilinear interpolant of the distance grid (the nearest exit's, or D = one
+    // exit's own field on the same grid)
+    __device__ __forceinline__ f2 goal(f3 p) const { return goalIn(V.nav, p); }
+    __device__ f2 goalIn(const float* D, f3 p) const {
         float fx = (p.x - V.nox) * V.ninv, fy = (p.y - V.noy) * V.ninv;
         fx = sclamp(fx, 0.0f, float(V.nnx - 1));
         fy = sclamp(fy, 0.0f, float(V.nny - 1));
         const int ix = smin(int(floorf(fx)), V.nnx - 2), iy = smin(int(floorf(fy)), V.nny - 2);
         const float wx = fx - float(ix), wy = fy - float(iy);
         const size_t r0 = size_t(iy) * size_t(V.nnx) + size_t(ix), r1 = r0 + size_t(V.nnx);
-        const float d00 = __ldg(V.nav + r0), d10 = __ldg(V.nav + r0 + 1), d01 = __ldg(V.nav + r1), d11 = __ldg(V.nav + r1 + 1);
+        const float d00 = __ldg(D + r0), d10 = __ldg(D + r0 + 1), d01 = __ldg(D + r1), d11 = __ldg(D + r1 + 1);
         f2 g{mix(d10 - d00, d11 - d01, wy), mix(d01 - d00, d11 - d10, wx)};
         return safeNormalize(f2{-g.x, -g.y}, P.safe_eps);
     }

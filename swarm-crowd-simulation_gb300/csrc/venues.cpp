@@ -179,16 +179,10 @@ extern "C" int swarm_hall_layout(const SwarmHallSpec* s, SwarmVenue* v) {
     return SWARM_OK;
 }
 
-extern "C" int swarm_hall_fields(const SwarmHallSpec* s, const SwarmVenue* v, float* wall, float* nav, float* exitBoxes) {
-    if (!validSpec(s) || !v || !wall || !nav) return SWARM_E_INVALID;
-    const std::vector<Box> boxes = wallBoxes(s);
-    const double hx = 0.5 * s->size_x, hy = 0.5 * s->size_y, t = s->wall_thickness;
-    // wall SDF
-    for (int j = 0; j < v->wall_ny; ++j)
-        for (int i = 0; i < v->wall_nx; ++i)
-            wall[size_t(j) * size_t(v->wall_nx) + size_t(i)] =
-                float(wallSdf(boxes, double(v->wall_origin_x) + i * double(v->wall_h), double(v->wall_origin_y) + j * double(v->wall_h)));
-    // fast marching on the nav grid: sources beyond the exit line, walls where the wall SDF is <= 0
+namespace {
+
+// The hall's nav node kinds: sources beyond the exit line, walls where the wall SDF is <= 0
+std::vector<uint8_t> hallNavKind(const SwarmVenue* v, const std::vector<Box>& boxes) {
     const int nx = v->nav_nx, ny = v->nav_ny;
     std::vector<uint8_t> kind(size_t(nx) * size_t(ny), 0);
     for (int j = 0; j < ny; ++j) {
@@ -199,24 +193,96 @@ extern "C" int swarm_hall_fields(const SwarmHallSpec* s, const SwarmVenue* v, fl
             else if (x < v->exit_lo_x || x > v->exit_hi_x || y < v->exit_lo_y || y > v->exit_hi_y) kind[k] = 1;
         }
     }
-    if (const int rc = fastMarch(nx, ny, v->nav_h, kind, nullptr, nav); rc != SWARM_OK) return rc;
-    // exit boxes: each door's opening, from the interior face out to the domain edge
-    if (exitBoxes) {
-        for (int d = 0; d < s->n_doors; ++d) {
-            const double c0 = s->door_center[d] - 0.5 * s->door_width[d], c1 = s->door_center[d] + 0.5 * s->door_width[d];
-            const double fx = -double(v->domain_min_x), fy = -double(v->domain_min_y);
-            double b[4];
-            switch (s->door_wall[d]) {
-                case 0: b[0] = -fx; b[1] = c0; b[2] = -hx; b[3] = c1; break;
-                case 1: b[0] = hx; b[1] = c0; b[2] = fx; b[3] = c1; break;
-                case 2: b[0] = c0; b[1] = -fy; b[2] = c1; b[3] = -hy; break;
-                default: b[0] = c0; b[1] = hy; b[2] = c1; b[3] = fy; break;
-            }
-            for (int q = 0; q < 4; ++q) exitBoxes[4 * d + q] = float(b[q]);
+    return kind;
+}
+
+// Each door's opening, from the interior face out to the domain edge (lo_x, lo_y, hi_x, hi_y)
+void hallExitBoxes(const SwarmHallSpec* s, const SwarmVenue* v, float* exitBoxes) {
+    const double hx = 0.5 * s->size_x, hy = 0.5 * s->size_y;
+    for (int d = 0; d < s->n_doors; ++d) {
+        const double c0 = s->door_center[d] - 0.5 * s->door_width[d], c1 = s->door_center[d] + 0.5 * s->door_width[d];
+        const double fx = -double(v->domain_min_x), fy = -double(v->domain_min_y);
+        double b[4];
+        switch (s->door_wall[d]) {
+            case 0: b[0] = -fx; b[1] = c0; b[2] = -hx; b[3] = c1; break;
+            case 1: b[0] = hx; b[1] = c0; b[2] = fx; b[3] = c1; break;
+            case 2: b[0] = c0; b[1] = -fy; b[2] = c1; b[3] = -hy; break;
+            default: b[0] = c0; b[1] = hy; b[2] = c1; b[3] = fy; break;
         }
+        for (int q = 0; q < 4; ++q) exitBoxes[4 * d + q] = float(b[q]);
     }
-    (void)t;
+}
+
+// Each exit's own distance field: the venue's nav kinds with only exit e's sources (every source node belongs to the
+// exit whose box lies nearest, the first on a tie; a box holds its own nodes at distance 0); the other exits'
+// sources become walls, so no path leaves through one door and comes back in through another. `hallOutside`: source
+// nodes outside every box are the outside of a hall, reached only through its doors: walls for every exit.
+int exitFields(const SwarmVenue* v, const std::vector<uint8_t>& kind, const float* speed, const float* boxes, int nExits,
+               float* fields, bool hallOutside) {
+    const int nx = v->nav_nx, ny = v->nav_ny;
+    const size_t m = size_t(nx) * size_t(ny);
+    std::vector<int8_t> owner(m, -1);
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+            const size_t k = size_t(j) * size_t(nx) + size_t(i);
+            if (kind[k] != 1) continue;
+            const double x = double(v->nav_origin_x) + i * double(v->nav_h), y = double(v->nav_origin_y) + j * double(v->nav_h);
+            double best = 0.0;
+            for (int e = 0; e < nExits; ++e) {
+                const double dx = std::max({double(boxes[4 * e]) - x, 0.0, x - double(boxes[4 * e + 2])});
+                const double dy = std::max({double(boxes[4 * e + 1]) - y, 0.0, y - double(boxes[4 * e + 3])});
+                const double d = dx * dx + dy * dy;
+                if (hallOutside && d > 0.0) continue;
+                if (owner[k] < 0 || d < best) { owner[k] = int8_t(e); best = d; }
+            }
+        }
+    for (int e = 0; e < nExits; ++e) {
+        std::vector<uint8_t> ke(kind);
+        for (size_t k = 0; k < m; ++k)
+            if (ke[k] == 1 && owner[k] != e) ke[k] = 3;
+        if (const int rc = fastMarch(nx, ny, v->nav_h, std::move(ke), speed, fields + size_t(e) * m); rc != SWARM_OK) return rc;
+    }
     return SWARM_OK;
+}
+
+}  // namespace
+
+extern "C" int swarm_hall_fields(const SwarmHallSpec* s, const SwarmVenue* v, float* wall, float* nav, float* exitBoxes) {
+    if (!validSpec(s) || !v || !wall || !nav) return SWARM_E_INVALID;
+    const std::vector<Box> boxes = wallBoxes(s);
+    // wall SDF
+    for (int j = 0; j < v->wall_ny; ++j)
+        for (int i = 0; i < v->wall_nx; ++i)
+            wall[size_t(j) * size_t(v->wall_nx) + size_t(i)] =
+                float(wallSdf(boxes, double(v->wall_origin_x) + i * double(v->wall_h), double(v->wall_origin_y) + j * double(v->wall_h)));
+    // fast marching on the nav grid
+    if (const int rc = fastMarch(v->nav_nx, v->nav_ny, v->nav_h, hallNavKind(v, boxes), nullptr, nav); rc != SWARM_OK) return rc;
+    if (exitBoxes) hallExitBoxes(s, v, exitBoxes);
+    return SWARM_OK;
+}
+
+extern "C" int swarm_hall_exit_fields(const SwarmHallSpec* s, const SwarmVenue* v, float* fields, float* width, uint8_t* type) {
+    if (!validSpec(s) || !v || !fields || s->n_doors < 1 || s->n_doors > SWARM_CHOICE_MAX_EXITS) return SWARM_E_INVALID;
+    std::vector<float> boxes(size_t(4) * size_t(s->n_doors));
+    hallExitBoxes(s, v, boxes.data());
+    for (int d = 0; d < s->n_doors; ++d) {
+        if (width) width[d] = s->door_width[d];
+        if (type) type[d] = 1;
+    }
+    // the per-exit fields see the hall's interior and its door openings only: every node outside the interior and
+    // outside the door boxes is a wall (the outside is reached through the doors alone)
+    std::vector<uint8_t> kind = hallNavKind(v, wallBoxes(s));
+    const double hx = 0.5 * s->size_x, hy = 0.5 * s->size_y;
+    for (int j = 0; j < v->nav_ny; ++j)
+        for (int i = 0; i < v->nav_nx; ++i) {
+            const double x = double(v->nav_origin_x) + i * double(v->nav_h), y = double(v->nav_origin_y) + j * double(v->nav_h);
+            if (std::fabs(x) <= hx && std::fabs(y) <= hy) continue;
+            bool door = false;
+            for (int d = 0; d < s->n_doors && !door; ++d)
+                door = x >= boxes[size_t(4 * d)] && x <= boxes[size_t(4 * d + 2)] && y >= boxes[size_t(4 * d + 1)] && y <= boxes[size_t(4 * d + 3)];
+            if (!door) kind[size_t(j) * size_t(v->nav_nx) + size_t(i)] = 3;
+        }
+    return exitFields(v, kind, nullptr, boxes.data(), s->n_doors, fields, true);
 }
 
 // ---- the seated bowl ----
@@ -354,6 +420,65 @@ extern "C" int swarm_bowl_layout(const SwarmBowlSpec* s, SwarmVenue* v) {
     return SWARM_OK;
 }
 
+namespace {
+
+// The bowl's nav node kinds (walls within the clearance, sources at the exits), speed factors and exit mask
+void bowlNav(const SwarmBowlSpec* s, const SwarmVenue* v, const Bowl& B, std::vector<uint8_t>& kind, std::vector<float>& speed,
+             uint8_t* mask) {
+    const int nn = v->nav_nx;
+    kind.assign(size_t(nn) * size_t(v->nav_ny), 0);
+    speed.assign(kind.size(), 0.0f);
+    parallelRows(v->nav_ny, [&](int j) {
+        for (int i = 0; i < nn; ++i) {
+            const double x = double(v->nav_origin_x) + i * double(v->nav_h), y = double(v->nav_origin_y) + j * double(v->nav_h);
+            const size_t k = size_t(j) * size_t(nn) + size_t(i);
+            double h, sp;
+            B.floorAt(x, y, h, sp);
+            speed[k] = float(sp);
+            const bool ex = B.isExit(x, y);
+            if (mask) mask[k] = ex ? 1 : 0;
+            // blocked within the clearance of a wall (the largest body radius): a thin row wall between nodes still
+            // cuts the field, and the paths round every wall end at a distance a body can keep, so e_goal never
+            // points into the wall an agent touches
+            kind[k] = B.sdf(x, y) <= double(s->clearance) ? 3 : (ex ? 1 : 0);
+        }
+    });
+}
+
+// Each exit's bounding box (lo_x, lo_y, hi_x, hi_y): the sectors' vomitories, then the perimeter exits
+void bowlExitBoxes(const SwarmBowlSpec* s, const Bowl& B, float* exitBoxes) {
+    auto bound = [&](int e, int k, double u0, double u1, double w0, double w1) {
+        double lo[2] = {1e30, 1e30}, hi[2] = {-1e30, -1e30};
+        for (int q = 0; q < 4; ++q) {
+            const double u = (q & 1) ? u1 : u0, w = (q & 2) ? w1 : w0;
+            const double x = (B.rin + w) * B.c[size_t(k)] - u * B.sn[size_t(k)], y = (B.rin + w) * B.sn[size_t(k)] + u * B.c[size_t(k)];
+            lo[0] = std::min(lo[0], x); lo[1] = std::min(lo[1], y); hi[0] = std::max(hi[0], x); hi[1] = std::max(hi[1], y);
+        }
+        exitBoxes[4 * e] = float(lo[0]); exitBoxes[4 * e + 1] = float(lo[1]);
+        exitBoxes[4 * e + 2] = float(hi[0]); exitBoxes[4 * e + 3] = float(hi[1]);
+    };
+    const double vw0 = s->vomitory_row * double(s->row_pitch);
+    for (int k = 0; k < s->sectors; ++k) {   // the vomitory between sector k and k + 1, in the bisector's frame
+        const double b = (k + 0.5) * B.dphi, cb = std::cos(b), sb = std::sin(b), cw = std::cos(0.5 * B.dphi);
+        const double r0 = (B.rin + vw0) / cw, r1 = (B.rin + vw0 + s->row_pitch) / cw, hw = 0.5 * s->vomitory_width;
+        double lo[2] = {1e30, 1e30}, hi[2] = {-1e30, -1e30};
+        for (int q = 0; q < 4; ++q) {
+            const double r = (q & 1) ? r1 : r0, t = (q & 2) ? hw : -hw;
+            const double x = r * cb - t * sb, y = r * sb + t * cb;
+            lo[0] = std::min(lo[0], x); lo[1] = std::min(lo[1], y); hi[0] = std::max(hi[0], x); hi[1] = std::max(hi[1], y);
+        }
+        exitBoxes[4 * k] = float(lo[0]); exitBoxes[4 * k + 1] = float(lo[1]);
+        exitBoxes[4 * k + 2] = float(hi[0]); exitBoxes[4 * k + 3] = float(hi[1]);
+    }
+    int e = s->sectors;
+    for (int k = 0; k < s->sectors; ++k)
+        if (B.exitSector[size_t(k)])
+            bound(e++, k, -0.5 * s->perimeter_exit_width, 0.5 * s->perimeter_exit_width, B.outerW + B.wallT,
+                  B.outerW + B.wallT + 3.0);
+}
+
+}  // namespace
+
 extern "C" int swarm_bowl_fields(const SwarmBowlSpec* s, const SwarmVenue* v, float* wall, float* nav, float* floorH,
                                  float* speedF, uint8_t* mask, float* exitBoxes) {
     if (!validBowl(s) || !v || !wall || !nav || !floorH || !speedF || !mask) return SWARM_E_INVALID;
@@ -370,55 +495,30 @@ extern "C" int swarm_bowl_fields(const SwarmBowlSpec* s, const SwarmVenue* v, fl
             speedF[k] = float(sp);
         }
     });
-    std::vector<uint8_t> kind(size_t(nn) * size_t(v->nav_ny), 0);
-    std::vector<float> speed(kind.size());
-    parallelRows(v->nav_ny, [&](int j) {
-        for (int i = 0; i < nn; ++i) {
-            const double x = double(v->nav_origin_x) + i * double(v->nav_h), y = double(v->nav_origin_y) + j * double(v->nav_h);
-            const size_t k = size_t(j) * size_t(nn) + size_t(i);
-            double h, sp;
-            B.floorAt(x, y, h, sp);
-            speed[k] = float(sp);
-            const bool ex = B.isExit(x, y);
-            mask[k] = ex ? 1 : 0;
-            // blocked within the clearance of a wall (the largest body radius): a thin row wall between nodes still
-            // cuts the field, and the paths round every wall end at a distance a body can keep, so e_goal never
-            // points into the wall an agent touches
-            kind[k] = B.sdf(x, y) <= double(s->clearance) ? 3 : (ex ? 1 : 0);
-        }
-    });
+    std::vector<uint8_t> kind;
+    std::vector<float> speed;
+    bowlNav(s, v, B, kind, speed, mask);
     if (const int rc = fastMarch(nn, v->nav_ny, v->nav_h, kind, speed.data(), nav); rc != SWARM_OK) return rc;
-    if (exitBoxes) {   // each exit's bounding box (the metrics' exit attribution)
-        auto bound = [&](int e, int k, double u0, double u1, double w0, double w1) {
-            double lo[2] = {1e30, 1e30}, hi[2] = {-1e30, -1e30};
-            for (int q = 0; q < 4; ++q) {
-                const double u = (q & 1) ? u1 : u0, w = (q & 2) ? w1 : w0;
-                const double x = (B.rin + w) * B.c[size_t(k)] - u * B.sn[size_t(k)], y = (B.rin + w) * B.sn[size_t(k)] + u * B.c[size_t(k)];
-                lo[0] = std::min(lo[0], x); lo[1] = std::min(lo[1], y); hi[0] = std::max(hi[0], x); hi[1] = std::max(hi[1], y);
-            }
-            exitBoxes[4 * e] = float(lo[0]); exitBoxes[4 * e + 1] = float(lo[1]);
-            exitBoxes[4 * e + 2] = float(hi[0]); exitBoxes[4 * e + 3] = float(hi[1]);
-        };
-        const double vw0 = s->vomitory_row * double(s->row_pitch);
-        for (int k = 0; k < s->sectors; ++k) {   // the vomitory between sector k and k + 1, in the bisector's frame
-            const double b = (k + 0.5) * B.dphi, cb = std::cos(b), sb = std::sin(b), cw = std::cos(0.5 * B.dphi);
-            const double r0 = (B.rin + vw0) / cw, r1 = (B.rin + vw0 + s->row_pitch) / cw, hw = 0.5 * s->vomitory_width;
-            double lo[2] = {1e30, 1e30}, hi[2] = {-1e30, -1e30};
-            for (int q = 0; q < 4; ++q) {
-                const double r = (q & 1) ? r1 : r0, t = (q & 2) ? hw : -hw;
-                const double x = r * cb - t * sb, y = r * sb + t * cb;
-                lo[0] = std::min(lo[0], x); lo[1] = std::min(lo[1], y); hi[0] = std::max(hi[0], x); hi[1] = std::max(hi[1], y);
-            }
-            exitBoxes[4 * k] = float(lo[0]); exitBoxes[4 * k + 1] = float(lo[1]);
-            exitBoxes[4 * k + 2] = float(hi[0]); exitBoxes[4 * k + 3] = float(hi[1]);
-        }
-        int e = s->sectors;
-        for (int k = 0; k < s->sectors; ++k)
-            if (B.exitSector[size_t(k)])
-                bound(e++, k, -0.5 * s->perimeter_exit_width, 0.5 * s->perimeter_exit_width, B.outerW + B.wallT,
-                      B.outerW + B.wallT + 3.0);
-    }
+    if (exitBoxes) bowlExitBoxes(s, B, exitBoxes);   // (the metrics' exit attribution)
     return SWARM_OK;
+}
+
+extern "C" int swarm_bowl_exit_fields(const SwarmBowlSpec* s, const SwarmVenue* v, float* fields, float* width, uint8_t* type) {
+    if (!validBowl(s) || !v || !fields) return SWARM_E_INVALID;
+    const int nExits = s->sectors + s->perimeter_exits;
+    if (nExits < 1 || nExits > SWARM_CHOICE_MAX_EXITS) return SWARM_E_INVALID;
+    const Bowl B(*s);
+    std::vector<uint8_t> kind;
+    std::vector<float> speed;
+    bowlNav(s, v, B, kind, speed, nullptr);
+    std::vector<float> boxes(size_t(4) * size_t(nExits));
+    bowlExitBoxes(s, B, boxes.data());
+    for (int e = 0; e < nExits; ++e) {   // the vomitories (avenues into the concourse), then the perimeter doors
+        const bool vom = e < s->sectors;
+        if (width) width[e] = vom ? s->vomitory_width : s->perimeter_exit_width;
+        if (type) type[e] = vom ? 0 : 1;
+    }
+    return exitFields(v, kind, speed.data(), boxes.data(), nExits, fields, false);
 }
 
 extern "C" int swarm_spawn_bowl(const SwarmBowlSpec* sp, float jitter, uint64_t seed, float r_lo, float r_hi, float v_mean,

@@ -14,7 +14,7 @@ import numpy as np
 
 from .abi import (METRIC_CELL_WORDS, SWARM_LOSS_NAV_DISTANCE, SWARM_OK, SWARM_VENUE_GRID, SWARM_VENUE_STADIUM,
                   SwarmAdjointStats, SwarmEvacuation, SwarmLossSpec, SwarmMetricCounters, SwarmNavFieldStats, SwarmParams,
-                  SwarmStageTimes, SwarmTuning, SwarmVenue, fptr)
+                  SwarmStageTimes, SwarmTuning, SwarmVenue, SwarmExitChoiceSpec, CHOICE_NONE, CHOICE_EMPTY, fptr)
 
 PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG_DIR, "libswarm_gb300.so")
@@ -84,6 +84,14 @@ def lib():
                                     C.POINTER(SwarmNavFieldStats)],
             "swarm_nav_field_cpu": [C.c_int, C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.POINTER(C.c_float)],
             "swarm_set_nav_solver": [C.c_int],
+            "swarm_hall_exit_fields": [C.c_void_p, C.POINTER(SwarmVenue), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                       C.c_void_p],
+            "swarm_bowl_exit_fields": [C.c_void_p, C.POINTER(SwarmVenue), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                       C.c_void_p],
+            "swarm_exit_choice_table": [C.POINTER(SwarmVenue), C.POINTER(SwarmExitChoiceSpec), C.c_void_p,
+                                        C.POINTER(C.c_float)],
+            "swarm_set_exit_choice": [H, C.POINTER(SwarmExitChoiceSpec)],
+            "swarm_get_exit_choice": [H, C.c_void_p, C.c_int, C.c_void_p],
             "swarm_bowl_layout": [C.c_void_p, C.POINTER(SwarmVenue)],
             "swarm_bowl_fields": [C.c_void_p, C.POINTER(SwarmVenue), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                   C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_void_p, C.POINTER(C.c_float)],
@@ -135,6 +143,33 @@ def sdf_read(path, res=130):
     out = np.empty(res ** 3, np.float32)
     _check(lib().swarm_sdf_read(os.fsencode(path), fptr(out), int(res)), "swarm_sdf_read")
     return out
+
+
+def _choice_spec(fields, widths, types, candidates):
+    f = np.ascontiguousarray(fields, dtype=np.float32)
+    w = np.ascontiguousarray(widths, dtype=np.float32)
+    t = np.ascontiguousarray(types, dtype=np.uint8)
+    spec = SwarmExitChoiceSpec(int(w.shape[0]), int(candidates), fptr(f), fptr(w),
+                               t.ctypes.data_as(C.POINTER(C.c_uint8)))
+    return spec, (f, w, t)
+
+
+def exit_choice_table(venue, fields, widths, types, candidates=24):
+    """swarm_exit_choice_table: the queue-aware choice's candidates per hash cell, (cells, K) exits and distances."""
+    spec, keep = _choice_spec(fields, widths, types, candidates)
+    v = venue.struct
+    cells = v.grid_res_x * v.grid_res_y
+    ex = np.empty((cells, candidates), np.uint8)
+    di = np.empty((cells, candidates), np.float32)
+    _check(lib().swarm_exit_choice_table(C.byref(v), C.byref(spec), ex.ctypes.data_as(C.c_void_p), fptr(di)),
+           "swarm_exit_choice_table")
+    return ex, di
+
+
+def exit_inv_capacity(widths):
+    """Seconds per queued agent of each exit, 60 / (w J) with J = 83.6 persons per metre per minute (float32, as the
+    library computes it)."""
+    return (60.0 / (np.asarray(widths, dtype=np.float32).astype(np.float64) * 83.6)).astype(np.float32)
 
 
 def nav_field(kind, h, speed=None, solver="gpu"):
@@ -251,6 +286,23 @@ class CrowdSim:
 
     def set_graph(self, enabled=True):
         self._ck(lib().swarm_set_graph(self._h, int(bool(enabled))), "set_graph")
+
+    def set_exit_choice(self, fields=None, widths=None, types=None, candidates=24):
+        """The queue-aware exit choice (fields: (n_exits, nav nodes) per-exit distances, widths in metres, types 0
+        avenue / 1 door); None: the nearest-exit field. Restarts the choice (no exit assigned)."""
+        if fields is None:
+            self._ck(lib().swarm_set_exit_choice(self._h, None), "set_exit_choice")
+            return
+        spec, _keep = _choice_spec(fields, widths, types, candidates)
+        self._ck(lib().swarm_set_exit_choice(self._h, C.byref(spec)), "set_exit_choice")
+
+    def exit_choice(self):
+        """(assigned exit per agent (CHOICE_NONE: none yet), counters: evaluations, eligible, switches, forced)"""
+        a = np.empty(self.n, np.uint32)
+        c = np.empty(4, np.uint32)
+        self._ck(lib().swarm_get_exit_choice(self._h, a.ctypes.data_as(C.c_void_p), self.n, c.ctypes.data_as(C.c_void_p)),
+                 "get_exit_choice")
+        return a, c
 
     def set_fused(self, enabled=True):
         """One persistent kernel per step (True, the default) or one kernel per phase (False)."""

@@ -90,6 +90,15 @@ class SwarmLossSpec(C.Structure):
     _fields_ = [("kind", _i), ("pad", _i)]
 
 
+class SwarmExitChoiceSpec(C.Structure):
+    _fields_ = [("n_exits", C.c_int32), ("candidates", C.c_int32), ("fields", C.POINTER(_f)),
+                ("width_m", C.POINTER(_f)), ("type", C.POINTER(C.c_uint8))]
+
+
+CHOICE_NONE = 0xFFFFFFFF
+CHOICE_EMPTY = 0xFF
+
+
 class SwarmAdjointStats(C.Structure):
     _fields_ = [("ms_checkpoint", _f), ("ms_recompute", _f), ("ms_reverse", _f), ("ms_total", _f),
                 ("launches", C.c_int64), ("tape_bytes", C.c_int64),

@@ -123,6 +123,23 @@ def _bowl(spec, name):
 Venue.bowl = staticmethod(_bowl)
 
 
+def exit_fields(venue):
+    """Each exit's own distance field on the venue's nav grid, for the queue-aware exit choice: (fields (n_exits,
+    nav nodes), clear widths (m), types (0 avenue, 1 door)). Halls: one per door; bowls: the vomitories, then the
+    perimeter exits. Solved as the venue's nearest-exit field (swarm_set_nav_solver picks the solver)."""
+    v = venue.struct
+    spec = venue.meta.get("spec")
+    bowl = isinstance(spec, BowlSpec)
+    n = spec.sectors + spec.perimeter_exits if bowl else spec.n_doors
+    fields = np.empty((n, v.nav_nx * v.nav_ny), np.float32)
+    widths = np.empty(n, np.float32)
+    types = np.empty(n, np.uint8)
+    fn = lib().swarm_bowl_exit_fields if bowl else lib().swarm_hall_exit_fields
+    _check(fn(C.byref(spec), C.byref(v), fptr(fields), fptr(widths), types.ctypes.data_as(C.c_void_p)),
+           "swarm_bowl_exit_fields" if bowl else "swarm_hall_exit_fields")
+    return fields, widths, types
+
+
 def spawn_bowl(spec, jitter=0.03, seed=0, r=(0.20, 0.25), v=(1.34, 0.26, 0.6, 2.0)):
     """One agent per seat at the seat centre, jittered: (boids (n, 8), radius (n,), v0 (n,))."""
     n = spec.sectors * spec.rows * spec.seats

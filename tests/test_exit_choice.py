@@ -1,0 +1,158 @@
+"""The queue-aware exit choice (the reference's ExitChoice::QueueAware: physics.comp PHYSICS_PASS 0, nav::choiceStep,
+src/exit_choice.cpp:580-790) on grid venues: per-exit distance fields, the candidate table, the oracle's choice pass,
+and the GPU's four stage kernels against it bit for bit (assignments, counters, and the steps they steer)."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+NONE = 0xFFFFFFFF
+EMPTY = 0xFF
+
+
+def _hall():
+    from swarm_gb300 import venues
+    # four doors of different widths; the crowd starts beside the +x door
+    venue = venues.Venue.hall(40.0, 30.0, [(0, 0.0, 4.0), (1, 5.0, 3.0), (2, -8.0, 2.0), (3, 10.0, 6.0)],
+                              name="choice hall")
+    b, r, v0 = venues.spawn_lattice(40, 40, spacing=0.5, center=(10.0, 3.0), jitter=0.05, seed=5)
+    return venue, b, r, v0
+
+
+def _small_bowl():
+    from swarm_gb300 import venues
+    spec = venues.bowl_spec(sectors=8, rows=8, seats=12, vomitory_row=4, perimeter_exits=2)
+    venue = venues.Venue.bowl(spec, "small bowl")
+    b, r, v0 = venues.spawn_bowl(spec, seed=2)
+    return venue, b, r, v0
+
+
+@pytest.fixture(scope="module")
+def hall(built):
+    from swarm_gb300 import venues
+    venue, b, r, v0 = _hall()
+    return venue, b, r, v0, venues.exit_fields(venue)
+
+
+@pytest.fixture(scope="module")
+def bowl(built):
+    from swarm_gb300 import venues
+    venue, b, r, v0 = _small_bowl()
+    return venue, b, r, v0, venues.exit_fields(venue)
+
+
+def _oracle(P, venue, b, r, v0, fields, widths, types, K=24):
+    import swarm_gb300
+    ex, di = swarm_gb300.exit_choice_table(venue, fields, widths, types, K)
+    ora = O.OracleSim(P, venue.struct)
+    ora.set_state(b)
+    ora.set_agent_params(r, v0)
+    ora.set_exit_choice(fields, swarm_gb300.exit_inv_capacity(widths), ex, di)
+    return ora
+
+
+def test_exit_fields_agree_with_the_nearest_exit_field(hall, bowl):
+    """Inside the venue the nearest exit's distance is the least of the exits' own distances (to the solver's
+    rounding where one exit's opening lies on a path to another)."""
+    for venue, *_, (fields, widths, types) in (hall, bowl):
+        v = venue.struct
+        nav = venue.arrays["nav"]
+        reach = fields < fields.max(axis=1, keepdims=True)
+        least = np.where(reach, fields, np.inf).min(axis=0)
+        both = reach.any(axis=0) & (nav < nav.max())
+        X = v.nav_origin_x + (np.arange(nav.size) % v.nav_nx) * v.nav_h
+        Y = v.nav_origin_y + (np.arange(nav.size) // v.nav_nx) * v.nav_h
+        if "spec" in venue.meta and hasattr(venue.meta["spec"], "n_doors"):
+            both &= (np.abs(X) < 20.0) & (np.abs(Y) < 15.0)   # the hall's interior
+        assert both.sum() > 10000
+        assert np.abs(least[both] - nav[both]).max() < 0.1
+        assert (fields.min(axis=1) == 0.0).all(), "every exit has sources"
+
+
+def test_candidate_table_rules(bowl):
+    """Ascending distances, distinct exits, the type rule (2 avenues and a door first, where reachable)."""
+    import swarm_gb300
+    venue, _, _, _, (fields, widths, types) = bowl
+    ex, di = swarm_gb300.exit_choice_table(venue, fields, widths, types, 6)
+    full = ex[:, 0] != EMPTY
+    assert full.sum() > 1000
+    for row_e, row_d in zip(ex[full], di[full]):
+        k = int((row_e != EMPTY).sum())
+        assert (row_e[:k] != EMPTY).all() and (row_e[k:] == EMPTY).all()
+        assert len(set(row_e[:k].tolist())) == k
+        assert (np.diff(row_d[:k]) >= 0).all()
+    # cells that reach every exit hold 2 vomitories (type 0) and 1 perimeter door (type 1) among 6 candidates
+    allreach = (ex != EMPTY).sum(axis=1) == 6
+    t = types[np.where(ex[allreach] == EMPTY, 0, ex[allreach])]
+    assert ((t == 0).sum(axis=1) >= 2).all() and ((t == 1).sum(axis=1) >= 1).all()
+
+
+def test_oracle_choice_assigns_switches_and_is_deterministic(hall):
+    import swarm_gb300
+    venue, b, r, v0, (fields, widths, types) = hall
+    P = swarm_gb300.params_si()
+    runs = []
+    for _ in range(2):
+        ora = _oracle(P, venue, b, r, v0, fields, widths, types)
+        ora.step(1)
+        a, c = ora.exit_choice()
+        active = ora.state()[:, 3] != 0
+        assert (a[active] != NONE).all(), "every agent holds an exit after its first step"
+        ora.step(239)   # four evaluations (every 60 steps at dt 0.05 s)
+        a, c = ora.exit_choice()
+        runs.append((ora.state().copy(), a.copy(), c.copy()))
+    (s0, a0, c0), (s1, a1, c1) = runs
+    assert np.array_equal(s0.view(np.uint32), s1.view(np.uint32)) and np.array_equal(a0, a1) and np.array_equal(c0, c1)
+    assert c0[0] > 0 and c0[2] > 0, f"evaluations and switches happen (counters {c0})"
+    used = set(a0[s0[:, 3] != 0].tolist())
+    assert len(used) >= 2, "the queue at the nearest door sends agents to others"
+
+
+def _pair(P, venue, b, r, v0, fields, widths, types):
+    import swarm_gb300
+    sim = swarm_gb300.CrowdSim(P, venue, b.shape[0])
+    sim.set_state(b)
+    sim.set_agent_params(r, v0)
+    sim.set_exit_choice(fields, widths, types)
+    ora = _oracle(P, venue, b, r, v0, fields, widths, types)
+    return sim, ora
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["hall", "bowl"])
+def test_exit_choice_gpu_vs_oracle(case, hall, bowl):
+    """Bit for bit, every 20 steps over 300 (five evaluations): states, assigned exits and counters."""
+    import swarm_gb300
+    venue, b, r, v0, (fields, widths, types) = hall if case == "hall" else bowl
+    P = swarm_gb300.params_si()
+    sim, ora = _pair(P, venue, b, r, v0, fields, widths, types)
+    for k in range(15):
+        sim.step(20)
+        ora.step(20)
+        assert np.array_equal(sim.state().view(np.uint32), ora.state().view(np.uint32)), f"after {20 * (k + 1)} steps"
+        ga, gc = sim.exit_choice()
+        oa, oc = ora.exit_choice()
+        assert np.array_equal(ga, oa) and np.array_equal(gc, oc), f"choice after {20 * (k + 1)} steps"
+    assert gc[2] > 0 or case == "bowl"
+    sim.close()
+
+
+@pytest.mark.gpu
+def test_exit_choice_per_phase_path_and_restart(hall):
+    """The per-phase kernels give the same bits as the fused step; a state upload restarts the choice."""
+    import swarm_gb300
+    venue, b, r, v0, (fields, widths, types) = hall
+    P = swarm_gb300.params_si()
+    out = []
+    for fused in (True, False):
+        sim = swarm_gb300.CrowdSim(P, venue, b.shape[0])
+        sim.set_agent_params(r, v0)
+        sim.set_fused(fused)
+        sim.set_exit_choice(fields, widths, types)
+        sim.set_state(b)
+        sim.step(130)
+        out.append((sim.state().copy(), sim.exit_choice()[0].copy()))
+        sim.set_state(b)   # restart: nothing assigned until the next step
+        assert (sim.exit_choice()[0] == NONE).all()
+        sim.close()
+    assert np.array_equal(out[0][0].view(np.uint32), out[1][0].view(np.uint32)) and np.array_equal(out[0][1], out[1][1])
