@@ -222,7 +222,46 @@ def bench_bowl(P, steps=50, warmup=5, cap=20000, chunk=100):
     wall_s = time.perf_counter() - t0
     out999 = np.nonzero(active <= n // 1000)[0]
     t999 = int(out999[0]) + 1 if out999.size else None
+    # the queue-aware exit choice: the 40 exits' own fields (GPU solver), then the step with the choice pass (same
+    # per-step timing) and the evacuation
+    prev = swarm_gb300.set_nav_solver("gpu")
+    t0 = time.perf_counter()
+    fields, widths, types = venues.exit_fields(venue)
+    fields_s = time.perf_counter() - t0
+    swarm_gb300.set_nav_solver(prev)
+    sim.set_exit_choice(fields, widths, types)
+    del fields
+    sim.set_state(boids)
+    with torch.cuda.stream(stream):
+        sim.step(warmup)
+    torch.cuda.synchronize()
+    qa_active, qa_ms = 0, 0.0
+    for k in range(steps):
+        qa_active += int((sim.state()[:, 3] != 0).sum())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xFF)
+            e0.record(stream)
+            sim.step(1)
+            e1.record(stream)
+        stream.synchronize()
+        qa_ms += e0.elapsed_time(e1)
+    sim.set_state(boids)
+    t0 = time.perf_counter()
+    qev, qactive = sim.run_evacuation(cap)
+    qwall_s = time.perf_counter() - t0
+    q999 = np.nonzero(qactive <= n // 1000)[0]
+    qt999 = int(q999[0]) + 1 if q999.size else None
+    _, counters = sim.exit_choice()
     sim.close()
+    queue_aware = {"exits": int(widths.shape[0]), "fields_s": fields_s,
+                   "value": qa_active / (qa_ms * 1e-3), "unit": UNIT, "ms_per_step": qa_ms / steps,
+                   "evacuation": {"t50_s": qev["t50_s"], "t90_s": qev["t90_s"], "t100_s": qev["t100_s"],
+                                  "steps_to_99.9pct": qt999,
+                                  "seconds_to_99.9pct": None if qt999 is None else qt999 * float(P.dt),
+                                  "left_after": {"steps": qev["steps"], "agents": qev["remaining"]}, "wall_s": qwall_s,
+                                  "counters": {"evaluations": int(counters[0]), "eligible": int(counters[1]),
+                                               "switches": int(counters[2]), "forced": int(counters[3])}}}
     return {"workload": "seated bowl, 32 sectors x 32 rows x 62 seats (63488 agents), seat 0.5 m, row pitch 0.8 m, "
                         "rise 0.4 m, 1.2 m gangway stairs (speed factor 0.6), 2.4 m vomitories at row 16, 8 perimeter "
                         "exits of 4 m; wall SDF 0.05 m, nav 0.1 m",
@@ -232,6 +271,7 @@ def bench_bowl(P, steps=50, warmup=5, cap=20000, chunk=100):
                            "steps_to_99.9pct": t999, "seconds_to_99.9pct": None if t999 is None else t999 * float(P.dt),
                            "left_after": {"steps": ev["steps"], "agents": ev["remaining"]}, "wall_s": wall_s,
                            "path": "swarm_run_evacuation (C ABI)"},
+            "queue_aware_exit_choice": queue_aware,
             "nav_field": bench_nav_field(venue)}
 
 
