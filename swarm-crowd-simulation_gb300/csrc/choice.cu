@@ -187,37 +187,53 @@ __global__ void k_choice_thr(ChoiceArgs C) {
     for (int b = 0; b < CHOICE_GAIN_BINS; ++b) h[b] = 0u;
 }
 
-// Stage 0: nav::apply (src/exit_choice.cpp:642-658) and the agent's counts for the next step
+// Stage 0: nav::apply (src/exit_choice.cpp:642-658) and the agent's counts for the next step. The counts are sums of
+// ones, aggregated before they reach global memory (the exit counts per block in shared memory, the queue-ahead bins
+// per warp): the same integers, a few atomics per block instead of one per agent on ~40 addresses.
 __global__ void __launch_bounds__(256) k_choice_apply(ChoiceArgs C) {
+    __shared__ uint32_t sQueue[CHOICE_STRIDE];
+    if (threadIdx.x < CHOICE_STRIDE) sQueue[threadIdx.x] = 0u;
+    __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= C.n) return;
-    const long long r = choiceRow(C, i);
-    if (r < 0) return;
-    const size_t row = size_t(r);
     const uint32_t par = C.step & 1u;
-    const uint32_t* aRead = C.ahead + size_t(par) * CHOICE_STRIDE * CHOICE_AHEAD_BINS;
-    uint32_t* aWrite = C.ahead + size_t(1u - par) * CHOICE_STRIDE * CHOICE_AHEAD_BINS;
-    const uint32_t cur = C.assign[i];
-    uint32_t ex = cur;
-    const bool hasPath = C.cExit[row] != SWARM_CHOICE_EMPTY;
-    const int curK = hasPath ? slotOf(C, row, cur) : -1;
-    if (hasPath && curK < 0) {   // forced (or the first choice)
-        float eBest;
-        ex = C.cExit[row + size_t(bestCandidate(C, row, aRead, eBest))];
-        if (cur != SWARM_CHOICE_NONE) atomicAdd(C.counters + 3, 1u);
-    } else if (C.evalStep && curK >= 0) {
-        const uint2 pd = C.pending[i];
-        if (pd.x != SWARM_CHOICE_NONE && pd.y >= C.threshold[cur]) {
-            ex = pd.x;
-            atomicAdd(C.counters + 2, 1u);
+    uint32_t aheadKey = 0xFFFFFFFFu;   // exit x CHOICE_AHEAD_BINS + bin of this agent's count (none: all ones)
+    const long long r = i < C.n ? choiceRow(C, i) : -1;
+    if (r >= 0) {
+        const size_t row = size_t(r);
+        const uint32_t* aRead = C.ahead + size_t(par) * CHOICE_STRIDE * CHOICE_AHEAD_BINS;
+        const uint32_t cur = C.assign[i];
+        uint32_t ex = cur;
+        const bool hasPath = C.cExit[row] != SWARM_CHOICE_EMPTY;
+        const int curK = hasPath ? slotOf(C, row, cur) : -1;
+        if (hasPath && curK < 0) {   // forced (or the first choice)
+            float eBest;
+            ex = C.cExit[row + size_t(bestCandidate(C, row, aRead, eBest))];
+            if (cur != SWARM_CHOICE_NONE) atomicAdd(C.counters + 3, 1u);
+        } else if (C.evalStep && curK >= 0) {
+            const uint2 pd = C.pending[i];
+            if (pd.x != SWARM_CHOICE_NONE && pd.y >= C.threshold[cur]) {
+                ex = pd.x;
+                atomicAdd(C.counters + 2, 1u);
+            }
+        }
+        C.assign[i] = ex;
+        if (ex != SWARM_CHOICE_NONE) {
+            atomicAdd(sQueue + ex, 1u);
+            const int k = slotOf(C, row, ex);
+            if (k >= 0) aheadKey = ex * uint32_t(CHOICE_AHEAD_BINS) + aheadBin(C.cDist[row + size_t(k)]);
         }
     }
-    C.assign[i] = ex;
-    if (ex != SWARM_CHOICE_NONE) {
-        atomicAdd(C.queue + (1u - par) * CHOICE_STRIDE + ex, 1u);
-        const int k = slotOf(C, row, ex);
-        if (k >= 0) atomicAdd(aWrite + size_t(ex) * CHOICE_AHEAD_BINS + aheadBin(C.cDist[row + size_t(k)]), 1u);
+    // the queue-ahead count: one atomic per distinct (exit, bin) in the warp
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned valid = __ballot_sync(0xffffffffu, aheadKey != 0xFFFFFFFFu);
+    if (aheadKey != 0xFFFFFFFFu) {
+        const unsigned peers = __match_any_sync(valid, aheadKey);
+        if (int(lane) == __ffs(peers) - 1)
+            atomicAdd(C.ahead + size_t(1u - par) * CHOICE_STRIDE * CHOICE_AHEAD_BINS + aheadKey, uint32_t(__popc(peers)));
     }
+    __syncthreads();
+    if (threadIdx.x < CHOICE_STRIDE && sQueue[threadIdx.x])
+        atomicAdd(C.queue + (1u - par) * CHOICE_STRIDE + threadIdx.x, sQueue[threadIdx.x]);
 }
 
 }  // namespace swarm_gpu
