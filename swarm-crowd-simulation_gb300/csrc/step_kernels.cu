@@ -874,7 +874,35 @@ __global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREA
     }
     stamp(A, 3);
     const int allTiles = (n + T - 1) / T;
-    for (int t = blockIdx.x; t < allTiles; t += gridDim.x) {
+    // Blocks that hold several tiles (a batch) run the final pass without tile windows: a window's staging and its two
+    // block barriers per tile cost more there than reading the neighbours from L2 (warp-aligned slots: the next step's
+    // count is warp-collective)
+    const bool tileless = !kTape && activeTiles > int(gridDim.x);
+    if (tileless) {
+        const float4* src = A.proj[in];
+        for (int base = tid - int(threadIdx.x & 31u); base < n; base += stride) {
+            const int s = base + int(threadIdx.x & 31u);
+            const bool own = s < nActive;
+            float4 b = own ? src[s] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            uint32_t nextKey = INACTIVE_CELL;
+            if (own) {
+                const VenueArgs& V = venueOfSlot<kB>(A, s);
+                const Venue ven{A.P, V};
+                if (A.projectInFinal && b.w >= 0.0f) {
+                    const uint4 ra = A.rowsA[s];
+                    const uint2 rb = A.rowsB[s];
+                    const uint32_t rk0[3] = {ra.x, ra.z, rb.x}, rk1[3] = {ra.y, ra.w, rb.y};
+                    const float ri = kUniform ? A.P.body_radius : A.prm[s].x;
+                    b = projectCore<Venue, GlobalNbr, false>(A, ven, b, s, ri, rk0, rk1, A.plane[s], GlobalNbr{src, A.prm});
+                }
+                nextKey = finalActive(A, V, ven, s, b);
+            } else if (s < n) {
+                finalInactive(A, s);
+            }
+            if (A.hashNext) countKey<true>(A, s < n ? A.sid[s] : 0u, nextKey, s < n);
+        }
+    }
+    for (int t = blockIdx.x; !tileless && t < allTiles; t += gridDim.x) {
         const int s = t * T + int(threadIdx.x);
         float4 b;
         bool own;
