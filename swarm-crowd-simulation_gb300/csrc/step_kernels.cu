@@ -863,7 +863,21 @@ __global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREA
         const float4* src = kTape ? A.proj[0] + size_t(it - 1) * size_t(n) : A.proj[in];
         float4* dst = kTape ? A.proj[0] + size_t(it) * size_t(n) : A.proj[in ^ 1];
         float4* corr = kTape ? A.tapeCorr + size_t(it - 1) * size_t(n) : nullptr;
-        for (int t = blockIdx.x; t < activeTiles; t += gridDim.x) {
+        if (!kTape && activeTiles > int(gridDim.x)) {   // several tiles per block: neighbours from L2, no windows
+            for (int s = tid; s < nActive; s += stride) {
+                float4 b = src[s];
+                if (b.w >= 0.0f) {
+                    const uint4 ra = A.rowsA[s];
+                    const uint2 rb = A.rowsB[s];
+                    const uint32_t rk0[3] = {ra.x, ra.z, rb.x}, rk1[3] = {ra.y, ra.w, rb.y};
+                    const float ri = kUniform ? A.P.body_radius : A.prm[s].x;
+                    const Venue ven{A.P, venueOfSlot<kB>(A, s)};
+                    b = projectCore<Venue, GlobalNbr, false>(A, ven, b, s, ri, rk0, rk1, A.plane[s], GlobalNbr{src, A.prm});
+                }
+                dst[s] = b;
+            }
+        }
+        for (int t = blockIdx.x; (kTape || activeTiles <= int(gridDim.x)) && t < activeTiles; t += gridDim.x) {
             float4 r;
             bool own;
             sweepTile(t, src, r, own, corr);
