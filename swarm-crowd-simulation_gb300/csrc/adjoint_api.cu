@@ -50,7 +50,6 @@ struct SwarmAdjoint {
     unsigned long long* stamps = nullptr;   // the fused reverse's phase spans
     uint4* rowsA = nullptr;
     uint2* rowsB = nullptr;
-    uint2* tileWin = nullptr;
     float4* proj[2] = {nullptr, nullptr};
     // reverse
     float4* lamX[2] = {nullptr, nullptr};
@@ -110,7 +109,7 @@ SwarmAdjoint* makeAdjoint(SwarmSim* h, int n, int K, int ckpt, int nseg, int ste
         a->alloc(&a->key, N) && a->alloc(&a->rank, N) && a->alloc(&a->count, NC) && a->alloc(&a->sidTmp, N) &&
         a->alloc(&a->tileSums, size_t(h->ncells) / 1024 + 2) && a->alloc(&a->cells, NC) && a->alloc(&a->contacts, N) &&
         a->alloc(&a->err, 1) && a->alloc(&a->barrier, 8) && a->alloc(&a->stamps, 8) && a->alloc(&a->rowsA, N) && a->alloc(&a->rowsB, N) &&
-        a->alloc(&a->tileWin, N / 64 + 2) && a->alloc(&a->proj[0], N) && a->alloc(&a->proj[1], N) &&
+        a->alloc(&a->proj[0], N) && a->alloc(&a->proj[1], N) &&
         a->alloc(&a->lamX[0], 2 * N) && a->alloc(&a->lamX[1], 2 * N) && a->alloc(&a->lamQ, N) && a->alloc(&a->lamPlane, N) &&
         a->alloc(&a->lamNv, N) && a->alloc(&a->lamPOld, N) && a->alloc(&a->lamSep, N) && a->alloc(&a->lamP, N) &&
         a->alloc(&a->lamV, N) && a->alloc(&a->lamC[0], N) && a->alloc(&a->lamC[1], N) && a->alloc(&a->lamR, N) &&
@@ -147,7 +146,7 @@ StepArgs forwardArgs(const SwarmSim* h, const SwarmAdjoint* a, int in, int j) {
     A.ctc = a->tapeCtc + size_t(j) * N;
     A.proj[0] = a->proj[0];
     A.proj[1] = a->proj[1];
-    A.rowsA = a->rowsA; A.rowsB = a->rowsB; A.tileWin = a->tileWin;
+    A.rowsA = a->rowsA; A.rowsB = a->rowsB;
     A.err = a->err;
     A.barrier = a->barrier;
     A.barrierExtra = 0;

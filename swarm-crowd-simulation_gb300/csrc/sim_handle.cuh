@@ -39,7 +39,6 @@ struct SwarmSim {
     uint8_t* ctc = nullptr;
     uint4* rowsA = nullptr;
     uint2* rowsB = nullptr;
-    uint2* tileWin = nullptr;
     float2* goal = nullptr;
     int* errFlag = nullptr;
     unsigned* barrier = nullptr;

@@ -80,7 +80,6 @@ struct StepArgs {
     uint8_t* ctc;           // the predict pass's contact bits
     uint4* rowsA;           // fused step: each slot's 3 x 3 neighbour rows (row 0 and row 1 ranges)
     uint2* rowsB;           //   (row 2 range)
-    uint2* tileWin;         //   each tile's neighbour window [lo, hi) in slots
     float2* goal;           // fused step: each active slot's e_goal, from the gather phase (predict's window reads it)
     int* err;
     unsigned* barrier;      // the fused kernel's grid barrier: arrival counter, generation

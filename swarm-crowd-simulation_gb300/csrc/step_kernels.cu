@@ -492,19 +492,12 @@ __global__ void __launch_bounds__(128) k_predict(StepArgs A) {
     if (s < A.n) predictItem<Venue, kB, kTape>(A, s);
 }
 
-// Where a sweep reads its neighbours: global memory, or a tile's window of slots staged in shared memory
+// Where a sweep reads its neighbours: the slot buffers in global memory (L2, and L1 for a block's reuse)
 struct GlobalNbr {
     const float4* in;
     const float2* prm;
     __device__ __forceinline__ float4 pos(uint32_t k) const { return in[k]; }
     __device__ __forceinline__ float r(uint32_t k) const { return prm[k].x; }
-};
-struct WindowNbr {
-    const float4* pos_;
-    const float* r_;
-    uint32_t lo;
-    __device__ __forceinline__ float4 pos(uint32_t k) const { return pos_[k - lo]; }
-    __device__ __forceinline__ float r(uint32_t k) const { return r_[k - lo]; }
 };
 
 // The 3 x 3 neighbour rows of slot s: slot ranges [rk0[j], rk1[j]) for the rows cy - 1 .. cy + 1
@@ -715,28 +708,18 @@ __device__ __forceinline__ bool gridBarrier(const StepArgs& A, unsigned expected
     return leave == 0;
 }
 
-// The sweeps' neighbour data for the fused kernel, once per step: each active slot's 3 x 3 rows, and each tile of
-// FUSED_THREADS slots' window [lo, hi) -- every slot any of its slots can read (cells c - resX - 1 .. c + resX + 1 of
-// its first and last cells), a contiguous range in key order.
+// The sweeps' neighbour rows for the fused kernel, once per step: each active slot's 3 x 3 rows as slot ranges
 template <bool kB>
-__device__ __forceinline__ void prepareSweepItem(const StepArgs& A, int s, int nActive, int tile) {
+__device__ __forceinline__ void prepareSweepItem(const StepArgs& A, int s) {
     const uint32_t cid = A.skey[s];
     const VenueArgs& V = venueOfSlot<kB>(A, s);
     uint32_t rk0[3], rk1[3];
     sweepRows(A, V, cid, rk0, rk1);
     A.rowsA[s] = make_uint4(rk0[0], rk1[0], rk0[1], rk1[1]);
     A.rowsB[s] = make_uint2(rk0[2], rk1[2]);
-    if (s % tile == 0) {
-        // (a tile spanning instances: each slot's rows lie inside its own instance's cells, within these bounds)
-        const int last = min(s + tile, nActive) - 1;
-        const int ncells = A.V.ncells;
-        const int c0 = int(cid), c1 = int(A.skey[last]);
-        const int res0 = V.resX, res1 = venueOfSlot<kB>(A, last).resX;
-        A.tileWin[s / tile] = make_uint2(A.start[max(c0 - res0 - 1, 0)], A.start[min(c1 + res1 + 2, ncells)]);
-    }
 }
 
-constexpr int WIN_CAP = 4096;   // slots a tile window may hold in shared memory (96 KB); larger windows read global memory
+constexpr int WIN_CAP = 4096;   // slots predict's perception window may hold in shared memory (128 KB); larger windows read global memory
 
 // The perception window of tile t (its active slots [t T, min((t + 1) T, nActive))): every slot within perc_ring cell
 // rows and columns of its first and last cells, a contiguous range in key order; (0, 0) for a tile with no active slot.
@@ -816,84 +799,40 @@ __global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREA
         if (s < n) {
             if (useWin) predictCore<Venue, kB, kTape>(A, s, PredWindow{smPos, smR, smSid, smGoal, A.P, win.x});
             else predictCore<Venue, kB, kTape>(A, s, PredGlobal{A});
-            if (s < nActive) prepareSweepItem<kB>(A, s, nActive, T);
+            if (s < nActive) prepareSweepItem<kB>(A, s);
         }
         __syncthreads();   // the window is reused by the next tile
     }
     if (!gridBarrier(A, gridDim.x)) return;
     stamp(A, 2);
     const int K = A.P.proj_iterations;
-    const int activeTiles = (nActive + T - 1) / T;
-    // one sweep (or the final pass) over tile t: stage its window, then each slot reads its neighbours from it
-    auto sweepTile = [&](int t, const float4* in, float4& result, bool& own, float4* corrOut) {
-        const int s = t * T + int(threadIdx.x);
-        own = s < nActive;
-        const uint2 win = t < activeTiles ? A.tileWin[t] : make_uint2(0u, 0u);
-        const bool useWin = win.y - win.x <= uint32_t(WIN_CAP);
-        float4 b = make_float4(0.0f, 0.0f, 0.0f, 0.0f), plane = b;
-        uint4 ra = make_uint4(0u, 0u, 0u, 0u);
-        uint2 rb = make_uint2(0u, 0u);
-        float ri = A.P.body_radius;
-        if (own) {
-            b = in[s];
-            ra = A.rowsA[s];
-            rb = A.rowsB[s];
-            plane = A.plane[s];
-            if (!kUniform) ri = A.prm[s].x;
-        }
-        if (useWin) {
-            for (uint32_t k = win.x + threadIdx.x; k < win.y; k += blockDim.x) {
-                smPos[k - win.x] = in[k];
-                if (!kUniform) smR[k - win.x] = A.prm[k].x;
-            }
-        }
-        __syncthreads();
-        if (own && b.w >= 0.0f) {
-            const Venue ven{A.P, venueOfSlot<kB>(A, s)};
-            const uint32_t rk0[3] = {ra.x, ra.z, rb.x}, rk1[3] = {ra.y, ra.w, rb.y};
-            float4* co = kTape ? corrOut + s : nullptr;
-            b = useWin ? projectCore<Venue, WindowNbr, kTape>(A, ven, b, s, ri, rk0, rk1, plane, WindowNbr{smPos, smR, win.x}, co)
-                       : projectCore<Venue, GlobalNbr, kTape>(A, ven, b, s, ri, rk0, rk1, plane, GlobalNbr{in, A.prm}, co);
-        }
-        result = b;
-        __syncthreads();   // the window is reused by the next tile
-    };
     int in = 0;
     for (int it = 1; it < K; ++it) {
         const float4* src = kTape ? A.proj[0] + size_t(it - 1) * size_t(n) : A.proj[in];
         float4* dst = kTape ? A.proj[0] + size_t(it) * size_t(n) : A.proj[in ^ 1];
         float4* corr = kTape ? A.tapeCorr + size_t(it - 1) * size_t(n) : nullptr;
-        if (!kTape && activeTiles > int(gridDim.x)) {   // several tiles per block: neighbours from L2, no windows
-            for (int s = tid; s < nActive; s += stride) {
-                float4 b = src[s];
-                if (b.w >= 0.0f) {
-                    const uint4 ra = A.rowsA[s];
-                    const uint2 rb = A.rowsB[s];
-                    const uint32_t rk0[3] = {ra.x, ra.z, rb.x}, rk1[3] = {ra.y, ra.w, rb.y};
-                    const float ri = kUniform ? A.P.body_radius : A.prm[s].x;
-                    const Venue ven{A.P, venueOfSlot<kB>(A, s)};
-                    b = projectCore<Venue, GlobalNbr, false>(A, ven, b, s, ri, rk0, rk1, A.plane[s], GlobalNbr{src, A.prm});
-                }
-                dst[s] = b;
+        // The sweeps read their neighbours straight from L2 (and L1, which catches a block's reuse): staging a
+        // tile window in shared memory and its two block barriers cost more than they save
+        for (int s = tid; s < nActive; s += stride) {
+            float4 b = src[s];
+            if (b.w >= 0.0f) {
+                const uint4 ra = A.rowsA[s];
+                const uint2 rb = A.rowsB[s];
+                const uint32_t rk0[3] = {ra.x, ra.z, rb.x}, rk1[3] = {ra.y, ra.w, rb.y};
+                const float ri = kUniform ? A.P.body_radius : A.prm[s].x;
+                const Venue ven{A.P, venueOfSlot<kB>(A, s)};
+                b = projectCore<Venue, GlobalNbr, kTape>(A, ven, b, s, ri, rk0, rk1, A.plane[s], GlobalNbr{src, A.prm},
+                                                         kTape ? corr + s : nullptr);
             }
-        }
-        for (int t = blockIdx.x; (kTape || activeTiles <= int(gridDim.x)) && t < activeTiles; t += gridDim.x) {
-            float4 r;
-            bool own;
-            sweepTile(t, src, r, own, corr);
-            if (own) dst[t * T + int(threadIdx.x)] = r;
+            dst[s] = b;
         }
         in ^= 1;
         if (!gridBarrier(A, gridDim.x)) return;
     }
     stamp(A, 3);
-    const int allTiles = (n + T - 1) / T;
-    // Blocks that hold several tiles (a batch) run the final pass without tile windows: a window's staging and its two
-    // block barriers per tile cost more there than reading the neighbours from L2 (warp-aligned slots: the next step's
-    // count is warp-collective)
-    const bool tileless = !kTape && activeTiles > int(gridDim.x);
-    if (tileless) {
-        const float4* src = A.proj[in];
+    // The final pass reads its neighbours from L2 too (warp-aligned slots: the next step's count is warp-collective)
+    {
+        const float4* src = kTape ? A.proj[0] + size_t(K > 0 ? K - 1 : 0) * size_t(n) : A.proj[in];
         for (int base = tid - int(threadIdx.x & 31u); base < n; base += stride) {
             const int s = base + int(threadIdx.x & 31u);
             const bool own = s < nActive;
@@ -907,31 +846,16 @@ __global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREA
                     const uint2 rb = A.rowsB[s];
                     const uint32_t rk0[3] = {ra.x, ra.z, rb.x}, rk1[3] = {ra.y, ra.w, rb.y};
                     const float ri = kUniform ? A.P.body_radius : A.prm[s].x;
-                    b = projectCore<Venue, GlobalNbr, false>(A, ven, b, s, ri, rk0, rk1, A.plane[s], GlobalNbr{src, A.prm});
+                    b = projectCore<Venue, GlobalNbr, kTape>(A, ven, b, s, ri, rk0, rk1, A.plane[s], GlobalNbr{src, A.prm},
+                                                             kTape && K > 0 ? A.tapeCorr + size_t(K - 1) * size_t(n) + s : nullptr);
                 }
+                if (kTape) A.tapeQK[s] = b;
                 nextKey = finalActive(A, V, ven, s, b);
             } else if (s < n) {
                 finalInactive(A, s);
             }
             if (A.hashNext) countKey<true>(A, s < n ? A.sid[s] : 0u, nextKey, s < n);
         }
-    }
-    for (int t = blockIdx.x; !tileless && t < allTiles; t += gridDim.x) {
-        const int s = t * T + int(threadIdx.x);
-        float4 b;
-        bool own;
-        const float4* src = kTape ? A.proj[0] + size_t(K > 0 ? K - 1 : 0) * size_t(n) : A.proj[in];
-        if (A.projectInFinal) sweepTile(t, src, b, own, kTape && K > 0 ? A.tapeCorr + size_t(K - 1) * size_t(n) : nullptr);
-        else { own = s < nActive; b = own ? src[s] : make_float4(0.0f, 0.0f, 0.0f, 0.0f); }
-        uint32_t nextKey = INACTIVE_CELL;
-        if (kTape && own) A.tapeQK[s] = b;
-        if (own) {
-            const VenueArgs& V = venueOfSlot<kB>(A, s);
-            nextKey = finalActive(A, V, Venue{A.P, V}, s, b);
-        }
-        else if (s < n) finalInactive(A, s);
-        // the next step's hash, counted here (all lanes of the warp together)
-        if (A.hashNext) countKey<true>(A, s < n ? A.sid[s] : 0u, nextKey, s < n);
     }
     // The caller's host buffer: the finished state in agent order, copied in order after the last barrier (coalesced
     // 16-byte stores over the host link; the final pass's own writes go to agents in slot order, scattered)

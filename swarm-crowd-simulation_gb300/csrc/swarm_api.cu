@@ -78,7 +78,7 @@ StepArgs SwarmSim::args(int in) const {
     A.key = key; A.rank = rank; A.count = count; A.start = start; A.cells = cells; A.tileSums = tileSums;
     A.sidTmp = sidTmp; A.sid = sid; A.skey = skey;
     A.pos0 = pos0; A.vel0 = vel0; A.prm = prm; A.proj[0] = proj0; A.proj[1] = proj1;
-    A.vel1 = vel1; A.plane = plane; A.ctc = ctc; A.rowsA = rowsA; A.rowsB = rowsB; A.tileWin = tileWin; A.goal = goal; A.err = errFlag; A.barrier = barrier; A.barrierExtra = barrierExtra;
+    A.vel1 = vel1; A.plane = plane; A.ctc = ctc; A.rowsA = rowsA; A.rowsB = rowsB; A.goal = goal; A.err = errFlag; A.barrier = barrier; A.barrierExtra = barrierExtra;
     A.stamps = timing ? stamps : nullptr;
     A.choiceAssign = choiceExits ? dAssign : nullptr;
     A.exitFields = dExitFields;
@@ -170,7 +170,7 @@ int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capac
               devAlloc(h, &h->skey, N) && devAlloc(h, &h->pos0, N) && devAlloc(h, &h->vel0, N) && devAlloc(h, &h->proj0, N) &&
               devAlloc(h, &h->proj1, N) && devAlloc(h, &h->vel1, N) && devAlloc(h, &h->plane, N) && devAlloc(h, &h->prm, N) &&
               devAlloc(h, &h->ctc, N) && devAlloc(h, &h->rowsA, N) && devAlloc(h, &h->rowsB, N) &&
-              devAlloc(h, &h->tileWin, N / 64 + 2) && devAlloc(h, &h->goal, N) && devAlloc(h, &h->errFlag, 1) && devAlloc(h, &h->barrier, 4) && devAlloc(h, &h->stamps, 8);
+              devAlloc(h, &h->goal, N) && devAlloc(h, &h->errFlag, 1) && devAlloc(h, &h->barrier, 4) && devAlloc(h, &h->stamps, 8);
     if (ok && V.kind == SWARM_VENUE_STADIUM) {
         const size_t nv = size_t(V.sdf_res) * size_t(V.sdf_res) * size_t(V.sdf_res);
         ok = devAlloc(h, &h->dSdf, nv) && cudaMemcpy(h->dSdf, V.sdf, nv * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
