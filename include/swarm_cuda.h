@@ -177,8 +177,8 @@ int swarm_step(SwarmHandle h, int steps);
 /* One call for callers holding the state in host memory: in_boids (n x 8 floats) into the device state, `steps`
  * steps, the result into out_boids, and waits for it. With pinned (page-locked, device-mapped) buffers and the fused
  * step there are no copy operations: the first step's hash phase reads in_boids over the coherent host link, and the
- * last step's kernel ends by writing its result into out_boids (the device state holds it too); otherwise one copy
- * each way. in_boids may equal out_boids. */
+ * last step's kernel ends by writing its result into out_boids (the device state holds it too); otherwise (or with
+ * the exit choice on) one copy each way. in_boids may equal out_boids. */
 int swarm_step_host(SwarmHandle h, const float* in_boids, float* out_boids, int n, int steps);
 /* CpuCrowdSim::setProjectionIterations / CrowdSim::setProjectionIterations (src/crowd_sim.cpp:480-483). */
 int swarm_set_iterations(SwarmHandle h, int k);

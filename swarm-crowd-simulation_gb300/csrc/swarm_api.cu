@@ -707,10 +707,11 @@ int swarm_step_host(SwarmHandle h, const float* in_boids, float* out_boids, int 
     const size_t bytes = size_t(n) * 32;
     // Pinned host buffers on the fused path: no copy operations. The first step's hash phase reads the input over the
     // coherent host link (into the device half it steps from), and the last step ends with its blocks copying the
-    // result, in order, into the output. Pageable buffers, or the per-phase path: a copy each way.
+    // result, in order, into the output. Pageable buffers, the per-phase path, or the exit choice (whose pass runs
+    // before the kernel, on the device state): a copy each way.
     const float4* dIn = nullptr;
     float4* dOut = nullptr;
-    if (h->fused && steps > 0) {
+    if (h->fused && steps > 0 && !h->choiceExits) {
         cudaPointerAttributes ai{}, ao{};
         if (cudaPointerGetAttributes(&ai, in_boids) == cudaSuccess && ai.type == cudaMemoryTypeHost && ai.devicePointer &&
             cudaPointerGetAttributes(&ao, out_boids) == cudaSuccess && ao.type == cudaMemoryTypeHost && ao.devicePointer) {

@@ -156,3 +156,45 @@ def test_exit_choice_per_phase_path_and_restart(hall):
         assert (sim.exit_choice()[0] == NONE).all()
         sim.close()
     assert np.array_equal(out[0][0].view(np.uint32), out[1][0].view(np.uint32)) and np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.gpu
+def test_exit_choice_through_step_host(hall):
+    """swarm_step_host with the choice on (pinned buffers) gives the same bits as uploading and stepping."""
+    import torch
+    import swarm_gb300
+    venue, b, r, v0, (fields, widths, types) = hall
+    P = swarm_gb300.params_si()
+    out = []
+    for host in (False, True):
+        sim = swarm_gb300.CrowdSim(P, venue, b.shape[0])
+        sim.set_agent_params(r, v0)
+        sim.set_exit_choice(fields, widths, types)
+        if host:
+            h_in = torch.from_numpy(b.copy()).pin_memory()
+            h_out = torch.zeros_like(h_in).pin_memory()
+            sim.step_host(h_in.data_ptr(), h_out.data_ptr(), b.shape[0], 70)
+            out.append((h_out.numpy().copy(), sim.exit_choice()[0].copy()))
+        else:
+            sim.set_state(b)
+            sim.step(70)
+            out.append((sim.state().copy(), sim.exit_choice()[0].copy()))
+        sim.close()
+    assert np.array_equal(out[0][0].view(np.uint32), out[1][0].view(np.uint32)) and np.array_equal(out[0][1], out[1][1])
+
+
+
+@pytest.mark.gpu
+def test_exit_choice_evacuation_runner_rolls_back_the_choice(bowl):
+    """The runner stops at the exact step the crowd empties by replaying a chunk from a saved copy; the choice's
+    state is part of that copy, so its result equals the oracle stepped as many steps."""
+    import swarm_gb300
+    venue, b, r, v0, (fields, widths, types) = bowl
+    P = swarm_gb300.params_si()
+    sim, ora = _pair(P, venue, b, r, v0, fields, widths, types)
+    ev, active = sim.run_evacuation(4000)
+    assert ev["remaining"] == 0 and 0 < ev["steps"] < 4000
+    ora.step(ev["steps"])
+    assert np.array_equal(sim.state().view(np.uint32), ora.state().view(np.uint32))
+    assert np.array_equal(sim.exit_choice()[0], ora.exit_choice()[0])
+    sim.close()
