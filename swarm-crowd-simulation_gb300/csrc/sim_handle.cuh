@@ -70,6 +70,7 @@ struct SwarmSim {
     uint32_t* dInstSlot = nullptr;
     std::vector<int> instStart;   // first agent of each instance, + the total
     float *dSdf = nullptr, *dWall = nullptr, *dNav = nullptr, *dFloor = nullptr, *dSpeed = nullptr;
+    float2* dWallFloor = nullptr;   // the wall SDF and floor heights interleaved (venues with a floor grid)
     uint8_t* dMask = nullptr;
     float speedMax = 1.0f;      // the largest of 1 and the venue's speed factors
     int ncells = 0;

@@ -34,6 +34,7 @@ struct VenueArgs {
     int32_t nnx, nny;
     float nox, noy, ninv;
     const float* floorH;
+    const float2* wallFloor;    // optional: (wall SDF, floor height) per wall-grid node, one sector for both lookups
     const float* speedF;
     const uint8_t* exitMask;    // optional: nonzero at the nav nodes beyond an exit
     uint32_t cellOffset;    // batched instances: this instance's first cell in the shared key space (0 otherwise)

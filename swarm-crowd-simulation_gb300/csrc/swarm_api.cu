@@ -67,7 +67,7 @@ StepArgs SwarmSim::args(int in) const {
     v.winv = V.wall_h > 0.0f ? 1.0f / V.wall_h : 0.0f;
     v.nav = dNav; v.nnx = V.nav_nx; v.nny = V.nav_ny; v.nox = V.nav_origin_x; v.noy = V.nav_origin_y;
     v.ninv = V.nav_h > 0.0f ? 1.0f / V.nav_h : 0.0f;
-    v.floorH = dFloor; v.speedF = dSpeed; v.exitMask = dMask;
+    v.floorH = dFloor; v.speedF = dSpeed; v.exitMask = dMask; v.wallFloor = dWallFloor;
     A.n = n;
     A.projectInFinal = P.proj_iterations > 0 ? 1 : 0;
     A.stateIn = state[in];
@@ -179,8 +179,13 @@ int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capac
         const size_t nw = size_t(V.wall_nx) * size_t(V.wall_ny), nn = size_t(V.nav_nx) * size_t(V.nav_ny);
         ok = devAlloc(h, &h->dWall, nw) && cudaMemcpy(h->dWall, V.wall_sdf, nw * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
              devAlloc(h, &h->dNav, nn) && cudaMemcpy(h->dNav, V.nav_dist, nn * 4, cudaMemcpyHostToDevice) == cudaSuccess;
-        if (ok && V.floor_height)
+        if (ok && V.floor_height) {
             ok = devAlloc(h, &h->dFloor, nw) && cudaMemcpy(h->dFloor, V.floor_height, nw * 4, cudaMemcpyHostToDevice) == cudaSuccess;
+            // the step's wall and floor lookups at one point read both: interleaved, one 32-byte sector serves both
+            std::vector<float2> wf(nw);
+            for (size_t i = 0; i < nw; ++i) wf[i] = make_float2(V.wall_sdf[i], V.floor_height[i]);
+            ok = ok && devAlloc(h, &h->dWallFloor, nw) && cudaMemcpy(h->dWallFloor, wf.data(), nw * 8, cudaMemcpyHostToDevice) == cudaSuccess;
+        }
         if (ok && V.exit_mask)
             ok = devAlloc(h, &h->dMask, nn) && cudaMemcpy(h->dMask, V.exit_mask, nn, cudaMemcpyHostToDevice) == cudaSuccess;
         if (ok && V.speed_factor) {

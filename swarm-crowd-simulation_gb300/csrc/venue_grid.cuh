@@ -21,7 +21,13 @@ struct GridVenue {
         const int ix = smin(int(floorf(fx)), V.wnx - 2), iy = smin(int(floorf(fy)), V.wny - 2);
         const float wx = fx - float(ix), wy = fy - float(iy);
         const size_t r0 = size_t(iy) * size_t(V.wnx) + size_t(ix), r1 = r0 + size_t(V.wnx);
-        const float c00 = __ldg(V.wall + r0), c10 = __ldg(V.wall + r0 + 1), c01 = __ldg(V.wall + r1), c11 = __ldg(V.wall + r1 + 1);
+        float c00, c10, c01, c11;
+        if (V.wallFloor) {
+            c00 = __ldg(V.wallFloor + r0).x; c10 = __ldg(V.wallFloor + r0 + 1).x;
+            c01 = __ldg(V.wallFloor + r1).x; c11 = __ldg(V.wallFloor + r1 + 1).x;
+        } else {
+            c00 = __ldg(V.wall + r0); c10 = __ldg(V.wall + r0 + 1); c01 = __ldg(V.wall + r1); c11 = __ldg(V.wall + r1 + 1);
+        }
         const float d = mix(mix(c00, c10, wx), mix(c01, c11, wx), wy);
         if (d >= reach) return f3{0.0f, 0.0f, WALL_NONE};
         f2 g{mix(c10 - c00, c11 - c01, wy) * V.winv, mix(c01 - c00, c11 - c10, wx) * V.winv};
@@ -34,7 +40,10 @@ struct GridVenue {
         const int ix = sclamp(int(floorf(fx)), 0, V.wnx - 1), iy = sclamp(int(floorf(fy)), 0, V.wny - 1);
         return size_t(iy) * size_t(V.wnx) + size_t(ix);
     }
-    __device__ __forceinline__ float floorHeight(f2 p) const { return V.floorH ? __ldg(V.floorH + floorNode(p)) : 0.0f; }
+    __device__ __forceinline__ float floorHeight(f2 p) const {
+        if (V.wallFloor) return __ldg(V.wallFloor + floorNode(p)).y;
+        return V.floorH ? __ldg(V.floorH + floorNode(p)) : 0.0f;
+    }
     __device__ __forceinline__ float speedFactor(f3 p) const { return V.speedF ? __ldg(V.speedF + floorNode(xy(p))) : 1.0f; }
     __device__ __forceinline__ float map(f3 p) const { return smin(wallDist(xy(p)), p.z - floorHeight(xy(p))); }
 
