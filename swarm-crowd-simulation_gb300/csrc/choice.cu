@@ -28,212 +28,36 @@
 #include <string>
 #include <vector>
 
-#include "device_math.cuh"
+#include "choice.cuh"
 #include "sim_handle.cuh"
 #include "step_kernels.cuh"
 
 namespace swarm_gpu {
 
-constexpr float CHOICE_T_S = 3.0f;            // re-evaluation interval (T_CHOICE_S)
-constexpr float CHOICE_REL_MARGIN = 0.10f;    // hysteresis: share of E_current ...
-constexpr float CHOICE_ABS_MARGIN_S = 5.0f;   // ... and seconds
-constexpr float CHOICE_SWITCH_SHARE = 0.10f;  // per evaluation at most this share of an exit's agents switch away
-constexpr uint32_t CHOICE_MIN_SWITCHES = 1;
-constexpr int CHOICE_GAIN_BINS = 256;         // 1 s gain bins; gains >= 255 s in the last
-constexpr int CHOICE_AHEAD_BINS = 1024;       // queue-ahead distance bins per exit (0.5 m; the last: 511.5 m on)
-constexpr int CHOICE_STRIDE = 64;             // counts per parity (exit ids 0 .. 62)
-constexpr float CHOICE_V_FREE = 1.34f;        // V_FREE_M_S, the estimate's walking speed
-constexpr double CHOICE_J = 83.6;             // EXIT_FLOW_P_M_MIN, persons per metre of clear width per minute
-constexpr int CHOICE_TYPE_MIN[2] = {2, 1};    // the type rule: nearest avenues, nearest doors
-
-// seconds per metre of the estimate's walk, folded once in double
-constexpr float CHOICE_S_PER_M = float(1.0 / double(CHOICE_V_FREE));
-
-inline int choiceSteps(float dt) { return std::max(1, int(double(CHOICE_T_S) / double(dt) + 0.5)); }
-
-struct ChoiceArgs {
-    VenueArgs V;
-    int n, nExits, K;
-    uint32_t step;
-    int evalStep;
-    const float4* state;          // the step's input state (agent order)
-    const uint8_t* cExit;         // ncells x K candidate exits
-    const float* cDist;           // ncells x K candidate distances
-    const float* invCap;          // per exit: seconds per queued agent, 60 / (w J)
-    uint32_t* assign;             // per agent (SWARM_CHOICE_NONE: none)
-    uint2* pending;               // per agent: (eligible switch's exit or NONE, gain bin)
-    uint32_t* hist;               // nExits x CHOICE_GAIN_BINS
-    uint32_t* threshold;          // per exit
-    uint32_t* queue;              // 2 x CHOICE_STRIDE (parities)
-    uint32_t* ahead;              // 2 x CHOICE_STRIDE x CHOICE_AHEAD_BINS
-    uint32_t* counters;           // evaluations, eligible, switches, forced
-};
-
-__device__ __forceinline__ uint32_t aheadBin(float d) {
-    return min(uint32_t(d * 2.0f), uint32_t(CHOICE_AHEAD_BINS - 1));
+// One block per exit; block 0 also clears the write parity's exit counts
+__global__ void __launch_bounds__(CHOICE_PREFIX_THREADS) k_choice_prefix(ChoiceArgs C, VenueArgs) {
+    choicePrefixBlock(C, blockIdx.x);
+    if (blockIdx.x == 0 && threadIdx.x < CHOICE_STRIDE) C.queue[(1u - (C.step & 1u)) * CHOICE_STRIDE + threadIdx.x] = 0u;
 }
 
-__device__ __forceinline__ float estimate(const ChoiceArgs& C, float d, uint32_t e, uint32_t queued) {
-    const float walk = d * CHOICE_S_PER_M;
-    const float wait = float(queued) * C.invCap[e];
-    return walk + wait;
-}
-
-__device__ __forceinline__ int slotOf(const ChoiceArgs& C, size_t row, uint32_t e) {
-    int k = -1;
-    for (int i = 0; i < C.K; ++i)
-        if (uint32_t(C.cExit[row + size_t(i)]) == e) k = i;
-    return k;
-}
-
-__device__ __forceinline__ int bestCandidate(const ChoiceArgs& C, size_t row, const uint32_t* aRead, float& eBest) {
-    int best = -1;
-    eBest = 0.0f;
-    for (int k = 0; k < C.K; ++k) {
-        const uint32_t ex = C.cExit[row + size_t(k)];
-        if (ex == SWARM_CHOICE_EMPTY) break;
-        const float d = C.cDist[row + size_t(k)];
-        const float e = estimate(C, d, ex, aRead[size_t(ex) * CHOICE_AHEAD_BINS + aheadBin(d)]);
-        if (best < 0 || e < eBest) { best = k; eBest = e; }
-    }
-    return best;
-}
-
-// The agent's cell (the step's hash of its start-of-step position, NaN sanitised as the hash does), or -1 when it
-// is evacuated
-__device__ __forceinline__ long long choiceRow(const ChoiceArgs& C, int i) {
-    float4 p = C.state[2 * size_t(i)];
-    if (isnan(p.x)) p = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
-    if (p.w == 0.0f) return -1;
-    const int x = sclamp(int((p.x - C.V.dminX) / C.V.dspanX * float(C.V.resX)), 0, C.V.resX - 1);
-    const int y = sclamp(int((p.y - C.V.dminY) / C.V.dspanY * float(C.V.resY)), 0, C.V.resY - 1);
-    return (long long)(x + y * C.V.resX) * C.K;
-}
-
-// Stage 3 of the reference (first of a step): per exit (one block each) the read parity's queue-ahead histogram to
-// exclusive prefix sums in place, the write parity's cleared; block 0 also clears the write parity's exit counts
-__global__ void __launch_bounds__(256) k_choice_prefix(ChoiceArgs C) {
-    __shared__ uint32_t warpTot[8];
-    const int e = blockIdx.x;
-    const uint32_t par = C.step & 1u;
-    uint32_t* aRead = C.ahead + (size_t(par) * CHOICE_STRIDE + size_t(e)) * CHOICE_AHEAD_BINS;
-    uint32_t* aWrite = C.ahead + (size_t(1u - par) * CHOICE_STRIDE + size_t(e)) * CHOICE_AHEAD_BINS;
-    constexpr int PER = CHOICE_AHEAD_BINS / 256;   // 4 bins a thread, in order
-    uint32_t v[PER], sum = 0;
-#pragma unroll
-    for (int j = 0; j < PER; ++j) { v[j] = aRead[threadIdx.x * PER + j]; sum += v[j]; }
-    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    uint32_t inc = sum;
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
-        if (int(lane) >= o) inc += u;
-    }
-    if (lane == 31) warpTot[warp] = inc;
-    __syncthreads();
-    uint32_t before = 0;
-    for (unsigned w = 0; w < warp; ++w) before += warpTot[w];
-    uint32_t run = before + inc - sum;
-#pragma unroll
-    for (int j = 0; j < PER; ++j) { aRead[threadIdx.x * PER + j] = run; run += v[j]; aWrite[threadIdx.x * PER + j] = 0u; }
-    if (e == 0 && threadIdx.x < CHOICE_STRIDE) C.queue[(1u - par) * CHOICE_STRIDE + threadIdx.x] = 0u;
-}
-
-// Stage 1: nav::evaluate (src/exit_choice.cpp:605-623) for every agent
-__global__ void __launch_bounds__(256) k_choice_eval(ChoiceArgs C) {
+__global__ void __launch_bounds__(256) k_choice_eval(ChoiceArgs C, VenueArgs V) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= C.n) return;
-    C.pending[i] = make_uint2(SWARM_CHOICE_NONE, 0u);
-    const long long r = choiceRow(C, i);
-    if (r < 0) return;
-    const size_t row = size_t(r);
-    if (C.cExit[row] == SWARM_CHOICE_EMPTY) return;
-    const uint32_t cur = C.assign[i];
-    const int curK = slotOf(C, row, cur);
-    if (curK < 0) return;
-    atomicAdd(C.counters + 0, 1u);
-    const uint32_t* aRead = C.ahead + size_t(C.step & 1u) * CHOICE_STRIDE * CHOICE_AHEAD_BINS;
-    float eBest;
-    const int best = bestCandidate(C, row, aRead, eBest);
-    const float dCur = C.cDist[row + size_t(curK)];
-    const float eCur = estimate(C, dCur, cur, aRead[size_t(cur) * CHOICE_AHEAD_BINS + aheadBin(dCur)]);
-    const float gain = eCur - eBest;
-    if (best != curK && gain > fmaxf(CHOICE_REL_MARGIN * eCur, CHOICE_ABS_MARGIN_S)) {
-        const uint32_t bin = min(uint32_t(gain), uint32_t(CHOICE_GAIN_BINS - 1));
-        C.pending[i] = make_uint2(uint32_t(C.cExit[row + size_t(best)]), bin);
-        atomicAdd(C.hist + size_t(cur) * CHOICE_GAIN_BINS + bin, 1u);
-        atomicAdd(C.counters + 1, 1u);
-    }
+    if (i < C.n) choiceEvalAgent(V, C, i);
 }
 
-// Stage 2: nav::switchThreshold (src/exit_choice.cpp:625-640) per exit, then the exit's histogram cleared
-__global__ void k_choice_thr(ChoiceArgs C) {
-    const int e = threadIdx.x;
-    if (e >= C.nExits) return;
-    uint32_t* h = C.hist + size_t(e) * CHOICE_GAIN_BINS;
-    const uint32_t queued = C.queue[(C.step & 1u) * CHOICE_STRIDE + uint32_t(e)];
-    const uint32_t cap = max(CHOICE_MIN_SWITCHES, uint32_t(float(queued) * CHOICE_SWITCH_SHARE));
-    uint32_t cum = 0, thr = uint32_t(CHOICE_GAIN_BINS);
-    for (int b = CHOICE_GAIN_BINS - 1; b >= 0; --b) {
-        const uint32_t c = h[b];
-        if (c == 0) continue;
-        if (cum + c > cap) {
-            if (cum == 0) thr = uint32_t(b);   // the highest bin alone exceeds the cap: it switches anyway
-            break;
-        }
-        cum += c;
-        thr = uint32_t(b);
-    }
-    C.threshold[e] = thr;
-    for (int b = 0; b < CHOICE_GAIN_BINS; ++b) h[b] = 0u;
-}
+// One warp per exit (grid: nExits x 32)
+__global__ void __launch_bounds__(32) k_choice_thr(ChoiceArgs C, VenueArgs) { choiceThrWarp(C, blockIdx.x); }
 
-// Stage 0: nav::apply (src/exit_choice.cpp:642-658) and the agent's counts for the next step. The counts are sums of
-// ones, aggregated before they reach global memory (the exit counts per block in shared memory, the queue-ahead bins
-// per warp): the same integers, a few atomics per block instead of one per agent on ~40 addresses.
-__global__ void __launch_bounds__(256) k_choice_apply(ChoiceArgs C) {
+// The exit counts aggregated per block in shared memory, the queue-ahead bins per warp: the same integers, a few
+// atomics per block instead of one per agent on ~40 addresses
+__global__ void __launch_bounds__(256) k_choice_apply(ChoiceArgs C, VenueArgs V) {
     __shared__ uint32_t sQueue[CHOICE_STRIDE];
     if (threadIdx.x < CHOICE_STRIDE) sQueue[threadIdx.x] = 0u;
     __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t par = C.step & 1u;
-    uint32_t aheadKey = 0xFFFFFFFFu;   // exit x CHOICE_AHEAD_BINS + bin of this agent's count (none: all ones)
-    const long long r = i < C.n ? choiceRow(C, i) : -1;
-    if (r >= 0) {
-        const size_t row = size_t(r);
-        const uint32_t* aRead = C.ahead + size_t(par) * CHOICE_STRIDE * CHOICE_AHEAD_BINS;
-        const uint32_t cur = C.assign[i];
-        uint32_t ex = cur;
-        const bool hasPath = C.cExit[row] != SWARM_CHOICE_EMPTY;
-        const int curK = hasPath ? slotOf(C, row, cur) : -1;
-        if (hasPath && curK < 0) {   // forced (or the first choice)
-            float eBest;
-            ex = C.cExit[row + size_t(bestCandidate(C, row, aRead, eBest))];
-            if (cur != SWARM_CHOICE_NONE) atomicAdd(C.counters + 3, 1u);
-        } else if (C.evalStep && curK >= 0) {
-            const uint2 pd = C.pending[i];
-            if (pd.x != SWARM_CHOICE_NONE && pd.y >= C.threshold[cur]) {
-                ex = pd.x;
-                atomicAdd(C.counters + 2, 1u);
-            }
-        }
-        C.assign[i] = ex;
-        if (ex != SWARM_CHOICE_NONE) {
-            atomicAdd(sQueue + ex, 1u);
-            const int k = slotOf(C, row, ex);
-            if (k >= 0) aheadKey = ex * uint32_t(CHOICE_AHEAD_BINS) + aheadBin(C.cDist[row + size_t(k)]);
-        }
-    }
-    // the queue-ahead count: one atomic per distinct (exit, bin) in the warp
-    const unsigned lane = threadIdx.x & 31u;
-    const unsigned valid = __ballot_sync(0xffffffffu, aheadKey != 0xFFFFFFFFu);
-    if (aheadKey != 0xFFFFFFFFu) {
-        const unsigned peers = __match_any_sync(valid, aheadKey);
-        if (int(lane) == __ffs(peers) - 1)
-            atomicAdd(C.ahead + size_t(1u - par) * CHOICE_STRIDE * CHOICE_AHEAD_BINS + aheadKey, uint32_t(__popc(peers)));
-    }
+    choiceAheadFlush(C, i < C.n ? choiceApplyAgent(V, C, i, sQueue) : 0xFFFFFFFFu);
     __syncthreads();
-    if (threadIdx.x < CHOICE_STRIDE && sQueue[threadIdx.x])
-        atomicAdd(C.queue + (1u - par) * CHOICE_STRIDE + threadIdx.x, sQueue[threadIdx.x]);
+    choiceQueueFlush(C, sQueue);
 }
 
 }  // namespace swarm_gpu
@@ -349,25 +173,34 @@ std::vector<std::pair<void*, size_t>> SwarmSim::choiceLive() const {
             {dChoiceAhead, size_t(2) * swarm_gpu::CHOICE_STRIDE * swarm_gpu::CHOICE_AHEAD_BINS * 4}, {dChoiceCounters, 16}};
 }
 
-int SwarmSim::enqueueChoice(int in) {
+namespace {
+
+ChoiceArgs choiceArgsOf(const SwarmSim& s, int in) {
     ChoiceArgs C{};
-    C.V = args(in).V;
-    C.n = n;
-    C.nExits = choiceExits;
-    C.K = choiceK;
-    C.step = choiceStep;
-    C.evalStep = choiceStep > 0u && choiceStep % uint32_t(swarm_gpu::choiceSteps(P.dt)) == 0u;
-    C.state = state[in];
-    C.cExit = dChoiceExit; C.cDist = dChoiceDist; C.invCap = dChoiceInvCap;
-    C.assign = dAssign; C.pending = dPending; C.hist = dChoiceHist; C.threshold = dChoiceThr; C.queue = dChoiceQueue;
-    C.ahead = dChoiceAhead; C.counters = dChoiceCounters;
+    C.n = s.n;
+    C.nExits = s.choiceExits;
+    C.K = s.choiceK;
+    C.step = s.choiceStep;
+    C.evalStep = s.choiceStep > 0u && s.choiceStep % uint32_t(swarm_gpu::choiceSteps(s.P.dt)) == 0u;
+    C.state = s.state[in];
+    C.cExit = s.dChoiceExit; C.cDist = s.dChoiceDist; C.invCap = s.dChoiceInvCap;
+    C.assign = s.dAssign; C.pending = s.dPending; C.hist = s.dChoiceHist; C.threshold = s.dChoiceThr;
+    C.queue = s.dChoiceQueue; C.ahead = s.dChoiceAhead; C.counters = s.dChoiceCounters;
+    return C;
+}
+
+}  // namespace
+
+int SwarmSim::enqueueChoice(int in) {
+    const ChoiceArgs C = choiceArgsOf(*this, in);
+    const swarm_gpu::VenueArgs V = args(in).V;
     const int blocks = (n + 255) / 256;
-    swarm_gpu::k_choice_prefix<<<choiceExits, 256, 0, stream>>>(C);
+    swarm_gpu::k_choice_prefix<<<choiceExits, swarm_gpu::CHOICE_PREFIX_THREADS, 0, stream>>>(C, V);
     if (C.evalStep) {
-        swarm_gpu::k_choice_eval<<<blocks, 256, 0, stream>>>(C);
-        swarm_gpu::k_choice_thr<<<1, swarm_gpu::CHOICE_STRIDE, 0, stream>>>(C);
+        swarm_gpu::k_choice_eval<<<blocks, 256, 0, stream>>>(C, V);
+        swarm_gpu::k_choice_thr<<<choiceExits, 32, 0, stream>>>(C, V);
     }
-    swarm_gpu::k_choice_apply<<<blocks, 256, 0, stream>>>(C);
+    swarm_gpu::k_choice_apply<<<blocks, 256, 0, stream>>>(C, V);
     ++choiceStep;
     launches += C.evalStep ? 4 : 2;
     return cudaGetLastError() == cudaSuccess ? SWARM_OK : fail(SWARM_E_CUDA, "exit choice launch");
