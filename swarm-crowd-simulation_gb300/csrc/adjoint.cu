@@ -802,7 +802,8 @@ __global__ void __launch_bounds__(128) k_adj_gather(AdjArgs A) {
 // Every block stays resident (a cooperative launch); the phases are separated by a grid barrier on one word: block 0
 // adds 2^31 - (blocks - 1), every other block 1, so the word's top bit flips once all have arrived; a block waits for
 // the flip at most ADJ_BARRIER_WAIT_NS of %globaltimer, then records ERR_TIMEOUT and leaves the kernel, as does every
-// block that finds ERR_TIMEOUT at a later barrier (the host reports SWARM_E_TIMEOUT).
+// waiting block that finds ERR_TIMEOUT set (the host reports SWARM_E_TIMEOUT). Only the last arrival's add flips the
+// bit: that block goes on without polling (its add acquires), and nothing is read before the add.
 constexpr uint64_t ADJ_BARRIER_WAIT_NS = 1000000000ull;
 
 __device__ __forceinline__ uint64_t adjNs() {
@@ -817,16 +818,17 @@ __device__ __forceinline__ bool adjBarrier(const AdjArgs& A) {
     __shared__ int leave;
     __syncthreads();
     if (threadIdx.x == 0) {
-        cuda::atomic_ref<int, cuda::thread_scope_device> err(*A.err);
-        int out = 1;
-        if (!(err.load(cuda::memory_order_relaxed) & ERR_TIMEOUT)) {
-            cuda::atomic_ref<unsigned, cuda::thread_scope_device> word(*A.barrier);
-            const unsigned add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
-            const unsigned old = word.fetch_add(add, cuda::memory_order_release);
+        cuda::atomic_ref<unsigned, cuda::thread_scope_device> word(*A.barrier);
+        const unsigned add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
+        const unsigned old = word.fetch_add(add, cuda::memory_order_acq_rel);
+        int out = 0;
+        if ((((old + add) ^ old) & 0x80000000u) == 0u) {
+            cuda::atomic_ref<int, cuda::thread_scope_device> err(*A.err);
             const uint64_t t0 = adjNs();
-            out = 0;
+            unsigned polls = 0;
             while (((word.load(cuda::memory_order_acquire) ^ old) & 0x80000000u) == 0u) {
                 if (adjNs() - t0 > ADJ_BARRIER_WAIT_NS) { err.fetch_or(ERR_TIMEOUT, cuda::memory_order_relaxed); out = 1; break; }
+                if (++polls % 64u == 0u && (err.load(cuda::memory_order_relaxed) & ERR_TIMEOUT)) { out = 1; break; }
             }
         }
         leave = out;

@@ -647,9 +647,9 @@ __global__ void __launch_bounds__(128) k_final(StepArgs A, int inBuf) {
 // Every block stays resident (a cooperative launch) and the phases are separated by grid barriers. A barrier is a
 // counter and a generation word: the last block to arrive resets the counter and advances the generation (release);
 // the others wait for the generation to move (acquire) for at most BARRIER_WAIT_NS of wall-clock time (%globaltimer),
-// after which the block records ERR_TIMEOUT and leaves the kernel; a block that finds ERR_TIMEOUT set at a barrier
-// leaves too, so no phase ever runs on data another block has not finished; the host reports SWARM_E_TIMEOUT and
-// resets the barrier words.
+// after which the block records ERR_TIMEOUT and leaves the kernel; a waiting block that finds ERR_TIMEOUT set leaves
+// too, and a block that left never arrives at the next barrier, so no phase ever runs on data another block has not
+// finished; the host reports SWARM_E_TIMEOUT and resets the barrier words.
 constexpr uint64_t BARRIER_WAIT_NS = 1000000000ull;   // 1 s; a healthy barrier waits microseconds
 
 __device__ __forceinline__ uint64_t globalNs() {
@@ -663,10 +663,6 @@ __device__ __forceinline__ void stamp(const StepArgs& A, int i) {
     if (A.stamps && blockIdx.x == 0 && threadIdx.x == 0) A.stamps[i] = globalNs();
 }
 
-// One word per barrier: block 0 adds 2^31 - (expected - 1), every other block adds 1, so the word's top bit flips
-// exactly when all `expected` blocks have arrived; each block waits for the flip of the value it saw (the scheme of
-// CUDA's cooperative groups grid sync). Release before the add, acquire on the poll.
-// Returns false (the same in every thread of the block) when the block must leave the kernel.
 // This block's share of an array of `bytes` bytes, prefetched into L2 by the copy engine (cp.async.bulk.prefetch: no
 // registers, no wait). The shares are whole 16-byte units of the array, the last one ends at the array's last full
 // 16-byte unit: every prefetched byte lies inside the array. A base that is not 16-byte aligned is skipped (a hint).
@@ -686,20 +682,29 @@ __device__ __forceinline__ void bulkPrefetchShare(const void* base, size_t bytes
     }
 }
 
+// One word per barrier: block 0 adds 2^31 - (expected - 1), every other block adds 1, so the word's top bit flips
+// exactly when all `expected` blocks have arrived, and only the last arrival's add flips it: that block goes on at
+// once (its add acquires what the earlier adds released), the others wait for the flip of the value they saw (the
+// scheme of CUDA's cooperative groups grid sync). Nothing is read before the add: the error word is polled only while
+// waiting, every BARRIER_ERR_POLLS polls.
+// Returns false (the same in every thread of the block) when the block must leave the kernel.
+constexpr unsigned BARRIER_ERR_POLLS = 64;
+
 __device__ __forceinline__ bool gridBarrier(const StepArgs& A, unsigned expected) {
     __shared__ int leave;
     __syncthreads();
     if (threadIdx.x == 0) {
-        cuda::atomic_ref<int, cuda::thread_scope_device> err(*A.err);
-        int out = 1;
-        if (!(err.load(cuda::memory_order_relaxed) & ERR_TIMEOUT)) {
-            cuda::atomic_ref<unsigned, cuda::thread_scope_device> word(A.barrier[0]);
-            const unsigned add = blockIdx.x == 0 ? 0x80000000u - (expected - 1u) : 1u;
-            const unsigned old = word.fetch_add(add, cuda::memory_order_release);
+        cuda::atomic_ref<unsigned, cuda::thread_scope_device> word(A.barrier[0]);
+        const unsigned add = blockIdx.x == 0 ? 0x80000000u - (expected - 1u) : 1u;
+        const unsigned old = word.fetch_add(add, cuda::memory_order_acq_rel);
+        int out = 0;
+        if ((((old + add) ^ old) & 0x80000000u) == 0u) {
+            cuda::atomic_ref<int, cuda::thread_scope_device> err(*A.err);
             const uint64_t t0 = globalNs();
-            out = 0;
+            unsigned polls = 0;
             while (((word.load(cuda::memory_order_acquire) ^ old) & 0x80000000u) == 0u) {
                 if (globalNs() - t0 > BARRIER_WAIT_NS) { err.fetch_or(ERR_TIMEOUT, cuda::memory_order_relaxed); out = 1; break; }
+                if (++polls % BARRIER_ERR_POLLS == 0u && (err.load(cuda::memory_order_relaxed) & ERR_TIMEOUT)) { out = 1; break; }
             }
         }
         leave = out;
