@@ -83,3 +83,33 @@ def test_product_has_no_cpu_fallback():
                 text = open(os.path.join(dirpath, f)).read()
                 for needle in ("import oracle", "from oracle", "liboracle", "oracle_create", "libswarm_ref"):
                     assert needle not in text, (f, needle)
+
+
+def _mirrors():
+    """Every ctypes mirror of a header struct, with the header's name."""
+    from swarm_gb300 import abi, venues
+    out = {name: cls for name, cls in vars(abi).items()
+           if isinstance(cls, type) and issubclass(cls, C.Structure) and name.startswith("Swarm")}
+    out["SwarmHallSpec"] = venues.HallSpec
+    out["SwarmBowlSpec"] = venues.BowlSpec
+    return out
+
+
+def test_every_struct_mirror_has_the_header_layout(tmp_path):
+    """Size and every field's offset of each ctypes mirror, against the header compiled by gcc."""
+    mirrors = _mirrors()
+    assert len(mirrors) >= 12
+    lines, want = [], []
+    for name, cls in sorted(mirrors.items()):
+        lines.append(f'printf("%zu\\n", sizeof({name}));')
+        want.append(C.sizeof(cls))
+        for field in cls._fields_:
+            lines.append(f'printf("%zu\\n", offsetof({name}, {field[0]}));')
+            want.append(getattr(cls, field[0]).offset)
+    src = tmp_path / "layout.c"
+    src.write_text('#include "swarm_cuda.h"\n#include <stdio.h>\n#include <stddef.h>\nint main(void){\n' +
+                   "\n".join(lines) + "\nreturn 0;}\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert got == want
