@@ -243,6 +243,37 @@ def test_grid_hall_65536_one_step_vs_oracle_and_invariants(built):
     assert np.array_equal(_bits(sim.state()), _bits(sim2.state()))
 
 
+def test_grid_terrace_1000_steps_compared_every_step(c0):
+    """The terrace workload's whole comparison run: 1 000 steps, the state bit for bit after every one."""
+    P, venue, (boids, r, v0) = c0
+    sim = _sim(P, venue, boids, r, v0)
+    ora = O.OracleSim(P, venue.struct)
+    ora.set_state(boids)
+    ora.set_agent_params(r, v0)
+    for s in range(1000):
+        sim.step(1)
+        ora.step(1)
+        assert np.array_equal(_bits(sim.state()), _bits(ora.state())), f"step {s + 1}"
+    assert (sim.state()[:, 3] == 0).sum() > 0, "the crowd has begun to leave"
+
+
+def test_grid_hall_65536_2000_steps_vs_oracle(built):
+    """The 140 m hall's whole run (2 000 steps, the doors congested for most of it): bit for bit every 250 steps."""
+    import swarm_gb300
+    from swarm_gb300 import venues
+    venue, (boids, r, v0) = venues.hall_c1()
+    P = swarm_gb300.params_si()
+    sim = _sim(P, venue, boids, r, v0)
+    ora = O.OracleSim(P, venue.struct)
+    ora.set_state(boids)
+    ora.set_agent_params(r, v0)
+    for k in range(8):
+        sim.step(250)
+        ora.step(250)
+        assert np.array_equal(_bits(sim.state()), _bits(ora.state())), f"after {250 * (k + 1)} steps"
+    assert np.array_equal(sim.grid()[1], ora.grid()[1]) and np.array_equal(sim.cells(), ora.cells())
+
+
 @pytest.mark.parametrize("fused,graph,timing", [(False, False, False), (False, False, True), (False, True, True),
                                                (False, True, False), (True, False, True)])
 def test_execution_modes_are_bit_identical(terrace, terrace_golden, fused, graph, timing):
