@@ -927,8 +927,9 @@ constexpr int FUSED_SMEM = WIN_CAP * (int(sizeof(float4)) + int(sizeof(float2)) 
 
 // The fused grid: one block per SM when the state fits (threads = n / SMs rounded up to a warp, 128..512; 128..1024
 // for a batch), else as many blocks as stay resident, each taking several tiles per phase
+// (The launch helpers' caches are per host thread: handles stepped from several threads share none of them.)
 static int smCount() {
-    static int sms = 0;
+    static thread_local int sms = 0;
     if (!sms) {
         int dev = 0;
         cudaGetDevice(&dev);
@@ -954,7 +955,7 @@ int fusedScanTile(const StepArgs& A) {
 
 template <class Venue, bool kPerAgent, bool kB, bool kTape = false>
 static cudaError_t fusedImpl(const StepArgs& A0, cudaStream_t st) {
-    static bool smemSet = false;
+    static thread_local bool smemSet = false;
     if (!smemSet) {
         cudaFuncSetAttribute(k_step_fused<Venue, kPerAgent, kB, kTape>, cudaFuncAttributeMaxDynamicSharedMemorySize, FUSED_SMEM);
         smemSet = true;
@@ -963,7 +964,7 @@ static cudaError_t fusedImpl(const StepArgs& A0, cudaStream_t st) {
     StepArgs A = A0;
     const int threads = fusedThreads(A);
     A.scanTile = fusedScanTile(A);
-    static int occThreads = -1, occPerSm = 0;   // the occupancy of the last block size asked for
+    static thread_local int occThreads = -1, occPerSm = 0;   // the occupancy of the last block size asked for
     if (occThreads != threads) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occPerSm, k_step_fused<Venue, kPerAgent, kB, kTape>, threads, FUSED_SMEM);
         occThreads = threads;
