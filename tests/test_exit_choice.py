@@ -87,6 +87,43 @@ def test_candidate_table_rules(bowl):
     assert ((t == 0).sum(axis=1) >= 2).all() and ((t == 1).sum(axis=1) >= 1).all()
 
 
+def test_candidate_table_rejects_invalid_specs(hall, stadium_sdf):
+    """swarm_exit_choice_table's argument checks (host code, no GPU): a grid venue, 1..63 exits, 1..24 candidates,
+    fields and types present, output buffers present."""
+    import ctypes as C
+    import swarm_gb300
+    from swarm_gb300.abi import SWARM_E_INVALID, SWARM_OK
+    from swarm_gb300.venues import Venue
+    venue, _, _, _, (fields, widths, types) = hall
+    L = swarm_gb300.lib()
+    v = venue.struct
+    cells = v.grid_res_x * v.grid_res_y
+    ex = np.empty((cells, 24), np.uint8)
+    di = np.empty((cells, 24), np.float32)
+    out = (ex.ctypes.data_as(C.c_void_p), di.ctypes.data_as(C.POINTER(C.c_float)))
+
+    def call(spec, venue_struct=v, outs=out):
+        return L.swarm_exit_choice_table(C.byref(venue_struct) if venue_struct is not None else None,
+                                         C.byref(spec) if spec is not None else None, *outs)
+
+    spec, keep = swarm_gb300._choice_spec(fields, widths, types, 24)
+    assert call(spec) == SWARM_OK
+    for n_exits, k in ((0, 24), (64, 24), (4, 0), (4, 25)):
+        bad, keep2 = swarm_gb300._choice_spec(fields, widths, types, 24)
+        bad.n_exits, bad.candidates = n_exits, k
+        assert call(bad) == SWARM_E_INVALID, (n_exits, k)
+    no_fields, _ = swarm_gb300._choice_spec(fields, widths, types, 24)
+    no_fields.fields = None
+    assert call(no_fields) == SWARM_E_INVALID
+    no_types, _ = swarm_gb300._choice_spec(fields, widths, types, 24)
+    no_types.type = None
+    assert call(no_types) == SWARM_E_INVALID
+    assert call(None) == SWARM_E_INVALID
+    assert call(spec, venue_struct=None) == SWARM_E_INVALID
+    assert call(spec, outs=(None, out[1])) == SWARM_E_INVALID
+    assert call(spec, venue_struct=Venue.stadium(stadium_sdf).struct) == SWARM_E_INVALID, "stadium: no exit fields"
+
+
 def test_oracle_choice_assigns_switches_and_is_deterministic(hall):
     import swarm_gb300
     venue, b, r, v0, (fields, widths, types) = hall
