@@ -3,6 +3,8 @@
  *
  * One handle = one simulation on one GPU: the agent state, the neighbour grid, the venue and a CUDA stream.
  * Every entry point returns SWARM_OK (0) or a negative status; swarm_last_error() gives the message.
+ * Threads: handles share no state, so different handles may be driven from different host threads at once; the calls
+ * on one handle must not overlap (as for the reference's CrowdSim object).
  * No C++ exception, no torch type and no CUDA type crosses this boundary (streams are passed as void*).
  *
  * Reference interface replaced (DedovSergei/swarm-crowd-simulation, paths within that project):
