@@ -15,14 +15,16 @@ e2e    the same metric through swarm_step_host: host state in pinned memory -> d
 roofline  the dominant kernel's algorithmic bytes per launch (bytes per agent x active agents) over its mean launch
        time (CUDA events recorded by the library around each stage during the timed steps), against the measured
        HBM copy bandwidth (MEASURED_PEAKS.json).
-cpu_baseline  the oracle port of the reference's CPU step (OpenMP, all host threads) on a bounded sample of the same
-       workload.
+cpu_baseline  the oracle port of the reference's CPU step (OpenMP, all host threads) on a fixed sample of the same
+       workload (400 consecutive steps after 2 warm-up steps from the spawn), with the host's core count and CPU model.
 batched  the 256-instance batch as one packed state against the same instances launched one at a time.
 bowl   the 63 488-agent seated bowl: the plain step (as value) and its evacuation run to completion.
 adjoint  loss and gradient of 400 steps of the 16 384-agent hall (checkpoints every 20 steps, and the full tape)
        against the plain forward of the same steps.
 --impl reference  the reference's CPU step (the oracle port: the reference's own build needs its source tree, which
-       only exists where the oracle was pinned) on the host cores, same workload, metric and unit.
+       only exists where the oracle was pinned) on the host cores, same workload, config, metric and unit, timed over
+       the same 400-step sample as cpu_baseline; the workload is built by the oracle library, so that process never
+       maps the CUDA library.
 """
 import argparse
 import json
@@ -382,29 +384,61 @@ def bench_adjoint(P, steps=400, ckpt=20):
     return out
 
 
-def cpu_baseline(budget_s=12.0, max_steps=400):
-    """The oracle port (OpenMP, every host thread) on the same workload: 2 warm-up steps, then steps until the budget."""
-    import numpy as np
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), for the baseline's record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+CPU_SAMPLE_STEPS = 400   # the CPU sample: this many consecutive steps of the workload from its spawn
+
+
+def cpu_baseline(warmup=2, steps=CPU_SAMPLE_STEPS):
+    """The oracle port of the reference's CPU step (OpenMP, every host thread) on the same workload: `warmup` steps
+    from the spawn, then `steps` consecutive steps timed one by one (wall clock), agent-steps counted per step. The
+    workload is built by the oracle library's host build of the venue builders, so this process never loads the CUDA
+    library."""
     import swarm_gb300
     from oracle import oracle as O
     O.build()
+    swarm_gb300.use_generator(O.lib())
     venue, (boids, r, v0) = workload()
     sim = O.OracleSim(swarm_gb300.params_si(), venue.struct)
     sim.set_state(boids)
     sim.set_agent_params(r, v0)
-    sim.step(2)
-    agent_steps, t_total, steps = 0, 0.0, 0
-    while t_total < budget_s and steps < max_steps:
+    sim.step(warmup)
+    agent_steps, t_total = 0, 0.0
+    for _ in range(steps):
         active = int((sim.state()[:, 3] != 0).sum())
         t0 = time.perf_counter()
         sim.step(1)
         t_total += time.perf_counter() - t0
         agent_steps += active
-        steps += 1
     threads = O.lib().oracle_max_threads()
-    return {"value": agent_steps / t_total, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{steps} consecutive steps of the same 65536-agent hall from its spawn (after 2 warm-up steps), "
-                      f"{t_total:.1f} s of wall clock on {threads} OpenMP threads"}
+    return {"value": agent_steps / t_total, "unit": UNIT, "cores": threads, "cpu_model": cpu_model(), "kind": "port",
+            "sample": f"{steps} consecutive steps of the 65536-agent hall after {warmup} warm-up steps from its spawn, "
+                      f"{t_total:.1f} s of wall clock on {threads} OpenMP threads",
+            "ms_per_step": t_total / steps * 1e3}
+
+
+def bench_config(n, world):
+    """The workload record both arms print (the same dict: the same workload)."""
+    return {"workload": WORKLOAD, "agents": n, "sweeps": 8, "dt_s": 0.05,
+            "l2": "GPU arm: flushed before every timed step (256 MiB write, outside the timed events)",
+            "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"}
 
 
 def replica_totals(dist, device, ms, agent_steps):
@@ -421,13 +455,18 @@ def replica_totals(dist, device, ms, agent_steps):
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the reference's CPU step (the oracle port; the reference's own build needs its source tree,
+    absent where the benchmark runs) on the host cores, the same workload, metric and unit. Each run times the same
+    fixed sample (CPU_SAMPLE_STEPS steps after args.warmup warm-up steps), whatever --steps asks, so that its number
+    does not depend on a short sample; rank 0 alone runs under torchrun."""
     if rank != 0:
         return 0
-    base = cpu_baseline(budget_s=max(5.0, 1.0 * args.steps), max_steps=args.steps)
+    base = cpu_baseline(warmup=args.warmup)
     line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 65536.0 / base["value"] * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD}, "cpu_baseline": base,
+            "steps": CPU_SAMPLE_STEPS, "warmup": args.warmup, "ms_per_step": base["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (generated hall and lattice spawn, seed 0)",
+            "config": bench_config(65536, world), "cpu_baseline": base,
             "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -607,14 +646,13 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (generated hall and lattice spawn, seed 0)",
-            "config": {"workload": WORKLOAD, "agents": n, "active_per_step": active_mean,
-                       "l2": "flushed before every timed step (256 MiB write, outside the timed events)",
-                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
-                       "step_fraction_of_hbm_roofline": value * B_STEP / (hbm * 1e9),
-                       "path": "one kernel per phase (CUDA graphs)" if args.phase_kernels else
-                               "one persistent cooperative kernel per step",
-                       "stage_ms_mean": {k: statistics.mean(s[k] for s in stages)
-                                         for k in ("sort", "predict", "project", "final_pass", "total")}},
+            "config": bench_config(n, world),
+            "details": {"active_per_step": active_mean,
+                        "step_fraction_of_hbm_roofline": value * B_STEP / (hbm * 1e9),
+                        "path": "one kernel per phase (CUDA graphs)" if args.phase_kernels else
+                                "one persistent cooperative kernel per step",
+                        "stage_ms_mean": {k: statistics.mean(s[k] for s in stages)
+                                          for k in ("sort", "predict", "project", "final_pass", "total")}},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "peak_kind": peak_kind,
                          "bytes_per_agent": dom_bytes, "mean_launch_ms": dom_ms,
@@ -624,7 +662,7 @@ def main():
             "gpu_launches": launches,
         }
         if congested:
-            line["config"]["congested"] = congested
+            line["details"]["congested"] = congested
         line["clocks"] = clk.summary()
         if not args.no_batch and world == 1:
             try:

@@ -180,7 +180,8 @@ int swarm_step(SwarmHandle h, int steps);
  * steps, the result into out_boids, and waits for it. With pinned (page-locked, device-mapped) buffers and the fused
  * step there are no copy operations: the first step's hash phase reads in_boids over the coherent host link, and the
  * last step's kernel ends by writing its result into out_boids (the device state holds it too); otherwise (or with
- * the exit choice on) one copy each way. in_boids may equal out_boids. */
+ * the exit choice on) one copy each way. in_boids may equal out_boids. Like swarm_synchronize it reads the device
+ * error flag before it returns: SWARM_E_TIMEOUT when a grid barrier gave up (out_boids then holds no result). */
 int swarm_step_host(SwarmHandle h, const float* in_boids, float* out_boids, int n, int steps);
 /* CpuCrowdSim::setProjectionIterations / CrowdSim::setProjectionIterations (src/crowd_sim.cpp:480-483). */
 int swarm_set_iterations(SwarmHandle h, int k);
@@ -346,14 +347,18 @@ int swarm_spawn_lattice(int nx, int ny, int n, float spacing, float cx, float cy
                         float* boids, float* radius, float* v0);
 
 /* ---- the key sort without device allocation ----
- * No counterpart in the reference. For callers that cannot allocate device memory while they run (host callbacks,
- * allocator-free deployments that fix their footprint at start-up): sorts one state already in device memory --
- * d_boids, n x 8 floats -- by cell over the given hash grid, exactly as the step's own sort, and writes the sorted
- * pairs (d_grid_id, d_boid_id: n each) and the cell table (d_cells: 2 x grid_res_x x grid_res_y) to the caller's
- * device arrays. Its working memory is a fixed array compiled into this library (about 1.8 MB per GPU that loads
- * it, held until exit): at most 65536 agents and 131072 cells, larger sizes return SWARM_E_INVALID. It calls no
- * allocator. The first call on a device looks up the array's address and should come before any stream capture.
- * All calls share the array: calls that overlap on the GPU race, so order them (one stream, or events). */
+ * No counterpart in the reference. For callers that cannot allocate device memory while they run: a plug-in step in
+ * a host application's frame loop (cudaMalloc / cudaFree may synchronise the whole device, and the host owns the
+ * memory budget), or a deployment that fixes its footprint at start-up. Sorts one state already in device memory --
+ * d_boids, n x 8 floats, 16-byte aligned -- by cell over the given hash grid, exactly as the step's own sort, and
+ * writes the sorted pairs (d_grid_id, d_boid_id: n each) and the cell table (d_cells: 2 x grid_res_x x grid_res_y) to
+ * the caller's device arrays. Its working memory is a fixed array compiled into this library (about 1.8 MB per GPU
+ * that loads it, held until exit): at most 65536 agents and 131072 cells; larger sizes or a misaligned state return
+ * SWARM_E_INVALID. It calls no allocator. The first call on a device looks up the array's address with that device
+ * current and keeps it; after a cudaDeviceReset the address is gone, so do not call it on that device again in the
+ * same process. Returns when its work on `stream` is done: SWARM_E_CUDA if a launch failed or the kernels met a slot
+ * out of range. All calls share the array: calls that overlap on the GPU (from several host threads) race and can
+ * give such an error, so order them. */
 int swarm_sort_grid_noalloc(const float* d_boids, int n, int grid_res_x, int grid_res_y, float domain_min_x,
                             float domain_min_y, float domain_span_x, float domain_span_y, uint32_t* d_grid_id,
                             uint32_t* d_boid_id, uint32_t* d_cells, void* stream);

@@ -18,10 +18,19 @@ _r = None
 
 
 def build(ref=False):
-    """make -C oracle (and the reference's own CPU step when ref and the reference tree exists)."""
+    """make -C oracle (and the reference's own CPU step when ref and the Makefile finds the reference tree)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    if ref and os.path.isdir(os.environ.get("REF_DIR", "/root/reference")):
+    if ref and subprocess.run(["make", "-s", "-C", HERE, "has-ref"], capture_output=True).returncode == 0:
         subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref"], check=True)
+
+
+def ref_dir():
+    """The reference tree that _ref/libswarm_ref.so was built from (recorded by `make ref`), or None."""
+    rec = os.path.join(HERE, "_ref", "ref_dir.txt")
+    if not os.path.exists(rec):
+        return None
+    d = open(rec).read().strip()
+    return d if os.path.isdir(d) else None
 
 
 def lib():

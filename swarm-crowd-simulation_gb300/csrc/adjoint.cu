@@ -920,13 +920,23 @@ void launch_adjoint_step(AdjArgs& A, cudaStream_t st, int64_t* launches) {
 }
 
 namespace {
-int g_sms = 0, g_perSm = 0;
+// SM count and resident blocks of the fused reverse, per host thread and device ordinal
+constexpr int ADJ_MAX_DEVICES = 64;
+thread_local int g_smsOf[ADJ_MAX_DEVICES], g_perSmOf[ADJ_MAX_DEVICES];
+thread_local int g_sms = 0, g_perSm = 0;
 void fusedConfig() {
-    if (g_sms) return;
     int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_perSm, k_adj_step_fused<ADJ_LANES>, ADJ_FUSED_THREADS, 0);
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= ADJ_MAX_DEVICES) dev = 0;
+    if (!g_smsOf[dev]) {
+        int sms = 0, perSm = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_adj_step_fused<ADJ_LANES>, ADJ_FUSED_THREADS, 0) == cudaSuccess) {
+            g_smsOf[dev] = sms;
+            g_perSmOf[dev] = perSm;
+        }
+    }
+    g_sms = g_smsOf[dev] > 0 ? g_smsOf[dev] : 1;
+    g_perSm = g_perSmOf[dev];
 }
 }  // namespace
 

@@ -927,15 +927,21 @@ constexpr int FUSED_SMEM = WIN_CAP * (int(sizeof(float4)) + int(sizeof(float2)) 
 
 // The fused grid: one block per SM when the state fits (threads = n / SMs rounded up to a warp, 128..512; 128..1024
 // for a batch), else as many blocks as stay resident, each taking several tiles per phase
-// (The launch helpers' caches are per host thread: handles stepped from several threads share none of them.)
+// (The launch helpers' caches are per host thread and per device ordinal: handles stepped from several threads share
+// none of them, and a thread that steps handles on several GPUs keeps each GPU's own.)
+constexpr int MAX_DEVICES = 64;
+
+static int currentDevice() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) dev = 0;
+    return dev;
+}
+
 static int smCount() {
-    static thread_local int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    }
-    return sms;
+    static thread_local int sms[MAX_DEVICES] = {};
+    const int dev = currentDevice();
+    if (!sms[dev]) cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
+    return sms[dev];
 }
 
 static int fusedThreads(const StepArgs& A) {
@@ -955,21 +961,33 @@ int fusedScanTile(const StepArgs& A) {
 
 template <class Venue, bool kPerAgent, bool kB, bool kTape = false>
 static cudaError_t fusedImpl(const StepArgs& A0, cudaStream_t st) {
-    static thread_local bool smemSet = false;
-    if (!smemSet) {
-        cudaFuncSetAttribute(k_step_fused<Venue, kPerAgent, kB, kTape>, cudaFuncAttributeMaxDynamicSharedMemorySize, FUSED_SMEM);
-        smemSet = true;
+    // the dynamic shared memory limit is a per-device attribute of the kernel: set once per device, kept only when set
+    static thread_local bool smemSet[MAX_DEVICES] = {};
+    const int dev = currentDevice();
+    if (!smemSet[dev]) {
+        const cudaError_t e = cudaFuncSetAttribute(k_step_fused<Venue, kPerAgent, kB, kTape>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, FUSED_SMEM);
+        if (e != cudaSuccess) return e;
+        smemSet[dev] = true;
     }
     const int sms = smCount();
     StepArgs A = A0;
     const int threads = fusedThreads(A);
     A.scanTile = fusedScanTile(A);
-    static thread_local int occThreads = -1, occPerSm = 0;   // the occupancy of the last block size asked for
-    if (occThreads != threads) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occPerSm, k_step_fused<Venue, kPerAgent, kB, kTape>, threads, FUSED_SMEM);
-        occThreads = threads;
+    // the occupancy of the last block size asked for, per device
+    static thread_local int occThreads[MAX_DEVICES], occPerSm[MAX_DEVICES];
+    static thread_local bool occInit = false;
+    if (!occInit) {
+        for (int d = 0; d < MAX_DEVICES; ++d) occThreads[d] = -1;
+        occInit = true;
     }
-    int perSm = occPerSm;
+    if (occThreads[dev] != threads) {
+        const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occPerSm[dev], k_step_fused<Venue, kPerAgent, kB, kTape>,
+                                                                            threads, FUSED_SMEM);
+        if (e != cudaSuccess) return e;
+        occThreads[dev] = threads;
+    }
+    int perSm = occPerSm[dev];
     if (A.fusedBlocksPerSm > 0 && A.fusedBlocksPerSm < perSm) perSm = A.fusedBlocksPerSm;
     const int resident = perSm * sms;
     if (resident <= 0) return cudaErrorCooperativeLaunchTooLarge;

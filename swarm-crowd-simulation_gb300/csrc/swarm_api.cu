@@ -732,14 +732,15 @@ int swarm_step_host(SwarmHandle h, const float* in_boids, float* out_boids, int 
         h->hostIn = nullptr;
         h->hostOut = nullptr;
         if (rc != SWARM_OK) return rc;
-        return cudaOk(h, cudaStreamSynchronize(h->stream), "step sync") ? SWARM_OK : SWARM_E_CUDA;
+        // a barrier that gave up ends the launch before the output copy: the device flag says so
+        return swarm_synchronize(h);
     }
     // the read half only: the final pass writes every agent of the other half
     if (!cudaOk(h, cudaMemcpyAsync(h->state[h->readIdx], in_boids, bytes, cudaMemcpyHostToDevice, h->stream), "upload")) return SWARM_E_CUDA;
     const int rc = stepImpl(h, steps, false);
     if (rc != SWARM_OK) return rc;
     if (!cudaOk(h, cudaMemcpyAsync(out_boids, h->state[h->readIdx], bytes, cudaMemcpyDeviceToHost, h->stream), "download")) return SWARM_E_CUDA;
-    return cudaOk(h, cudaStreamSynchronize(h->stream), "step sync") ? SWARM_OK : SWARM_E_CUDA;
+    return swarm_synchronize(h);
 }
 
 int swarm_synchronize(SwarmHandle h) {

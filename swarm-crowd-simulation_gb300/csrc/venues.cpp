@@ -126,8 +126,12 @@ void fastMarchCpu(int nx, int ny, double h, std::vector<uint8_t> state, const fl
 std::atomic<int> navSolver{SWARM_NAV_CPU};
 
 // The builders' solver: fast marching here, or the GPU solver (the same floats) when selected
+// (SWARM_HOST_ONLY: this file compiled alone, without the CUDA library, for a host process that only builds venues;
+// there the GPU solver cannot be selected.)
 int fastMarch(int nx, int ny, double h, std::vector<uint8_t> state, const float* speed, float* out) {
+#ifndef SWARM_HOST_ONLY
     if (navSolver.load() == SWARM_NAV_GPU) return swarm_nav_field_gpu(nx, ny, h, state.data(), speed, out, nullptr);
+#endif
     fastMarchCpu(nx, ny, h, std::move(state), speed, out);
     return SWARM_OK;
 }
@@ -136,6 +140,9 @@ int fastMarch(int nx, int ny, double h, std::vector<uint8_t> state, const float*
 
 extern "C" int swarm_set_nav_solver(int solver) {
     if (solver != SWARM_NAV_CPU && solver != SWARM_NAV_GPU) return SWARM_E_INVALID;
+#ifdef SWARM_HOST_ONLY
+    if (solver == SWARM_NAV_GPU) return SWARM_E_INVALID;
+#endif
     return navSolver.exchange(solver);
 }
 

@@ -25,6 +25,87 @@ class SwarmError(RuntimeError):
     pass
 
 
+_H = C.c_void_p
+_SIG = {
+    "swarm_params_reference": [C.POINTER(SwarmParams)],
+    "swarm_params_si": [C.POINTER(SwarmParams)],
+    "swarm_create": [C.POINTER(SwarmParams), C.POINTER(SwarmVenue), C.c_int, C.POINTER(_H)],
+    "swarm_destroy": [_H],
+    "swarm_batch_create": [C.POINTER(SwarmParams), C.c_void_p, C.c_void_p, C.c_int, C.POINTER(_H)],
+    "swarm_set_stream": [_H, C.c_void_p],
+    "swarm_last_error": [_H, C.c_char_p, C.c_int],
+    "swarm_upload_state": [_H, C.POINTER(C.c_float), C.c_int],
+    "swarm_download_state": [_H, C.POINTER(C.c_float), C.c_int],
+    "swarm_upload_state_device": [_H, C.c_void_p, C.c_int],
+    "swarm_download_state_device": [_H, C.c_void_p, C.c_int],
+    "swarm_set_agent_params": [_H, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int],
+    "swarm_step": [_H, C.c_int],
+    "swarm_set_iterations": [_H, C.c_int],
+    "swarm_step_host": [_H, C.c_void_p, C.c_void_p, C.c_int, C.c_int],
+    "swarm_set_drive_table": [_H, C.POINTER(C.c_float), C.c_int],
+    "swarm_set_graph": [_H, C.c_int],
+    "swarm_set_fused": [_H, C.c_int],
+    "swarm_set_tuning": [_H, C.POINTER(SwarmTuning)],
+    "swarm_autotune": [_H, C.c_int, C.POINTER(SwarmTuning)],
+    "swarm_test_barrier_timeout": [_H],
+    "swarm_synchronize": [_H],
+    "swarm_get_grid": [_H, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_int],
+    "swarm_get_cells": [_H, C.POINTER(C.c_uint32), C.c_int],
+    "swarm_get_contacts": [_H, C.POINTER(C.c_uint8), C.c_int],
+    "swarm_set_timing": [_H, C.c_int],
+    "swarm_stage_times": [_H, C.POINTER(SwarmStageTimes)],
+    "swarm_launch_count": [_H, C.POINTER(C.c_int64)],
+    "swarm_metrics_enable": [_H, C.c_int, C.c_void_p],
+    "swarm_metrics_reset": [_H],
+    "swarm_metrics_read": [_H, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int],
+    "swarm_metric_thresholds_grid": [C.POINTER(SwarmVenue), C.c_int, C.c_void_p],
+    "swarm_hall_layout": [C.c_void_p, C.POINTER(SwarmVenue)],
+    "swarm_hall_fields": [C.c_void_p, C.POINTER(SwarmVenue), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                          C.POINTER(C.c_float)],
+    "swarm_adjoint_run": [_H, C.POINTER(SwarmLossSpec), C.c_int, C.c_int, C.POINTER(C.c_double),
+                          C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                          C.POINTER(SwarmAdjointStats)],
+    "swarm_adjoint_set_tape_budget": [_H, C.c_int64],
+    "swarm_set_relaxation_time": [_H, C.c_float],
+    "swarm_run_evacuation": [_H, C.c_int, C.c_void_p, C.POINTER(SwarmEvacuation)],
+    "swarm_snapshot_write": [C.c_char_p, C.POINTER(C.c_float), C.c_int],
+    "swarm_snapshot_read": [C.c_char_p, C.POINTER(C.c_float), C.c_int],
+    "swarm_snapshot_count": [C.c_char_p],
+    "swarm_sdf_read": [C.c_char_p, C.POINTER(C.c_float), C.c_int],
+    "swarm_nav_field_gpu": [C.c_int, C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.POINTER(C.c_float),
+                            C.POINTER(SwarmNavFieldStats)],
+    "swarm_nav_field_cpu": [C.c_int, C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.POINTER(C.c_float)],
+    "swarm_set_nav_solver": [C.c_int],
+    "swarm_hall_exit_fields": [C.c_void_p, C.POINTER(SwarmVenue), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                               C.c_void_p],
+    "swarm_bowl_exit_fields": [C.c_void_p, C.POINTER(SwarmVenue), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                               C.c_void_p],
+    "swarm_exit_choice_table": [C.POINTER(SwarmVenue), C.POINTER(SwarmExitChoiceSpec), C.c_void_p,
+                                C.POINTER(C.c_float)],
+    "swarm_set_exit_choice": [_H, C.POINTER(SwarmExitChoiceSpec)],
+    "swarm_get_exit_choice": [_H, C.c_void_p, C.c_int, C.c_void_p],
+    "swarm_bowl_layout": [C.c_void_p, C.POINTER(SwarmVenue)],
+    "swarm_bowl_fields": [C.c_void_p, C.POINTER(SwarmVenue), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                          C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_void_p, C.POINTER(C.c_float)],
+    "swarm_spawn_bowl": [C.c_void_p, C.c_float, C.c_uint64, C.c_float, C.c_float, C.c_float, C.c_float,
+                         C.c_float, C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)],
+    "swarm_spawn_lattice": [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_uint64,
+                            C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                            C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)],
+}
+
+
+def bind(L):
+    """Sets the C signatures of every entry point of _SIG that the library L exports (the CUDA library, or a host
+    build of the venue builders) and returns L."""
+    for name, args in _SIG.items():
+        if hasattr(L, name):
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = C.c_int
+    return L
+
+
 def lib():
     """The loaded CUDA library (raises if it has not been built)."""
     global _lib
@@ -32,94 +113,36 @@ def lib():
         if not os.path.exists(LIB_PATH):
             raise ImportError(f"{LIB_PATH} is missing: build it with `python swarm-crowd-simulation_gb300/build.py` "
                               "(or __graft_entry__.build()); there is no CPU fallback")
-        L = C.CDLL(LIB_PATH)
-        H = C.c_void_p
-        sig = {
-            "swarm_params_reference": [C.POINTER(SwarmParams)],
-            "swarm_params_si": [C.POINTER(SwarmParams)],
-            "swarm_create": [C.POINTER(SwarmParams), C.POINTER(SwarmVenue), C.c_int, C.POINTER(H)],
-            "swarm_destroy": [H],
-            "swarm_batch_create": [C.POINTER(SwarmParams), C.c_void_p, C.c_void_p, C.c_int, C.POINTER(H)],
-            "swarm_set_stream": [H, C.c_void_p],
-            "swarm_last_error": [H, C.c_char_p, C.c_int],
-            "swarm_upload_state": [H, C.POINTER(C.c_float), C.c_int],
-            "swarm_download_state": [H, C.POINTER(C.c_float), C.c_int],
-            "swarm_upload_state_device": [H, C.c_void_p, C.c_int],
-            "swarm_download_state_device": [H, C.c_void_p, C.c_int],
-            "swarm_set_agent_params": [H, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int],
-            "swarm_step": [H, C.c_int],
-            "swarm_set_iterations": [H, C.c_int],
-            "swarm_step_host": [H, C.c_void_p, C.c_void_p, C.c_int, C.c_int],
-            "swarm_set_drive_table": [H, C.POINTER(C.c_float), C.c_int],
-            "swarm_set_graph": [H, C.c_int],
-            "swarm_set_fused": [H, C.c_int],
-            "swarm_set_tuning": [H, C.POINTER(SwarmTuning)],
-            "swarm_autotune": [H, C.c_int, C.POINTER(SwarmTuning)],
-            "swarm_test_barrier_timeout": [H],
-            "swarm_synchronize": [H],
-            "swarm_get_grid": [H, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_int],
-            "swarm_get_cells": [H, C.POINTER(C.c_uint32), C.c_int],
-            "swarm_get_contacts": [H, C.POINTER(C.c_uint8), C.c_int],
-            "swarm_set_timing": [H, C.c_int],
-            "swarm_stage_times": [H, C.POINTER(SwarmStageTimes)],
-            "swarm_launch_count": [H, C.POINTER(C.c_int64)],
-            "swarm_metrics_enable": [H, C.c_int, C.c_void_p],
-            "swarm_metrics_reset": [H],
-            "swarm_metrics_read": [H, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int],
-            "swarm_metric_thresholds_grid": [C.POINTER(SwarmVenue), C.c_int, C.c_void_p],
-            "swarm_hall_layout": [C.c_void_p, C.POINTER(SwarmVenue)],
-            "swarm_hall_fields": [C.c_void_p, C.POINTER(SwarmVenue), C.POINTER(C.c_float), C.POINTER(C.c_float),
-                                  C.POINTER(C.c_float)],
-            "swarm_adjoint_run": [H, C.POINTER(SwarmLossSpec), C.c_int, C.c_int, C.POINTER(C.c_double),
-                                  C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
-                                  C.POINTER(SwarmAdjointStats)],
-            "swarm_adjoint_set_tape_budget": [H, C.c_int64],
-            "swarm_set_relaxation_time": [H, C.c_float],
-            "swarm_run_evacuation": [H, C.c_int, C.c_void_p, C.POINTER(SwarmEvacuation)],
-            "swarm_snapshot_write": [C.c_char_p, C.POINTER(C.c_float), C.c_int],
-            "swarm_snapshot_read": [C.c_char_p, C.POINTER(C.c_float), C.c_int],
-            "swarm_snapshot_count": [C.c_char_p],
-            "swarm_sdf_read": [C.c_char_p, C.POINTER(C.c_float), C.c_int],
-            "swarm_nav_field_gpu": [C.c_int, C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.POINTER(C.c_float),
-                                    C.POINTER(SwarmNavFieldStats)],
-            "swarm_nav_field_cpu": [C.c_int, C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.POINTER(C.c_float)],
-            "swarm_set_nav_solver": [C.c_int],
-            "swarm_hall_exit_fields": [C.c_void_p, C.POINTER(SwarmVenue), C.POINTER(C.c_float), C.POINTER(C.c_float),
-                                       C.c_void_p],
-            "swarm_bowl_exit_fields": [C.c_void_p, C.POINTER(SwarmVenue), C.POINTER(C.c_float), C.POINTER(C.c_float),
-                                       C.c_void_p],
-            "swarm_exit_choice_table": [C.POINTER(SwarmVenue), C.POINTER(SwarmExitChoiceSpec), C.c_void_p,
-                                        C.POINTER(C.c_float)],
-            "swarm_set_exit_choice": [H, C.POINTER(SwarmExitChoiceSpec)],
-            "swarm_get_exit_choice": [H, C.c_void_p, C.c_int, C.c_void_p],
-            "swarm_bowl_layout": [C.c_void_p, C.POINTER(SwarmVenue)],
-            "swarm_bowl_fields": [C.c_void_p, C.POINTER(SwarmVenue), C.POINTER(C.c_float), C.POINTER(C.c_float),
-                                  C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_void_p, C.POINTER(C.c_float)],
-            "swarm_spawn_bowl": [C.c_void_p, C.c_float, C.c_uint64, C.c_float, C.c_float, C.c_float, C.c_float,
-                                 C.c_float, C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)],
-            "swarm_spawn_lattice": [C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_uint64,
-                                    C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
-                                    C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)],
-        }
-        for name, args in sig.items():
-            f = getattr(L, name)
-            f.argtypes = args
-            f.restype = C.c_int
-        _lib = L
+        _lib = bind(C.CDLL(LIB_PATH))
     return _lib
+
+
+_gen = None
+
+
+def use_generator(L):
+    """The library the venue builders, spawns and parameter presets call from now on: a ctypes library exporting the
+    host entry points of csrc/venues.cpp and csrc/params.cpp (None: the CUDA library). The builders are host code, so
+    a host-only build of the same sources gives the same venues without loading the CUDA library."""
+    global _gen
+    _gen = None if L is None else bind(L)
+
+
+def generator():
+    return _gen if _gen is not None else lib()
 
 
 def params_reference():
     """The reference's constants (model units, K = 32), folded as the reference folds them."""
     p = SwarmParams()
-    _check(lib().swarm_params_reference(C.byref(p)), "swarm_params_reference")
+    _check(generator().swarm_params_reference(C.byref(p)), "swarm_params_reference")
     return p
 
 
 def params_si():
     """The SI preset of the grid venues (dt 0.05 s, K = 8, tau 0.5 s, per-agent radius and v0)."""
     p = SwarmParams()
-    _check(lib().swarm_params_si(C.byref(p)), "swarm_params_si")
+    _check(generator().swarm_params_si(C.byref(p)), "swarm_params_si")
     return p
 
 

@@ -10,7 +10,7 @@ import math
 
 import numpy as np
 
-from . import _check, lib
+from . import _check, generator
 from .abi import SWARM_VENUE_STADIUM, SwarmVenue, fptr
 
 SDF_RES = 130
@@ -56,7 +56,7 @@ class Venue:
         """Per 1 m cell threshold masses of a grid venue (walkable area sampled from its wall SDF)."""
         res = res or self.struct.metric_res
         out = np.empty((res * res, 4), np.uint32)
-        _check(lib().swarm_metric_thresholds_grid(C.byref(self.struct), int(res), out.ctypes.data_as(C.c_void_p)),
+        _check(generator().swarm_metric_thresholds_grid(C.byref(self.struct), int(res), out.ctypes.data_as(C.c_void_p)),
                "swarm_metric_thresholds_grid")
         return res, out
 
@@ -92,11 +92,11 @@ class Venue:
         for i, (w, c, width) in enumerate(doors):
             spec.door_wall[i], spec.door_center[i], spec.door_width[i] = int(w), float(c), float(width)
         v = SwarmVenue()
-        _check(lib().swarm_hall_layout(C.byref(spec), C.byref(v)), "swarm_hall_layout")
+        _check(generator().swarm_hall_layout(C.byref(spec), C.byref(v)), "swarm_hall_layout")
         wall = np.empty(v.wall_nx * v.wall_ny, np.float32)
         nav = np.empty(v.nav_nx * v.nav_ny, np.float32)
         boxes = np.empty(max(1, 4 * v.n_exits), np.float32)
-        _check(lib().swarm_hall_fields(C.byref(spec), C.byref(v), fptr(wall), fptr(nav), fptr(boxes)), "swarm_hall_fields")
+        _check(generator().swarm_hall_fields(C.byref(spec), C.byref(v), fptr(wall), fptr(nav), fptr(boxes)), "swarm_hall_fields")
         v.wall_sdf = fptr(wall)
         v.nav_dist = fptr(nav)
         v.exit_boxes = fptr(boxes)
@@ -106,12 +106,12 @@ class Venue:
 
 def _bowl(spec, name):
     v = SwarmVenue()
-    _check(lib().swarm_bowl_layout(C.byref(spec), C.byref(v)), "swarm_bowl_layout")
+    _check(generator().swarm_bowl_layout(C.byref(spec), C.byref(v)), "swarm_bowl_layout")
     nw, nn = v.wall_nx * v.wall_ny, v.nav_nx * v.nav_ny
     wall, floor, speed = np.empty(nw, np.float32), np.empty(nw, np.float32), np.empty(nw, np.float32)
     nav, mask = np.empty(nn, np.float32), np.empty(nn, np.uint8)
     boxes = np.empty(4 * v.n_exits, np.float32)
-    _check(lib().swarm_bowl_fields(C.byref(spec), C.byref(v), fptr(wall), fptr(nav), fptr(floor), fptr(speed),
+    _check(generator().swarm_bowl_fields(C.byref(spec), C.byref(v), fptr(wall), fptr(nav), fptr(floor), fptr(speed),
                                    mask.ctypes.data_as(C.c_void_p), fptr(boxes)), "swarm_bowl_fields")
     v.wall_sdf, v.nav_dist, v.floor_height, v.speed_factor = fptr(wall), fptr(nav), fptr(floor), fptr(speed)
     v.exit_mask = mask.ctypes.data_as(C.POINTER(C.c_uint8))
@@ -134,7 +134,7 @@ def exit_fields(venue):
     fields = np.empty((n, v.nav_nx * v.nav_ny), np.float32)
     widths = np.empty(n, np.float32)
     types = np.empty(n, np.uint8)
-    fn = lib().swarm_bowl_exit_fields if bowl else lib().swarm_hall_exit_fields
+    fn = generator().swarm_bowl_exit_fields if bowl else generator().swarm_hall_exit_fields
     _check(fn(C.byref(spec), C.byref(v), fptr(fields), fptr(widths), types.ctypes.data_as(C.c_void_p)),
            "swarm_bowl_exit_fields" if bowl else "swarm_hall_exit_fields")
     return fields, widths, types
@@ -146,7 +146,7 @@ def spawn_bowl(spec, jitter=0.03, seed=0, r=(0.20, 0.25), v=(1.34, 0.26, 0.6, 2.
     boids = np.empty((n, 8), np.float32)
     rad = np.empty(n, np.float32)
     v0 = np.empty(n, np.float32)
-    _check(lib().swarm_spawn_bowl(C.byref(spec), jitter, seed, r[0], r[1], v[0], v[1], v[2], v[3], fptr(boids), fptr(rad),
+    _check(generator().swarm_spawn_bowl(C.byref(spec), jitter, seed, r[0], r[1], v[0], v[1], v[2], v[3], fptr(boids), fptr(rad),
                                   fptr(v0)), "swarm_spawn_bowl")
     return boids, rad, v0
 
@@ -158,7 +158,7 @@ def spawn_lattice(nx, ny, n=None, spacing=0.5, center=(0.0, 0.0), jitter=0.05, s
     boids = np.empty((n, 8), np.float32)
     rad = np.empty(n, np.float32)
     v0 = np.empty(n, np.float32)
-    _check(lib().swarm_spawn_lattice(nx, ny, n, spacing, center[0], center[1], jitter, seed, r[0], r[1], v[0], v[1], v[2],
+    _check(generator().swarm_spawn_lattice(nx, ny, n, spacing, center[0], center[1], jitter, seed, r[0], r[1], v[0], v[1], v[2],
                                      v[3], fptr(boids), fptr(rad), fptr(v0)), "swarm_spawn_lattice")
     return boids, rad, v0
 

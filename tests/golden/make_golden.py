@@ -26,11 +26,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "..", ".."))
 from oracle import oracle as O  # noqa: E402
 
-REF_DIR = os.environ.get("REF_DIR", "/root/reference")
-
-
 def main():
-    sdf_path = os.path.join(REF_DIR, "stadium.sdf")
+    O.build(ref=True)
+    ref_dir = O.ref_dir()
+    assert ref_dir, "the reference tree is needed: REF_DIR=<tree> make -C oracle ref"
+    sdf_path = os.path.join(ref_dir, "stadium.sdf")
     raw = open(sdf_path, "rb").read()
     with open(os.path.join(HERE, "stadium_sdf.zlib"), "wb") as f:
         f.write(zlib.compress(raw, 9))

@@ -79,7 +79,7 @@ def test_thread_invariance(terrace, terrace_golden):
 @pytest.mark.skipif(not O.ref_available(), reason="the reference tree is not in this container")
 def test_live_reference_matches_oracle_at_16384_with_fewer_iterations(terrace, stadium_sdf):
     P, venue = terrace
-    assert O.ref_load_sdf(os.path.join(os.environ.get("REF_DIR", "/root/reference"), "stadium.sdf"))
+    assert O.ref_load_sdf(os.path.join(O.ref_dir(), "stadium.sdf"))
     spawn = O.ref_spawn_terrace(16384, 7)
     for k in (32, 3, 1, 0):
         ref = O.RefSim("terrace")

@@ -59,6 +59,26 @@ def test_step_host_pinned_and_pageable_match_the_device_path(scene, steps, fused
     sim.close()
 
 
+def test_step_host_reports_a_barrier_timeout(scene):
+    """A grid barrier that gives up ends the fused launch before the copy into the caller's pinned output: the call
+    must return SWARM_E_TIMEOUT (-4), not success with a stale output, and the handle must step normally after."""
+    import torch
+    import swarm_gb300
+    P, venue, b, r, v0 = scene
+    n = b.shape[0]
+    ref = _device_reference(P, venue, b, r, v0, 1)
+    sim = swarm_gb300.CrowdSim(P, venue, n)
+    sim.set_agent_params(r, v0)
+    lib = swarm_gb300.lib()
+    h_in = torch.from_numpy(b.copy()).pin_memory()
+    h_out = torch.zeros_like(h_in).pin_memory()
+    assert lib.swarm_test_barrier_timeout(sim._h) == 0
+    assert lib.swarm_step_host(sim._h, h_in.data_ptr(), h_out.data_ptr(), n, 1) == -4
+    assert lib.swarm_step_host(sim._h, h_in.data_ptr(), h_out.data_ptr(), n, 1) == 0
+    assert np.array_equal(_bits(h_out.numpy()), _bits(ref))
+    sim.close()
+
+
 def test_step_host_in_place_and_continued_on_the_device(scene):
     """One pinned buffer as input and output, twice in a row, then two device steps: the same bits as five device
     steps from the start."""

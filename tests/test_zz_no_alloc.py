@@ -1,5 +1,6 @@
 """The key sort without device allocation (swarm_sort_grid_noalloc): for callers that cannot allocate device memory
-while they run, e.g. inside host callbacks or in deployments that fix their whole footprint at start-up. Called
+while they run, e.g. a plug-in step in a host frame loop (where cudaMalloc / cudaFree may synchronise the device) or a
+deployment that fixes its whole footprint at start-up. Called
 through the C ABI on device arrays, it must give exactly the step's own sort (the sorted pairs and the cell table
 that swarm_get_grid / swarm_get_cells return), on two calls in a row, whose shared working array keeps the first
 call's contents. Integer outputs: the comparison is exact."""
@@ -75,6 +76,8 @@ def test_noalloc_rejects_sizes_beyond_its_limit(built):
     f.restype = C.c_int
     f.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float,
                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
-    dummy = C.c_void_p(16)   # never dereferenced: the size checks come first
+    dummy = C.c_void_p(16)   # never dereferenced: the size and alignment checks come first
     assert f(dummy, 65537, 10, 10, 0.0, 0.0, 1.0, 1.0, dummy, dummy, dummy, None) == -1
     assert f(dummy, 100, 400, 400, 0.0, 0.0, 1.0, 1.0, dummy, dummy, dummy, None) == -1
+    # a state that is not 16-byte aligned (it is read as float4) is refused before any launch
+    assert f(C.c_void_p(24), 100, 10, 10, 0.0, 0.0, 1.0, 1.0, dummy, dummy, dummy, None) == -1
