@@ -44,8 +44,41 @@ enum {
     /* A plan venue on grids, SI units, per-agent radius and desired speed: a horizontal wall SDF, a geodesic
      * distance-to-exit field whose negative normalised gradient is the walking direction, an optional floor
      * heightfield and stair speed factors. The synthetic halls and the seated bowl are built as these. */
-    SWARM_VENUE_GRID = 1
+    SWARM_VENUE_GRID = 1,
+    /* The reference's analytic seated venues (venues S, M and L: swarm::SeatedLayout, include/swarm/venue.hpp:99-138),
+     * model units, uniform body: a closed-form heightfield of square-ring rows, gangway inclines, barrier, concourse and
+     * walls, evaluated exactly (src/venue.cpp:411-908, shaders/venue_seated.glsl), the pitch fence of the terrace, and
+     * e_goal from the reference's navigation field (its GpuNavCell table) or the drive table. */
+    SWARM_VENUE_SEATED = 2
 };
+
+/* swarm::SeatedLayout (include/swarm/venue.hpp:99-138): the seated venue's breakpoints in model units, as the reference's
+ * buildSeatedLayout computes them (src/venue.cpp:170-327) -- the values its shader preamble emits (VS_* literals). In the
+ * folded frame lat = min(|x|, |y|), dep = max(|x|, |y|). */
+#define SWARM_SEATED_MAX_GANGWAYS 8
+#define SWARM_SEATED_MAX_DOORS 8
+typedef struct SwarmSeatedLayout {
+    float stand_front, row0, row_depth, clearway;
+    int32_t rows;
+    float conc_front, conc_back, outer_face, landing_end;
+    float avenue_half, lat0, gangway_lo, gangway_hi, exit_lo, exit_hi, corner_inset;
+    float seat_inset, face_margin, wall_above, wall_clear;
+    float first_row, row_rise, seat_top, barrier_top, concourse_z, wall_top, rake;
+    int32_t max_band_steps;
+    int32_t gangways;                                   /* straight gangways per wing */
+    float gw_lo[SWARM_SEATED_MAX_GANGWAYS], gw_hi[SWARM_SEATED_MAX_GANGWAYS];
+    int32_t gw_row[SWARM_SEATED_MAX_GANGWAYS], gw_seated[SWARM_SEATED_MAX_GANGWAYS];
+    int32_t doors;                                      /* concourse doors per wing */
+    float door_lo[SWARM_SEATED_MAX_DOORS], door_hi[SWARM_SEATED_MAX_DOORS];
+    float corner_door_lo;                               /* >= 1e8: no corner door */
+} SwarmSeatedLayout;
+
+/* The reference's GpuNavCell (include/swarm/gpu_types.hpp:42-46): one cell of a seated venue's navigation field -- the
+ * anchor (the first vertex of the cell's shortest any-angle path to an exit), the distance, and info = the exit id
+ * (bits 0-7) | SWARM_NAV_FIT | SWARM_NAV_REACHABLE. */
+typedef struct SwarmNavCell { float anchor_x, anchor_y, dist; uint32_t info; } SwarmNavCell;
+#define SWARM_NAV_FIT 0x100u
+#define SWARM_NAV_REACHABLE 0x200u
 
 /* Every model constant of the step (the reference's include/swarm/sim_params.hpp, including its folded constant
  * expressions). swarm_params_reference() fills the reference's values (model units, K = 32);
@@ -94,7 +127,10 @@ typedef struct SwarmParams {
     float metric_cells_per_unit;  /* metric cells per length unit */
     float metric_speed_scale;     /* m/s per speed unit */
     float r_pair_max;             /* per-agent body: the largest radius any agent may have (bounds the search disk) */
-    float pad2[5];
+    /* incline speed and stair spacing on seated venues (sim_params.hpp:429-480): V_STAIR_UP, V_STAIR_DOWN,
+     * 1 / INCLINE_REF_SLOPE, T_HEADWAY (model units) */
+    float v_stair_up, v_stair_down, incline_inv_ref_slope, t_headway;
+    float pad2[1];
 } SwarmParams;
 
 /* The venue: the neighbour grid, the exit test, and the static fields of its kind. Host pointers; swarm_create
@@ -129,6 +165,17 @@ typedef struct SwarmVenue {
      * parked when the nav node nearest to it is an exit node (or it leaves the domain) instead of by the exit
      * rectangle: exits anywhere in the plan, such as vomitories inside a seating bowl. */
     const uint8_t* exit_mask;
+    /* seated venues (SWARM_VENUE_SEATED): the layout; the navigation field (nav_res x nav_res cells, x fastest, cell
+     * (i, j) covering origin + [i, i + 1) x cell: nav::Grid, include/swarm/nav_field.hpp:69-79; NULL: e_goal comes from
+     * the drive table alone, zero without one); the model options (ModelOptions, include/swarm/exit_choice.hpp:82-90):
+     * incline_speed = the free speed by the slope along e_goal, stair_headway = the headway time gap by the slope, with
+     * stair_t_up / stair_t_down its values on a full-slope incline (T_HEADWAY_STAIR_UP / _DOWN, model time) */
+    const SwarmSeatedLayout* seated;
+    const SwarmNavCell* nav_cells;
+    int32_t nav_res;
+    float nav_grid_origin, nav_grid_cell, nav_grid_inv_cell;
+    int32_t incline_speed, stair_headway;
+    float stair_t_up, stair_t_down;
 } SwarmVenue;
 
 typedef struct SwarmSim* SwarmHandle;

@@ -15,6 +15,13 @@
 
 #include <glad/glad.h>
 
+// the seated venues' test scenarios (header-only harness code of the reference: the dense forced scenario's plans and
+// drive directions) and this project's C ABI types (the export format of the layout and the navigation table)
+#include <tools/venue_s.hpp>
+#include <swarm/nav_field.hpp>
+#include <swarm/exit_choice.hpp>
+#include "../include/swarm_cuda.h"
+
 #include <cstdint>
 #include <cstring>
 #include <exception>
@@ -33,6 +40,7 @@ std::string g_err;
 struct RefSim {
     swarm::CpuCrowdSim sim;
     std::vector<swarm::GpuBoid> scratch;
+    std::vector<glm::vec2> drive;   // the forced e_goal table (setDriveTable keeps a pointer to it)
 };
 
 swarm::CpuCrowdSim::SortMode sortMode(int m) {
@@ -77,8 +85,160 @@ void* ref_create(const char* venue, int sort, int threads) {
     try {
         const swarm::Venue& v = swarm::venueByName(venue);
         std::vector<float> sdf = v.seated() ? std::vector<float>{} : swarm::sdfVolumeCPU();
-        return new RefSim{ swarm::CpuCrowdSim(v, std::move(sdf), threads, sortMode(sort)), {} };
+        return new RefSim{ swarm::CpuCrowdSim(v, std::move(sdf), threads, sortMode(sort)), {}, {} };
     } catch (const std::exception& e) { g_err = e.what(); return nullptr; }
+}
+
+// CpuCrowdSim with explicit ModelOptions (include/swarm/exit_choice.hpp:82-90): exit_choice 0 nearest / 1 queue-aware,
+// incline 0/1, stair 0 off / 1 empirical / 2 conservative
+void* ref_create_opts(const char* venue, int sort, int threads, int exit_choice, int incline, int stair) {
+    try {
+        const swarm::Venue& v = swarm::venueByName(venue);
+        std::vector<float> sdf = v.seated() ? std::vector<float>{} : swarm::sdfVolumeCPU();
+        swarm::ModelOptions o;
+        o.exitChoice = exit_choice ? swarm::ExitChoice::QueueAware : swarm::ExitChoice::Nearest;
+        o.inclineSpeed = incline != 0;
+        o.stairFlow = stair == 1 ? swarm::StairFlow::Empirical : stair == 2 ? swarm::StairFlow::Conservative : swarm::StairFlow::Off;
+        return new RefSim{ swarm::CpuCrowdSim(v, o, std::move(sdf), threads, sortMode(sort)), {}, {} };
+    } catch (const std::exception& e) { g_err = e.what(); return nullptr; }
+}
+
+// setDriveTable: e_goal of agent i = dirs[2i..2i+1] from the next step on; NULL: the venue's own goal
+int ref_set_drive(void* h, const float* dirs, int n) {
+    try {
+        RefSim* r = static_cast<RefSim*>(h);
+        if (!dirs) { r->sim.setDriveTable(nullptr); return 0; }
+        r->drive.resize(size_t(n));
+        std::memcpy(r->drive.data(), dirs, size_t(n) * sizeof(glm::vec2));
+        r->sim.setDriveTable(&r->drive);
+        return 0;
+    } catch (const std::exception& e) { g_err = e.what(); return -1; }
+}
+
+// A seated venue's layout in the C ABI's format, and its neighbour grid and exit test
+int ref_seated_layout(const char* venue, SwarmSeatedLayout* out, int* grid_res, float* domain_min, float* domain_span,
+                      float* exit_depth, float* exit_max_z) {
+    try {
+        const swarm::Venue& v = swarm::venueByName(venue);
+        if (!v.seated()) { g_err = "not a seated venue"; return -1; }
+        const swarm::SeatedLayout& L = v.layout;
+        SwarmSeatedLayout o{};
+        o.stand_front = L.standFront; o.row0 = L.row0; o.row_depth = L.rowDepth; o.clearway = L.clearway; o.rows = L.rows;
+        o.conc_front = L.concFront; o.conc_back = L.concBack; o.outer_face = L.outerFace; o.landing_end = L.landingEnd;
+        o.avenue_half = L.avenueHalf; o.lat0 = L.lat0; o.gangway_lo = L.gangwayLo; o.gangway_hi = L.gangwayHi;
+        o.exit_lo = L.exitLo; o.exit_hi = L.exitHi; o.corner_inset = L.cornerInset; o.seat_inset = L.seatInset;
+        o.face_margin = L.faceMargin; o.wall_above = L.wallAbove; o.wall_clear = L.wallClear;
+        o.first_row = L.firstRow; o.row_rise = L.rowRise; o.seat_top = L.seatTop; o.barrier_top = L.barrierTop;
+        o.concourse_z = L.concourseZ; o.wall_top = L.wallTop; o.rake = L.rake; o.max_band_steps = L.maxBandSteps;
+        o.gangways = L.gangways;
+        for (int i = 0; i < SWARM_SEATED_MAX_GANGWAYS; ++i) {
+            o.gw_lo[i] = L.gwLo[size_t(i)]; o.gw_hi[i] = L.gwHi[size_t(i)];
+            o.gw_row[i] = L.gwRow[size_t(i)]; o.gw_seated[i] = L.gwSeated[size_t(i)];
+        }
+        o.doors = L.doors;
+        for (int i = 0; i < SWARM_SEATED_MAX_DOORS; ++i) { o.door_lo[i] = L.doorLo[size_t(i)]; o.door_hi[i] = L.doorHi[size_t(i)]; }
+        o.corner_door_lo = L.cornerDoorLo;
+        *out = o;
+        *grid_res = v.gridRes; *domain_min = v.domainMin; *domain_span = v.domainSpan;
+        *exit_depth = v.exitDepth; *exit_max_z = v.exitMaxZ;
+        return 0;
+    } catch (const std::exception& e) { g_err = e.what(); return -1; }
+}
+
+// sim_params.hpp's incline and stair constants: V_STAIR_UP, V_STAIR_DOWN, INCLINE_INV_REF_SLOPE, T_HEADWAY,
+// T_HEADWAY_STAIR_UP, T_HEADWAY_STAIR_DOWN, T_HEADWAY_STAIR_UP_CONSERVATIVE, T_HEADWAY_STAIR_DOWN_CONSERVATIVE
+int ref_incline_constants(float* out8) {
+    const float v[8] = {swarm::V_STAIR_UP, swarm::V_STAIR_DOWN, swarm::INCLINE_INV_REF_SLOPE, swarm::T_HEADWAY,
+                        swarm::T_HEADWAY_STAIR_UP, swarm::T_HEADWAY_STAIR_DOWN, swarm::T_HEADWAY_STAIR_UP_CONSERVATIVE,
+                        swarm::T_HEADWAY_STAIR_DOWN_CONSERVATIVE};
+    std::memcpy(out8, v, sizeof v);
+    return 0;
+}
+
+// The venue's navigation field as its GPU table (nav::gpuCells of nav::forVenue: built, or read from the cache
+// directory SWARM_NAV_CACHE); returns the grid's res (cells per axis), writes its origin, cell and 1 / cell
+int ref_nav_table(const char* venue, SwarmNavCell* out, int capacity, float* origin, float* cell, float* inv_cell) {
+    try {
+        const swarm::Venue& v = swarm::venueByName(venue);
+        const swarm::nav::Field& f = swarm::nav::forVenue(v);
+        const std::vector<swarm::GpuNavCell> cells = swarm::nav::gpuCells(f);
+        if (out) {
+            if (capacity < int(cells.size())) { g_err = "capacity"; return -1; }
+            std::memcpy(out, cells.data(), cells.size() * sizeof(swarm::GpuNavCell));
+        }
+        *origin = f.grid.origin; *cell = f.grid.cell; *inv_cell = f.grid.invCell;
+        return f.grid.res;
+    } catch (const std::exception& e) { g_err = e.what(); return -1; }
+}
+
+// The reference's own seated-venue functions, point by point (the harness's counterpart, same op codes):
+// 0 seated::floorHeight | 1 cellKey | 2 sdfGrad | 3 wall | 4 stepUpScan | 5 floorSlope | 6 nav::goal (forVenue's field)
+int ref_seated_eval(const char* venue, int op, int n, const float* in, float* out) {
+    try {
+        const swarm::Venue& v = swarm::venueByName(venue);
+        const swarm::SeatedLayout& L = v.layout;
+        const swarm::nav::Field* f = op == 6 ? &swarm::nav::forVenue(v) : nullptr;
+        for (int i = 0; i < n; ++i) {
+            switch (op) {
+            case 0: out[i] = swarm::seated::floorHeight(L, glm::vec2(in[2 * i], in[2 * i + 1])); break;
+            case 1: { const glm::vec2 k = swarm::seated::cellKey(L, glm::vec2(in[2 * i], in[2 * i + 1])); out[2 * i] = k.x; out[2 * i + 1] = k.y; break; }
+            case 2: {
+                const glm::vec4 g = swarm::seated::sdfGrad(L, glm::vec3(in[3 * i], in[3 * i + 1], in[3 * i + 2]));
+                out[4 * i] = g.x; out[4 * i + 1] = g.y; out[4 * i + 2] = g.z; out[4 * i + 3] = g.w;
+                break;
+            }
+            case 3: {
+                const glm::vec3 w = swarm::seated::wall(L, glm::vec3(in[4 * i], in[4 * i + 1], in[4 * i + 2]), in[4 * i + 3]);
+                out[3 * i] = w.x; out[3 * i + 1] = w.y; out[3 * i + 2] = w.z;
+                break;
+            }
+            case 4: {
+                glm::vec2 nn;
+                const float t = swarm::seated::stepUpScan(L, glm::vec2(in[5 * i], in[5 * i + 1]), glm::vec2(in[5 * i + 2], in[5 * i + 3]), in[5 * i + 4], nn);
+                out[3 * i] = t; out[3 * i + 1] = nn.x; out[3 * i + 2] = nn.y;
+                break;
+            }
+            case 5: out[i] = swarm::seated::floorSlope(L, glm::vec2(in[4 * i], in[4 * i + 1]), glm::vec2(in[4 * i + 2], in[4 * i + 3])); break;
+            case 6: {
+                const glm::vec2 e = swarm::nav::goal(*f, L, glm::vec3(in[3 * i], in[3 * i + 1], in[3 * i + 2]));
+                out[2 * i] = e.x; out[2 * i + 1] = e.y;
+                break;
+            }
+            default: return -1;
+            }
+        }
+        return 0;
+    } catch (const std::exception& e) { g_err = e.what(); return -1; }
+}
+
+// The dense forced scenario of the reference's venue tests (tools/venue_s.hpp denseSetup): every seat occupied, padded
+// with parked agents to a power of two; returns the agent count
+int ref_dense_setup(const char* venue, float* boids, int capacity) {
+    try {
+        const swarm::Venue& v = swarm::venueByName(venue);
+        const swarm::venue_s::Setup st = swarm::venue_s::denseSetup(v.layout);
+        if (boids) {
+            if (capacity < int(st.boids.size())) { g_err = "capacity"; return -1; }
+            std::memcpy(boids, st.boids.data(), st.boids.size() * sizeof(swarm::GpuBoid));
+        }
+        return int(st.boids.size());
+    } catch (const std::exception& e) { g_err = e.what(); return -1; }
+}
+
+// Its drive table for a state (tools/venue_s.hpp driveTable over denseSetup's plans): out[2i..2i+1] = e_goal of agent i
+int ref_dense_drive(const char* venue, const float* state, int n, float* out) {
+    try {
+        const swarm::Venue& v = swarm::venueByName(venue);
+        static std::vector<swarm::venue_s::Plan> plans;
+        static std::string plansOf;
+        if (plansOf != venue) { plans = swarm::venue_s::denseSetup(v.layout).plans; plansOf = venue; }
+        std::vector<swarm::GpuBoid> s(static_cast<size_t>(n));
+        std::memcpy(s.data(), state, size_t(n) * sizeof(swarm::GpuBoid));
+        std::vector<glm::vec2> t;
+        swarm::venue_s::driveTable(v.layout, plans, s, t);
+        std::memcpy(out, t.data(), t.size() * sizeof(glm::vec2));
+        return 0;
+    } catch (const std::exception& e) { g_err = e.what(); return -1; }
 }
 
 void ref_destroy(void* h) { delete static_cast<RefSim*>(h); }

@@ -136,6 +136,11 @@ extern "C" int swarm_params_reference(SwarmParams* p) {
     p->metric_cells_per_unit = 31.25f;
     p->metric_speed_scale = float(double(kWorldScale) / double(kTimeScale));
     p->r_pair_max = bodyRadius;
+    // incline speed and stair spacing (sim_params.hpp:447-454), folded in double from the decimal literals
+    p->v_stair_up = float(foldDecimal(0.58f) * foldDecimal(kTimeScale) / foldDecimal(kWorldScale));
+    p->v_stair_down = float(foldDecimal(0.655f) * foldDecimal(kTimeScale) / foldDecimal(kWorldScale));
+    p->incline_inv_ref_slope = float(1.0 / foldDecimal(0.50952545f));
+    p->t_headway = tHeadway;
     return SWARM_OK;
 }
 
@@ -199,5 +204,9 @@ extern "C" int swarm_params_si(SwarmParams* p) {
     p->metric_cells_per_unit = 1.0f;
     p->metric_speed_scale = 1.0f;
     p->r_pair_max = 0.25f;   // the spawn's largest radius; swarm_set_agent_params checks every radius against it
+    p->v_stair_up = 0.58f;
+    p->v_stair_down = 0.655f;
+    p->incline_inv_ref_slope = ref.incline_inv_ref_slope;
+    p->t_headway = 0.3f;
     return SWARM_OK;
 }

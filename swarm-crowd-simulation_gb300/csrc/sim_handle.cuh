@@ -41,6 +41,7 @@ struct SwarmSim {
     uint2* rowsB = nullptr;
     float2* goal = nullptr;
     int* errFlag = nullptr;
+    int* errHost = nullptr;     // pinned host word: errFlag copied in stream order (swarm_step_host reads it after one sync)
     unsigned* barrier = nullptr;
     unsigned long long* stamps = nullptr;
     bool fused = true;          // the whole step as one persistent kernel when the grid fits on the GPU
@@ -70,6 +71,8 @@ struct SwarmSim {
     uint32_t* dInstSlot = nullptr;
     std::vector<int> instStart;   // first agent of each instance, + the total
     float *dSdf = nullptr, *dWall = nullptr, *dNav = nullptr, *dFloor = nullptr, *dSpeed = nullptr;
+    SwarmSeatedLayout seatLayout{};     // seated venues: the layout (kernel parameters)
+    float4* dNavCells = nullptr;        //   and the navigation field's cells (null: drive table / router)
     float2* dWallFloor = nullptr;   // the wall SDF and floor heights interleaved (venues with a floor grid)
     uint8_t* dMask = nullptr;
     float speedMax = 1.0f;      // the largest of 1 and the venue's speed factors
@@ -114,6 +117,16 @@ struct SwarmSim {
     void dropGraphs() {
         for (auto& g : graph) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
         for (auto& row : stageGraph) for (auto& g : row) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    }
+    // A set device error flag: clear it and the barrier words and counts a wait that gave up left behind, and report
+    int deviceError(int flag);
+    // The end of a host-buffer call: the error flag copied into errHost behind the step's work, one stream sync, then
+    // the flag read from host memory (no second, blocking copy)
+    int finishWithFlag() {
+        if (cudaMemcpyAsync(errHost, errFlag, sizeof(int), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+            cudaStreamSynchronize(stream) != cudaSuccess)
+            return fail(SWARM_E_CUDA, "step sync");
+        return *errHost ? deviceError(*errHost) : SWARM_OK;
     }
     int enqueueStages(int in, int s0, int s1);
     int captureStages(int in, int s0, int s1, cudaGraphExec_t* out);

@@ -38,6 +38,14 @@ struct VenueArgs {
     const float* speedF;
     const uint8_t* exitMask;    // optional: nonzero at the nav nodes beyond an exit
     uint32_t cellOffset;    // batched instances: this instance's first cell in the shared key space (0 otherwise)
+    // seated (the reference's analytic venues): the layout, read from the kernel parameters (uniform across a warp);
+    // the navigation field's cells (anchor x, anchor y, distance, info bits), navRes^2, x fastest
+    SwarmSeatedLayout seat;
+    const float4* navCells;
+    int32_t navRes;
+    float navOrigin, navCell, navInv;
+    int32_t incline, stairHw;   // the incline speed; the stair spacing, with its time gaps up / down
+    float stairTUp, stairTDown;
 };
 
 struct StepArgs {

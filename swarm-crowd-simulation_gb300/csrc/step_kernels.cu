@@ -23,6 +23,7 @@
 
 #include "device_math.cuh"
 #include "venue_grid.cuh"
+#include "venue_seated.cuh"
 #include "venue_stadium.cuh"
 
 namespace swarm_gpu {
@@ -298,7 +299,8 @@ __global__ void k_rank_gather(StepArgs A) {
 // ---- the physics passes ----
 template <class Venue>
 struct Body {
-    static constexpr bool kUniform = std::is_same<Venue, Stadium>::value;
+    // the reference's own venues: one body radius and free speed for every agent (model units)
+    static constexpr bool kUniform = std::is_same<Venue, Stadium>::value || std::is_same<Venue, Seated>::value;
 };
 
 template <class Venue>
@@ -390,7 +392,11 @@ __device__ __forceinline__ void predictCore(const StepArgs& A, int s, const Nbr&
     // cannot lower v_des; the separation ends at R_SEP_ij, nearer still. 1 % slack covers the float rounding.
     const float vFreeSelf = kUniform ? P.v_max : A.prm[s].y * ven.speedFactor(xyz(p));
     const float dcMax = kUniform ? P.body_diam : ri + P.r_pair_max;
-    const float reach = smax(dcMax + vFreeSelf / P.headway_rate, kUniform ? P.r_sep : dcMax + P.sep_margin) * 1.01f + margin;
+    // (seated venues: the stair spacing's time gaps are longer than T_HEADWAY, its free speeds lower than V_MAX)
+    float headway;
+    if constexpr (std::is_same<Venue, Seated>::value) headway = vFreeSelf * ven.maxHeadwayTime();
+    else headway = vFreeSelf / P.headway_rate;
+    const float reach = smax(dcMax + headway, kUniform ? P.r_sep : dcMax + P.sep_margin) * 1.01f + margin;
     const float rPerc = smin(sqrtf(P.r_perc2) + margin, reach);
     const float reach2 = reach * reach;
     // every row's slot range first (independent loads, issued together), then the rows in order
@@ -448,7 +454,9 @@ __device__ __forceinline__ void predictCore(const StepArgs& A, int s, const Nbr&
     }
     if constexpr (kTape) A.tapePred[s] = make_float4(sep.x, sep.y, sAhead, __int_as_float(jstar));
     float vDes;
-    if (kUniform) {
+    if constexpr (std::is_same<Venue, Seated>::value) {
+        vDes = ven.desiredSpeed(xy(p), eGoal, sAhead);   // the incline speed and stair spacing when on
+    } else if (kUniform) {
         vDes = sclamp((sAhead - P.body_diam) * P.headway_rate, 0.0f, P.v_max) * length(eGoal);
     } else {
         const float vFree = A.prm[s].y * ven.speedFactor(xyz(p));
@@ -1007,6 +1015,7 @@ static cudaError_t fusedImpl(const StepArgs& A0, cudaStream_t st) {
 
 cudaError_t launch_step_fused(const StepArgs& A, cudaStream_t st) {
     if (A.V.kind == SWARM_VENUE_STADIUM) return fusedImpl<Stadium, false, false>(A, st);
+    if (A.V.kind == SWARM_VENUE_SEATED) return fusedImpl<Seated, false, false>(A, st);
     if (A.venueTable) return fusedImpl<GridVenue, true, true>(A, st);
     return fusedImpl<GridVenue, true, false>(A, st);
 }
@@ -1043,6 +1052,7 @@ cudaError_t launch_step_fused_taped(const StepArgs& A, cudaStream_t st) {
 void launch_stage(const StepArgs& A, int stage, cudaStream_t st, int64_t* launches) {
     if (stage == 0) { launch_sort(A, st, launches); return; }
     if (A.V.kind == SWARM_VENUE_STADIUM) stageImpl<Stadium, false>(A, stage, st, launches);
+    else if (A.V.kind == SWARM_VENUE_SEATED) stageImpl<Seated, false>(A, stage, st, launches);
     else if (A.venueTable) stageImpl<GridVenue, true>(A, stage, st, launches);
     else stageImpl<GridVenue, false>(A, stage, st, launches);
 }

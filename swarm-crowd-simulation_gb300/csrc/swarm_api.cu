@@ -48,7 +48,17 @@ SwarmSim::~SwarmSim() {
     for (auto& e : ev) if (e) cudaEventDestroy(e);
     for (void* p : allocs) cudaFree(p);
     for (void* p : choiceAllocs) cudaFree(p);
+    if (errHost) cudaFreeHost(errHost);
     if (ownStream) cudaStreamDestroy(ownStream);
+}
+
+int SwarmSim::deviceError(int flag) {
+    cudaMemset(errFlag, 0, 4);
+    cudaMemset(barrier, 0, 16);   // a barrier that gave up leaves its counter behind
+    cudaMemset(count, 0, (size_t(ncells) + 1) * 4);
+    counted = false;
+    if (flag & 1) return fail(SWARM_E_TIMEOUT, "a device-side wait gave up (flag " + std::to_string(flag) + ")");
+    return fail(SWARM_E_CUDA, "a device-side bounds check failed (flag " + std::to_string(flag) + ")");
 }
 
 StepArgs SwarmSim::args(int in) const {
@@ -68,6 +78,14 @@ StepArgs SwarmSim::args(int in) const {
     v.nav = dNav; v.nnx = V.nav_nx; v.nny = V.nav_ny; v.nox = V.nav_origin_x; v.noy = V.nav_origin_y;
     v.ninv = V.nav_h > 0.0f ? 1.0f / V.nav_h : 0.0f;
     v.floorH = dFloor; v.speedF = dSpeed; v.exitMask = dMask; v.wallFloor = dWallFloor;
+    v.seat = seatLayout;
+    v.navCells = dNavCells;
+    v.navRes = V.nav_res; v.navOrigin = V.nav_grid_origin; v.navCell = V.nav_grid_cell; v.navInv = V.nav_grid_inv_cell;
+    // the stair spacing is part of the stair model: off without the incline speed (effectiveModelOptions,
+    // src/exit_choice.cpp:60-64)
+    v.incline = V.incline_speed ? 1 : 0;
+    v.stairHw = V.incline_speed && V.stair_headway ? 1 : 0;
+    v.stairTUp = V.stair_t_up; v.stairTDown = V.stair_t_down;
     A.n = n;
     A.projectInFinal = P.proj_iterations > 0 ? 1 : 0;
     A.stateIn = state[in];
@@ -149,7 +167,16 @@ int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capac
     h->capacity = n_capacity;
     const SwarmVenue& V = *venue;
     auto bad = [&](const char* m) { delete h; (void)m; return SWARM_E_INVALID; };
-    if (V.kind != SWARM_VENUE_STADIUM && V.kind != SWARM_VENUE_GRID) return bad("venue kind");
+    if (V.kind != SWARM_VENUE_STADIUM && V.kind != SWARM_VENUE_GRID && V.kind != SWARM_VENUE_SEATED) return bad("venue kind");
+    if (V.kind == SWARM_VENUE_SEATED) {
+        if (!V.seated || !params->uniform_body) return bad("seated layout");
+        const SwarmSeatedLayout& L = *V.seated;
+        if (L.rows < 1 || L.gangways < 1 || L.gangways > SWARM_SEATED_MAX_GANGWAYS || L.doors < 1 ||
+            L.doors > SWARM_SEATED_MAX_DOORS || L.max_band_steps < 0 || !(L.row_depth > 0.0f))
+            return bad("seated layout");
+        if (V.nav_cells && (V.nav_res < 1 || !(V.nav_grid_cell > 0.0f) || !(V.nav_grid_inv_cell > 0.0f))) return bad("nav grid");
+        h->seatLayout = L;
+    }
     if (V.grid_res_x <= 0 || V.grid_res_y <= 0 || !(V.domain_span_x > 0.0f) || !(V.domain_span_y > 0.0f)) return bad("grid");
     if (params->proj_iterations < 0 || params->perc_ring < 1 || params->perc_ring > 4) return bad("params");   // the predict pass holds <= 9 rows
     if (V.kind == SWARM_VENUE_STADIUM && (!V.sdf || V.sdf_res < 2 || !(V.sdf_spacing > 0.0f))) return bad("sdf");
@@ -170,10 +197,16 @@ int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capac
               devAlloc(h, &h->skey, N) && devAlloc(h, &h->pos0, N) && devAlloc(h, &h->vel0, N) && devAlloc(h, &h->proj0, N) &&
               devAlloc(h, &h->proj1, N) && devAlloc(h, &h->vel1, N) && devAlloc(h, &h->plane, N) && devAlloc(h, &h->prm, N) &&
               devAlloc(h, &h->ctc, N) && devAlloc(h, &h->rowsA, N) && devAlloc(h, &h->rowsB, N) &&
-              devAlloc(h, &h->goal, N) && devAlloc(h, &h->errFlag, 1) && devAlloc(h, &h->barrier, 4) && devAlloc(h, &h->stamps, 8);
+              devAlloc(h, &h->goal, N) && devAlloc(h, &h->errFlag, 1) && devAlloc(h, &h->barrier, 4) && devAlloc(h, &h->stamps, 8) &&
+              cudaHostAlloc(reinterpret_cast<void**>(&h->errHost), sizeof(int), cudaHostAllocDefault) == cudaSuccess;
     if (ok && V.kind == SWARM_VENUE_STADIUM) {
         const size_t nv = size_t(V.sdf_res) * size_t(V.sdf_res) * size_t(V.sdf_res);
         ok = devAlloc(h, &h->dSdf, nv) && cudaMemcpy(h->dSdf, V.sdf, nv * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
+    }
+    if (ok && V.kind == SWARM_VENUE_SEATED && V.nav_cells) {
+        const size_t nc = size_t(V.nav_res) * size_t(V.nav_res);
+        ok = devAlloc(h, &h->dNavCells, nc) &&
+             cudaMemcpy(h->dNavCells, V.nav_cells, nc * sizeof(float4), cudaMemcpyHostToDevice) == cudaSuccess;
     }
     if (ok && V.kind == SWARM_VENUE_GRID) {
         const size_t nw = size_t(V.wall_nx) * size_t(V.wall_ny), nn = size_t(V.nav_nx) * size_t(V.nav_ny);
@@ -197,6 +230,7 @@ int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capac
     // host pointers of the venue are not kept
     h->V.sdf = nullptr; h->V.wall_sdf = nullptr; h->V.nav_dist = nullptr; h->V.floor_height = nullptr;
     h->V.speed_factor = nullptr; h->V.exit_boxes = nullptr; h->V.exit_mask = nullptr;
+    h->V.seated = nullptr; h->V.nav_cells = nullptr;
     if (!ok) { delete h; return SWARM_E_OOM; }
     if (cudaMemset(h->count, 0, (size_t(h->ncells) + 1) * 4) != cudaSuccess || cudaMemset(h->errFlag, 0, 4) != cudaSuccess ||
         cudaMemset(h->barrier, 0, 16) != cudaSuccess ||
@@ -733,14 +767,14 @@ int swarm_step_host(SwarmHandle h, const float* in_boids, float* out_boids, int 
         h->hostOut = nullptr;
         if (rc != SWARM_OK) return rc;
         // a barrier that gave up ends the launch before the output copy: the device flag says so
-        return swarm_synchronize(h);
+        return h->finishWithFlag();
     }
     // the read half only: the final pass writes every agent of the other half
     if (!cudaOk(h, cudaMemcpyAsync(h->state[h->readIdx], in_boids, bytes, cudaMemcpyHostToDevice, h->stream), "upload")) return SWARM_E_CUDA;
     const int rc = stepImpl(h, steps, false);
     if (rc != SWARM_OK) return rc;
     if (!cudaOk(h, cudaMemcpyAsync(out_boids, h->state[h->readIdx], bytes, cudaMemcpyDeviceToHost, h->stream), "download")) return SWARM_E_CUDA;
-    return swarm_synchronize(h);
+    return h->finishWithFlag();
 }
 
 int swarm_synchronize(SwarmHandle h) {
@@ -748,15 +782,7 @@ int swarm_synchronize(SwarmHandle h) {
     if (!cudaOk(h, cudaStreamSynchronize(h->stream), "synchronize")) return SWARM_E_CUDA;
     int flag = 0;
     cudaMemcpy(&flag, h->errFlag, 4, cudaMemcpyDeviceToHost);
-    if (flag) {
-        cudaMemset(h->errFlag, 0, 4);
-        cudaMemset(h->barrier, 0, 16);   // a barrier that gave up leaves its counter behind
-        cudaMemset(h->count, 0, (size_t(h->ncells) + 1) * 4);
-        h->counted = false;
-        if (flag & 1) return h->fail(SWARM_E_TIMEOUT, "a device-side wait gave up (flag " + std::to_string(flag) + ")");
-        return h->fail(SWARM_E_CUDA, "a device-side bounds check failed (flag " + std::to_string(flag) + ")");
-    }
-    return SWARM_OK;
+    return flag ? h->deviceError(flag) : SWARM_OK;
 }
 
 int swarm_get_grid(SwarmHandle h, uint32_t* grid_id, uint32_t* boid_id, int n) {

@@ -14,6 +14,9 @@ SWARM_E_STATE = -5
 
 SWARM_VENUE_STADIUM = 0
 SWARM_VENUE_GRID = 1
+SWARM_VENUE_SEATED = 2
+SWARM_NAV_FIT = 0x100
+SWARM_NAV_REACHABLE = 0x200
 
 INACTIVE_CELL = 0xFFFFFFFF
 
@@ -46,8 +49,27 @@ class SwarmParams(C.Structure):
         ("avenue_half", _f), ("walkway_min", _f), ("walkway_max", _f), ("walkway_centre", _f),
         ("aisle_max", _f), ("aisle_centre", _f), ("avenue_target_depth", _f), ("pitch_recovery_depth", _f),
         ("park_coord", _f),
-        ("metric_cells_per_unit", _f), ("metric_speed_scale", _f), ("r_pair_max", _f), ("pad2", _f * 5),
+        ("metric_cells_per_unit", _f), ("metric_speed_scale", _f), ("r_pair_max", _f),
+        ("v_stair_up", _f), ("v_stair_down", _f), ("incline_inv_ref_slope", _f), ("t_headway", _f), ("pad2", _f * 1),
     ]
+
+
+class SwarmSeatedLayout(C.Structure):
+    """swarm::SeatedLayout (reference include/swarm/venue.hpp:99-138), model units."""
+    _fields_ = [
+        ("stand_front", _f), ("row0", _f), ("row_depth", _f), ("clearway", _f), ("rows", _i),
+        ("conc_front", _f), ("conc_back", _f), ("outer_face", _f), ("landing_end", _f),
+        ("avenue_half", _f), ("lat0", _f), ("gangway_lo", _f), ("gangway_hi", _f), ("exit_lo", _f), ("exit_hi", _f),
+        ("corner_inset", _f), ("seat_inset", _f), ("face_margin", _f), ("wall_above", _f), ("wall_clear", _f),
+        ("first_row", _f), ("row_rise", _f), ("seat_top", _f), ("barrier_top", _f), ("concourse_z", _f),
+        ("wall_top", _f), ("rake", _f), ("max_band_steps", _i), ("gangways", _i),
+        ("gw_lo", _f * 8), ("gw_hi", _f * 8), ("gw_row", _i * 8), ("gw_seated", _i * 8),
+        ("doors", _i), ("door_lo", _f * 8), ("door_hi", _f * 8), ("corner_door_lo", _f),
+    ]
+
+
+class SwarmNavCell(C.Structure):
+    _fields_ = [("anchor_x", _f), ("anchor_y", _f), ("dist", _f), ("info", C.c_uint32)]
 
 
 class SwarmVenue(C.Structure):
@@ -63,6 +85,9 @@ class SwarmVenue(C.Structure):
         ("floor_height", C.POINTER(_f)), ("speed_factor", C.POINTER(_f)), ("exit_boxes", C.POINTER(_f)),
         ("metric_res", _i), ("metric_center_x", _f), ("metric_center_y", _f),
         ("exit_mask", C.POINTER(C.c_uint8)),
+        ("seated", C.POINTER(SwarmSeatedLayout)), ("nav_cells", C.c_void_p), ("nav_res", _i),
+        ("nav_grid_origin", _f), ("nav_grid_cell", _f), ("nav_grid_inv_cell", _f),
+        ("incline_speed", _i), ("stair_headway", _i), ("stair_t_up", _f), ("stair_t_down", _f),
     ]
 
 

@@ -11,7 +11,7 @@ import math
 import numpy as np
 
 from . import _check, generator
-from .abi import SWARM_VENUE_STADIUM, SwarmVenue, fptr
+from .abi import SWARM_NAV_REACHABLE, SWARM_VENUE_SEATED, SWARM_VENUE_STADIUM, SwarmSeatedLayout, SwarmVenue, fptr
 
 SDF_RES = 130
 
@@ -80,6 +80,44 @@ class Venue:
         return Venue(v, {"sdf": sdf}, "terrace")
 
     @staticmethod
+    def seated(layout, grid_res, domain_min, domain_span, exit_depth, exit_max_z, nav_cells=None, nav_grid=None,
+               incline_speed=False, stair_times=None, name="seated"):
+        """One of the reference's analytic seated venues (venues S, M, L; model units, reference constants).
+
+        layout: its swarm::SeatedLayout as a SwarmSeatedLayout (or the struct's raw bytes); the neighbour grid
+        (grid_res cells per axis over [domain_min, domain_min + domain_span]) and the exit test (max(|x|, |y|) >
+        exit_depth below exit_max_z); nav_cells: its navigation field as the reference's GpuNavCell table (n x 4
+        float32 words, the 4th the info bits), nav_grid = (res, origin, cell, 1 / cell); None: e_goal from the drive
+        table (or the terrace's router). incline_speed: the free speed by the slope along e_goal; stair_times = (up,
+        down): the stair spacing's time gaps on a full-slope incline (model time), None: the level spacing."""
+        if not isinstance(layout, SwarmSeatedLayout):
+            layout = SwarmSeatedLayout.from_buffer_copy(bytes(np.ascontiguousarray(layout, dtype=np.uint8)))
+        v = SwarmVenue()
+        v.kind = SWARM_VENUE_SEATED
+        v.grid_res_x = v.grid_res_y = int(grid_res)
+        v.domain_min_x = v.domain_min_y = float(domain_min)
+        v.domain_span_x = v.domain_span_y = float(domain_span)
+        v.exit_hi_x = float(exit_depth)
+        v.exit_max_z = float(exit_max_z)
+        v.metric_res = 64
+        v.seated = C.pointer(layout)
+        arrays = {"layout": layout}
+        if nav_cells is not None:
+            cells = np.ascontiguousarray(nav_cells, dtype=np.float32).reshape(-1, 4)
+            res, origin, cell, inv = nav_grid
+            if cells.shape[0] != int(res) * int(res):
+                raise ValueError("nav_cells must hold res x res cells")
+            v.nav_cells = cells.ctypes.data_as(C.c_void_p)
+            v.nav_res = int(res)
+            v.nav_grid_origin, v.nav_grid_cell, v.nav_grid_inv_cell = float(origin), float(cell), float(inv)
+            arrays["nav_cells"] = cells
+        v.incline_speed = 1 if incline_speed else 0
+        if stair_times is not None:
+            v.stair_headway = 1
+            v.stair_t_up, v.stair_t_down = float(stair_times[0]), float(stair_times[1])
+        return Venue(v, arrays, name)
+
+    @staticmethod
     def hall(size_x, size_y, doors, wall_thickness=0.3, exit_depth=0.5, margin=1.0, wall_h=0.05, nav_h=0.1, cell=0.5,
              name="hall"):
         """doors: [(wall, centre, width)], wall 0: -x, 1: +x, 2: -y, 3: +y; centre along the wall from its midpoint."""
@@ -121,6 +159,24 @@ def _bowl(spec, name):
 
 
 Venue.bowl = staticmethod(_bowl)
+
+
+def nav_cells_from_anchors(anchor, info, nav_grid):
+    """A seated venue's GpuNavCell table from each cell's anchor cell index and info word: the anchor's position is
+    that cell's centre, origin + (i + 0.5) x cell in double rounded once (the reference's nav::Grid::centre); the
+    distance word is 0 where the cell is reachable, +infinity where not (the step reads only the anchor and the info
+    bits)."""
+    res, origin, cell, _ = nav_grid
+    res = int(res)
+    anchor = np.asarray(anchor, dtype=np.int64)
+    info = np.asarray(info, dtype=np.uint32)
+    centre = (np.float64(np.float32(origin)) + (np.arange(res, dtype=np.float64) + 0.5) * np.float64(np.float32(cell))).astype(np.float32)
+    out = np.empty((anchor.size, 4), np.float32)
+    out[:, 0] = centre[anchor % res]
+    out[:, 1] = centre[anchor // res]
+    out[:, 2] = np.where((info & SWARM_NAV_REACHABLE) != 0, np.float32(0.0), np.float32(np.inf))
+    out[:, 3] = info.view(np.float32)
+    return out
 
 
 def exit_fields(venue):

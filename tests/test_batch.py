@@ -78,3 +78,40 @@ def test_launch_configurations_give_the_same_bits_and_autotune_restores_state(bu
     assert np.array_equal(_bits(sim.state()), _bits(boids))   # the trials' state is restored
     sim.step(10)
     assert np.array_equal(_bits(sim.state()), _bits(want))
+
+
+@pytest.mark.gpu
+def test_full_batch_256_instances_equal_solo_runs_and_oracle(built):
+    """The batched workload at full size (256 halls, N log-uniform in [1 024, 65 536], 3.78 M agents), 20 steps:
+    every instance bit-identical to its solo CUDA run, and 8 instances (the 4 smallest, the 4 largest) to the
+    oracle."""
+    import swarm_gb300
+    from swarm_gb300 import venues
+    vens, boids, r, v0, counts = venues.build_batch(256, 0)
+    assert len(vens) == 256 and counts.min() >= 1024 and counts.max() <= 65536
+    P = swarm_gb300.params_si()
+    steps = 20
+    batch = swarm_gb300.BatchSim(P, vens, counts)
+    batch.set_state(boids)
+    batch.set_agent_params(r, v0)
+    batch.set_graph(True)
+    batch.step(steps)
+    out = batch.state()
+    starts = batch.starts
+    batch.close()
+    order = np.argsort(counts, kind="stable")
+    check_oracle = set(order[:4].tolist()) | set(order[-4:].tolist())
+    for i, v in enumerate(vens):
+        a, b = starts[i], starts[i + 1]
+        solo = swarm_gb300.CrowdSim(P, v, int(b - a))
+        solo.set_state(boids[a:b])
+        solo.set_agent_params(r[a:b], v0[a:b])
+        solo.step(steps)
+        assert np.array_equal(_bits(out[a:b]), _bits(solo.state())), f"instance {i} ({b - a} agents): batch != solo"
+        solo.close()
+        if i in check_oracle:
+            ora = O.OracleSim(P, v.struct)
+            ora.set_state(boids[a:b])
+            ora.set_agent_params(r[a:b], v0[a:b])
+            ora.step(steps)
+            assert np.array_equal(_bits(out[a:b]), _bits(ora.state())), f"instance {i}: batch != oracle"

@@ -1,0 +1,234 @@
+"""The reference's analytic seated venue S on the GPU, through the C ABI, against the unmodified reference's own outputs
+(tests/golden/seated_S.npz, written by tests/golden/make_seated_golden.py from the reference's CPU step built from its
+own sources) and its pinned state hashes (tools/golden_state.hpp:45, :62). The sorted pairs, the cell table and the
+contact bits are compared exactly; states within the step's stated tolerance (TOL) and then bit for bit.
+
+Three models of the reference: the dense forced scenario (every seat occupied, e_goal from a drive table: the contact
+model alone), the nearest exit at the level speed (e_goal from the navigation field's anchors: navCell's NOFIT ring and
+surface rule, navGoal's wall rule), and the incline speed with the stair spacing."""
+import os
+import zlib
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "seated_S.npz")
+TOL = 1e-5                          # model units (length, length per model time), per component
+PIN_DENSE = 0xa2abaea7c0139b09      # golden_state.hpp:45  CPU counting venue S dense
+PIN_NEAREST = 0xb1d6dac42f5dcd09    # golden_state.hpp:62  CPU counting venue S nearest exit, level speed
+
+
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+def fnv1a(a):
+    """golden::stateHash (tools/golden_state.hpp:121-126): 64-bit FNV-1a over the raw state bytes."""
+    h = 0xcbf29ce484222325
+    for x in np.ascontiguousarray(a).view(np.uint8).tobytes():
+        h = ((h ^ x) * 0x100000001b3) & 0xFFFFFFFFFFFFFFFF
+    return h
+
+
+def assert_state(got, want, what):
+    assert got.shape == want.shape
+    assert np.array_equal(got[:, 3], want[:, 3]), f"{what}: evacuation flags differ"
+    d = np.abs(got.astype(np.float64) - want.astype(np.float64)).max()
+    assert d <= TOL, f"{what}: max |diff| {d:.3g}"
+    assert np.array_equal(_bits(got), _bits(want)), f"{what}: not bit-exact"
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return dict(np.load(GOLDEN))
+
+
+@pytest.fixture(scope="module")
+def nav_cells(golden):
+    from swarm_gb300 import venues
+    delta = np.frombuffer(zlib.decompress(golden["nav_anchor_delta_z"].tobytes()), np.int32)
+    info = np.frombuffer(zlib.decompress(golden["nav_info_z"].tobytes()), np.uint32)
+    return venues.nav_cells_from_anchors(np.cumsum(delta.astype(np.int64)), info, golden["nav_grid"])
+
+
+def drive_tables(golden):
+    n = golden["dense_spawn"].shape[0]
+    x = np.frombuffer(zlib.decompress(golden["dense_drive_xor_z"].tobytes()), np.uint32).reshape(-1, n, 2)
+    return np.bitwise_xor.accumulate(x, axis=0).view(np.float32)
+
+
+def _venue(golden, cells=None, incline=False):
+    from swarm_gb300.venues import Venue
+    g = golden["grid"]
+    inc = golden["incline"]
+    return Venue.seated(golden["layout"], int(g[0]), g[1], g[2], g[3], g[4], nav_cells=cells,
+                        nav_grid=golden["nav_grid"] if cells is not None else None, incline_speed=incline,
+                        stair_times=(inc[4], inc[5]) if incline else None, name="S")
+
+
+def _sim(golden, state, cells=None, incline=False):
+    import swarm_gb300
+    sim = swarm_gb300.CrowdSim(swarm_gb300.params_reference(), _venue(golden, cells, incline), state.shape[0])
+    sim.set_state(state)
+    return sim
+
+
+def _one_step_matches(sim, golden, prefix):
+    key, ids = sim.grid()
+    assert np.array_equal(key, golden[prefix + "grid1_key"]), "gridID sequence"
+    assert np.array_equal(ids, golden[prefix + "grid1_id"]), "sorted boidIDs"
+    assert np.array_equal(sim.cells(), golden[prefix + "cells1"]), "cell table"
+    assert np.array_equal(sim.contacts(), golden[prefix + "contacts1"]), "contact branches"
+    assert_state(sim.state(), golden[prefix + "state1"], "one step")
+
+
+def test_reference_constants_are_the_incline_and_stair_constants(built, golden):
+    """swarm_params_reference's incline and stair constants are sim_params.hpp's folded values (the reference's own)."""
+    import swarm_gb300
+    p = swarm_gb300.params_reference()
+    inc = golden["incline"]
+    assert (np.float32(p.v_stair_up), np.float32(p.v_stair_down), np.float32(p.incline_inv_ref_slope),
+            np.float32(p.t_headway)) == tuple(inc[:4])
+    assert np.float32(1.0) / np.float32(p.headway_rate) != 0.0
+
+
+def test_fixture_decodes_to_the_reference_table(golden, nav_cells):
+    """The compact navigation table decodes to a whole GpuNavCell grid whose reachable cells anchor inside it."""
+    res = int(golden["nav_grid"][0])
+    assert nav_cells.shape == (res * res, 4)
+    info = nav_cells[:, 3].view(np.uint32)
+    reach = (info & 0x200) != 0
+    assert 0.5 < reach.mean() < 0.9
+    assert np.isfinite(nav_cells[reach, 0]).all()
+    assert drive_tables(golden).shape == (250, golden["dense_spawn"].shape[0], 2)
+
+
+@pytest.mark.gpu
+def test_dense_forced_one_step_vs_reference(golden):
+    sim = _sim(golden, golden["dense_spawn"])
+    sim.set_drive_table(drive_tables(golden)[0])
+    sim.step(1)
+    _one_step_matches(sim, golden, "dense_")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fused", [True, False])
+def test_dense_forced_250_steps_reproduce_the_reference_pin(golden, fused):
+    """tools/golden_state.hpp:45: the dense forced scenario's state after 250 steps hashes to the reference's pin."""
+    tables = drive_tables(golden)
+    sim = _sim(golden, golden["dense_spawn"])
+    sim.set_fused(fused)
+    for t in tables:
+        sim.set_drive_table(t)
+        sim.step(1)
+    st = sim.state()
+    assert_state(st, golden["dense_state250"], "250 steps")
+    assert fnv1a(st) == PIN_DENSE
+
+
+@pytest.mark.gpu
+def test_nearest_exit_one_step_vs_reference(golden, nav_cells):
+    sim = _sim(golden, golden["nearest_spawn"], nav_cells)
+    sim.step(1)
+    _one_step_matches(sim, golden, "nearest_")
+
+
+@pytest.mark.gpu
+def test_nearest_exit_250_steps_reproduce_the_reference_pin(golden, nav_cells):
+    """tools/golden_state.hpp:62: venue S's full seat spawn, nearest exit, level speed, 250 steps."""
+    sim = _sim(golden, golden["nearest_spawn"], nav_cells)
+    done = 0
+    for k in (10, 50, 250):
+        sim.step(k - done)
+        done = k
+        assert_state(sim.state(), golden["nearest_state%d" % k], f"{k} steps")
+    assert fnv1a(sim.state()) == PIN_NEAREST
+
+
+@pytest.mark.gpu
+def test_incline_speed_and_stair_spacing_vs_reference(golden, nav_cells):
+    """The incline free speed and the stair spacing (EMPIRICAL time gaps) on the gangway inclines: the reference's
+    states after 1, 50 and 250 steps."""
+    sim = _sim(golden, golden["nearest_spawn"], nav_cells, incline=True)
+    sim.step(1)
+    _one_step_matches(sim, golden, "incline_")
+    sim.step(49)
+    assert_state(sim.state(), golden["incline_state50"], "50 steps")
+    sim.step(200)
+    st = sim.state()
+    assert_state(st, golden["incline_state250"], "250 steps")
+    assert fnv1a(st) == int(golden["incline_hash250"][0])
+
+
+@pytest.mark.gpu
+def test_seated_execution_modes_are_bit_identical(golden, nav_cells):
+    """The fused persistent step and the per-phase kernels (and their graphs) give the same bits on the seated venue."""
+    a = _sim(golden, golden["nearest_spawn"], nav_cells, incline=True)
+    b = _sim(golden, golden["nearest_spawn"], nav_cells, incline=True)
+    b.set_fused(False)
+    b.set_graph(True)
+    for _ in range(3):
+        a.step(7)
+        b.step(7)
+        assert np.array_equal(_bits(a.state()), _bits(b.state()))
+    assert np.array_equal(a.cells(), b.cells())
+    assert np.array_equal(a.contacts(), b.contacts())
+
+
+def test_geometry_equals_the_reference_point_by_point(tmp_path, golden, nav_cells):
+    """The seated venue's geometry and navigation lookup as compiled into the CUDA step (csrc/venue_seated.cuh, built
+    for the host by tests/seated_harness.cu) against the reference's own functions (seated::floorHeight, cellKey,
+    sdfGrad, wall, stepUpScan, floorSlope, nav::goal) at random points of venue S and at the fixture's agent positions:
+    bit for bit. Needs the reference's CPU build (this container)."""
+    import ctypes as C
+    import subprocess
+    from oracle import oracle as O
+    if not O.ref_available():
+        pytest.skip("the reference's CPU build is not here")
+    os.environ.setdefault("SWARM_NAV_CACHE", str(tmp_path / "navcache"))
+    import swarm_gb300
+    from swarm_gb300.abi import SwarmSeatedLayout
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    so = tmp_path / "libseated_harness.so"
+    subprocess.run([os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc"), "-gencode", "arch=compute_103a,code=sm_103a",
+                    "-O2", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-Xcompiler",
+                    "-fPIC,-ffp-contract=off", "-shared", "-o", str(so), os.path.join(root, "tests", "seated_harness.cu")],
+                   check=True)
+    H = C.CDLL(str(so))
+    V = C.c_void_p
+    H.hs_eval.argtypes = [V, V, C.c_int, C.c_int, V, V, V, C.c_int, C.c_float, C.c_float, C.c_float]
+    R = O.ref_lib()
+    R.ref_seated_eval.argtypes = [C.c_char_p, C.c_int, C.c_int, V, V]
+    lay = SwarmSeatedLayout.from_buffer_copy(bytes(golden["layout"]))
+    P = swarm_gb300.params_reference()
+    ng = golden["nav_grid"]
+
+    def both(op, inp, width):
+        inp = np.ascontiguousarray(inp, np.float32)
+        n = inp.shape[0]
+        a = np.zeros((n, width), np.float32)
+        b = np.zeros((n, width), np.float32)
+        assert R.ref_seated_eval(b"S", op, n, inp.ctypes.data, a.ctypes.data) == 0
+        assert H.hs_eval(C.byref(lay), C.byref(P), op, n, inp.ctypes.data, b.ctypes.data, nav_cells.ctypes.data,
+                         int(ng[0]), ng[1], ng[2], ng[3]) == 0
+        bad = np.nonzero((a.view(np.uint32) != b.view(np.uint32)).any(axis=1))[0]
+        assert bad.size == 0, f"op {op}: {bad.size} of {n} differ, e.g. at {inp[bad[0]]}: {a[bad[0]]} vs {b[bad[0]]}"
+        return a
+
+    rng = np.random.default_rng(7)
+    pos = np.concatenate([golden[k][:, :3] for k in golden if k.startswith(("dense_state", "nearest_state", "incline_state"))])
+    pos = pos[np.abs(pos[:, 0]) < 2.0]
+    xy = np.concatenate([rng.uniform(-1.0, 1.0, (100000, 2)), pos[:, :2]]).astype(np.float32)
+    fh = both(0, xy, 1)[:, 0]
+    both(1, xy, 2)
+    z = fh + rng.uniform(-0.01, 0.03, xy.shape[0]).astype(np.float32)
+    both(2, np.c_[xy, z], 4)
+    reach = rng.choice([P.feeler_reach, P.plane_probe_reach, lay.face_margin, P.step_up_sample], xy.shape[0]).astype(np.float32)
+    both(3, np.c_[xy, z + lay.wall_above, reach], 3)
+    both(3, np.c_[xy, fh + P.step_up_tol, reach], 3)
+    f0 = fh - rng.choice([0.0, P.step_up_floor_reach], xy.shape[0]).astype(np.float32)
+    both(4, np.c_[xy, xy + rng.normal(0.0, 0.004, xy.shape).astype(np.float32), f0], 3)
+    e = rng.normal(0.0, 1.0, xy.shape)
+    both(5, np.c_[xy, (e / np.linalg.norm(e, axis=1, keepdims=True)).astype(np.float32)], 1)
+    both(6, np.c_[xy, fh + P.body_radius], 2)
+    both(6, pos, 2)
