@@ -465,6 +465,14 @@ int swarm_snapshot_read(const char* path, float* boids, int n);
 int swarm_snapshot_count(const char* path);
 /* The baked terrace volume (src/sdf.cpp:84-107 loadSDFVolume): res^3 float32, exactly (stadium.sdf: res 130). */
 int swarm_sdf_read(const char* path, float* sdf, int res);
+/* A seated venue's navigation-field cache file as the reference writes it (nav::save / nav::load,
+ * src/nav_field.cpp:554-656; nav::cacheFile, include/swarm/nav_field.hpp:226-233), read into the GPU table the seated
+ * venue takes (SwarmVenue::nav_cells): per cell the anchor's centre, the distance and the info bits, exactly as
+ * nav::gpuCells makes them (src/nav_field.cpp:443-454). Checks the magic, the version (2), the sizes and the FNV-1a
+ * checksum; expected_key: the venue's nav::cacheKey, or 0 to accept any. cells NULL: a size query (res, origin, cell
+ * and 1 / cell only); else capacity >= res^2. */
+int swarm_nav_cache_read(const char* path, uint64_t expected_key, SwarmNavCell* cells, int64_t capacity, int32_t* res,
+                         float* origin, float* cell, float* inv_cell);
 
 /* ---- the adjoint: gradients of an evacuation loss ----
  * No counterpart in the reference, which has no differentiation. The loss of `steps` steps from the handle's state:

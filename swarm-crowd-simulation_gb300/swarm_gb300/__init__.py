@@ -72,6 +72,8 @@ _SIG = {
     "swarm_snapshot_read": [C.c_char_p, C.POINTER(C.c_float), C.c_int],
     "swarm_snapshot_count": [C.c_char_p],
     "swarm_sdf_read": [C.c_char_p, C.POINTER(C.c_float), C.c_int],
+    "swarm_nav_cache_read": [C.c_char_p, C.c_uint64, C.c_void_p, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_float),
+                             C.POINTER(C.c_float), C.POINTER(C.c_float)],
     "swarm_nav_field_gpu": [C.c_int, C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.POINTER(C.c_float),
                             C.POINTER(SwarmNavFieldStats)],
     "swarm_nav_field_cpu": [C.c_int, C.c_int, C.c_double, C.c_void_p, C.c_void_p, C.POINTER(C.c_float)],
@@ -150,6 +152,19 @@ def snapshot_write(path, boids):
     """A workload snapshot: the raw GpuBoid array (the reference's bench_common saveSnapshot format)."""
     b = np.ascontiguousarray(boids, dtype=np.float32).reshape(-1, 8)
     _check(lib().swarm_snapshot_write(os.fsencode(path), fptr(b), b.shape[0]), "swarm_snapshot_write")
+
+
+def nav_cache_read(path, expected_key=0):
+    """A seated venue's navigation-field cache file as the reference writes it, as the GPU table: (cells (res^2, 4)
+    float32 -- anchor x, anchor y, distance, info bits --, (res, origin, cell, 1 / cell))."""
+    res, o, c, ic = C.c_int32(), C.c_float(), C.c_float(), C.c_float()
+    p = os.fsencode(path)
+    _check(lib().swarm_nav_cache_read(p, expected_key, None, 0, C.byref(res), C.byref(o), C.byref(c), C.byref(ic)),
+           "swarm_nav_cache_read")
+    cells = np.empty((res.value * res.value, 4), np.float32)
+    _check(lib().swarm_nav_cache_read(p, expected_key, cells.ctypes.data_as(C.c_void_p), cells.shape[0], C.byref(res),
+                                      C.byref(o), C.byref(c), C.byref(ic)), "swarm_nav_cache_read")
+    return cells, (res.value, o.value, c.value, ic.value)
 
 
 def snapshot_read(path):
