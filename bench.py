@@ -19,6 +19,8 @@ cpu_baseline  the oracle port of the reference's CPU step (OpenMP, all host thre
        workload (400 consecutive steps after 2 warm-up steps from the spawn), with the host's core count and CPU model.
 batched  the 256-instance batch as one packed state against the same instances launched one at a time.
 bowl   the 63 488-agent seated bowl: the plain step (as value) and its evacuation run to completion.
+reference_venue_L  the reference's own seated venue L (63 424 agents) with the reference's constants (K = 32), beside
+       the reference's published GPU step on that venue.
 adjoint  loss and gradient of 400 steps of the 16 384-agent hall (checkpoints every 20 steps, and the full tape)
        against the plain forward of the same steps.
 --impl reference  the reference's CPU step (the oracle port: the reference's own build needs its source tree, which
@@ -277,6 +279,63 @@ def bench_bowl(P, steps=50, warmup=5, cap=20000, chunk=100):
             "nav_field": bench_nav_field(venue)}
 
 
+def bench_venue_l(steps=30, warmup=5):
+    """The reference's own largest venue in reference-parity mode: seated venue L (63 424 seats in N = 65 536; the
+    reference's layout, navigation field and full seat spawn from tests/golden/seated_L.npz, written by the unmodified
+    reference), the reference's constants (model units, K = 32: 31 sweeps and the final pass), nearest exit at the level
+    speed, and again with the incline speed and stair spacing. CUDA events per step on the handle's stream, the L2
+    flushed by a 256 MiB write before each step. The reference publishes its own GPU step on this venue and spawn
+    (OpenGL on an AMD RX 7800 XT, default model): 1.861 ms a step, of which 0.2039 ms is its queue-aware exit choice
+    (results/benchmarks/thesis/perf_tables.md:17, :45) -- a pass not run here."""
+    import zlib
+    import torch
+    import swarm_gb300
+    from swarm_gb300 import venues
+    g = dict(np.load(os.path.join(ROOT, "tests", "golden", "seated_L.npz")))
+    delta = np.frombuffer(zlib.decompress(g["nav_anchor_delta_z"].tobytes()), np.int32)
+    info = np.frombuffer(zlib.decompress(g["nav_info_z"].tobytes()), np.uint32)
+    cells = venues.nav_cells_from_anchors(np.cumsum(delta.astype(np.int64)), info, g["nav_grid"])
+    spawn = np.frombuffer(zlib.decompress(g["spawn_z"].tobytes()), np.float32).reshape(-1, 8).copy()
+    gr = g["grid"]
+    P = swarm_gb300.params_reference()
+    K = P.proj_iterations
+    b_step = 336.0 + 48.0 * (K - 1)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    out = {"workload": "reference venue L (63424 seated of 65536), reference constants (model units, K=32), full seat "
+                       "spawn (seed 1337)", "agents": int(spawn.shape[0]), "bytes_per_agent_step": b_step,
+           "published_reference_gpu": {"ms_per_step": 1.861, "exit_choice_ms": 0.2039,
+                                       "hardware": "AMD RX 7800 XT, OpenGL 4.3 (published, not measured here)"}}
+    for label, incline in (("nearest_exit_level_speed", False), ("incline_speed_stair_spacing", True)):
+        inc = g["incline"]
+        venue = venues.Venue.seated(g["layout"], int(gr[0]), gr[1], gr[2], gr[3], gr[4], nav_cells=cells,
+                                    nav_grid=g["nav_grid"], incline_speed=incline,
+                                    stair_times=(inc[4], inc[5]) if incline else None, name="L")
+        stream = torch.cuda.Stream()
+        sim = swarm_gb300.CrowdSim(P, venue, spawn.shape[0])
+        sim.set_stream(stream.cuda_stream)
+        sim.set_state(spawn)
+        with torch.cuda.stream(stream):
+            sim.step(warmup)
+        torch.cuda.synchronize()
+        active, total = 0, 0.0
+        for k in range(steps):
+            active += int((sim.state()[:, 3] != 0).sum())
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xFF)
+                e0.record(stream)
+                sim.step(1)
+                e1.record(stream)
+            stream.synchronize()
+            total += e0.elapsed_time(e1)
+        sim.synchronize()
+        sim.close()
+        value = active / (total * 1e-3)
+        out[label] = {"value": value, "unit": UNIT, "ms_per_step": total / steps, "steps": steps, "warmup": warmup,
+                      "fraction_of_hbm_roofline": value * b_step / (peaks()[0] * 1e9)}
+    return out
+
+
 def bowl_venue():
     """The seated bowl's venue alone (its nav grid is the solver's workload)."""
     from swarm_gb300 import venues
@@ -484,7 +543,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
     ap.add_argument("--no-bowl", action="store_true", help="skip the seated-bowl measurement")
     ap.add_argument("--adjoint-steps", type=int, default=400, help="steps of the adjoint measurement (400: the workload)")
-    ap.add_argument("--only", choices=["adjoint", "bowl", "batched", "navfield"], default=None,
+    ap.add_argument("--only", choices=["adjoint", "bowl", "batched", "navfield", "venue_l"], default=None,
                     help="run only this sub-measurement and print its object (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -498,7 +557,7 @@ def main():
         P = swarm_gb300.params_si()
         fn = {"adjoint": lambda: bench_adjoint(P, steps=args.adjoint_steps), "bowl": lambda: bench_bowl(P),
               "batched": lambda: bench_batched(P),
-              "navfield": lambda: bench_nav_field(bowl_venue())}[args.only]
+              "navfield": lambda: bench_nav_field(bowl_venue()), "venue_l": lambda: bench_venue_l()}[args.only]
         print(json.dumps({args.only: fn()}))
         return 0
 
@@ -674,6 +733,11 @@ def main():
                 line["bowl"] = bench_bowl(P)
             except Exception as e:  # reported, not fatal
                 line["bowl"] = {"error": str(e)[:300]}
+        if not args.no_bowl and world == 1:
+            try:
+                line["reference_venue_L"] = bench_venue_l()
+            except Exception as e:  # reported, not fatal
+                line["reference_venue_L"] = {"error": str(e)[:300]}
         if not args.no_adjoint and world == 1:
             try:
                 line["adjoint"] = bench_adjoint(P, steps=args.adjoint_steps)

@@ -23,6 +23,12 @@ Contents:
                     "CPU counting venue S nearest exit, level speed" (golden_state.hpp:62)
   incline_*         the same spawn under {nearest exit, incline speed, stair spacing EMPIRICAL}: states after 1, 50 and
                     250 steps (the reference's output; the reference pins this model only with the queue-aware choice)
+
+and tests/golden/seated_M.npz, seated_L.npz: the generated venues M (15 832 seats, N = 16 384) and L (63 424 seats,
+N = 65 536) -- several straight gangways, doors per gangway head, corner doors, merged corner gangways -- with the
+layout, grid, compact navigation table as above, the full seat spawn spawnSeatedCrowd(venue, N, 1.0, 1337) (zlib), and
+the FNV-1a hashes of the reference's states after 1, 10 and 50 steps under {nearest exit, level speed} and after 10
+steps under {nearest exit, incline speed, stair spacing EMPIRICAL}.
 """
 import ctypes as C
 import os
@@ -80,17 +86,11 @@ def _one_step_record(prefix, sim, out):
     out[prefix + "contacts1"] = sim.contacts()
 
 
-def main():
-    os.environ.setdefault("SWARM_NAV_CACHE", os.path.join("/tmp", "swarm_navcache"))
-    O.build(ref=True)
-    assert O.ref_available(), "the reference tree is needed: REF_DIR=<tree> make -C oracle ref"
-    L = _bind(O.ref_lib())
-    out = {}
-
+def _venue_records(L, venue, out):
+    """The layout, grid, incline constants and compact navigation table of a seated venue into out."""
     lay = SwarmSeatedLayout()
     res, dmin, dspan, edep, emaxz = C.c_int(), C.c_float(), C.c_float(), C.c_float(), C.c_float()
-    assert L.ref_seated_layout(b"S", C.byref(lay), C.byref(res), C.byref(dmin), C.byref(dspan), C.byref(edep), C.byref(emaxz)) == 0
-    assert res.value == 40
+    assert L.ref_seated_layout(venue, C.byref(lay), C.byref(res), C.byref(dmin), C.byref(dspan), C.byref(edep), C.byref(emaxz)) == 0
     out["layout"] = np.frombuffer(bytes(lay), np.uint8)
     out["grid"] = np.array([res.value, dmin.value, dspan.value, edep.value, emaxz.value], np.float64)
     inc = np.empty(8, np.float32)
@@ -99,9 +99,9 @@ def main():
 
     # the navigation field, compact
     org, cell, inv = C.c_float(), C.c_float(), C.c_float()
-    nres = L.ref_nav_table(b"S", None, 0, C.byref(org), C.byref(cell), C.byref(inv))
+    nres = L.ref_nav_table(venue, None, 0, C.byref(org), C.byref(cell), C.byref(inv))
     nav = np.empty((nres * nres, 4), np.float32)
-    L.ref_nav_table(b"S", nav.ctypes.data, nres * nres, C.byref(org), C.byref(cell), C.byref(inv))
+    L.ref_nav_table(venue, nav.ctypes.data, nres * nres, C.byref(org), C.byref(cell), C.byref(inv))
     info = nav[:, 3].view(np.uint32).copy()
     centre = (np.float64(org.value) + (np.arange(nres, dtype=np.float64) + 0.5) * np.float64(cell.value)).astype(np.float32)
     cx = np.searchsorted(centre, nav[:, 0])
@@ -117,6 +117,37 @@ def main():
     out["nav_grid"] = np.array([nres, org.value, cell.value, inv.value], np.float64)
     out["nav_anchor_delta_z"] = np.frombuffer(zlib.compress(delta.tobytes(), 9), np.uint8)
     out["nav_info_z"] = np.frombuffer(zlib.compress(info.tobytes(), 9), np.uint8)
+    return res.value
+
+
+def generated_venue(L, name, n):
+    """seated_M.npz / seated_L.npz: the venue, its full seat spawn and the reference's state hashes."""
+    out = {}
+    _venue_records(L, name, out)
+    spawn = np.empty((n, 8), np.float32)
+    assert L.ref_spawn_seated(name, n, 1.0, 1337, spawn.ctypes.data) == 0
+    out["spawn_z"] = np.frombuffer(zlib.compress(spawn.tobytes(), 9), np.uint8)
+    out["n"] = np.array([n, int((spawn[:, 3] != 0).sum())], np.int64)
+    for prefix, incline, stair, keep in (("nearest_", 0, 0, (1, 10, 50)), ("incline_", 1, 1, (10,))):
+        sim = _sim(L, name, incline, stair)
+        sim.set_state(spawn)
+        done = 0
+        for k in keep:
+            sim.step(k - done)
+            done = k
+            out[prefix + "hash%d" % k] = np.array([fnv1a(sim.state())], np.uint64)
+    path = os.path.join(HERE, "seated_%s.npz" % name.decode())
+    np.savez_compressed(path, **out)
+    print("wrote", os.path.basename(path), os.path.getsize(path), "bytes")
+
+
+def main():
+    os.environ.setdefault("SWARM_NAV_CACHE", os.path.join("/tmp", "swarm_navcache"))
+    O.build(ref=True)
+    assert O.ref_available(), "the reference tree is needed: REF_DIR=<tree> make -C oracle ref"
+    L = _bind(O.ref_lib())
+    out = {}
+    assert _venue_records(L, b"S", out) == 40
 
     # the dense forced scenario
     n = L.ref_dense_setup(b"S", None, 0)
@@ -161,6 +192,8 @@ def main():
     out["incline_hash250"] = np.array([fnv1a(out["incline_state250"])], np.uint64)
     np.savez_compressed(os.path.join(HERE, "seated_S.npz"), **out)
     print("wrote seated_S.npz:", os.path.getsize(os.path.join(HERE, "seated_S.npz")), "bytes")
+    generated_venue(L, b"M", 16384)
+    generated_venue(L, b"L", 65536)
 
 
 if __name__ == "__main__":

@@ -175,40 +175,46 @@ def test_seated_execution_modes_are_bit_identical(golden, nav_cells):
     assert np.array_equal(a.contacts(), b.contacts())
 
 
-def test_geometry_equals_the_reference_point_by_point(tmp_path, golden, nav_cells):
-    """The seated venue's geometry and navigation lookup as compiled into the CUDA step (csrc/venue_seated.cuh, built
-    for the host by tests/seated_harness.cu) against the reference's own functions (seated::floorHeight, cellKey,
-    sdfGrad, wall, stepUpScan, floorSlope, nav::goal) at random points of venue S and at the fixture's agent positions:
-    bit for bit. Needs the reference's CPU build (this container)."""
+def _harness(tmp_path):
     import ctypes as C
     import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    so = tmp_path / "libseated_harness.so"
+    if not so.exists():
+        subprocess.run([os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc"), "-gencode", "arch=compute_103a,code=sm_103a",
+                        "-O2", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-Xcompiler",
+                        "-fPIC,-ffp-contract=off", "-shared", "-o", str(so), os.path.join(root, "tests", "seated_harness.cu")],
+                       check=True)
+    H = C.CDLL(str(so))
+    V = C.c_void_p
+    H.hs_eval.argtypes = [V, V, C.c_int, C.c_int, V, V, V, C.c_int, C.c_float, C.c_float, C.c_float]
+    return H
+
+
+def _geometry_check(tmp_path, venue, golden, nav_cells, positions, npts):
+    """Every geometry operation of the product (host build) against the reference's own, bit for bit, at npts random
+    points of the venue's domain and at the given agent positions."""
+    import ctypes as C
     from oracle import oracle as O
     if not O.ref_available():
         pytest.skip("the reference's CPU build is not here")
     os.environ.setdefault("SWARM_NAV_CACHE", str(tmp_path / "navcache"))
     import swarm_gb300
     from swarm_gb300.abi import SwarmSeatedLayout
-    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    so = tmp_path / "libseated_harness.so"
-    subprocess.run([os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc"), "-gencode", "arch=compute_103a,code=sm_103a",
-                    "-O2", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-Xcompiler",
-                    "-fPIC,-ffp-contract=off", "-shared", "-o", str(so), os.path.join(root, "tests", "seated_harness.cu")],
-                   check=True)
-    H = C.CDLL(str(so))
-    V = C.c_void_p
-    H.hs_eval.argtypes = [V, V, C.c_int, C.c_int, V, V, V, C.c_int, C.c_float, C.c_float, C.c_float]
+    H = _harness(tmp_path)
     R = O.ref_lib()
-    R.ref_seated_eval.argtypes = [C.c_char_p, C.c_int, C.c_int, V, V]
+    R.ref_seated_eval.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
     lay = SwarmSeatedLayout.from_buffer_copy(bytes(golden["layout"]))
     P = swarm_gb300.params_reference()
     ng = golden["nav_grid"]
+    half = -float(golden["grid"][1])
 
     def both(op, inp, width):
         inp = np.ascontiguousarray(inp, np.float32)
         n = inp.shape[0]
         a = np.zeros((n, width), np.float32)
         b = np.zeros((n, width), np.float32)
-        assert R.ref_seated_eval(b"S", op, n, inp.ctypes.data, a.ctypes.data) == 0
+        assert R.ref_seated_eval(venue, op, n, inp.ctypes.data, a.ctypes.data) == 0
         assert H.hs_eval(C.byref(lay), C.byref(P), op, n, inp.ctypes.data, b.ctypes.data, nav_cells.ctypes.data,
                          int(ng[0]), ng[1], ng[2], ng[3]) == 0
         bad = np.nonzero((a.view(np.uint32) != b.view(np.uint32)).any(axis=1))[0]
@@ -216,9 +222,8 @@ def test_geometry_equals_the_reference_point_by_point(tmp_path, golden, nav_cell
         return a
 
     rng = np.random.default_rng(7)
-    pos = np.concatenate([golden[k][:, :3] for k in golden if k.startswith(("dense_state", "nearest_state", "incline_state"))])
-    pos = pos[np.abs(pos[:, 0]) < 2.0]
-    xy = np.concatenate([rng.uniform(-1.0, 1.0, (100000, 2)), pos[:, :2]]).astype(np.float32)
+    pos = positions[np.abs(positions[:, 0]) < 2.0 * half]
+    xy = np.concatenate([rng.uniform(-half, half, (npts, 2)), pos[:, :2]]).astype(np.float32)
     fh = both(0, xy, 1)[:, 0]
     both(1, xy, 2)
     z = fh + rng.uniform(-0.01, 0.03, xy.shape[0]).astype(np.float32)
@@ -232,3 +237,50 @@ def test_geometry_equals_the_reference_point_by_point(tmp_path, golden, nav_cell
     both(5, np.c_[xy, (e / np.linalg.norm(e, axis=1, keepdims=True)).astype(np.float32)], 1)
     both(6, np.c_[xy, fh + P.body_radius], 2)
     both(6, pos, 2)
+
+
+def test_geometry_equals_the_reference_point_by_point(tmp_path, golden, nav_cells):
+    """The seated venue's geometry and navigation lookup as compiled into the CUDA step (csrc/venue_seated.cuh, built
+    for the host by tests/seated_harness.cu) against the reference's own functions (seated::floorHeight, cellKey,
+    sdfGrad, wall, stepUpScan, floorSlope, nav::goal) at random points of venue S and at the fixture's agent positions:
+    bit for bit. Needs the reference's CPU build (this container)."""
+    pos = np.concatenate([golden[k][:, :3] for k in golden if k.startswith(("dense_state", "nearest_state", "incline_state"))])
+    _geometry_check(tmp_path, b"S", golden, nav_cells, pos, 100000)
+
+
+def _generated(name):
+    from swarm_gb300 import venues
+    g = dict(np.load(os.path.join(os.path.dirname(GOLDEN), "seated_%s.npz" % name)))
+    delta = np.frombuffer(zlib.decompress(g["nav_anchor_delta_z"].tobytes()), np.int32)
+    info = np.frombuffer(zlib.decompress(g["nav_info_z"].tobytes()), np.uint32)
+    cells = venues.nav_cells_from_anchors(np.cumsum(delta.astype(np.int64)), info, g["nav_grid"])
+    spawn = np.frombuffer(zlib.decompress(g["spawn_z"].tobytes()), np.float32).reshape(-1, 8).copy()
+    return g, cells, spawn
+
+
+@pytest.mark.parametrize("name", ["M", "L"])
+def test_geometry_of_the_generated_venues_equals_the_reference(tmp_path, name):
+    """The same comparison on the generated venues M and L: several straight gangways per wing, a door per gangway
+    head, corner doors, straight gangways merging with the corner gangway."""
+    g, cells, spawn = _generated(name)
+    _geometry_check(tmp_path, name.encode(), g, cells, spawn[spawn[:, 3] != 0, :3], 60000)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["M", "L"])
+def test_generated_venue_runs_reproduce_the_reference(name):
+    """Venues M (15 832 seated, N = 16 384) and L (63 424 seated, N = 65 536) from their full seat spawns: the states
+    after 1, 10 and 50 steps at the nearest exit and level speed, and after 10 steps with the incline speed and stair
+    spacing, hash to the reference's own states (FNV-1a of the raw state)."""
+    import swarm_gb300
+    g, cells, spawn = _generated(name)
+    assert spawn.shape[0] == int(g["n"][0]) and int((spawn[:, 3] != 0).sum()) == int(g["n"][1])
+    for prefix, incline, keep in (("nearest_", False, (1, 10, 50)), ("incline_", True, (10,))):
+        sim = swarm_gb300.CrowdSim(swarm_gb300.params_reference(), _venue(g, cells, incline), spawn.shape[0])
+        sim.set_state(spawn)
+        done = 0
+        for k in keep:
+            sim.step(k - done)
+            done = k
+            assert fnv1a(sim.state()) == int(g[prefix + "hash%d" % k][0]), f"{name} {prefix}{k} steps"
+        sim.close()
