@@ -71,7 +71,7 @@ struct SwarmSim {
     uint32_t* dInstSlot = nullptr;
     std::vector<int> instStart;   // first agent of each instance, + the total
     float *dSdf = nullptr, *dWall = nullptr, *dNav = nullptr, *dFloor = nullptr, *dSpeed = nullptr;
-    SwarmSeatedLayout seatLayout{};     // seated venues: the layout (kernel parameters)
+    SwarmSeatedLayout* dSeat = nullptr;  // seated venues: the layout (device copy)
     float4* dNavCells = nullptr;        //   and the navigation field's cells (null: drive table / router)
     float2* dWallFloor = nullptr;   // the wall SDF and floor heights interleaved (venues with a floor grid)
     uint8_t* dMask = nullptr;

@@ -38,9 +38,9 @@ struct VenueArgs {
     const float* speedF;
     const uint8_t* exitMask;    // optional: nonzero at the nav nodes beyond an exit
     uint32_t cellOffset;    // batched instances: this instance's first cell in the shared key space (0 otherwise)
-    // seated (the reference's analytic venues): the layout, read from the kernel parameters (uniform across a warp);
-    // the navigation field's cells (anchor x, anchor y, distance, info bits), navRes^2, x fastest
-    SwarmSeatedLayout seat;
+    // seated (the reference's analytic venues): the layout (a device copy); the navigation field's cells (anchor x,
+    // anchor y, distance, info bits), navRes^2, x fastest
+    const SwarmSeatedLayout* seatDev;
     const float4* navCells;
     int32_t navRes;
     float navOrigin, navCell, navInv;

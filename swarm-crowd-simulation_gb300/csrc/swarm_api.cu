@@ -78,7 +78,7 @@ StepArgs SwarmSim::args(int in) const {
     v.nav = dNav; v.nnx = V.nav_nx; v.nny = V.nav_ny; v.nox = V.nav_origin_x; v.noy = V.nav_origin_y;
     v.ninv = V.nav_h > 0.0f ? 1.0f / V.nav_h : 0.0f;
     v.floorH = dFloor; v.speedF = dSpeed; v.exitMask = dMask; v.wallFloor = dWallFloor;
-    v.seat = seatLayout;
+    v.seatDev = dSeat;
     v.navCells = dNavCells;
     v.navRes = V.nav_res; v.navOrigin = V.nav_grid_origin; v.navCell = V.nav_grid_cell; v.navInv = V.nav_grid_inv_cell;
     // the stair spacing is part of the stair model: off without the incline speed (effectiveModelOptions,
@@ -175,7 +175,6 @@ int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capac
             L.doors > SWARM_SEATED_MAX_DOORS || L.max_band_steps < 0 || !(L.row_depth > 0.0f))
             return bad("seated layout");
         if (V.nav_cells && (V.nav_res < 1 || !(V.nav_grid_cell > 0.0f) || !(V.nav_grid_inv_cell > 0.0f))) return bad("nav grid");
-        h->seatLayout = L;
     }
     if (V.grid_res_x <= 0 || V.grid_res_y <= 0 || !(V.domain_span_x > 0.0f) || !(V.domain_span_y > 0.0f)) return bad("grid");
     if (params->proj_iterations < 0 || params->perc_ring < 1 || params->perc_ring > 4) return bad("params");   // the predict pass holds <= 9 rows
@@ -203,6 +202,8 @@ int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capac
         const size_t nv = size_t(V.sdf_res) * size_t(V.sdf_res) * size_t(V.sdf_res);
         ok = devAlloc(h, &h->dSdf, nv) && cudaMemcpy(h->dSdf, V.sdf, nv * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
     }
+    if (ok && V.kind == SWARM_VENUE_SEATED)
+        ok = devAlloc(h, &h->dSeat, 1) && cudaMemcpy(h->dSeat, V.seated, sizeof(SwarmSeatedLayout), cudaMemcpyHostToDevice) == cudaSuccess;
     if (ok && V.kind == SWARM_VENUE_SEATED && V.nav_cells) {
         const size_t nc = size_t(V.nav_res) * size_t(V.nav_res);
         ok = devAlloc(h, &h->dNavCells, nc) &&

@@ -32,55 +32,63 @@ SWARM_HD __forceinline__ f3 gnormalize(f3 v) {
     return {v.x * r, v.y * r, v.z * r};
 }
 
-struct SeatedGeom {
-    const SwarmSeatedLayout& L;
+// The constants of the step-up scan (passed by value: the out-of-line functions read no kernel parameter)
+struct StepUpConst {
+    float sample, tol;
+    int maxSamples;
+};
 
-    SWARM_HD __forceinline__ float rowFront(int k) const { return L.row0 + float(k) * L.row_depth; }   // venue.cpp:417
-    SWARM_HD __forceinline__ float rowTread(int k) const { return L.first_row + float(k) * L.row_rise; }
-    SWARM_HD __forceinline__ int bandCount() const { return 6 + 2 * L.rows; }   // venue.cpp:486
+// (Out-of-line functions reach the layout through a pointer to global memory: a reference into the kernel's
+// parameter space would make every thread copy the parameters to its stack.)
+struct SeatedGeom {
+    const SwarmSeatedLayout* __restrict__ L;
+
+    SWARM_HD __forceinline__ float rowFront(int k) const { return L->row0 + float(k) * L->row_depth; }   // venue.cpp:417
+    SWARM_HD __forceinline__ float rowTread(int k) const { return L->first_row + float(k) * L->row_rise; }
+    SWARM_HD __forceinline__ int bandCount() const { return 6 + 2 * L->rows; }   // venue.cpp:486
     SWARM_HD __forceinline__ int activeGangways(int r) const {                  // venue.cpp:329-333
         int n = 0;
-        for (int i = 0; i < L.gangways; ++i) n += L.gw_row[i] <= r ? 1 : 0;
+        for (int i = 0; i < L->gangways; ++i) n += L->gw_row[i] <= r ? 1 : 0;
         return n;
     }
     SWARM_HD __forceinline__ bool mergedCorner(int r) const {                   // venue.cpp:335-338
         const int n = activeGangways(r);
-        return n > 0 && r < L.gw_seated[n - 1];
+        return n > 0 && r < L->gw_seated[n - 1];
     }
 
     // venue.cpp:488-504
     SWARM_HD void band(int j, float& lo, float& hi) const {
         const int nb = bandCount();
-        if (j <= 0) { lo = 0.0f; hi = L.stand_front; return; }
-        if (j == 1) { lo = L.stand_front; hi = L.row0; return; }
+        if (j <= 0) { lo = 0.0f; hi = L->stand_front; return; }
+        if (j == 1) { lo = L->stand_front; hi = L->row0; return; }
         if (j < nb - 4) {
             const int k = (j - 2) >> 1;
             const float d = rowFront(k);
-            if (((j - 2) & 1) == 0) { lo = d; hi = d + L.clearway; }
-            else { lo = d + L.clearway; hi = rowFront(k + 1); }
+            if (((j - 2) & 1) == 0) { lo = d; hi = d + L->clearway; }
+            else { lo = d + L->clearway; hi = rowFront(k + 1); }
             return;
         }
-        if (j == nb - 4) { lo = L.conc_front; hi = L.conc_back; return; }
-        if (j == nb - 3) { lo = L.conc_back; hi = L.outer_face; return; }
-        if (j == nb - 2) { lo = L.outer_face; hi = L.landing_end; return; }
-        lo = L.landing_end;
+        if (j == nb - 4) { lo = L->conc_front; hi = L->conc_back; return; }
+        if (j == nb - 3) { lo = L->conc_back; hi = L->outer_face; return; }
+        if (j == nb - 2) { lo = L->outer_face; hi = L->landing_end; return; }
+        lo = L->landing_end;
         hi = SEATED_BIG;
     }
 
     // venue.cpp:506-520
     SWARM_HD int bandOf(float dep) const {
         const int nb = bandCount();
-        if (dep < L.stand_front) return 0;
-        if (dep < L.row0) return 1;
-        if (dep < L.conc_front) {
-            int k = sclamp(int(floorf((dep - L.row0) / L.row_depth)), 0, L.rows - 1);
+        if (dep < L->stand_front) return 0;
+        if (dep < L->row0) return 1;
+        if (dep < L->conc_front) {
+            int k = sclamp(int(floorf((dep - L->row0) / L->row_depth)), 0, L->rows - 1);
             if (dep < rowFront(k)) --k;
-            else if (k + 1 < L.rows && dep >= rowFront(k + 1)) ++k;
-            return 2 + 2 * k + (dep >= rowFront(k) + L.clearway ? 1 : 0);
+            else if (k + 1 < L->rows && dep >= rowFront(k + 1)) ++k;
+            return 2 + 2 * k + (dep >= rowFront(k) + L->clearway ? 1 : 0);
         }
-        if (dep < L.conc_back) return nb - 4;
-        if (dep < L.outer_face) return nb - 3;
-        if (dep < L.landing_end) return nb - 2;
+        if (dep < L->conc_back) return nb - 4;
+        if (dep < L->outer_face) return nb - 3;
+        if (dep < L->landing_end) return nb - 2;
         return nb - 1;
     }
 
@@ -95,65 +103,65 @@ struct SeatedGeom {
             l0 = 0.0f; l1 = hi; kind = SK_GROUND;
             return true;
         }
-        const bool cornerDoor = L.corner_door_lo < 1e8f;
+        const bool cornerDoor = L->corner_door_lo < 1e8f;
         if (j == nb - 2) {
             const int i = c >> 1;
-            if (i < L.doors) {
-                if ((c & 1) == 0) { l0 = i == 0 ? 0.0f : L.door_hi[i - 1]; l1 = L.door_lo[i]; kind = SK_GROUND; }
-                else { l0 = L.door_lo[i]; l1 = L.door_hi[i]; kind = SK_CONC; }
+            if (i < L->doors) {
+                if ((c & 1) == 0) { l0 = i == 0 ? 0.0f : L->door_hi[i - 1]; l1 = L->door_lo[i]; kind = SK_GROUND; }
+                else { l0 = L->door_lo[i]; l1 = L->door_hi[i]; kind = SK_CONC; }
                 return true;
             }
-            if (c == 2 * L.doors) { l0 = L.door_hi[L.doors - 1]; l1 = cornerDoor ? L.corner_door_lo : hi; kind = SK_GROUND; return true; }
-            if (c == 2 * L.doors + 1 && cornerDoor) { l0 = L.corner_door_lo; l1 = hi; kind = SK_CONC; return true; }
+            if (c == 2 * L->doors) { l0 = L->door_hi[L->doors - 1]; l1 = cornerDoor ? L->corner_door_lo : hi; kind = SK_GROUND; return true; }
+            if (c == 2 * L->doors + 1 && cornerDoor) { l0 = L->corner_door_lo; l1 = hi; kind = SK_CONC; return true; }
             return false;
         }
-        if (c == 0) { l0 = 0.0f; l1 = L.avenue_half; kind = SK_GROUND; return true; }
+        if (c == 0) { l0 = 0.0f; l1 = L->avenue_half; kind = SK_GROUND; return true; }
         if (j == nb - 3) {
             const int i = (c - 1) >> 1;
-            if (i < L.doors) {
-                if ((c & 1) == 1) { l0 = i == 0 ? L.avenue_half : L.door_hi[i - 1]; l1 = L.door_lo[i]; kind = SK_WALL; }
-                else { l0 = L.door_lo[i]; l1 = L.door_hi[i]; kind = SK_CONC; }
+            if (i < L->doors) {
+                if ((c & 1) == 1) { l0 = i == 0 ? L->avenue_half : L->door_hi[i - 1]; l1 = L->door_lo[i]; kind = SK_WALL; }
+                else { l0 = L->door_lo[i]; l1 = L->door_hi[i]; kind = SK_CONC; }
                 return true;
             }
-            if (c == 2 * L.doors + 1) { l0 = L.door_hi[L.doors - 1]; l1 = cornerDoor ? L.corner_door_lo : hi; kind = SK_WALL; return true; }
-            if (c == 2 * L.doors + 2 && cornerDoor) { l0 = L.corner_door_lo; l1 = hi; kind = SK_CONC; return true; }
+            if (c == 2 * L->doors + 1) { l0 = L->door_hi[L->doors - 1]; l1 = cornerDoor ? L->corner_door_lo : hi; kind = SK_WALL; return true; }
+            if (c == 2 * L->doors + 2 && cornerDoor) { l0 = L->corner_door_lo; l1 = hi; kind = SK_CONC; return true; }
             return false;
         }
         if (j == nb - 4) {
-            if (c == 1) { l0 = L.avenue_half; l1 = L.lat0; kind = SK_WALL; return true; }
+            if (c == 1) { l0 = L->avenue_half; l1 = L->lat0; kind = SK_WALL; return true; }
             if (c > 2) return false;
-            l0 = L.lat0; l1 = hi; kind = SK_CONC;
+            l0 = L->lat0; l1 = hi; kind = SK_CONC;
             return true;
         }
         int segKind = SK_BARRIER, gapKind = SK_GROUND;
         bool seatBand = true;
-        float corner = hi - L.corner_inset - L.seat_inset;
+        float corner = hi - L->corner_inset - L->seat_inset;
         if (j >= 2) {
             row = (j - 2) >> 1;
             seatBand = ((j - 2) & 1) != 0;
             segKind = seatBand ? SK_SEAT : SK_TREAD;
             gapKind = SK_INCLINE;
-            if (!seatBand) corner = lo - L.corner_inset;
+            if (!seatBand) corner = lo - L->corner_inset;
         }
-        if (c == 1) { l0 = L.avenue_half; l1 = L.lat0; kind = SK_SIDE; return true; }
+        if (c == 1) { l0 = L->avenue_half; l1 = L->lat0; kind = SK_SIDE; return true; }
         const int r = (j - 1) >> 1;
         const int n = activeGangways(r);
         const bool merged = mergedCorner(r);
         const int i = (c - 2) >> 1;
         if (i < n) {
             if ((c & 1) == 0) {
-                l0 = i == 0 ? L.lat0 : (seatBand ? L.gw_hi[i - 1] + L.seat_inset : L.gw_hi[i - 1]);
-                l1 = seatBand ? L.gw_lo[i] - L.seat_inset : L.gw_lo[i];
+                l0 = i == 0 ? L->lat0 : (seatBand ? L->gw_hi[i - 1] + L->seat_inset : L->gw_hi[i - 1]);
+                l1 = seatBand ? L->gw_lo[i] - L->seat_inset : L->gw_lo[i];
                 kind = segKind;
             } else {
-                l0 = seatBand ? L.gw_lo[i] - L.seat_inset : L.gw_lo[i];
-                l1 = merged && i == n - 1 ? hi : (seatBand ? L.gw_hi[i] + L.seat_inset : L.gw_hi[i]);
+                l0 = seatBand ? L->gw_lo[i] - L->seat_inset : L->gw_lo[i];
+                l1 = merged && i == n - 1 ? hi : (seatBand ? L->gw_hi[i] + L->seat_inset : L->gw_hi[i]);
                 kind = gapKind;
             }
             return true;
         }
         if (merged) return false;
-        if (c == 2 + 2 * n) { l0 = seatBand ? L.gw_hi[n - 1] + L.seat_inset : L.gw_hi[n - 1]; l1 = corner; kind = segKind; return true; }
+        if (c == 2 + 2 * n) { l0 = seatBand ? L->gw_hi[n - 1] + L->seat_inset : L->gw_hi[n - 1]; l1 = corner; kind = segKind; return true; }
         if (c == 3 + 2 * n) { l0 = corner; l1 = hi; kind = gapKind; return true; }
         return false;
     }
@@ -162,12 +170,12 @@ struct SeatedGeom {
     SWARM_HD float cellTop(int kind, int row, float dep) const {
         switch (kind) {
         case SK_TREAD: return rowTread(row);
-        case SK_SEAT: return rowTread(row) + L.seat_top;
-        case SK_INCLINE: return L.rake * (dep - L.row0);
-        case SK_BARRIER: return L.barrier_top;
-        case SK_WALL: return L.wall_top;
-        case SK_CONC: return L.concourse_z;
-        case SK_SIDE: return row < 0 ? L.barrier_top : rowTread(row) + L.seat_top;
+        case SK_SEAT: return rowTread(row) + L->seat_top;
+        case SK_INCLINE: return L->rake * (dep - L->row0);
+        case SK_BARRIER: return L->barrier_top;
+        case SK_WALL: return L->wall_top;
+        case SK_CONC: return L->concourse_z;
+        case SK_SIDE: return row < 0 ? L->barrier_top : rowTread(row) + L->seat_top;
         default: return 0.0f;
         }
     }
@@ -220,7 +228,7 @@ struct SeatedGeom {
         int kind, row;
         ownCell(j, f.x, l0, l1, kind, row);
         if (kind != SK_INCLINE) return 0.0f;
-        const f2 g = unfoldDir(p, f2{0.0f, L.rake});
+        const f2 g = unfoldDir(p, f2{0.0f, L->rake});
         const float a = g.x * e.x, b = g.y * e.y;
         return a + b;
     }
@@ -248,14 +256,14 @@ struct SeatedGeom {
         const float latC = sclamp(pf.x, l0, l1);
         f3 q;
         if (kind == SK_INCLINE) {
-            const f2 n2 = nearestRegion2(pf.y, pf.z, lo, hi, L.rake, L.row0, !airColumn);
+            const f2 n2 = nearestRegion2(pf.y, pf.z, lo, hi, L->rake, L->row0, !airColumn);
             q = f3{latC, n2.x, n2.y};
             if (airColumn && q.x > q.y) {
                 const float s0 = smax(l0, lo), s1 = smin(l1, hi);
                 if (s0 > s1) return make_float4(q.x, q.y, q.z, SEATED_BIG);
                 const float r2 = 1.41421356f;
                 const float m = 0.5f * (pf.x + pf.y);
-                const f2 w = nearestRegion2(m * r2, pf.z, s0 * r2, s1 * r2, L.rake / r2, L.row0 * r2, false);
+                const f2 w = nearestRegion2(m * r2, pf.z, s0 * r2, s1 * r2, L->rake / r2, L->row0 * r2, false);
                 const float s = w.x / r2;
                 q = f3{s, s, w.y};
             }
@@ -298,7 +306,7 @@ struct SeatedGeom {
         };
         visit(jp, 0.0f);
         bool down = true, up = true;
-        for (int s = 1; s <= L.max_band_steps && (down || up); ++s) {
+        for (int s = 1; s <= L->max_band_steps && (down || up); ++s) {
             for (int side = 0; side < 2; ++side) {
                 bool& open = side == 0 ? down : up;
                 if (!open) continue;
@@ -324,7 +332,7 @@ struct SeatedGeom {
                 const f2 hn = gnormalize(h);
                 gf = f3{hn.x, hn.y, 0.0f};
             } else {
-                gf = bestKind == SK_INCLINE ? gnormalize(f3{0.0f, -L.rake, 1.0f}) : f3{0.0f, 0.0f, 1.0f};
+                gf = bestKind == SK_INCLINE ? gnormalize(f3{0.0f, -L->rake, 1.0f}) : f3{0.0f, 0.0f, 1.0f};
             }
         }
         const f2 g = unfoldDir(xy(p), f2{gf.x, gf.y});
@@ -360,7 +368,7 @@ struct SeatedGeom {
         };
         visit(jp);
         bool down = true, up = true;
-        for (int s = 1; s <= L.max_band_steps && (down || up); ++s) {
+        for (int s = 1; s <= L->max_band_steps && (down || up); ++s) {
             for (int side = 0; side < 2; ++side) {
                 bool& open = side == 0 ? down : up;
                 if (!open) continue;
@@ -389,10 +397,10 @@ struct SeatedGeom {
     }
 
     // venue.cpp:807-835 stepUpScan: the fraction of the move p0 -> p1 an agent whose start floor is f0 may take
-    SWARM_HD __noinline__ float stepUpScan(const SwarmParams& P, f2 p0, f2 p1, float f0, f2& n) const {
+    SWARM_HD __noinline__ float stepUpScan(StepUpConst P, f2 p0, f2 p1, float f0, f2& n) const {
         n = f2{0.0f, 0.0f};
         const float len = length(p1 - p0);
-        const int ns = sclamp(int(ceilf(len / P.step_up_sample)), 1, P.step_up_max_samples);
+        const int ns = sclamp(int(ceilf(len / P.sample)), 1, P.maxSamples);
         float lo = 0.0f;
         f2 key = cellKey(p0);
         for (int i = 1; i <= ns; ++i) {
@@ -406,9 +414,9 @@ struct SeatedGeom {
                     else b = tm;
                 }
                 const float ha = floorHeight(mix(p0, p1, a)), hb = floorHeight(mix(p0, p1, b));
-                if (hb > f0 + P.step_up_tol && hb - ha > L.rake * len * (b - a) + P.step_up_tol) {
+                if (hb > f0 + P.tol && hb - ha > L->rake * len * (b - a) + P.tol) {
                     const f2 pa = mix(p0, p1, a);
-                    const f3 w = wall(f3{pa.x, pa.y, ha + P.step_up_tol}, P.step_up_sample);
+                    const f3 w = wall(f3{pa.x, pa.y, ha + P.tol}, P.sample);
                     n = w.z < WALL_NONE ? f2{w.x, w.y} : (p0 - p1) / smax(len, 1e-30f);
                     return a;
                 }
@@ -418,6 +426,66 @@ struct SeatedGeom {
             lo = t;
         }
         return 1.0f;
+    }
+
+    // cpu_crowd_sim.cpp:264-270: the heightfield's floor under c (the step's floorUnderReach on a seated venue)
+    SWARM_HD __forceinline__ bool floorUnderReach(f3 c, float zFrom, float down, float bodyRadius, float& zFloor) const {
+        const float h = floorHeight(xy(c));
+        zFloor = h;
+        if (c.z <= h) return h <= smax(zFrom, c.z) + bodyRadius;
+        return h >= c.z - down;
+    }
+
+    // cpu_crowd_sim.cpp:601-617 venueBlockedWall: a blocked move's point may lie in a wall's clearance band; the wall
+    // contact there, kept only if the push climbs no face
+    SWARM_HD __noinline__ void blockedWall(StepUpConst su, float feelerReach, float bodyRadius, float settleReach, float f0,
+                                           f3 pOld, f3& np, f3& nv) const {
+        const f3 w = wall(np + f3{0.0f, 0.0f, L->wall_above}, feelerReach);
+        if (w.z >= L->wall_clear) return;
+        const f2 pushed = xy(np) + f2{w.x, w.y} * (L->wall_clear - w.z);
+        f2 n;
+        if (stepUpScan(su, xy(np), pushed, f0, n) < 1.0f) return;
+        const float vDotN = dot(xy(nv), f2{w.x, w.y});
+        if (vDotN < 0.0f) setXY(nv, xy(nv) - f2{w.x, w.y} * vDotN);
+        float zFloor;
+        if (floorUnderReach(f3{pushed.x, pushed.y, pOld.z}, pOld.z, settleReach, bodyRadius, zFloor)) {
+            np = f3{pushed.x, pushed.y, zFloor + bodyRadius};
+            nv.z = 0.0f;
+        } else {
+            setXY(np, pushed);
+        }
+    }
+
+    // cpu_crowd_sim.cpp:622-650 venueEdgeMargin: every centre face_margin off the side face of a column higher than its
+    // feet; on such a column's edge: onto it unless that climbs; lifted and left over a lower floor: settled from the
+    // start-of-step height; airborne: off the face, still falling
+    SWARM_HD __noinline__ void edgeMargin(StepUpConst su, float bodyRadius, float settleReach, f3 pOld, float f0, f3& np,
+                                          f3& nv) const {
+        const float margin = L->face_margin;
+        float feet = np.z - bodyRadius;
+        const float fl = floorHeight(xy(np));
+        if (feet > fl + margin) {
+            const f3 w = wall(f3{np.x, np.y, fl + su.tol}, margin);
+            if (w.z < margin) {
+                const f2 into = xy(np) - f2{w.x, w.y} * (w.z + margin);
+                const float top = floorHeight(into);
+                if (fabsf(top - feet) <= margin && top <= f0 + su.tol) { setXY(np, into); return; }
+            }
+            if (np.z <= pOld.z) {
+                const f3 wa = wall(f3{np.x, np.y, feet + su.tol}, margin);
+                if (wa.z < margin) setXY(np, xy(np) + f2{wa.x, wa.y} * (margin - wa.z));
+                return;
+            }
+            float zFloor;
+            if (!floorUnderReach(f3{np.x, np.y, pOld.z}, pOld.z, settleReach, bodyRadius, zFloor)) { np.z = pOld.z; return; }
+            np.z = zFloor + bodyRadius;
+            nv.z = 0.0f;
+            feet = zFloor;
+        }
+        const f3 w = wall(f3{np.x, np.y, feet + su.tol}, margin);
+        if (w.z >= margin) return;
+        setXY(np, xy(np) + f2{w.x, w.y} * (margin - w.z));
+        np.z = floorHeight(xy(np)) + bodyRadius;
     }
 };
 
@@ -433,7 +501,8 @@ SWARM_HD __forceinline__ float4 loadCell(const float4* p) {
 
 struct SeatedNav {
     SeatedGeom G;
-    const SwarmParams& P;
+    StepUpConst su;
+    float goalDeadzone, feelerReach, safeEps;
     const float4* cells;
     int res;
     float origin, cell, inv;
@@ -452,7 +521,7 @@ struct SeatedNav {
     SWARM_HD __forceinline__ bool reaches(f2 x, f2 c) const {   // nav_field.cpp:381-385 surfaceReaches
         if (G.cellKey(c) == G.cellKey(x)) return true;
         f2 n;
-        return G.stepUpScan(P, x, c, G.floorHeight(x), n) >= 1.0f;
+        return G.stepUpScan(su, x, c, G.floorHeight(x), n) >= 1.0f;
     }
     // nav_field.cpp:387-421 directionCell: the cell containing x, or its nearest FIT neighbour with a path when it is
     // NOFIT; then the surface rule (the nearest such cell whose centre the agent may walk straight to)
@@ -502,14 +571,14 @@ struct SeatedNav {
         if (ci & SWARM_NAV_REACHABLE) {
             const f2 d = f2{c.x, c.y} - x;
             const float l = length(d);
-            e = l > P.goal_deadzone ? d / l : f2{0.0f, 0.0f};
+            e = l > goalDeadzone ? d / l : f2{0.0f, 0.0f};
         }
-        const f3 w = G.wall(p, P.feeler_reach);
+        const f3 w = G.wall(p, feelerReach);
         const float into = dot(e, f2{w.x, w.y});
-        if (w.z < P.feeler_reach && into < 0.0f) {
+        if (w.z < feelerReach && into < 0.0f) {
             e = e - f2{w.x, w.y} * into;
             const float l = length(e);
-            e = l > P.safe_eps ? e / l : f2{0.0f, 0.0f};
+            e = l > safeEps ? e / l : f2{0.0f, 0.0f};
         }
         return e;
     }
@@ -519,18 +588,16 @@ struct Seated {
     const SwarmParams& P;
     const VenueArgs& V;
 
-    __device__ __forceinline__ SeatedGeom geo() const { return SeatedGeom{V.seat}; }
+    __device__ __forceinline__ SeatedGeom geo() const { return SeatedGeom{V.seatDev}; }
+    __device__ __forceinline__ StepUpConst stepUp() const { return StepUpConst{P.step_up_sample, P.step_up_tol, P.step_up_max_samples}; }
     __device__ __forceinline__ Stadium fence() const { return Stadium{P, V}; }   // the pitch fence and the router
 
     __device__ __forceinline__ float map(f3 p) const { return geo().sdfGrad(p).w; }             // cpu_crowd_sim.cpp:225-229
     __device__ __forceinline__ float4 mapExactGrad(f3 p) const { return geo().sdfGrad(p); }     // cpu_crowd_sim.cpp:239-242
 
     // cpu_crowd_sim.cpp:264-270: the heightfield's floor
-    __device__ bool floorUnderReach(f3 c, float zFrom, float down, float& zFloor) const {
-        const float h = geo().floorHeight(xy(c));
-        zFloor = h;
-        if (c.z <= h) return h <= smax(zFrom, c.z) + P.body_radius;
-        return h >= c.z - down;
+    __device__ __forceinline__ bool floorUnderReach(f3 c, float zFrom, float down, float& zFloor) const {
+        return geo().floorUnderReach(c, zFrom, down, P.body_radius, zFloor);
     }
     __device__ bool restOnFloor(f3& np, f3& nv, float zFrom) const {   // cpu_crowd_sim.cpp:317-325
         float zFloor;
@@ -572,7 +639,7 @@ struct Seated {
     __device__ bool clearWalls(f3& np, f3& nv, f3& wall) const {
         bool moved = false;
         wall = f3{0.0f, 0.0f, 0.0f};
-        const SwarmSeatedLayout& L = V.seat;
+        const SwarmSeatedLayout& L = *V.seatDev;
         for (int pass = 0; pass < P.wall_passes; ++pass) {
             const f3 w = geo().wall(np + f3{0.0f, 0.0f, L.wall_above}, P.feeler_reach);
             if (w.z >= L.wall_clear) {
@@ -589,7 +656,7 @@ struct Seated {
     }
     // cpu_crowd_sim.cpp:423-427 wallPlaneProbe, the analytic branch
     __device__ f3 wallPlaneProbe(f3 np, float) const {
-        const SwarmSeatedLayout& L = V.seat;
+        const SwarmSeatedLayout& L = *V.seatDev;
         const f3 w = geo().wall(np + f3{0.0f, 0.0f, L.wall_above}, P.plane_probe_reach);
         return w.z >= 0.0f && w.z < WALL_NONE ? f3{w.x, w.y, smax(w.z - L.wall_clear, 0.0f)} : f3{0.0f, 0.0f, 0.0f};
     }
@@ -652,59 +719,15 @@ struct Seated {
 
     // cpu_crowd_sim.cpp:536-537 venueStepUpScan
     __device__ __forceinline__ float venueStepUpScan(f2 p0, f2 p1, float f0, f2& n) const {
-        return geo().stepUpScan(P, p0, p1, f0, n);
+        return geo().stepUpScan(stepUp(), p0, p1, f0, n);
     }
 
-    // cpu_crowd_sim.cpp:601-617 venueBlockedWall: a blocked move's point may lie in a wall's clearance band; the wall
-    // contact there, kept only if the push climbs no face
-    __device__ __noinline__ void venueBlockedWall(float f0, f3 pOld, f3& np, f3& nv) const {
-        const SwarmSeatedLayout& L = V.seat;
-        const f3 w = geo().wall(np + f3{0.0f, 0.0f, L.wall_above}, P.feeler_reach);
-        if (w.z >= L.wall_clear) return;
-        const f2 pushed = xy(np) + f2{w.x, w.y} * (L.wall_clear - w.z);
-        f2 n;
-        if (venueStepUpScan(xy(np), pushed, f0, n) < 1.0f) return;
-        const float vDotN = dot(xy(nv), f2{w.x, w.y});
-        if (vDotN < 0.0f) setXY(nv, xy(nv) - f2{w.x, w.y} * vDotN);
-        float zFloor;
-        if (floorUnderReach(f3{pushed.x, pushed.y, pOld.z}, pOld.z, P.floor_settle_reach, zFloor)) {
-            np = f3{pushed.x, pushed.y, zFloor + P.body_radius};
-            nv.z = 0.0f;
-        } else {
-            setXY(np, pushed);
-        }
+    // cpu_crowd_sim.cpp:601-617 venueBlockedWall, 622-650 venueEdgeMargin (out of line, on the geometry)
+    __device__ __forceinline__ void venueBlockedWall(float f0, f3 pOld, f3& np, f3& nv) const {
+        geo().blockedWall(stepUp(), P.feeler_reach, P.body_radius, P.floor_settle_reach, f0, pOld, np, nv);
     }
-
-    // cpu_crowd_sim.cpp:622-650 venueEdgeMargin: every centre faceMargin off the side face of a column higher than its
-    // feet; on such a column's edge: onto it unless that climbs; lifted and left over a lower floor: settled from the
-    // start-of-step height; airborne: off the face, still falling
-    __device__ __noinline__ void venueEdgeMargin(f3 pOld, float f0, f3& np, f3& nv) const {
-        const SeatedGeom G = geo();
-        const float margin = V.seat.face_margin;
-        float feet = np.z - P.body_radius;
-        const float fl = G.floorHeight(xy(np));
-        if (feet > fl + margin) {
-            const f3 w = G.wall(f3{np.x, np.y, fl + P.step_up_tol}, margin);
-            if (w.z < margin) {
-                const f2 into = xy(np) - f2{w.x, w.y} * (w.z + margin);
-                const float top = G.floorHeight(into);
-                if (fabsf(top - feet) <= margin && top <= f0 + P.step_up_tol) { setXY(np, into); return; }
-            }
-            if (np.z <= pOld.z) {
-                const f3 wa = G.wall(f3{np.x, np.y, feet + P.step_up_tol}, margin);
-                if (wa.z < margin) setXY(np, xy(np) + f2{wa.x, wa.y} * (margin - wa.z));
-                return;
-            }
-            float zFloor;
-            if (!floorUnderReach(f3{np.x, np.y, pOld.z}, pOld.z, P.floor_settle_reach, zFloor)) { np.z = pOld.z; return; }
-            np.z = zFloor + P.body_radius;
-            nv.z = 0.0f;
-            feet = zFloor;
-        }
-        const f3 w = G.wall(f3{np.x, np.y, feet + P.step_up_tol}, margin);
-        if (w.z >= margin) return;
-        setXY(np, xy(np) + f2{w.x, w.y} * (margin - w.z));
-        np.z = G.floorHeight(xy(np)) + P.body_radius;
+    __device__ __forceinline__ void venueEdgeMargin(f3 pOld, float f0, f3& np, f3& nv) const {
+        geo().edgeMargin(stepUp(), P.body_radius, P.floor_settle_reach, pOld, f0, np, nv);
     }
 
     // cpu_crowd_sim.cpp:566-597 limitStepUp, the analytic branch
@@ -745,7 +768,8 @@ struct Seated {
     // e_goal: the navigation field's anchor lookup; without a field, the egress router (cpu_crowd_sim.cpp:213-218)
     __device__ __forceinline__ f2 goal(f3 p) const {
         if (!V.navCells) return fence().goal(p);
-        return SeatedNav{geo(), P, V.navCells, V.navRes, V.navOrigin, V.navCell, V.navInv}.goal(p);
+        return SeatedNav{geo(), stepUp(), P.goal_deadzone, P.feeler_reach, P.safe_eps, V.navCells, V.navRes, V.navOrigin,
+                         V.navCell, V.navInv}.goal(p);
     }
 
     __device__ __forceinline__ bool exits(float4 p) const { return fence().exits(p); }   // cpu_crowd_sim.cpp:662-668

@@ -9,7 +9,7 @@ using namespace swarm_gpu;
 // 4 stepUpScan(x0, y0, x1, y1, f0) -> (t, n.x, n.y) | 5 floorSlope(x, y, ex, ey) -> 1 | 6 nav goal(x, y, z) -> 2
 extern "C" int hs_eval(const SwarmSeatedLayout* L, const SwarmParams* P, int op, int n, const float* in, float* out,
                        const float* nav, int navRes, float navOrigin, float navCell, float navInv) {
-    const SeatedGeom G{*L};
+    const SeatedGeom G{L};
     for (int i = 0; i < n; ++i) {
         switch (op) {
         case 0: out[i] = G.floorHeight(f2{in[2 * i], in[2 * i + 1]}); break;
@@ -26,13 +26,14 @@ extern "C" int hs_eval(const SwarmSeatedLayout* L, const SwarmParams* P, int op,
         }
         case 4: {
             f2 nn;
-            const float t = G.stepUpScan(*P, f2{in[5 * i], in[5 * i + 1]}, f2{in[5 * i + 2], in[5 * i + 3]}, in[5 * i + 4], nn);
+            const float t = G.stepUpScan(StepUpConst{P->step_up_sample, P->step_up_tol, P->step_up_max_samples}, f2{in[5 * i], in[5 * i + 1]}, f2{in[5 * i + 2], in[5 * i + 3]}, in[5 * i + 4], nn);
             out[3 * i] = t; out[3 * i + 1] = nn.x; out[3 * i + 2] = nn.y;
             break;
         }
         case 5: out[i] = G.floorSlope(f2{in[4 * i], in[4 * i + 1]}, f2{in[4 * i + 2], in[4 * i + 3]}); break;
         case 6: {
-            const SeatedNav N{G, *P, reinterpret_cast<const float4*>(nav), navRes, navOrigin, navCell, navInv};
+            const SeatedNav N{G, StepUpConst{P->step_up_sample, P->step_up_tol, P->step_up_max_samples}, P->goal_deadzone,
+                               P->feeler_reach, P->safe_eps, reinterpret_cast<const float4*>(nav), navRes, navOrigin, navCell, navInv};
             const f2 e = N.goal(f3{in[3 * i], in[3 * i + 1], in[3 * i + 2]});
             out[2 * i] = e.x; out[2 * i + 1] = e.y;
             break;
