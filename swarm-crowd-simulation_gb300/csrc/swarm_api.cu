@@ -10,6 +10,7 @@
 #include "metrics.cuh"
 #include "sim_handle.cuh"
 #include "step_kernels.cuh"
+#include "venue_seated.cuh"
 
 #include <cuda_runtime.h>
 
@@ -202,8 +203,12 @@ int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capac
         const size_t nv = size_t(V.sdf_res) * size_t(V.sdf_res) * size_t(V.sdf_res);
         ok = devAlloc(h, &h->dSdf, nv) && cudaMemcpy(h->dSdf, V.sdf, nv * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
     }
-    if (ok && V.kind == SWARM_VENUE_SEATED)
-        ok = devAlloc(h, &h->dSeat, 1) && cudaMemcpy(h->dSeat, V.seated, sizeof(SwarmSeatedLayout), cudaMemcpyHostToDevice) == cudaSuccess;
+    if (ok && V.kind == SWARM_VENUE_SEATED) {   // the layout with its band and cell tables
+        const std::vector<unsigned char> blob = swarm_gpu::seatedBlob(*V.seated);
+        unsigned char* d = nullptr;
+        ok = devAlloc(h, &d, blob.size()) && cudaMemcpy(d, blob.data(), blob.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+        h->dSeat = reinterpret_cast<SwarmSeatedLayout*>(d);
+    }
     if (ok && V.kind == SWARM_VENUE_SEATED && V.nav_cells) {
         const size_t nc = size_t(V.nav_res) * size_t(V.nav_res);
         ok = devAlloc(h, &h->dNavCells, nc) &&

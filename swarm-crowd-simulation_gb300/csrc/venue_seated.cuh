@@ -13,6 +13,7 @@
 #include "venue_stadium.cuh"
 
 #include <cstring>
+#include <vector>
 
 namespace swarm_gpu {
 
@@ -31,6 +32,16 @@ SWARM_HD __forceinline__ f3 gnormalize(f3 v) {
     const float r = 1.0f / sqrtf(dot(v, v));
     return {v.x * r, v.y * r, v.z * r};
 }
+
+// The seated venue on the device is one blob: the layout, then its band table ((lo, hi) per band), the first cell of
+// each band (bands + 1 entries) and the cell table ((l0, l1, kind, top) per cell), each array 16-byte aligned. The
+// tables hold exactly what the band and cell functions compute (SeatedGeom::bandCompute / cellCompute /
+// cellTopCompute, the same source compiled for the host), so a lookup gives the computed bits without redoing the
+// band walk in every query.
+struct SeatedTablesHeader {
+    SwarmSeatedLayout layout;
+    int32_t bands, cells, band_off, start_off, cell_off, pad[3];   // byte offsets from the blob's start
+};
 
 // The constants of the step-up scan (passed by value: the out-of-line functions read no kernel parameter)
 struct StepUpConst {
@@ -56,8 +67,8 @@ struct SeatedGeom {
         return n > 0 && r < L->gw_seated[n - 1];
     }
 
-    // venue.cpp:488-504
-    SWARM_HD void band(int j, float& lo, float& hi) const {
+    // venue.cpp:488-504 (computed; the step reads the venue's band table, built from this)
+    SWARM_HD void bandCompute(int j, float& lo, float& hi) const {
         const int nb = bandCount();
         if (j <= 0) { lo = 0.0f; hi = L->stand_front; return; }
         if (j == 1) { lo = L->stand_front; hi = L->row0; return; }
@@ -92,11 +103,11 @@ struct SeatedGeom {
         return nb - 1;
     }
 
-    // venue.cpp:522-594: cell c of band j, ascending in lat
-    SWARM_HD bool cell(int j, int c, float& l0, float& l1, int& kind, int& row) const {
+    // venue.cpp:522-594: cell c of band j, ascending in lat (computed; the step reads the venue's cell table)
+    SWARM_HD bool cellCompute(int j, int c, float& l0, float& l1, int& kind, int& row) const {
         const int nb = bandCount();
         float lo, hi;
-        band(j, lo, hi);
+        bandCompute(j, lo, hi);
         row = -1;
         if (j == 0 || j == nb - 1) {
             if (c > 0) return false;
@@ -166,8 +177,8 @@ struct SeatedGeom {
         return false;
     }
 
-    // venue.cpp:596-607
-    SWARM_HD float cellTop(int kind, int row, float dep) const {
+    // venue.cpp:596-607 (computed; the cell table holds each cell's top, an incline's excepted)
+    SWARM_HD float cellTopCompute(int kind, int row, float dep) const {
         switch (kind) {
         case SK_TREAD: return rowTread(row);
         case SK_SEAT: return rowTread(row) + L->seat_top;
@@ -180,11 +191,38 @@ struct SeatedGeom {
         }
     }
 
+    // ---- the band and cell tables (the step's lookups) ----
+    SWARM_HD __forceinline__ const SeatedTablesHeader& H() const { return *reinterpret_cast<const SeatedTablesHeader*>(L); }
+    SWARM_HD __forceinline__ const char* base() const { return reinterpret_cast<const char*>(L); }
+    SWARM_HD __forceinline__ void band(int j, float& lo, float& hi) const {
+        const float2 b = reinterpret_cast<const float2*>(base() + H().band_off)[j];
+        lo = b.x;
+        hi = b.y;
+    }
+    // cell c of band j: its lateral bounds, kind and top height (cellTopCompute at dep 0: exact but for an incline)
+    SWARM_HD __forceinline__ bool cell(int j, int c, float& l0, float& l1, int& kind, float& top) const {
+        const int32_t* start = reinterpret_cast<const int32_t*>(base() + H().start_off);
+        const int e = start[j] + c;
+        if (e >= start[j + 1]) return false;
+        const float4 t = reinterpret_cast<const float4*>(base() + H().cell_off)[e];
+        l0 = t.x;
+        l1 = t.y;
+        int32_t k;
+        memcpy(&k, &t.z, 4);
+        kind = k;
+        top = t.w;
+        return true;
+    }
+    SWARM_HD __forceinline__ float cellTop(int kind, float top, float dep) const {
+        return kind == SK_INCLINE ? L->rake * (dep - L->row0) : top;
+    }
+
     // venue.cpp:421-430: the cell of band j containing lat
-    SWARM_HD int ownCell(int j, float lat, float& l0, float& l1, int& kind, int& row) const {
+    SWARM_HD int ownCell(int j, float lat, float& l0, float& l1, int& kind, float& row) const {
         int c = 0;
         float a, b;
-        int k, r;
+        int k;
+        float r;
         for (; cell(j, c, a, b, k, r); ++c) {
             l0 = a; l1 = b; kind = k; row = r;
             if (lat < b) return c;
@@ -207,7 +245,8 @@ struct SeatedGeom {
         const f2 f = fold(p);
         const int j = bandOf(f.y);
         float l0, l1;
-        int kind, row;
+        int kind;
+        float row;
         ownCell(j, f.x, l0, l1, kind, row);
         return {float(j), l0};
     }
@@ -215,7 +254,8 @@ struct SeatedGeom {
         const f2 f = fold(p);
         const int j = bandOf(f.y);
         float l0, l1;
-        int kind, row;
+        int kind;
+        float row;
         ownCell(j, f.x, l0, l1, kind, row);
         return cellTop(kind, row, f.y);
     }
@@ -225,7 +265,8 @@ struct SeatedGeom {
         const f2 f = fold(p);
         const int j = bandOf(f.y);
         float l0, l1;
-        int kind, row;
+        int kind;
+        float row;
         ownCell(j, f.x, l0, l1, kind, row);
         if (kind != SK_INCLINE) return 0.0f;
         const f2 g = unfoldDir(p, f2{0.0f, L->rake});
@@ -252,7 +293,7 @@ struct SeatedGeom {
     }
 
     // venue.cpp:456-477 nearestInCell: the nearest point of a cell's solid (or air) column; squared distance in .w
-    SWARM_HD float4 nearestInCell(float lo, float hi, float l0, float l1, int kind, int row, f3 pf, bool airColumn) const {
+    SWARM_HD float4 nearestInCell(float lo, float hi, float l0, float l1, int kind, float row, f3 pf, bool airColumn) const {
         const float latC = sclamp(pf.x, l0, l1);
         f3 q;
         if (kind == SK_INCLINE) {
@@ -282,7 +323,8 @@ struct SeatedGeom {
         const int nb = bandCount();
         const int jp = bandOf(pf.y);
         float l0, l1;
-        int kind, row;
+        int kind;
+        float row;
         ownCell(jp, pf.x, l0, l1, kind, row);
         const bool inAir = pf.z > cellTop(kind, row, pf.y);
         float best = SEATED_BIG;
@@ -293,7 +335,8 @@ struct SeatedGeom {
             float lo, hi;
             band(j, lo, hi);
             float a, b;
-            int k, r;
+            int k;
+            float r;
             for (int c = 0; cell(j, c, a, b, k, r); ++c) {
                 const float lg = smax(smax(a - pf.x, pf.x - b), 0.0f);
                 if (g2 + lg * lg >= best) {
@@ -345,7 +388,8 @@ struct SeatedGeom {
         const int nb = bandCount();
         const int jp = bandOf(f.y);
         float l0, l1;
-        int kind, row;
+        int kind;
+        float row;
         ownCell(jp, f.x, l0, l1, kind, row);
         const bool inWall = kind != SK_INCLINE && cellTop(kind, row, f.y) > c.z;
         float best = inWall ? SEATED_BIG : reach * reach;
@@ -356,7 +400,8 @@ struct SeatedGeom {
             float lo, hi;
             band(j, lo, hi);
             float a, b;
-            int k, r;
+            int k;
+            float r;
             for (int cc = 0; cell(j, cc, a, b, k, r); ++cc) {
                 const bool isWall = k != SK_INCLINE && cellTop(k, r, lo) > c.z;
                 if (isWall == inWall) continue;
@@ -488,6 +533,46 @@ struct SeatedGeom {
         np.z = floorHeight(xy(np)) + bodyRadius;
     }
 };
+
+
+// The seated venue's device blob for a layout (a host function): the layout, its band table and its cell table
+inline std::vector<unsigned char> seatedBlob(const SwarmSeatedLayout& layout) {
+    SeatedTablesHeader h{};
+    h.layout = layout;
+    const SeatedGeom G{&h.layout};
+    const int nb = G.bandCount();
+    std::vector<float2> bands(static_cast<size_t>(nb));
+    std::vector<int32_t> start(static_cast<size_t>(nb) + 1, 0);
+    std::vector<float4> cells;
+    for (int j = 0; j < nb; ++j) {
+        G.bandCompute(j, bands[size_t(j)].x, bands[size_t(j)].y);
+        start[size_t(j)] = int32_t(cells.size());
+        float l0, l1;
+        int kind, row;
+        for (int c = 0; G.cellCompute(j, c, l0, l1, kind, row); ++c) {
+            float4 t;
+            t.x = l0;
+            t.y = l1;
+            const int32_t kk = kind;
+            memcpy(&t.z, &kk, 4);
+            t.w = kind == SK_INCLINE ? 0.0f : G.cellTopCompute(kind, row, 0.0f);
+            cells.push_back(t);
+        }
+    }
+    start[size_t(nb)] = int32_t(cells.size());
+    auto up16 = [](size_t x) { return (x + 15) / 16 * 16; };
+    h.bands = nb;
+    h.cells = int32_t(cells.size());
+    h.band_off = int32_t(up16(sizeof h));
+    h.start_off = int32_t(up16(size_t(h.band_off) + bands.size() * sizeof(float2)));
+    h.cell_off = int32_t(up16(size_t(h.start_off) + start.size() * sizeof(int32_t)));
+    std::vector<unsigned char> blob(size_t(h.cell_off) + cells.size() * sizeof(float4), 0);
+    memcpy(blob.data(), &h, sizeof h);
+    memcpy(blob.data() + h.band_off, bands.data(), bands.size() * sizeof(float2));
+    memcpy(blob.data() + h.start_off, start.data(), start.size() * sizeof(int32_t));
+    memcpy(blob.data() + h.cell_off, cells.data(), cells.size() * sizeof(float4));
+    return blob;
+}
 
 // The navigation field's lookup (src/nav_field.cpp:375-441; physics.comp navCell / navDirection / navGoal): cells of
 // the reference's GpuNavCell (anchor x, anchor y, distance, info bits), res x res, x fastest

@@ -9,7 +9,8 @@ using namespace swarm_gpu;
 // 4 stepUpScan(x0, y0, x1, y1, f0) -> (t, n.x, n.y) | 5 floorSlope(x, y, ex, ey) -> 1 | 6 nav goal(x, y, z) -> 2
 extern "C" int hs_eval(const SwarmSeatedLayout* L, const SwarmParams* P, int op, int n, const float* in, float* out,
                        const float* nav, int navRes, float navOrigin, float navCell, float navInv) {
-    const SeatedGeom G{L};
+    const std::vector<unsigned char> blob = seatedBlob(*L);   // the layout and its tables, as the step holds them
+    const SeatedGeom G{reinterpret_cast<const SwarmSeatedLayout*>(blob.data())};
     for (int i = 0; i < n; ++i) {
         switch (op) {
         case 0: out[i] = G.floorHeight(f2{in[2 * i], in[2 * i + 1]}); break;
