@@ -133,6 +133,7 @@ def bench_batched(P, steps=10, warmup=3):
     batch.set_state(boids)
     batch.set_agent_params(r, v0)
     tuning = batch.autotune(steps=2)
+    batch.set_graph(True)   # single steps replay the fused launch from a CUDA graph
     dev = torch.empty((n, 8), dtype=torch.float32, device="cuda")
     with torch.cuda.stream(stream):
         for _ in range(warmup):
@@ -150,6 +151,18 @@ def bench_batched(P, steps=10, warmup=3):
             e1.record(stream)
         stream.synchronize()
         t_batch += e0.elapsed_time(e1)
+    # the same steps chained: one persistent launch runs them all, a grid barrier between steps (the working set is far
+    # larger than L2 either way)
+    batch.set_state(start)
+    torch.cuda.synchronize()
+    c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        c0.record(stream)
+        batch.step(steps)
+        c1.record(stream)
+    stream.synchronize()
+    t_chain = c0.elapsed_time(c1)
+    batch.synchronize()
     batch.close()
     # one at a time: each instance its own handle, all on one stream, stepped in turn
     solos = []
@@ -180,6 +193,8 @@ def bench_batched(P, steps=10, warmup=3):
         sim.close()
     return {"workload": "256 halls, N log-uniform [1024, 65536] (total %d agents), 1-2 exits U[1.5, 6] m, seed 0" % n,
             "value": active / (t_batch * 1e-3), "unit": UNIT, "ms_per_step": t_batch / steps,
+            "chained": {"value": active / (t_chain * 1e-3), "ms_per_step": t_chain / steps, "launches": 1,
+                        "fraction_of_hbm_roofline": active / (t_chain * 1e-3) * B_STEP / (peaks()[0] * 1e9)},
             "one_at_a_time": {"value": active / (t_solo * 1e-3), "ms_per_step": t_solo / steps,
                               "launches_per_step": len(vens)},
             "speedup_vs_one_at_a_time": t_solo / t_batch, "tuning": tuning,
@@ -682,6 +697,31 @@ def main():
                      "value": sum(c_active) / (sum(c_ms) * 1e-3), "ms_per_step": statistics.mean(c_ms),
                      "active_per_step": statistics.mean(c_active)}
 
+    # the same steps chained in one persistent launch (a grid barrier between steps, no launch per step): the state
+    # stays L2-resident between steps here, as in a simulation run; the per-step figure above flushes L2 before each
+    chained = None
+    if rank == 0 and world == 1:
+        ch = swarm_gb300.CrowdSim(P, venue, n)
+        ch.set_stream(stream.cuda_stream)
+        ch.set_state(start_state)
+        ch.set_agent_params(r, v0)
+        with torch.cuda.stream(stream):
+            ch.step(args.warmup)
+        ch.set_state(start_state)
+        torch.cuda.synchronize()
+        c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.fill_(0)
+            c0.record(stream)
+            ch.step(args.steps)
+            c1.record(stream)
+        stream.synchronize()
+        ch.synchronize()
+        c_ms = c0.elapsed_time(c1)
+        chained = {"value": agent_steps / (c_ms * 1e-3), "ms_per_step": c_ms / args.steps, "launches": ch.launch_count(),
+                   "l2": "flushed once before the run, warm between its steps"}
+        ch.close()
+
     # e2e through swarm_step_host with pinned host buffers
     e2e_sim = swarm_gb300.CrowdSim(P, venue, n)
     e2e_sim.set_agent_params(r, v0)
@@ -722,6 +762,8 @@ def main():
         }
         if congested:
             line["details"]["congested"] = congested
+        if chained:
+            line["details"]["chained_steps"] = chained
         line["clocks"] = clk.summary()
         if not args.no_batch and world == 1:
             try:

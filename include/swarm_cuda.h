@@ -243,8 +243,11 @@ int swarm_set_graph(SwarmHandle h, int enabled);
 int swarm_set_fused(SwarmHandle h, int enabled);
 /* The launch configuration: the fused persistent kernel (fused = 1) with `threads` per block (0: the state size over
  * the SMs, rounded up to a warp, 128..512, or 128..1024 for a batch) and at most `blocks_per_sm` blocks per SM (0: as many as fit; fewer blocks
- * mean more agents per thread), or one kernel per phase (fused = 0: one Jacobi sweep per launch). */
-typedef struct SwarmTuning { int32_t fused, threads, blocks_per_sm; float ms_per_step; } SwarmTuning;
+ * mean more agents per thread), or one kernel per phase (fused = 0: one Jacobi sweep per launch). steps_per_launch
+ * (fused only): the steps of one swarm_step call that one persistent launch runs, with one more grid barrier between
+ * steps (0: all of them; 1: a launch per step); steps with the exit choice, the metrics or stage timing on take a
+ * launch each. Every configuration gives the same bits. */
+typedef struct SwarmTuning { int32_t fused, threads, blocks_per_sm; float ms_per_step; int32_t steps_per_launch; } SwarmTuning;
 int swarm_set_tuning(SwarmHandle h, const SwarmTuning* tuning);
 /* Times `steps` steps of each candidate configuration from the current state (restored after every trial and at the
  * end), keeps the fastest in force and returns it. The results of every configuration are the same bits. */

@@ -46,7 +46,7 @@ struct SwarmSim {
     unsigned long long* stamps = nullptr;
     bool fused = true;          // the whole step as one persistent kernel when the grid fits on the GPU
     int barrierExtra = 0;       // the timeout test's missing block (swarm_test_barrier_timeout)
-    SwarmTuning tuning{1, 0, 0, 0.0f};   // the launch configuration (swarm_autotune / swarm_set_tuning)
+    SwarmTuning tuning{1, 0, 0, 0.0f, 0};   // the launch configuration (swarm_autotune / swarm_set_tuning)
     bool counted = false;       // the counts hold the current state's keys (a fused step's final pass counted them)
     int countedTile = 0;        // the scan tile (cells) of the tile sums that counting left
     // swarm_step_host on the fused path with pinned buffers: the caller's input and output as the device sees them
@@ -81,6 +81,7 @@ struct SwarmSim {
     bool useGraph = false;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};        // a whole step, per state half read
     cudaGraphExec_t stageGraph[2][4] = {};                  // its four stages (timing on)
+    cudaGraphExec_t fusedGraph[2] = {nullptr, nullptr};     // one fused step from counted keys, per state half read
     bool timing = false;
     cudaEvent_t ev[6] = {};
     SwarmStageTimes times{};
@@ -117,6 +118,7 @@ struct SwarmSim {
     void dropGraphs() {
         for (auto& g : graph) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
         for (auto& row : stageGraph) for (auto& g : row) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+        for (auto& g : fusedGraph) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
     }
     // A set device error flag: clear it and the barrier words and counts a wait that gave up left behind, and report
     int deviceError(int flag);

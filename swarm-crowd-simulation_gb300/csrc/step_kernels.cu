@@ -69,19 +69,19 @@ __device__ __forceinline__ void countKey(const StepArgs& A, uint32_t i, uint32_t
 
 // calc_grid.comp (CpuCrowdSim::hash, cpu_crowd_sim.cpp:983-993), with its NaN sanitiser. All lanes of a warp together.
 template <bool kB, bool kTiles = false>
-__device__ __forceinline__ void hashItem(const StepArgs& A, int i) {
+__device__ __forceinline__ void hashItem(const StepArgs& A, int i, float4* stateIn, const float4* hostIn) {
     const bool valid = i < A.n;
     uint32_t key = 0;
     if (valid) {
         float4 p;
-        if (A.hostIn) {   // the state straight from the caller's host buffer: into the device half this step reads
-            p = A.hostIn[2 * size_t(i)];
-            A.stateIn[2 * size_t(i) + 1] = A.hostIn[2 * size_t(i) + 1];
+        if (hostIn) {   // the state straight from the caller's host buffer: into the device half this step reads
+            p = hostIn[2 * size_t(i)];
+            stateIn[2 * size_t(i) + 1] = hostIn[2 * size_t(i) + 1];
             if (isnan(p.x)) p = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
-            A.stateIn[2 * size_t(i)] = p;
+            stateIn[2 * size_t(i)] = p;
         } else {
-            p = A.stateIn[2 * size_t(i)];
-            if (isnan(p.x)) { p = make_float4(0.0f, 0.0f, 0.0f, 1.0f); A.stateIn[2 * size_t(i)] = p; }
+            p = stateIn[2 * size_t(i)];
+            if (isnan(p.x)) { p = make_float4(0.0f, 0.0f, 0.0f, 1.0f); stateIn[2 * size_t(i)] = p; }
         }
         key = p.w == 0.0f ? INACTIVE_CELL : cellID(venueOfAgent<kB>(A, uint32_t(i)), p);
     }
@@ -89,7 +89,7 @@ __device__ __forceinline__ void hashItem(const StepArgs& A, int i) {
 }
 
 template <bool kB>
-__global__ void k_hash(StepArgs A) { hashItem<kB>(A, blockIdx.x * blockDim.x + threadIdx.x); }
+__global__ void k_hash(StepArgs A) { hashItem<kB>(A, blockIdx.x * blockDim.x + threadIdx.x, A.stateIn, A.hostIn); }
 
 // The exclusive scan of the ncells + 1 counts, in tiles of SCAN_TILE: k_scan_reduce writes each tile's total,
 // k_scan_apply scans its tile on top of the totals of the tiles before it, writes the run starts and the cell table,
@@ -252,15 +252,15 @@ __device__ __forceinline__ f2 obstacleTerm(const SwarmParams& P, const Venue& ve
 
 // Venue (not void): also each slot's e_goal, for the fused step's predict window
 template <bool kPerAgent, bool kB, class Venue = void>
-__device__ __forceinline__ void rankGatherItem(const StepArgs& A, int s) {
+__device__ __forceinline__ void rankGatherItem(const StepArgs& A, int s, float4* stateIn) {
     const int nActive = int(A.start[A.V.ncells]);
     const uint32_t me = A.sidTmp[s];
     if (me >= uint32_t(A.n)) { atomicOr(A.err, ERR_BOUNDS); return; }
     if (s >= nActive) { A.sid[s] = me; A.skey[s] = INACTIVE_CELL; return; }
     // The agent's own records (and its e_goal lookup) do not depend on its rank: every load comes before the first
     // store, so these overlap the cell lookup and the rank loop instead of following them
-    float4 p = A.stateIn[2 * size_t(me)];
-    const float4 v = A.stateIn[2 * size_t(me) + 1];
+    float4 p = stateIn[2 * size_t(me)];
+    const float4 v = stateIn[2 * size_t(me) + 1];
     const uint32_t c = A.key[me];
     float2 prm = make_float2(0.0f, 0.0f);
     if (kPerAgent) prm = A.aparam[me];
@@ -282,7 +282,7 @@ __device__ __forceinline__ void rankGatherItem(const StepArgs& A, int s) {
     const uint32_t t = cs.x + r;
     A.sid[t] = me;
     A.skey[t] = c;
-    if (bad) A.stateIn[2 * size_t(me)] = p;
+    if (bad) stateIn[2 * size_t(me)] = p;
     A.pos0[t] = p;
     A.vel0[t] = v;
     if (kPerAgent) A.prm[t] = prm;
@@ -293,7 +293,7 @@ __device__ __forceinline__ void rankGatherItem(const StepArgs& A, int s) {
 template <bool kPerAgent, bool kB>
 __global__ void k_rank_gather(StepArgs A) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < A.n) rankGatherItem<kPerAgent, kB>(A, s);
+    if (s < A.n) rankGatherItem<kPerAgent, kB>(A, s, A.stateIn);
 }
 
 // ---- the physics passes ----
@@ -599,12 +599,13 @@ __global__ void __launch_bounds__(128) k_project(StepArgs A, int inBuf) {
 // The final pass of an active slot whose last sweep gave b (cpu_crowd_sim.cpp:835-866)
 // Returns the agent's cell key for the next step (INACTIVE_CELL once parked; a NaN position hashes as (0, 0, 0, 1))
 template <class Venue>
-__device__ __forceinline__ uint32_t finalActive(const StepArgs& A, const VenueArgs& V, const Venue& ven, int s, float4 b) {
+__device__ __forceinline__ uint32_t finalActive(const StepArgs& A, const VenueArgs& V, const Venue& ven, int s, float4 b,
+                                                float4* stateOut) {
     const SwarmParams& P = A.P;
     const uint32_t self = A.sid[s];
     if (b.w < 0.0f) {   // parked this step
-        A.stateOut[2 * size_t(self)] = make_float4(P.park_coord, P.park_coord, P.park_coord, 0.0f);
-        A.stateOut[2 * size_t(self) + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        stateOut[2 * size_t(self)] = make_float4(P.park_coord, P.park_coord, P.park_coord, 0.0f);
+        stateOut[2 * size_t(self) + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         A.contacts[self] = A.ctc[s];
         return INACTIVE_CELL;
     }
@@ -621,28 +622,28 @@ __device__ __forceinline__ uint32_t finalActive(const StepArgs& A, const VenueAr
     }
     if (ven.limitStepUp(pOld, np, nv, ri)) contact |= C_STEP_UP;
     const float4 out = make_float4(np.x, np.y, np.z, 1.0f);
-    A.stateOut[2 * size_t(self)] = out;
-    A.stateOut[2 * size_t(self) + 1] = make_float4(nv.x, nv.y, nv.z, length(nv));
+    stateOut[2 * size_t(self)] = out;
+    stateOut[2 * size_t(self) + 1] = make_float4(nv.x, nv.y, nv.z, length(nv));
     A.contacts[self] = uint8_t(contact);
     return cellID(V, isnan(out.x) ? make_float4(0.0f, 0.0f, 0.0f, 1.0f) : out);
 }
 
 // An agent evacuated before this step: carried over (its next key: inactive)
-__device__ __forceinline__ void finalInactive(const StepArgs& A, int s) {
+__device__ __forceinline__ void finalInactive(const StepArgs& A, int s, const float4* stateIn, float4* stateOut) {
     const uint32_t self = A.sid[s];
-    A.stateOut[2 * size_t(self)] = A.stateIn[2 * size_t(self)];
-    A.stateOut[2 * size_t(self) + 1] = A.stateIn[2 * size_t(self) + 1];
+    stateOut[2 * size_t(self)] = stateIn[2 * size_t(self)];
+    stateOut[2 * size_t(self) + 1] = stateIn[2 * size_t(self) + 1];
     A.contacts[self] = 0;
 }
 
 template <class Venue, bool kB, bool kTape = false>
 __device__ __forceinline__ void finalItem(const StepArgs& A, int s, int inBuf) {
-    if (s >= int(A.start[A.V.ncells])) { finalInactive(A, s); return; }
+    if (s >= int(A.start[A.V.ncells])) { finalInactive(A, s, A.stateIn, A.stateOut); return; }
     const VenueArgs& V = venueOfSlot<kB>(A, s);
     const Venue ven{A.P, V};
     const float4 b = A.projectInFinal ? projectSlot<Venue, kTape>(A, V, ven, A.proj[inBuf], s) : A.proj[inBuf][s];
     if constexpr (kTape) A.tapeQK[s] = b;
-    finalActive(A, V, ven, s, b);
+    finalActive(A, V, ven, s, b, A.stateOut);
 }
 
 template <class Venue, bool kB, bool kTape = false>
@@ -772,109 +773,125 @@ __global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREA
         bulkPrefetchShare(A.rank, size_t(n) * 4u);
         if (kPerAgent) bulkPrefetchShare(A.aparam, size_t(n) * 8u);
     }
-    // The scan runs in tiles of A.scanTile cells (8 counts a thread, or 16 on sparse venues). Whoever counted the
-    // keys -- the previous fused step's final pass, or the hash here -- also summed them per tile, so the scan starts
-    // at its apply phase (the tile sums were zero before that counting: cleared below, or by the host).
-    if (!A.hashed) {
-        for (int base = tid - int(threadIdx.x & 31u); base < n; base += stride)
-            hashItem<kB, true>(A, base + int(threadIdx.x & 31u));
+    // A.steps steps in this launch: the state halves swap after every step, each later step starts from the counts
+    // the previous final pass left (one more grid barrier between steps), the host buffers serve the first and the
+    // last step only
+    float4* sIn = A.stateIn;
+    float4* sOut = A.stateOut;
+    const int steps = A.steps > 1 ? A.steps : 1;
+    for (int step = 0; step < steps; ++step) {
+        const bool last = step + 1 == steps;
+        if (step > 0) {
+            float4* t = sIn;
+            sIn = sOut;
+            sOut = t;
+        }
+        // The scan runs in tiles of A.scanTile cells (8 counts a thread, or 16 on sparse venues). Whoever counted the
+        // keys -- the previous fused step's final pass, or the hash here -- also summed them per tile, so the scan starts
+        // at its apply phase (the tile sums were zero before that counting: cleared below, or by the host).
+        if (step == 0 && !A.hashed) {
+            for (int base = tid - int(threadIdx.x & 31u); base < n; base += stride)
+                hashItem<kB, true>(A, base + int(threadIdx.x & 31u), sIn, A.hostIn);
+            if (!gridBarrier(A, gridDim.x)) return;
+        }
+        const bool wide = A.scanTile > T * SCAN_ITEMS;
+        const int tiles = (A.V.ncells + 1 + A.scanTile - 1) / A.scanTile;
+        for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
+            if (wide) scanApplyTile<2 * SCAN_ITEMS>(A, t, warpSums, &prefix);
+            else scanApplyTile<SCAN_ITEMS>(A, t, warpSums, &prefix);
+        }
+        // barrierExtra: the timeout test's block that never arrives
+        if (!gridBarrier(A, gridDim.x + (step == 0 ? unsigned(A.barrierExtra) : 0u))) return;
+        for (int t = tid; t < tiles; t += stride) A.tileSums[t] = 0u;   // read by every apply tile above; summed again below
+        for (int i = tid; i < n; i += stride) scatterItem(A, i);
         if (!gridBarrier(A, gridDim.x)) return;
-    }
-    const bool wide = A.scanTile > T * SCAN_ITEMS;
-    const int tiles = (A.V.ncells + 1 + A.scanTile - 1) / A.scanTile;
-    for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
-        if (wide) scanApplyTile<2 * SCAN_ITEMS>(A, t, warpSums, &prefix);
-        else scanApplyTile<SCAN_ITEMS>(A, t, warpSums, &prefix);
-    }
-    if (!gridBarrier(A, gridDim.x + unsigned(A.barrierExtra))) return;   // barrierExtra: the timeout test's block that never arrives
-    for (int t = tid; t < tiles; t += stride) A.tileSums[t] = 0u;   // read by every apply tile above; summed again below
-    for (int i = tid; i < n; i += stride) scatterItem(A, i);
-    if (!gridBarrier(A, gridDim.x)) return;
-    for (int s = tid; s < n; s += stride) rankGatherItem<kPerAgent, kB, Venue>(A, s);
-    if (!gridBarrier(A, gridDim.x)) return;
-    stamp(A, 1);
-    const int nActive = int(A.start[A.V.ncells]);
-    // predict, tile by tile: the tile's perception window staged in shared memory (global reads when it is larger)
-    const int allTilesP = (n + T - 1) / T;
-    for (int t = blockIdx.x; t < allTilesP; t += gridDim.x) {
-        const int s = t * T + int(threadIdx.x);
-        const uint2 win = predWindow<kB>(A, t, T, nActive);
-        const bool useWin = win.y > win.x && win.y - win.x <= uint32_t(WIN_CAP);
-        if (useWin) {
-            for (uint32_t k = win.x + threadIdx.x; k < win.y; k += blockDim.x) {
-                smPos[k - win.x] = A.pos0[k];
-                smGoal[k - win.x] = A.goal[k];
-                smR[k - win.x] = kUniform ? 0.0f : A.prm[k].x;
-                smSid[k - win.x] = A.sid[k];
-            }
-        }
-        __syncthreads();
-        if (s < n) {
-            if (useWin) predictCore<Venue, kB, kTape>(A, s, PredWindow{smPos, smR, smSid, smGoal, A.P, win.x});
-            else predictCore<Venue, kB, kTape>(A, s, PredGlobal{A});
-            if (s < nActive) prepareSweepItem<kB>(A, s);
-        }
-        __syncthreads();   // the window is reused by the next tile
-    }
-    if (!gridBarrier(A, gridDim.x)) return;
-    stamp(A, 2);
-    const int K = A.P.proj_iterations;
-    int in = 0;
-    for (int it = 1; it < K; ++it) {
-        const float4* src = kTape ? A.proj[0] + size_t(it - 1) * size_t(n) : A.proj[in];
-        float4* dst = kTape ? A.proj[0] + size_t(it) * size_t(n) : A.proj[in ^ 1];
-        float4* corr = kTape ? A.tapeCorr + size_t(it - 1) * size_t(n) : nullptr;
-        // The sweeps read their neighbours straight from L2 (and L1, which catches a block's reuse): staging a
-        // tile window in shared memory and its two block barriers cost more than they save
-        for (int s = tid; s < nActive; s += stride) {
-            float4 b = src[s];
-            if (b.w >= 0.0f) {
-                const uint4 ra = A.rowsA[s];
-                const uint2 rb = A.rowsB[s];
-                const uint32_t rk0[3] = {ra.x, ra.z, rb.x}, rk1[3] = {ra.y, ra.w, rb.y};
-                const float ri = kUniform ? A.P.body_radius : A.prm[s].x;
-                const Venue ven{A.P, venueOfSlot<kB>(A, s)};
-                b = projectCore<Venue, GlobalNbr, kTape>(A, ven, b, s, ri, rk0, rk1, A.plane[s], GlobalNbr{src, A.prm},
-                                                         kTape ? corr + s : nullptr);
-            }
-            dst[s] = b;
-        }
-        in ^= 1;
+        for (int s = tid; s < n; s += stride) rankGatherItem<kPerAgent, kB, Venue>(A, s, sIn);
         if (!gridBarrier(A, gridDim.x)) return;
-    }
-    stamp(A, 3);
-    // The final pass reads its neighbours from L2 too (warp-aligned slots: the next step's count is warp-collective)
-    {
-        const float4* src = kTape ? A.proj[0] + size_t(K > 0 ? K - 1 : 0) * size_t(n) : A.proj[in];
-        for (int base = tid - int(threadIdx.x & 31u); base < n; base += stride) {
-            const int s = base + int(threadIdx.x & 31u);
-            const bool own = s < nActive;
-            float4 b = own ? src[s] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            uint32_t nextKey = INACTIVE_CELL;
-            if (own) {
-                const VenueArgs& V = venueOfSlot<kB>(A, s);
-                const Venue ven{A.P, V};
-                if (A.projectInFinal && b.w >= 0.0f) {
+        stamp(A, 1);
+        const int nActive = int(A.start[A.V.ncells]);
+        // predict, tile by tile: the tile's perception window staged in shared memory (global reads when it is larger)
+        const int allTilesP = (n + T - 1) / T;
+        for (int t = blockIdx.x; t < allTilesP; t += gridDim.x) {
+            const int s = t * T + int(threadIdx.x);
+            const uint2 win = predWindow<kB>(A, t, T, nActive);
+            const bool useWin = win.y > win.x && win.y - win.x <= uint32_t(WIN_CAP);
+            if (useWin) {
+                for (uint32_t k = win.x + threadIdx.x; k < win.y; k += blockDim.x) {
+                    smPos[k - win.x] = A.pos0[k];
+                    smGoal[k - win.x] = A.goal[k];
+                    smR[k - win.x] = kUniform ? 0.0f : A.prm[k].x;
+                    smSid[k - win.x] = A.sid[k];
+                }
+            }
+            __syncthreads();
+            if (s < n) {
+                if (useWin) predictCore<Venue, kB, kTape>(A, s, PredWindow{smPos, smR, smSid, smGoal, A.P, win.x});
+                else predictCore<Venue, kB, kTape>(A, s, PredGlobal{A});
+                if (s < nActive) prepareSweepItem<kB>(A, s);
+            }
+            __syncthreads();   // the window is reused by the next tile
+        }
+        if (!gridBarrier(A, gridDim.x)) return;
+        stamp(A, 2);
+        const int K = A.P.proj_iterations;
+        int in = 0;
+        for (int it = 1; it < K; ++it) {
+            const float4* src = kTape ? A.proj[0] + size_t(it - 1) * size_t(n) : A.proj[in];
+            float4* dst = kTape ? A.proj[0] + size_t(it) * size_t(n) : A.proj[in ^ 1];
+            float4* corr = kTape ? A.tapeCorr + size_t(it - 1) * size_t(n) : nullptr;
+            // The sweeps read their neighbours straight from L2 (and L1, which catches a block's reuse): staging a
+            // tile window in shared memory and its two block barriers cost more than they save
+            for (int s = tid; s < nActive; s += stride) {
+                float4 b = src[s];
+                if (b.w >= 0.0f) {
                     const uint4 ra = A.rowsA[s];
                     const uint2 rb = A.rowsB[s];
                     const uint32_t rk0[3] = {ra.x, ra.z, rb.x}, rk1[3] = {ra.y, ra.w, rb.y};
                     const float ri = kUniform ? A.P.body_radius : A.prm[s].x;
+                    const Venue ven{A.P, venueOfSlot<kB>(A, s)};
                     b = projectCore<Venue, GlobalNbr, kTape>(A, ven, b, s, ri, rk0, rk1, A.plane[s], GlobalNbr{src, A.prm},
-                                                             kTape && K > 0 ? A.tapeCorr + size_t(K - 1) * size_t(n) + s : nullptr);
+                                                             kTape ? corr + s : nullptr);
                 }
-                if (kTape) A.tapeQK[s] = b;
-                nextKey = finalActive(A, V, ven, s, b);
-            } else if (s < n) {
-                finalInactive(A, s);
+                dst[s] = b;
             }
-            if (A.hashNext) countKey<true>(A, s < n ? A.sid[s] : 0u, nextKey, s < n);
+            in ^= 1;
+            if (!gridBarrier(A, gridDim.x)) return;
         }
+        stamp(A, 3);
+        // The final pass reads its neighbours from L2 too (warp-aligned slots: the next step's count is warp-collective)
+        {
+            const float4* src = kTape ? A.proj[0] + size_t(K > 0 ? K - 1 : 0) * size_t(n) : A.proj[in];
+            for (int base = tid - int(threadIdx.x & 31u); base < n; base += stride) {
+                const int s = base + int(threadIdx.x & 31u);
+                const bool own = s < nActive;
+                float4 b = own ? src[s] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                uint32_t nextKey = INACTIVE_CELL;
+                if (own) {
+                    const VenueArgs& V = venueOfSlot<kB>(A, s);
+                    const Venue ven{A.P, V};
+                    if (A.projectInFinal && b.w >= 0.0f) {
+                        const uint4 ra = A.rowsA[s];
+                        const uint2 rb = A.rowsB[s];
+                        const uint32_t rk0[3] = {ra.x, ra.z, rb.x}, rk1[3] = {ra.y, ra.w, rb.y};
+                        const float ri = kUniform ? A.P.body_radius : A.prm[s].x;
+                        b = projectCore<Venue, GlobalNbr, kTape>(A, ven, b, s, ri, rk0, rk1, A.plane[s], GlobalNbr{src, A.prm},
+                                                                 kTape && K > 0 ? A.tapeCorr + size_t(K - 1) * size_t(n) + s : nullptr);
+                    }
+                    if (kTape) A.tapeQK[s] = b;
+                    nextKey = finalActive(A, V, ven, s, b, sOut);
+                } else if (s < n) {
+                    finalInactive(A, s, sIn, sOut);
+                }
+                if (!last || A.hashNext) countKey<true>(A, s < n ? A.sid[s] : 0u, nextKey, s < n);
+            }
+        }
+        if (!last && !gridBarrier(A, gridDim.x)) return;   // the next step reads these counts and this state
     }
     // The caller's host buffer: the finished state in agent order, copied in order after the last barrier (coalesced
     // 16-byte stores over the host link; the final pass's own writes go to agents in slot order, scattered)
     if (A.hostOut) {
         if (!gridBarrier(A, gridDim.x)) return;
-        for (size_t k = size_t(tid); k < 2 * size_t(n); k += size_t(stride)) A.hostOut[k] = A.stateOut[k];
+        for (size_t k = size_t(tid); k < 2 * size_t(n); k += size_t(stride)) A.hostOut[k] = sOut[k];
     }
     if (A.stamps) {   // the end: the last block out records it
         __syncthreads();

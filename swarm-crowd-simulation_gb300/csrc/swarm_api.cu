@@ -478,7 +478,7 @@ int swarm_metrics_read(SwarmHandle h, SwarmMetricCounters* counters, SwarmMetric
 static int stepImpl(SwarmHandle h, int steps, bool countLast = true);
 
 int swarm_set_tuning(SwarmHandle h, const SwarmTuning* t) {
-    if (!h || !t || t->threads < 0 || t->blocks_per_sm < 0) return SWARM_E_INVALID;
+    if (!h || !t || t->threads < 0 || t->blocks_per_sm < 0 || t->steps_per_launch < 0) return SWARM_E_INVALID;
     if (t->threads > (h->instances ? 1024 : 512))
         return h->fail(SWARM_E_INVALID, "threads above " + std::to_string(h->instances ? 1024 : 512) + " per block");
     h->tuning = *t;
@@ -494,9 +494,10 @@ int swarm_autotune(SwarmHandle h, int steps, SwarmTuning* best) {
     std::vector<SwarmTuning> cands;
     for (int threads : {0, 128, 256, 512, 768, 1024}) {
         if (threads > 512 && !h->instances) continue;   // wider blocks: the batched kernel only
-        for (int bps : {0, 1, 2}) cands.push_back(SwarmTuning{1, threads, bps, 0.0f});
+        for (int bps : {0, 1, 2}) cands.push_back(SwarmTuning{1, threads, bps, 0.0f, 0});
     }
-    cands.push_back(SwarmTuning{0, 0, 0, 0.0f});
+    cands.push_back(SwarmTuning{1, 0, 0, 0.0f, 1});   // a launch per step
+    cands.push_back(SwarmTuning{0, 0, 0, 0.0f, 0});
     // snapshot of the state (and the metrics' running sums are not touched: the trials run with metrics off)
     float4* snap = nullptr;
     const size_t bytes = size_t(h->n) * 32;
@@ -560,6 +561,7 @@ int swarm_test_barrier_timeout(SwarmHandle h) {
 int swarm_set_fused(SwarmHandle h, int enabled) {
     if (!h) return SWARM_E_INVALID;
     h->fused = enabled != 0;
+    h->dropGraphs();
     return SWARM_OK;
 }
 
@@ -577,8 +579,13 @@ int swarm_set_timing(SwarmHandle h, int enabled) {
 static int stepImpl(SwarmHandle h, int steps, bool countLast) {
     h->launches = 0;
     const int perStep = 7 + std::max(h->P.proj_iterations - 1, 0);
-    for (int s = 0; s < steps; ++s) {
+    // steps one fused launch may run: all of them (or the tuning's steps_per_launch), unless something runs between
+    // steps on the host's side (the exit choice's pass, the metrics) or each step is timed
+    const bool chain = h->fused && !h->choiceExits && !h->metricRes && !h->timing;
+    const int chunkMax = !chain ? 1 : (h->tuning.steps_per_launch > 0 ? h->tuning.steps_per_launch : std::max(steps, 1));
+    for (int s = 0; s < steps;) {
         const int in = h->readIdx;
+        const int chunk = h->fused ? std::min(chunkMax, steps - s) : 1;
         if (h->choiceExits && h->enqueueChoice(in) != SWARM_OK) return SWARM_E_CUDA;
         if (h->fused) {
             if (h->timing && !cudaOk(h, cudaEventRecord(h->ev[0], h->stream), "event")) return SWARM_E_CUDA;
@@ -589,11 +596,30 @@ static int stepImpl(SwarmHandle h, int steps, bool countLast) {
             if (!h->counted && !cudaOk(h, cudaMemsetAsync(h->tileSums, 0, (size_t(h->ncells) / 1024 + 2) * 4, h->stream), "tile sums"))
                 return SWARM_E_CUDA;
             A.hashed = h->counted ? 1 : 0;
-            A.hashNext = (countLast || s + 1 < steps) ? 1 : 0;
+            A.hashNext = (countLast || s + chunk < steps) ? 1 : 0;
+            A.steps = chunk;
             A.hostIn = s == 0 ? h->hostIn : nullptr;
-            A.hostOut = s + 1 == steps ? h->hostOut : nullptr;
+            A.hostOut = s + chunk == steps ? h->hostOut : nullptr;
             if (A.hostIn && A.hashed) return h->fail(SWARM_E_STATE, "a host input needs the hash phase (counts left over)");
-            if (!cudaOk(h, swarm_gpu::launch_step_fused(A, h->stream), "fused step launch")) return SWARM_E_CUDA;
+            // one step from counted keys, with counting, no host buffers and nothing timed: replayed from a graph
+            // (one per state half) when graphs are on
+            const bool steady = h->useGraph && !h->timing && chunk == 1 && A.hashed && A.hashNext && !A.hostIn &&
+                                !A.hostOut && !A.barrierExtra;
+            if (steady && !h->fusedGraph[in]) {
+                cudaGraph_t g = nullptr;
+                if (!cudaOk(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "capture")) return SWARM_E_CUDA;
+                const cudaError_t le = swarm_gpu::launch_step_fused(A, h->stream);
+                const cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
+                if (!cudaOk(h, le, "fused step capture") || !cudaOk(h, ce, "capture end")) { if (g) cudaGraphDestroy(g); return SWARM_E_CUDA; }
+                const bool inst = cudaOk(h, cudaGraphInstantiate(&h->fusedGraph[in], g, 0), "graph instantiate");
+                cudaGraphDestroy(g);
+                if (!inst) return SWARM_E_CUDA;
+            }
+            if (steady) {
+                if (!cudaOk(h, cudaGraphLaunch(h->fusedGraph[in], h->stream), "graph launch")) return SWARM_E_CUDA;
+            } else if (!cudaOk(h, swarm_gpu::launch_step_fused(A, h->stream), "fused step launch")) {
+                return SWARM_E_CUDA;
+            }
             h->barrierExtra = 0;
             h->counted = A.hashNext != 0;
             h->countedTile = tile;
@@ -621,7 +647,8 @@ static int stepImpl(SwarmHandle h, int steps, bool countLast) {
             if (h->useGraph) h->launches += perStep;
         }
         if (h->metricRes && h->enqueueMetrics(in) != SWARM_OK) return SWARM_E_CUDA;
-        h->readIdx ^= 1;
+        h->readIdx ^= chunk & 1;
+        s += chunk;
     }
     h->timesValid = false;
     return SWARM_OK;

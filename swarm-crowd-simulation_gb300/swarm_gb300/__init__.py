@@ -346,8 +346,8 @@ class CrowdSim:
         """One persistent kernel per step (True, the default) or one kernel per phase (False)."""
         self._ck(lib().swarm_set_fused(self._h, int(bool(enabled))), "set_fused")
 
-    def set_tuning(self, fused=True, threads=0, blocks_per_sm=0):
-        t = SwarmTuning(int(bool(fused)), int(threads), int(blocks_per_sm), 0.0)
+    def set_tuning(self, fused=True, threads=0, blocks_per_sm=0, steps_per_launch=0):
+        t = SwarmTuning(int(bool(fused)), int(threads), int(blocks_per_sm), 0.0, int(steps_per_launch))
         self._ck(lib().swarm_set_tuning(self._h, C.byref(t)), "set_tuning")
 
     def autotune(self, steps=3):
@@ -355,7 +355,7 @@ class CrowdSim:
         t = SwarmTuning()
         self._ck(lib().swarm_autotune(self._h, int(steps), C.byref(t)), "autotune")
         return {"fused": bool(t.fused), "threads": t.threads, "blocks_per_sm": t.blocks_per_sm,
-                "ms_per_step": t.ms_per_step}
+                "ms_per_step": t.ms_per_step, "steps_per_launch": t.steps_per_launch}
 
     def download_device(self, dst_ptr):
         """The state into device memory at dst_ptr (n x 8 floats)."""

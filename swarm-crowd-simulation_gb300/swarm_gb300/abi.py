@@ -150,4 +150,5 @@ METRIC_CELL_WORDS = 16   # SwarmMetricCell: 16 uint32 (last_mass, last_speed_mas
 
 
 class SwarmTuning(C.Structure):
-    _fields_ = [("fused", C.c_int32), ("threads", C.c_int32), ("blocks_per_sm", C.c_int32), ("ms_per_step", C.c_float)]
+    _fields_ = [("fused", C.c_int32), ("threads", C.c_int32), ("blocks_per_sm", C.c_int32), ("ms_per_step", C.c_float),
+                ("steps_per_launch", C.c_int32)]

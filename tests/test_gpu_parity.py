@@ -358,3 +358,39 @@ def test_evacuation_runner_stops_at_max_steps(terrace, terrace_golden):
     assert stats["steps"] == 300 and active.shape == (300,)
     assert np.array_equal(active, ref["active"][:300])
     assert stats["remaining"] == int(ref["active"][299]) and stats["t100_step"] == -1
+
+
+def test_chained_steps_and_fused_graphs_are_bit_identical(built):
+    """Several steps in one persistent launch (a grid barrier between steps), a bounded number of steps per launch, the
+    fused step replayed from a CUDA graph, and a chained call on pinned host buffers: the bits of one launch per step."""
+    import torch
+    import swarm_gb300
+    from swarm_gb300 import venues
+    venue, (boids, r, v0) = venues.terrace_c0()
+    P = swarm_gb300.params_si()
+    ref = _sim(P, venue, boids, r, v0)
+    ref.set_tuning(True, 0, 0, 1)
+    for _ in range(12):
+        ref.step(1)
+    want = _bits(ref.state())
+    one = _sim(P, venue, boids, r, v0)
+    one.step(12)
+    assert one.launch_count() == 1, "twelve steps in one launch"
+    assert np.array_equal(_bits(one.state()), want)
+    assert np.array_equal(one.cells(), ref.cells()) and np.array_equal(one.contacts(), ref.contacts())
+    chunked = _sim(P, venue, boids, r, v0)
+    chunked.set_tuning(True, 0, 0, 5)
+    chunked.step(12)
+    assert chunked.launch_count() == 3
+    assert np.array_equal(_bits(chunked.state()), want)
+    graphed = _sim(P, venue, boids, r, v0)
+    graphed.set_graph(True)
+    for _ in range(12):
+        graphed.step(1)
+    assert np.array_equal(_bits(graphed.state()), want)
+    host = swarm_gb300.CrowdSim(P, venue, boids.shape[0])
+    host.set_agent_params(r, v0)
+    buf = torch.from_numpy(boids.copy()).pin_memory()
+    host.step_host(buf.data_ptr(), buf.data_ptr(), boids.shape[0], 5)
+    host.step_host(buf.data_ptr(), buf.data_ptr(), boids.shape[0], 7)
+    assert np.array_equal(_bits(buf.numpy()), want)
