@@ -201,7 +201,7 @@ def bench_batched(P, steps=10, warmup=3):
             "fraction_of_hbm_roofline": active / (t_batch * 1e-3) * B_STEP / (peaks()[0] * 1e9)}
 
 
-def bench_bowl(P, steps=50, warmup=5, cap=20000, chunk=100):
+def bench_bowl(P, steps=50, warmup=5, cap=20000, chunk=100, evacuation=True):
     """The seated bowl (32 sectors x 32 rows x 62 seats = 63 488 agents; stairs, vomitories, perimeter exits): the
     plain step timed as the main workload (CUDA events per step on the handle's stream, the L2 flushed by a 256 MiB
     write before each), then the evacuation run from the seats (checked every `chunk` steps): the steps until 99.9 %
@@ -234,6 +234,10 @@ def bench_bowl(P, steps=50, warmup=5, cap=20000, chunk=100):
         stream.synchronize()
         total_ms += e0.elapsed_time(e1)
     value = active / (total_ms * 1e-3)
+    if not evacuation:   # the timed steps alone (a profiling run)
+        sim.close()
+        return {"value": value, "unit": UNIT, "ms_per_step": total_ms / steps, "steps": steps, "warmup": warmup,
+                "fraction_of_hbm_roofline": value * B_STEP / (peaks()[0] * 1e9)}
     # the evacuation from the seats, through the headless runner (active counts kept on the device every step)
     sim.set_state(boids)
     t0 = time.perf_counter()
@@ -558,7 +562,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
     ap.add_argument("--no-bowl", action="store_true", help="skip the seated-bowl measurement")
     ap.add_argument("--adjoint-steps", type=int, default=400, help="steps of the adjoint measurement (400: the workload)")
-    ap.add_argument("--only", choices=["adjoint", "bowl", "batched", "navfield", "venue_l"], default=None,
+    ap.add_argument("--only", choices=["adjoint", "bowl", "bowl_step", "batched", "navfield", "venue_l"], default=None,
                     help="run only this sub-measurement and print its object (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -572,7 +576,8 @@ def main():
         P = swarm_gb300.params_si()
         fn = {"adjoint": lambda: bench_adjoint(P, steps=args.adjoint_steps), "bowl": lambda: bench_bowl(P),
               "batched": lambda: bench_batched(P),
-              "navfield": lambda: bench_nav_field(bowl_venue()), "venue_l": lambda: bench_venue_l()}[args.only]
+              "navfield": lambda: bench_nav_field(bowl_venue()), "venue_l": lambda: bench_venue_l(),
+              "bowl_step": lambda: bench_bowl(P, steps=10, evacuation=False)}[args.only]
         print(json.dumps({args.only: fn()}))
         return 0
 
