@@ -250,13 +250,19 @@ extern "C" int swarm_adjoint_run(SwarmHandle h, const SwarmLossSpec* loss, int s
             }
             continue;
         }
+        if (h->fused) {   // the segment's C untaped steps in one persistent launch (a grid barrier between steps)
+            if (!good) break;
+            StepArgs A = forwardArgs(h, a, in, 0);
+            chain(A, false);
+            A.steps = C;
+            good = ok(h, swarm_gpu::launch_step_fused(A, st), "adjoint forward");
+            launches += 1;
+            in ^= C & 1;
+            continue;
+        }
         for (int j = 0; good && j < C; ++j) {
             StepArgs A = forwardArgs(h, a, in, 0);
-            if (h->fused) {
-                chain(A, false);
-                good = ok(h, swarm_gpu::launch_step_fused(A, st), "adjoint forward");
-                launches += 1;
-            } else {
+            {
                 for (int s2 = 0; s2 < 4; ++s2) swarm_gpu::launch_stage(A, s2, st, &launches);
                 good = ok(h, cudaGetLastError(), "adjoint forward");
             }
