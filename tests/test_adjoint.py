@@ -6,7 +6,8 @@ directional derivative <grad, u> from the adjoint must match the dual's along u 
 direction's scale (the FP32 accumulation of the reverse pass is the only difference). The loss must match the
 oracle's to 1e-9 relative (both sum D in double, in different orders). Gradients do not depend on the checkpoint
 interval and repeat bit for bit. Against FP64 central differences (eps 1e-4): every single-agent parameter whose
-perturbed runs keep the branch set of the FP32 run agrees to 1e-3 relative.
+perturbed runs keep the branch set of the FP32 run agrees to 1e-3 relative; on the 16 384-agent C4 hall, every
+front agent whose perturbed runs keep their branches, save one whose FP32 and FP64 trajectories are shown to part.
 
 Every call goes through the C ABI (swarm_gb300 is a ctypes layer over include/swarm_cuda.h)."""
 import numpy as np
@@ -205,27 +206,67 @@ def test_adjoint_c4_400_steps_matches_dual(hall_c4):
     assert err.max() <= GRAD_RTOL, f"{got} vs {dl}: {err}"
 
 
-def test_adjoint_c4_vs_fp64_central_differences(hall_c4):
-    """FP64 central differences (eps 1e-4) on the desired speed of the 16 agents at the crowd's front (the lattice
-    columns nearest the exits, walking freely; inside the lattice the headway clamp makes dL/dv0 exactly 0) over the
-    hall's first 40 steps. Where the +-eps FP64 runs keep the FP64 run's branches, the FP32 adjoint agrees with FD to
-    1e-3 for most agents and to 5e-3 for all: over 16 384 agents the FP32 and FP64 trajectories part at a few near-tie
-    decisions, so the FP32 gradient differs from the FP64 one by up to ~1e-3 (FD matches the FP64 dual to 1e-6)."""
-    P, venue, b, r, v0 = hall_c4
-    n, steps, eps = b.shape[0], 40, 1e-4
-    _, (L, gv, gr, gt) = _gpu(P, venue, b, r, v0, steps, 20)
+def _c4_front_fd(P, venue, b, r, v0, steps, eps=1e-4):
+    """FP64 central differences on the desired speed of the 16 agents at the crowd's front (the lattice columns
+    nearest the exits, walking freely; inside the lattice the headway clamp makes dL/dv0 exactly 0), with the FP64
+    dual along the same 16 directions. Returns (agents, kept: the +-eps FP64 runs took the FP64 run's branches, fd,
+    the FP64 dual)."""
+    n = b.shape[0]
     _, _, sig64, _ = O.grad_eval(64, P, venue.struct, b, r, v0, P.tau_relax, steps)
     front = np.argsort(-np.abs(b[:, 0]) + 0.2 * np.abs(b[:, 1]))[:16]
-    errs = []
-    for i in front:
+    d64 = np.zeros(16)
+    for c in range(0, 16, 8):
+        dv = np.zeros((8, n))
+        dv[np.arange(8), front[c:c + 8]] = 1.0
+        _, dl, _, _ = O.grad_eval(64, P, venue.struct, b, r, v0, P.tau_relax, steps, dirs=(np.zeros((8, n)), dv, np.zeros(8)))
+        d64[c:c + 8] = dl
+    kept, fd = np.zeros(16, bool), np.zeros(16)
+    for k, i in enumerate(front):
         d = np.zeros(n)
         d[i] = eps
         Lp, _, sp, _ = O.grad_eval(64, P, venue.struct, b, r, v0 + d, P.tau_relax, steps)
         Lm, _, sm, _ = O.grad_eval(64, P, venue.struct, b, r, v0 - d, P.tau_relax, steps)
-        if not (sp == sig64 and sm == sig64):
-            continue
-        fd = (Lp - Lm) / (2 * eps)
-        errs.append(abs(float(gv[i]) - fd) / abs(fd))
-    errs = np.array(errs)
-    assert len(errs) >= 12, f"only {len(errs)} of 16 kept their branches"
-    assert errs.max() <= 5e-3 and (errs <= GRAD_RTOL).mean() >= 0.75, errs
+        kept[k] = sp == sig64 and sm == sig64
+        fd[k] = (Lp - Lm) / (2 * eps)
+    return front, kept, fd, d64
+
+
+def test_adjoint_c4_vs_fp64_central_differences_20_steps(hall_c4):
+    """The C4 hall (16 384 agents), 20 steps: every front agent whose +-eps FP64 runs keep their branches agrees with
+    FP64 central differences (eps 1e-4) to GRAD_RTOL (measured: 2.7e-5 at most)."""
+    P, venue, b, r, v0 = hall_c4
+    steps = 20
+    _, (L, gv, gr, gt) = _gpu(P, venue, b, r, v0, steps, 20)
+    front, kept, fd, _ = _c4_front_fd(P, venue, b, r, v0, steps)
+    assert kept.sum() >= 12, f"only {kept.sum()} of 16 kept their branches"
+    err = np.abs(gv[front].astype(np.float64) - fd) / np.abs(fd)
+    assert err[kept].max() <= GRAD_RTOL, list(zip(front[kept], err[kept]))
+
+
+def test_adjoint_c4_vs_fp64_central_differences(hall_c4):
+    """The C4 hall, 40 steps: every front agent whose +-eps FP64 runs keep their branches agrees with FP64 central
+    differences (eps 1e-4) to GRAD_RTOL, except where the FP32 trajectory has parted from the FP64 one. Such an agent
+    is excluded only with the proof of both halves: the FP64 dual matches FD to 1e-5 (FD is the FP64 program's
+    derivative) and the adjoint matches the FP32 dual to GRAD_RTOL (it is the FP32 program's derivative), while the
+    two duals differ by more than GRAD_RTOL (over 16 384 agents the FP32 and FP64 runs part at a few near-tie
+    decisions). Measured: one of the 14 kept agents (1.3e-3), the rest within 8.4e-5."""
+    P, venue, b, r, v0 = hall_c4
+    n, steps = b.shape[0], 40
+    _, (L, gv, gr, gt) = _gpu(P, venue, b, r, v0, steps, 20)
+    front, kept, fd, d64 = _c4_front_fd(P, venue, b, r, v0, steps)
+    assert kept.sum() >= 12, f"only {kept.sum()} of 16 kept their branches"
+    g = gv[front].astype(np.float64)
+    err = np.abs(g - fd) / np.abs(fd)
+    over = kept & (err > GRAD_RTOL)
+    if over.any():
+        idx = np.flatnonzero(over)
+        dv = np.zeros((len(idx), n))
+        dv[np.arange(len(idx)), front[idx]] = 1.0
+        _, d32, _, _ = O.grad_eval(32, P, venue.struct, b, r, v0, P.tau_relax, steps,
+                                   dirs=(np.zeros_like(dv), dv, np.zeros(len(idx))))
+        for j, k in enumerate(idx):
+            why = (front[k], g[k], fd[k], d64[k], d32[j])
+            assert abs(d64[k] - fd[k]) <= 1e-5 * abs(fd[k]), why
+            assert abs(g[k] - d32[j]) <= GRAD_RTOL * abs(d32[j]), why
+            assert abs(d32[j] - d64[k]) > GRAD_RTOL * abs(d64[k]), why
+    assert over.sum() <= 2, list(zip(front[over], err[over]))
