@@ -383,6 +383,37 @@ int swarm_set_exit_choice(SwarmHandle h, const SwarmExitChoiceSpec* spec);
  * evaluations, eligible agents, switches, forced choices (4 values; either pointer may be NULL). */
 int swarm_get_exit_choice(SwarmHandle h, uint32_t* assigned, int n, uint32_t* counters);
 
+/* The seated venues' queue-aware exit choice on the reference's own candidate table (nav::ChoiceTable,
+ * include/swarm/exit_choice.hpp:146-168, as nav::choiceForVenue builds or caches it, src/exit_choice.cpp:445-474; the
+ * choice pass nav::choiceStep :683-790, e_goal nav::choiceGoal :568-578 = physics.comp navChoiceGoal). The table lives
+ * on the navigation field's grid: per cell an index word (SWARM_CHOICE_INDEX_FIT: the cell's class; the low bits: its
+ * entry + 1, 0 without candidates) and, per entry, the reference's GpuNavChoiceCell: 24 slots (anchor cell index bits
+ * 0-24, exit id bits 25-30 (63: empty), the class bit 31) and the candidates' walking distances in 16-bit quanta (two
+ * a word; 0xFFFF: empty). The stages are those of swarm_set_exit_choice on the table's numbers: E = q x quantum x
+ * seconds_per_unit + A x inv_cap_s[e], the queue ahead's bins q >> 6. */
+#define SWARM_CHOICE_INDEX_FIT 0x80000000u
+#define SWARM_CHOICE_INDEX_MASK 0x7FFFFFFFu
+typedef struct SwarmNavChoiceCell {
+    uint32_t slot[24];
+    uint32_t dist[12];
+} SwarmNavChoiceCell;
+typedef struct SwarmSeatedChoiceSpec {
+    int32_t n_exits;              /* 1 .. SWARM_CHOICE_MAX_EXITS (the table's exit count) */
+    int32_t grid_res;             /* the table's grid: the venue's navigation grid (SwarmVenue::nav_res) */
+    const uint32_t* index;        /* grid_res^2 index words, x fastest */
+    const SwarmNavChoiceCell* entries;
+    int64_t n_entries;
+    const float* inv_cap_s;       /* n_exits: seconds per queued agent, 60 / (w J) (nav::setChoiceCapacities) */
+    float seconds_per_unit;       /* seconds of walking per model unit (CHOICE_S_PER_UNIT) */
+    float dist_quantum;           /* the distances' quantum, model units (2^-12) */
+    int32_t choice_steps;         /* steps between evaluations (the reference's CHOICE_STEPS: 17 at its DT) */
+} SwarmSeatedChoiceSpec;
+/* Queue-aware exit choice on a seated venue (spec) or off (NULL). The table is checked (sizes, every index word's
+ * entry within n_entries, every slot's exit < n_exits or empty, every anchor inside the grid) and copied to the
+ * device; the choice restarts (no exit assigned, step 0) here and at every state upload. swarm_get_exit_choice reads
+ * its assignments and counters. */
+int swarm_set_seated_choice(SwarmHandle h, const SwarmSeatedChoiceSpec* spec);
+
 /* One agent per seat (sectors x rows x seats, by sector, row, seat) at the seat centre jittered U(-jitter, jitter)
  * per axis, on the floor (z = floor + radius), at rest; radius and desired speed as swarm_spawn_lattice. */
 int swarm_spawn_bowl(const SwarmBowlSpec* spec, float jitter, uint64_t seed, float r_lo, float r_hi, float v_mean,
@@ -476,6 +507,15 @@ int swarm_sdf_read(const char* path, float* sdf, int res);
  * and 1 / cell only); else capacity >= res^2. */
 int swarm_nav_cache_read(const char* path, uint64_t expected_key, SwarmNavCell* cells, int64_t capacity, int32_t* res,
                          float* origin, float* cell, float* inv_cell);
+/* A seated venue's exit-choice cache file as the reference writes it (nav::saveChoice / nav::loadChoice,
+ * src/exit_choice.cpp:358-427; nav::choiceCacheFile :344-348): magic "SWCHOI01", version 6, 24 candidates, the grid,
+ * the key, the index and entries, each exit's clear width and name, the FNV-1a checksum of everything after the magic.
+ * expected_key: the venue's nav::choiceCacheKey, or 0 to accept any. With index and entries NULL: a size query (res,
+ * n_entries, exits). Else index_capacity >= res^2 and entry_capacity >= n_entries; width_m (n_exits doubles, may be
+ * NULL) receives the clear widths, from which nav::setChoiceCapacities derives inv_cap_s = 60 / (w x 83.6). */
+int swarm_choice_cache_read(const char* path, uint64_t expected_key, uint32_t* index, int64_t index_capacity,
+                            SwarmNavChoiceCell* entries, int64_t entry_capacity, double* width_m, int32_t* res,
+                            float* origin, float* cell, float* inv_cell, int32_t* n_exits, int64_t* n_entries);
 
 /* ---- the adjoint: gradients of an evacuation loss ----
  * No counterpart in the reference, which has no differentiation. The loss of `steps` steps from the handle's state:

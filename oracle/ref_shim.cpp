@@ -171,6 +171,47 @@ int ref_nav_table(const char* venue, SwarmNavCell* out, int capacity, float* ori
     } catch (const std::exception& e) { g_err = e.what(); return -1; }
 }
 
+// The queue-aware exit choice's candidate table of a seated venue (nav::choiceForVenue, src/exit_choice.cpp:445-474;
+// built, or read from the cache directory SWARM_NAV_CACHE): per grid cell its index word into index_out (cells words,
+// when non-null), the entries (GpuNavChoiceCell: 24 slot words, 12 distance words) into entries_out (when non-null,
+// at most max_entries), meta = {exitCount, secondsPerUnit, distQuantum, invCapS[0 .. exitCount)}. Returns the entry
+// count; *grid_res: the table grid's cells per axis.
+long long ref_choice_table(const char* venue, uint32_t* index_out, long long cells, uint32_t* entries_out, long long max_entries,
+                           float* meta, int* grid_res) {
+    try {
+        const swarm::Venue& v = swarm::venueByName(venue);
+        const swarm::nav::ChoiceTable& t = swarm::nav::choiceForVenue(v);
+        *grid_res = t.grid.res;
+        meta[0] = float(t.exitCount);
+        meta[1] = t.secondsPerUnit;
+        meta[2] = t.distQuantum;
+        for (int e = 0; e < t.exitCount; ++e) meta[3 + e] = t.invCapS[size_t(e)];
+        if (index_out) {
+            if (cells < (long long)t.index.size()) { g_err = "index capacity"; return -1; }
+            std::memcpy(index_out, t.index.data(), t.index.size() * 4);
+        }
+        if (entries_out) {
+            if (max_entries < (long long)t.entries.size()) { g_err = "entry capacity"; return -1; }
+            std::memcpy(entries_out, t.entries.data(), t.entries.size() * sizeof(swarm::GpuNavChoiceCell));
+        }
+        return (long long)t.entries.size();
+    } catch (const std::exception& e) { g_err = e.what(); return -1; }
+}
+
+// The exit choice's state of a queue-aware CpuCrowdSim (cpu_crowd_sim.hpp:97-103): each agent's assigned exit,
+// GpuChoiceCounters (132 words) and the choice step
+int ref_choice_state(void* h, uint32_t* assign, int n, uint32_t* counters, uint32_t* step) {
+    try {
+        const swarm::CpuCrowdSim& s = static_cast<RefSim*>(h)->sim;
+        const std::vector<uint32_t>& a = s.assignedExits();
+        if (n < int(a.size())) { g_err = "capacity"; return -1; }
+        std::memcpy(assign, a.data(), a.size() * 4);
+        std::memcpy(counters, &s.choiceCounters(), sizeof(swarm::GpuChoiceCounters));
+        *step = s.choiceStep();
+        return int(a.size());
+    } catch (const std::exception& e) { g_err = e.what(); return -1; }
+}
+
 // The reference's own seated-venue functions, point by point (the harness's counterpart, same op codes):
 // 0 seated::floorHeight | 1 cellKey | 2 sdfGrad | 3 wall | 4 stepUpScan | 5 floorSlope | 6 nav::goal (forVenue's field)
 int ref_seated_eval(const char* venue, int op, int n, const float* in, float* out) {

@@ -31,8 +31,113 @@
 #include "choice.cuh"
 #include "sim_handle.cuh"
 #include "step_kernels.cuh"
+#include "venue_seated.cuh"
 
 namespace swarm_gpu {
+
+// ---- the seated venues: the reference's own table (nav::evaluate :605-623 and nav::apply :641-656 on its
+// GpuNavChoiceCell; navEstimate :580-584 with the table's quantised distances) ----
+
+// An agent's candidates: its choice cell's 36 words (null: a cell without candidates, every slot empty)
+struct SeatedCands {
+    const uint32_t* w;
+    __device__ __forceinline__ uint32_t exit(int k) const { return w ? (__ldg(w + k) >> 25) & 63u : CHOICE_SLOT_EMPTY; }
+    __device__ __forceinline__ uint32_t q(int k) const {   // distance quanta (nav::slotDistQ)
+        return w ? (__ldg(w + 24 + (k >> 1)) >> ((k & 1) * 16)) & 0xFFFFu : 0xFFFFu;
+    }
+    __device__ __forceinline__ int slotOf(uint32_t e) const {   // the last slot holding e (:586-591)
+        int k = -1;
+        for (int i = 0; i < 24; ++i)
+            if (exit(i) == e) k = i;
+        return k;
+    }
+};
+
+__device__ __forceinline__ SeatedCands seatedCands(const VenueArgs& V, const ChoiceArgs& C, float4 p) {
+    const SeatedChoice sc{SeatedNav{SeatedGeom{V.seatDev}, StepUpConst{C.suSample, C.suTol, C.suMax}, 0.0f, 0.0f, 0.0f,
+                                    nullptr, V.navRes, V.navOrigin, V.navCell, V.navInv},
+                          C.chIndex, C.chEntries};
+    return SeatedCands{sc.entry(sc.cellOf(f2{p.x, p.y}))};
+}
+
+// slotDist (exit_choice.hpp:172-175): q x quantum, exact in float (an empty slot: +infinity, never read here)
+__device__ __forceinline__ float seatedDist(const ChoiceArgs& C, uint32_t q) {
+    return q == 0xFFFFu ? __int_as_float(0x7f800000) : float(q) * C.quantum;
+}
+__device__ __forceinline__ uint32_t seatedBin(uint32_t q) { return min(q >> 6, uint32_t(CHOICE_AHEAD_BINS - 1)); }
+__device__ __forceinline__ float seatedEstimate(const ChoiceArgs& C, uint32_t q, uint32_t e, uint32_t queued) {
+    const float walk = seatedDist(C, q) * C.sPerUnit;
+    const float wait = float(queued) * C.invCap[e];
+    return walk + wait;
+}
+
+// navBest (:593-603): the first candidate of least E on the queues ahead
+__device__ __forceinline__ int seatedBest(const ChoiceArgs& C, const SeatedCands& c, const uint32_t* aRead, float& eBest) {
+    int best = -1;
+    eBest = 0.0f;
+    for (int k = 0; k < 24; ++k) {
+        const uint32_t ex = c.exit(k);
+        if (ex == CHOICE_SLOT_EMPTY) break;
+        const uint32_t q = c.q(k);
+        const float e = seatedEstimate(C, q, ex, aRead[size_t(ex) * CHOICE_AHEAD_BINS + seatedBin(q)]);
+        if (best < 0 || e < eBest) { best = k; eBest = e; }
+    }
+    return best;
+}
+
+// nav::evaluate for agent i (from its start-of-step position; an evacuated agent: none)
+__device__ __forceinline__ void seatedEvalAgent(const VenueArgs& V, const ChoiceArgs& C, int i) {
+    C.pending[i] = make_uint2(SWARM_CHOICE_NONE, 0u);
+    const float4 p = C.state[2 * size_t(i)];
+    if (p.w == 0.0f) return;
+    const SeatedCands c = seatedCands(V, C, p);
+    if (c.exit(0) == CHOICE_SLOT_EMPTY) return;
+    const uint32_t cur = C.assign[i];
+    const int curK = c.slotOf(cur);
+    if (curK < 0) return;
+    atomicAdd(C.counters + 0, 1u);
+    const uint32_t* aRead = C.ahead + size_t(C.step & 1u) * CHOICE_STRIDE * CHOICE_AHEAD_BINS;
+    float eBest;
+    const int best = seatedBest(C, c, aRead, eBest);
+    const uint32_t qc = c.q(curK);
+    const float eCur = seatedEstimate(C, qc, cur, aRead[size_t(cur) * CHOICE_AHEAD_BINS + seatedBin(qc)]);
+    const float gain = eCur - eBest;
+    if (best != curK && gain > fmaxf(CHOICE_REL_MARGIN * eCur, CHOICE_ABS_MARGIN_S)) {
+        const uint32_t bin = min(uint32_t(gain), uint32_t(CHOICE_GAIN_BINS - 1));
+        C.pending[i] = make_uint2(c.exit(best), bin);
+        atomicAdd(C.hist + size_t(cur) * CHOICE_GAIN_BINS + bin, 1u);
+        atomicAdd(C.counters + 1, 1u);
+    }
+}
+
+// nav::apply for agent i, then its counts (choiceStep :743-760): its exit's queue (the block's shared counts), and the
+// key of its queue-ahead count at its own distance to that exit (all ones: none)
+__device__ __forceinline__ uint32_t seatedApplyAgent(const VenueArgs& V, const ChoiceArgs& C, int i, uint32_t* sQueue) {
+    const float4 p = C.state[2 * size_t(i)];
+    if (p.w == 0.0f) return 0xFFFFFFFFu;
+    const SeatedCands c = seatedCands(V, C, p);
+    const uint32_t* aRead = C.ahead + size_t(C.step & 1u) * CHOICE_STRIDE * CHOICE_AHEAD_BINS;
+    const uint32_t cur = C.assign[i];
+    uint32_t ex = cur;
+    const bool hasPath = c.exit(0) != CHOICE_SLOT_EMPTY;
+    const int curK = hasPath ? c.slotOf(cur) : -1;
+    if (hasPath && curK < 0) {   // forced (or the first choice)
+        float eBest;
+        ex = c.exit(seatedBest(C, c, aRead, eBest));
+        if (cur != SWARM_CHOICE_NONE) atomicAdd(C.counters + 3, 1u);
+    } else if (C.evalStep && curK >= 0) {
+        const uint2 pd = C.pending[i];
+        if (pd.x != SWARM_CHOICE_NONE && pd.y >= C.threshold[cur]) {
+            ex = pd.x;
+            atomicAdd(C.counters + 2, 1u);
+        }
+    }
+    C.assign[i] = ex;
+    if (ex == SWARM_CHOICE_NONE) return 0xFFFFFFFFu;
+    atomicAdd(sQueue + ex, 1u);
+    const int k = c.slotOf(ex);
+    return k >= 0 ? ex * uint32_t(CHOICE_AHEAD_BINS) + seatedBin(c.q(k)) : 0xFFFFFFFFu;
+}
 
 // One block per exit; block 0 also clears the write parity's exit counts
 __global__ void __launch_bounds__(CHOICE_PREFIX_THREADS) k_choice_prefix(ChoiceArgs C, VenueArgs) {
@@ -42,7 +147,9 @@ __global__ void __launch_bounds__(CHOICE_PREFIX_THREADS) k_choice_prefix(ChoiceA
 
 __global__ void __launch_bounds__(256) k_choice_eval(ChoiceArgs C, VenueArgs V) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < C.n) choiceEvalAgent(V, C, i);
+    if (i >= C.n) return;
+    if (C.chIndex) seatedEvalAgent(V, C, i);
+    else choiceEvalAgent(V, C, i);
 }
 
 // One warp per exit (grid: nExits x 32)
@@ -55,7 +162,8 @@ __global__ void __launch_bounds__(256) k_choice_apply(ChoiceArgs C, VenueArgs V)
     if (threadIdx.x < CHOICE_STRIDE) sQueue[threadIdx.x] = 0u;
     __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    choiceAheadFlush(C, i < C.n ? choiceApplyAgent(V, C, i, sQueue) : 0xFFFFFFFFu);
+    const uint32_t key = i >= C.n ? 0xFFFFFFFFu : C.chIndex ? seatedApplyAgent(V, C, i, sQueue) : choiceApplyAgent(V, C, i, sQueue);
+    choiceAheadFlush(C, key);
     __syncthreads();
     choiceQueueFlush(C, sQueue);
 }
@@ -163,6 +271,7 @@ void SwarmSim::freeChoice() {
     dExitFields = nullptr; dChoiceExit = nullptr; dChoiceDist = nullptr; dChoiceInvCap = nullptr; dAssign = nullptr;
     dPending = nullptr; dChoiceHist = nullptr; dChoiceThr = nullptr; dChoiceQueue = nullptr; dChoiceAhead = nullptr;
     dChoiceCounters = nullptr;
+    dChIndex = nullptr; dChEntries = nullptr; chSPerUnit = 0.0f; chQuantum = 0.0f; choiceEvery = 0;
 }
 
 std::vector<std::pair<void*, size_t>> SwarmSim::choiceLive() const {
@@ -181,11 +290,14 @@ ChoiceArgs choiceArgsOf(const SwarmSim& s, int in) {
     C.nExits = s.choiceExits;
     C.K = s.choiceK;
     C.step = s.choiceStep;
-    C.evalStep = s.choiceStep > 0u && s.choiceStep % uint32_t(swarm_gpu::choiceSteps(s.P.dt)) == 0u;
+    const int every = s.choiceEvery > 0 ? s.choiceEvery : swarm_gpu::choiceSteps(s.P.dt);
+    C.evalStep = s.choiceStep > 0u && s.choiceStep % uint32_t(every) == 0u;   // nav::evaluationStep
     C.state = s.state[in];
     C.cExit = s.dChoiceExit; C.cDist = s.dChoiceDist; C.invCap = s.dChoiceInvCap;
     C.assign = s.dAssign; C.pending = s.dPending; C.hist = s.dChoiceHist; C.threshold = s.dChoiceThr;
     C.queue = s.dChoiceQueue; C.ahead = s.dChoiceAhead; C.counters = s.dChoiceCounters;
+    C.chIndex = s.dChIndex; C.chEntries = s.dChEntries; C.sPerUnit = s.chSPerUnit; C.quantum = s.chQuantum;
+    C.suSample = s.P.step_up_sample; C.suTol = s.P.step_up_tol; C.suMax = s.P.step_up_max_samples;
     return C;
 }
 
@@ -255,5 +367,57 @@ extern "C" int swarm_get_exit_choice(SwarmHandle h, uint32_t* assigned, int n, u
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) return h->fail(SWARM_E_CUDA, "sync");
     if (assigned && cudaMemcpy(assigned, h->dAssign, size_t(n) * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return h->fail(SWARM_E_CUDA, "download");
     if (counters && cudaMemcpy(counters, h->dChoiceCounters, 16, cudaMemcpyDeviceToHost) != cudaSuccess) return h->fail(SWARM_E_CUDA, "download");
+    return SWARM_OK;
+}
+
+extern "C" int swarm_set_seated_choice(SwarmHandle h, const SwarmSeatedChoiceSpec* c) {
+    if (!h) return SWARM_E_INVALID;
+    h->dropGraphs();
+    h->freeChoice();
+    if (!c) return SWARM_OK;
+    if (h->instances) return h->fail(SWARM_E_INVALID, "the exit choice runs on one venue (not a batch)");
+    if (h->V.kind != SWARM_VENUE_SEATED || !h->dNavCells || h->V.nav_res <= 0)
+        return h->fail(SWARM_E_INVALID, "seated exit choice: a seated venue with its navigation field");
+    if (c->grid_res != h->V.nav_res) return h->fail(SWARM_E_INVALID, "seated exit choice: the table's grid is the navigation grid");
+    const int E = c->n_exits;
+    if (E < 1 || E > SWARM_CHOICE_MAX_EXITS || c->n_entries < 0 || !c->index || (c->n_entries > 0 && !c->entries) || !c->inv_cap_s ||
+        !(c->seconds_per_unit > 0.0f) || !(c->dist_quantum > 0.0f) || c->choice_steps < 1)
+        return h->fail(SWARM_E_INVALID, "seated exit choice: 1..63 exits, index, entries, capacities, quantum and steps");
+    const size_t cells = size_t(c->grid_res) * size_t(c->grid_res), ne = size_t(c->n_entries);
+    for (size_t i = 0; i < cells; ++i)
+        if ((c->index[i] & SWARM_CHOICE_INDEX_MASK) > ne) return h->fail(SWARM_E_INVALID, "seated exit choice: an index word beyond the entries");
+    for (size_t e = 0; e < ne; ++e)
+        for (int k = 0; k < 24; ++k) {
+            const uint32_t w = c->entries[e].slot[k], ex = (w >> 25) & 63u;
+            if (ex == swarm_gpu::CHOICE_SLOT_EMPTY) continue;
+            if (ex >= uint32_t(E) || size_t(w & ((1u << 25) - 1u)) >= cells)
+                return h->fail(SWARM_E_INVALID, "seated exit choice: a slot's exit or anchor outside the table");
+        }
+    const size_t N = size_t(h->capacity);
+    auto alloc = [&](auto** p, size_t bytes) {
+        void* q = nullptr;
+        if (cudaMalloc(&q, std::max<size_t>(bytes, 16)) != cudaSuccess) return false;
+        h->choiceAllocs.push_back(q);
+        *p = static_cast<std::remove_pointer_t<decltype(p)>>(q);
+        return true;
+    };
+    const bool ok = alloc(&h->dChIndex, cells * 4) && alloc(&h->dChEntries, ne * sizeof(SwarmNavChoiceCell)) &&
+                    alloc(&h->dChoiceInvCap, size_t(E) * 4) && alloc(&h->dAssign, N * 4) && alloc(&h->dPending, N * 8) &&
+                    alloc(&h->dChoiceHist, size_t(E) * swarm_gpu::CHOICE_GAIN_BINS * 4) &&
+                    alloc(&h->dChoiceThr, size_t(swarm_gpu::CHOICE_STRIDE) * 4) &&
+                    alloc(&h->dChoiceQueue, size_t(2) * swarm_gpu::CHOICE_STRIDE * 4) &&
+                    alloc(&h->dChoiceAhead, size_t(2) * swarm_gpu::CHOICE_STRIDE * swarm_gpu::CHOICE_AHEAD_BINS * 4) &&
+                    alloc(&h->dChoiceCounters, 16);
+    if (!ok) { h->freeChoice(); return h->fail(SWARM_E_OOM, "seated exit choice buffers"); }
+    const bool up = cudaMemcpy(h->dChIndex, c->index, cells * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
+                    (ne == 0 || cudaMemcpy(h->dChEntries, c->entries, ne * sizeof(SwarmNavChoiceCell), cudaMemcpyHostToDevice) == cudaSuccess) &&
+                    cudaMemcpy(h->dChoiceInvCap, c->inv_cap_s, size_t(E) * 4, cudaMemcpyHostToDevice) == cudaSuccess;
+    if (!up) { h->freeChoice(); return h->fail(SWARM_E_CUDA, "seated exit choice upload"); }
+    h->choiceExits = E;
+    h->choiceK = 24;
+    h->chSPerUnit = c->seconds_per_unit;
+    h->chQuantum = c->dist_quantum;
+    h->choiceEvery = c->choice_steps;
+    if (!h->resetChoice()) { h->freeChoice(); return h->fail(SWARM_E_CUDA, "exit choice reset"); }
     return SWARM_OK;
 }

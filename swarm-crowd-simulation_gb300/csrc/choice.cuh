@@ -31,6 +31,14 @@ struct ChoiceArgs {
     uint32_t* queue;              // 2 x CHOICE_STRIDE (parities)
     uint32_t* ahead;              // 2 x CHOICE_STRIDE x CHOICE_AHEAD_BINS
     uint32_t* counters;           // evaluations, eligible, switches, forced
+    // a seated venue's own table (chIndex non-null: swarm_set_seated_choice; cExit / cDist unused): index words and
+    // entries on the navigation grid, the estimate's seconds per model unit, the distance quantum, and the step-up
+    // constants of the choice cell's surface rule
+    const uint32_t* chIndex;
+    const uint32_t* chEntries;
+    float sPerUnit, quantum;
+    float suSample, suTol;
+    int32_t suMax;
 };
 
 constexpr float CHOICE_T_S = 3.0f;            // re-evaluation interval (T_CHOICE_S)

@@ -140,3 +140,56 @@ extern "C" int swarm_nav_cache_read(const char* path, uint64_t expected_key, Swa
     }
     return SWARM_OK;
 }
+
+namespace {
+constexpr char CHOICE_MAGIC[8] = {'S', 'W', 'C', 'H', 'O', 'I', '0', '1'};
+constexpr uint32_t CHOICE_VERSION = 6;   // nav::CHOICE_VERSION (include/swarm/exit_choice.hpp:121)
+constexpr uint32_t CHOICE_K = 24;        // nav::CHOICE_K
+}  // namespace
+
+// nav::loadChoice (src/exit_choice.cpp:399-427): the header, then index and entries straight into the caller's
+// buffers, the exits' widths and names, the checksum; nothing may follow it
+extern "C" int swarm_choice_cache_read(const char* path, uint64_t expected_key, uint32_t* index, int64_t index_capacity,
+                                       SwarmNavChoiceCell* entries, int64_t entry_capacity, double* width_m, int32_t* res_out,
+                                       float* origin, float* cell, float* inv_cell, int32_t* n_exits, int64_t* n_entries) {
+    if (!path || !res_out || !origin || !cell || !inv_cell || !n_exits || !n_entries) return SWARM_E_INVALID;
+    if ((index == nullptr) != (entries == nullptr)) return SWARM_E_INVALID;
+    NavCacheReader in(path);
+    char magic[8];
+    if (!in.read(magic, 8, false) || std::memcmp(magic, CHOICE_MAGIC, 8) != 0) return SWARM_E_INVALID;
+    uint32_t version = 0, k = 0, res = 0, exits = 0;
+    uint64_t key = 0, ne = 0;
+    float o = 0.0f, c = 0.0f, ic = 0.0f;
+    if (!in.read(&version, 4) || !in.read(&k, 4) || !in.read(&res, 4) || !in.read(&o, 4) || !in.read(&c, 4) ||
+        !in.read(&ic, 4) || !in.read(&exits, 4) || !in.read(&key, 8))
+        return SWARM_E_INVALID;
+    if (version != CHOICE_VERSION || k != CHOICE_K || res == 0 || res > 100000 || exits > SWARM_CHOICE_MAX_EXITS)
+        return SWARM_E_INVALID;
+    if (expected_key != 0 && key != expected_key) return SWARM_E_INVALID;
+    const size_t cells = size_t(res) * size_t(res);
+    if (!in.read(&ne, 8) || ne > cells) return SWARM_E_INVALID;
+    *res_out = int32_t(res);
+    *origin = o;
+    *cell = c;
+    *inv_cell = ic;
+    *n_exits = int32_t(exits);
+    *n_entries = int64_t(ne);
+    if (!index) return SWARM_OK;   // a size query: the header alone
+    if (index_capacity < int64_t(cells) || entry_capacity < int64_t(ne)) return SWARM_E_INVALID;
+    if (!in.read(index, cells * 4) || !in.read(entries, size_t(ne) * sizeof(SwarmNavChoiceCell))) return SWARM_E_INVALID;
+    for (uint32_t e = 0; e < exits; ++e) {
+        double w = 0.0;
+        uint32_t len = 0;
+        if (!in.read(&w, 8) || !in.read(&len, 4) || len > 1000) return SWARM_E_INVALID;
+        std::vector<char> name(len);
+        if (len && !in.read(name.data(), len)) return SWARM_E_INVALID;
+        if (width_m) width_m[e] = w;
+    }
+    uint64_t sum = 0;
+    if (!in.read(&sum, 8, false) || sum != in.hash) return SWARM_E_INVALID;
+    char extra;
+    if (std::fread(&extra, 1, 1, in.f) != 0) return SWARM_E_INVALID;   // nothing after the checksum
+    for (size_t i = 0; i < cells; ++i)
+        if ((index[i] & SWARM_CHOICE_INDEX_MASK) > ne) return SWARM_E_INVALID;   // an entry the file does not hold
+    return SWARM_OK;
+}

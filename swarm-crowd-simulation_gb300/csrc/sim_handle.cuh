@@ -100,6 +100,12 @@ struct SwarmSim {
     uint2* dPending = nullptr;              // per agent
     uint32_t *dChoiceHist = nullptr, *dChoiceThr = nullptr, *dChoiceQueue = nullptr, *dChoiceAhead = nullptr,
              *dChoiceCounters = nullptr;
+    // a seated venue's own table (swarm_set_seated_choice): index words, entries, the estimate's terms, the steps
+    // between evaluations (0: from dt, the grid venues' 3 s)
+    uint32_t* dChIndex = nullptr;
+    uint32_t* dChEntries = nullptr;
+    float chSPerUnit = 0.0f, chQuantum = 0.0f;
+    int32_t choiceEvery = 0;
     std::vector<void*> choiceAllocs;
     bool resetChoice();                     // no exit assigned, counts clear, step 0
     void freeChoice();                      // off, buffers freed

@@ -46,6 +46,9 @@ struct VenueArgs {
     float navOrigin, navCell, navInv;
     int32_t incline, stairHw;   // the incline speed; the stair spacing, with its time gaps up / down
     float stairTUp, stairTDown;
+    // the queue-aware exit choice's candidate table on the navigation grid (null: off): index words, entries
+    const uint32_t* choiceIndex;
+    const uint32_t* choiceEntries;
 };
 
 struct StepArgs {

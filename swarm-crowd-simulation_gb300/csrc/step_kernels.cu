@@ -312,6 +312,11 @@ __device__ __forceinline__ f2 goalOf(const StepArgs& A, const Venue& ven, f3 p, 
             if (e != SWARM_CHOICE_NONE) return ven.goalIn(A.exitFields + size_t(e) * A.navNodes, p);
         }
     }
+    if constexpr (std::is_same<Venue, Seated>::value) {
+        // the reference's table: its goal whatever the assignment (none yet: no candidate matches, e_goal 0 but the
+        // wall rule)
+        if (A.choiceAssign && ven.V.choiceIndex) return ven.choiceGoal(p, A.choiceAssign[id]);
+    }
     return ven.goal(p);
 }
 

@@ -87,6 +87,8 @@ StepArgs SwarmSim::args(int in) const {
     v.incline = V.incline_speed ? 1 : 0;
     v.stairHw = V.incline_speed && V.stair_headway ? 1 : 0;
     v.stairTUp = V.stair_t_up; v.stairTDown = V.stair_t_down;
+    v.choiceIndex = dChIndex;
+    v.choiceEntries = dChEntries;
     A.n = n;
     A.projectInFinal = P.proj_iterations > 0 ? 1 : 0;
     A.stateIn = state[in];

@@ -669,6 +669,102 @@ struct SeatedNav {
     }
 };
 
+// The queue-aware exit choice's table lookup (src/exit_choice.cpp:512-578; physics.comp navChoiceCell /
+// navChoiceDirection / navChoiceGoal): the reference's ChoiceTable on the navigation grid -- per cell an index word
+// (SWARM_CHOICE_INDEX_FIT | its entry + 1) and per entry the GpuNavChoiceCell's 36 words (24 slots: anchor bits 0-24,
+// exit bits 25-30; then 12 words of two 16-bit distances)
+SWARM_HD __forceinline__ uint32_t loadWord(const uint32_t* p) {
+#ifdef __CUDA_ARCH__
+    return __ldg(p);
+#else
+    return *p;
+#endif
+}
+
+constexpr uint32_t CHOICE_SLOT_EMPTY = 63u;   // the exit id of an empty slot (nav::CHOICE_EMPTY)
+
+struct SeatedChoice {
+    SeatedNav nav;                 // the grid, the surface rule and the goal's constants (its cells are not read)
+    const uint32_t* index;
+    const uint32_t* entries;
+
+    SWARM_HD __forceinline__ bool fit(int i) const { return (loadWord(index + i) & SWARM_CHOICE_INDEX_FIT) != 0u; }
+    SWARM_HD __forceinline__ bool reachable(int i) const { return (loadWord(index + i) & SWARM_CHOICE_INDEX_MASK) != 0u; }
+    // cell i's candidates (36 words), or null for a cell without any (ChoiceTable::at's empty cell)
+    SWARM_HD __forceinline__ const uint32_t* entry(int i) const {
+        const uint32_t e = loadWord(index + i) & SWARM_CHOICE_INDEX_MASK;
+        return e ? entries + size_t(e - 1u) * 36u : nullptr;
+    }
+    // choiceCell (:512-548): the cell containing x; a NOFIT cell takes the FIT cell with candidates of its 3 x 3 ring
+    // whose centre is nearest, else of the 5 x 5 ring's outer cells; then the surface rule over the 3 x 3 cells
+    SWARM_HD __noinline__ int cellOf(f2 x) const {
+        const int res = nav.res;
+        const f2 g{(x.x - nav.origin) * nav.inv, (x.y - nav.origin) * nav.inv};
+        const int cx = sclamp(int(floorf(g.x)), 0, res - 1), cy = sclamp(int(floorf(g.y)), 0, res - 1);
+        int i = cx + cy * res;
+        if (!fit(i)) {
+            float best = 1e9f;
+            for (int r = 1; r <= 2 && best == 1e9f; r++)
+                for (int dy = -r; dy <= r; dy++)
+                    for (int dx = -r; dx <= r; dx++) {
+                        if (max(abs(dx), abs(dy)) != r) continue;
+                        const int mx = cx + dx, my = cy + dy;
+                        if (mx < 0 || my < 0 || mx >= res || my >= res) continue;
+                        const int j = mx + my * res;
+                        if (!fit(j) || !reachable(j)) continue;
+                        const f2 q{g.x - (float(mx) + 0.5f), g.y - (float(my) + 0.5f)};
+                        const float d2 = q.x * q.x + q.y * q.y;
+                        if (d2 < best) { best = d2; i = j; }
+                    }
+        }
+        if (!nav.reaches(x, nav.cellCentre(i))) {
+            float best = 1e9f;
+            int pick = i;
+            for (int dy = -1; dy <= 1; dy++)
+                for (int dx = -1; dx <= 1; dx++) {
+                    const int mx = cx + dx, my = cy + dy;
+                    if (mx < 0 || my < 0 || mx >= res || my >= res) continue;
+                    const int j = mx + my * res;
+                    if (j == i || !fit(j) || !reachable(j)) continue;
+                    const f2 q{g.x - (float(mx) + 0.5f), g.y - (float(my) + 0.5f)};
+                    const float d2 = q.x * q.x + q.y * q.y;
+                    if (d2 < best && nav.reaches(x, nav.cellCentre(j))) { best = d2; pick = j; }
+                }
+            i = pick;
+        }
+        return i;
+    }
+    // choiceDirection / choiceGoal (:557-578): towards the anchor of the exit's own field in x's choice cell (its centre
+    // in float, anchorCentre :550-555), 0 within the dead zone or when the exit is no candidate there; the component
+    // into a wall or step face beside the agent removed
+    SWARM_HD __noinline__ f2 goal(f3 p, uint32_t exit) const {
+        const f2 x = xy(p);
+        const uint32_t* c = entry(cellOf(x));
+        f2 e{0.0f, 0.0f};
+        if (c) {
+            for (int k = 0; k < 24; ++k) {
+                const uint32_t w = loadWord(c + k);
+                if (((w >> 25) & 63u) != exit) continue;   // (an exit appears at most once)
+                const uint32_t a = w & ((1u << 25) - 1u);
+                const float ax = float(a % uint32_t(nav.res)) + 0.5f, ay = float(a / uint32_t(nav.res)) + 0.5f;
+                const float px = ax * nav.cell, py = ay * nav.cell;
+                const f2 d = f2{nav.origin + px, nav.origin + py} - x;
+                const float l = length(d);
+                e = l > nav.goalDeadzone ? d / l : f2{0.0f, 0.0f};
+                break;
+            }
+        }
+        const f3 w = nav.G.wall(p, nav.feelerReach);
+        const float into = dot(e, f2{w.x, w.y});
+        if (w.z < nav.feelerReach && into < 0.0f) {
+            e = e - f2{w.x, w.y} * into;
+            const float l = length(e);
+            e = l > nav.safeEps ? e / l : f2{0.0f, 0.0f};
+        }
+        return e;
+    }
+};
+
 struct Seated {
     const SwarmParams& P;
     const VenueArgs& V;
@@ -855,6 +951,13 @@ struct Seated {
         if (!V.navCells) return fence().goal(p);
         return SeatedNav{geo(), stepUp(), P.goal_deadzone, P.feeler_reach, P.safe_eps, V.navCells, V.navRes, V.navOrigin,
                          V.navCell, V.navInv}.goal(p);
+    }
+    // e_goal under the queue-aware exit choice: the assigned exit's anchor in the agent's choice cell
+    // (cpu_crowd_sim.cpp:214, nav::choiceGoal)
+    __device__ __forceinline__ f2 choiceGoal(f3 p, uint32_t exit) const {
+        return SeatedChoice{SeatedNav{geo(), stepUp(), P.goal_deadzone, P.feeler_reach, P.safe_eps, nullptr, V.navRes,
+                                      V.navOrigin, V.navCell, V.navInv},
+                            V.choiceIndex, V.choiceEntries}.goal(p, exit);
     }
 
     __device__ __forceinline__ bool exits(float4 p) const { return fence().exits(p); }   // cpu_crowd_sim.cpp:662-668

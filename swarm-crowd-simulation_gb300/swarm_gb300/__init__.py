@@ -14,7 +14,8 @@ import numpy as np
 
 from .abi import (METRIC_CELL_WORDS, SWARM_LOSS_NAV_DISTANCE, SWARM_OK, SWARM_VENUE_GRID, SWARM_VENUE_STADIUM,
                   SwarmAdjointStats, SwarmEvacuation, SwarmLossSpec, SwarmMetricCounters, SwarmNavFieldStats, SwarmParams,
-                  SwarmStageTimes, SwarmTuning, SwarmVenue, SwarmExitChoiceSpec, CHOICE_NONE, CHOICE_EMPTY, fptr)
+                  SwarmStageTimes, SwarmTuning, SwarmVenue, SwarmExitChoiceSpec, SwarmSeatedChoiceSpec, CHOICE_NONE,
+                  CHOICE_EMPTY, fptr)
 
 PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG_DIR, "libswarm_gb300.so")
@@ -86,6 +87,10 @@ _SIG = {
                                 C.POINTER(C.c_float)],
     "swarm_set_exit_choice": [_H, C.POINTER(SwarmExitChoiceSpec)],
     "swarm_get_exit_choice": [_H, C.c_void_p, C.c_int, C.c_void_p],
+    "swarm_set_seated_choice": [_H, C.POINTER(SwarmSeatedChoiceSpec)],
+    "swarm_choice_cache_read": [C.c_char_p, C.c_uint64, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p,
+                                C.POINTER(C.c_int32), C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                C.POINTER(C.c_int32), C.POINTER(C.c_int64)],
     "swarm_bowl_layout": [C.c_void_p, C.POINTER(SwarmVenue)],
     "swarm_bowl_fields": [C.c_void_p, C.POINTER(SwarmVenue), C.POINTER(C.c_float), C.POINTER(C.c_float),
                           C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_void_p, C.POINTER(C.c_float)],
@@ -165,6 +170,24 @@ def nav_cache_read(path, expected_key=0):
     _check(lib().swarm_nav_cache_read(p, expected_key, cells.ctypes.data_as(C.c_void_p), cells.shape[0], C.byref(res),
                                       C.byref(o), C.byref(c), C.byref(ic)), "swarm_nav_cache_read")
     return cells, (res.value, o.value, c.value, ic.value)
+
+
+def choice_cache_read(path, expected_key=0):
+    """A seated venue's exit-choice cache file as the reference writes it: (index (res^2,) uint32, entries (n, 36)
+    uint32 -- 24 slot words, 12 distance words --, clear widths (n_exits,) float64, (res, origin, cell, 1 / cell))."""
+    res, o, c, ic = C.c_int32(), C.c_float(), C.c_float(), C.c_float()
+    ne, nx = C.c_int64(), C.c_int32()
+    p = os.fsencode(path)
+    _check(lib().swarm_choice_cache_read(p, expected_key, None, 0, None, 0, None, C.byref(res), C.byref(o), C.byref(c),
+                                         C.byref(ic), C.byref(nx), C.byref(ne)), "swarm_choice_cache_read")
+    index = np.empty(res.value * res.value, np.uint32)
+    entries = np.empty((max(ne.value, 1), 36), np.uint32)
+    widths = np.empty(max(nx.value, 1), np.float64)
+    _check(lib().swarm_choice_cache_read(p, expected_key, index.ctypes.data_as(C.c_void_p), index.shape[0],
+                                         entries.ctypes.data_as(C.c_void_p), entries.shape[0],
+                                         widths.ctypes.data_as(C.c_void_p), C.byref(res), C.byref(o), C.byref(c),
+                                         C.byref(ic), C.byref(nx), C.byref(ne)), "swarm_choice_cache_read")
+    return index, entries[:ne.value], widths[:nx.value], (res.value, o.value, c.value, ic.value)
 
 
 def snapshot_read(path):
@@ -333,6 +356,22 @@ class CrowdSim:
             return
         spec, _keep = _choice_spec(fields, widths, types, candidates)
         self._ck(lib().swarm_set_exit_choice(self._h, C.byref(spec)), "set_exit_choice")
+
+    def set_seated_choice(self, index=None, entries=None, inv_cap_s=None, seconds_per_unit=0.0, dist_quantum=0.0,
+                          choice_steps=17):
+        """The queue-aware exit choice of a seated venue on the reference's own candidate table (index: res^2 words on
+        the navigation grid; entries: (n, 36) uint32 GpuNavChoiceCell words; inv_cap_s: seconds per queued agent per
+        exit); None: off. Restarts the choice (no exit assigned)."""
+        if index is None:
+            self._ck(lib().swarm_set_seated_choice(self._h, None), "set_seated_choice")
+            return
+        idx = np.ascontiguousarray(index, dtype=np.uint32)
+        ent = np.ascontiguousarray(entries, dtype=np.uint32).reshape(-1, 36)
+        cap = np.ascontiguousarray(inv_cap_s, dtype=np.float32)
+        spec = SwarmSeatedChoiceSpec(int(cap.shape[0]), int(round(np.sqrt(idx.shape[0]))), idx.ctypes.data,
+                                     ent.ctypes.data, int(ent.shape[0]), fptr(cap), float(seconds_per_unit),
+                                     float(dist_quantum), int(choice_steps))
+        self._ck(lib().swarm_set_seated_choice(self._h, C.byref(spec)), "set_seated_choice")
 
     def exit_choice(self):
         """(assigned exit per agent (CHOICE_NONE: none yet), counters: evaluations, eligible, switches, forced)"""

@@ -122,6 +122,18 @@ class SwarmExitChoiceSpec(C.Structure):
 
 CHOICE_NONE = 0xFFFFFFFF
 CHOICE_EMPTY = 0xFF
+CHOICE_INDEX_FIT = 0x80000000
+CHOICE_INDEX_MASK = 0x7FFFFFFF
+
+
+class SwarmNavChoiceCell(C.Structure):
+    _fields_ = [("slot", C.c_uint32 * 24), ("dist", C.c_uint32 * 12)]
+
+
+class SwarmSeatedChoiceSpec(C.Structure):
+    _fields_ = [("n_exits", C.c_int32), ("grid_res", C.c_int32), ("index", C.c_void_p), ("entries", C.c_void_p),
+                ("n_entries", C.c_int64), ("inv_cap_s", C.POINTER(_f)), ("seconds_per_unit", _f),
+                ("dist_quantum", _f), ("choice_steps", C.c_int32)]
 
 
 class SwarmAdjointStats(C.Structure):

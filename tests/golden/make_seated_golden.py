@@ -24,6 +24,15 @@ Contents:
   incline_*         the same spawn under {nearest exit, incline speed, stair spacing EMPIRICAL}: states after 1, 50 and
                     250 steps (the reference's output; the reference pins this model only with the queue-aware choice)
 
+tests/golden/seated_S_choice.npz: venue S's queue-aware exit choice as the reference builds it (nav::choiceForVenue) in
+a compact form -- per exit its anchor and its 16-bit distance at every entry (delta-coded along the entries, lzma), the
+exit of every slot (lzma), the capacity terms; the index words follow from the navigation table's FIT and REACHABLE
+bits (checked here), the empty slots are constant (checked) -- and the reference's routed runs of the seat spawn
+under its default model {queue-aware, incline speed, stair spacing EMPIRICAL}: the assignments and counters after
+steps 1, 17 and 18 (the first evaluation), the states after 1 and 18 steps, the state hashes after 50 and 250 steps
+(the last: the pin "CPU counting venue S routed", golden_state.hpp:55), and the 250-step hash with the level spacing
+(pin golden_state.hpp:69). Written alone by `python tests/golden/make_seated_golden.py choice`.
+
 and tests/golden/seated_M.npz, seated_L.npz: the generated venues M (15 832 seats, N = 16 384) and L (63 424 seats,
 N = 65 536) -- several straight gangways, doors per gangway head, corner doors, merged corner gangways -- with the
 layout, grid, compact navigation table as above, the full seat spawn spawnSeatedCrowd(venue, N, 1.0, 1337) (zlib), and
@@ -31,6 +40,7 @@ the FNV-1a hashes of the reference's states after 1, 10 and 50 steps under {near
 steps under {nearest exit, incline speed, stair spacing EMPIRICAL}.
 """
 import ctypes as C
+import lzma
 import os
 import sys
 import zlib
@@ -43,10 +53,15 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "swarm-crowd-simulation_gb300"))
 from oracle import oracle as O  # noqa: E402
 from swarm_gb300.abi import SwarmSeatedLayout  # noqa: E402
+sys.path.insert(0, HERE)
+from seated_choice import EMPTY_SLOT, choice_index, decode_choice_entries  # noqa: E402
 
 PIN_DENSE = 0xa2abaea7c0139b09     # golden_state.hpp:45  CPU counting venue S dense
 PIN_NEAREST = 0xb1d6dac42f5dcd09   # golden_state.hpp:62  CPU counting venue S nearest exit, level speed
+PIN_ROUTED = 0x434356ac8d65471d    # golden_state.hpp:55  CPU counting venue S routed
+PIN_ROUTED_LEVEL = 0x22ad15f59ee18632   # golden_state.hpp:69  CPU counting venue S routed, level spacing
 STEPS = 250                        # golden_state.hpp:19  GOLDEN_STEPS
+CHOICE_STEPS = 17                  # sim_params.hpp:417-418
 
 
 def fnv1a(a):
@@ -141,11 +156,93 @@ def generated_venue(L, name, n):
     print("wrote", os.path.basename(path), os.path.getsize(path), "bytes")
 
 
+def _lz(a):
+    return np.frombuffer(lzma.compress(np.ascontiguousarray(a).tobytes(), preset=9 | lzma.PRESET_EXTREME), np.uint8)
+
+
+def choice_records(L):
+    """seated_S_choice.npz (see the module docstring)."""
+    V = C.c_void_p
+    L.ref_choice_table.restype = C.c_longlong
+    L.ref_choice_table.argtypes = [C.c_char_p, V, C.c_longlong, V, C.c_longlong, V, V]
+    L.ref_choice_state.argtypes = [V, V, C.c_int, V, V]
+    meta = np.zeros(3 + 64, np.float32)
+    res = C.c_int()
+    ne = L.ref_choice_table(b"S", None, 0, None, 0, meta.ctypes.data, C.byref(res))
+    assert ne > 0, L.ref_last_error()
+    cells = res.value * res.value
+    index = np.empty(cells, np.uint32)
+    entries = np.empty((ne, 36), np.uint32)
+    assert L.ref_choice_table(b"S", index.ctypes.data, cells, entries.ctypes.data, ne, meta.ctypes.data, C.byref(res)) == ne
+    E = int(meta[0])
+    # the index from the navigation table: the class bit, and entries numbered in grid order over FIT + REACHABLE cells
+    g = np.load(os.path.join(HERE, "seated_S.npz"))
+    info = np.frombuffer(zlib.decompress(g["nav_info_z"].tobytes()), np.uint32)
+    assert int(g["nav_grid"][0]) == res.value
+    assert np.array_equal(choice_index(info), index), "the index follows from the navigation table"
+    slot, dist = entries[:, :24], entries[:, 24:]
+    ex = ((slot >> 25) & 63).astype(np.uint8)
+    q = np.stack([(dist[:, k >> 1] >> ((k & 1) * 16)) & 0xFFFF for k in range(24)], 1)
+    assert np.all(slot[ex == 63] == EMPTY_SLOT) and np.all(q[ex == 63] == 0xFFFF) and np.all(slot >> 31 == 1)
+    rows = np.arange(ne)
+    anchor = np.zeros((E, ne), np.int64)
+    dq = np.zeros((E, ne), np.int64)
+    seen = np.zeros((E, ne), bool)
+    for k in range(24):
+        m = ex[:, k] != 63
+        e = ex[m, k].astype(np.int64)
+        anchor[e, rows[m]] = slot[m, k] & 0x1FFFFFF
+        dq[e, rows[m]] = q[m, k]
+        seen[e, rows[m]] = True
+    assert seen.all(), "every exit is a candidate of every entry (the venue has fewer exits than slots)"
+    out = {"choice_meta": meta[:3 + E].copy(), "choice_grid": np.array([res.value, ne, CHOICE_STEPS], np.int64),
+           "choice_order_lz": _lz(ex),
+           "choice_anchor_lz": _lz(np.diff(anchor, axis=1, prepend=0).astype(np.int32)),
+           "choice_q_lz": _lz(np.diff(dq, axis=1, prepend=0).astype(np.int32))}
+    # the decoding the tests use gives the reference's words back
+    assert np.array_equal(decode_choice_entries(out), entries)
+
+    spawn = np.empty((4096, 8), np.float32)
+    assert L.ref_spawn_seated(b"S", 4096, 1.0, 1337, spawn.ctypes.data) == 0
+    sim = O.RefSim.__new__(O.RefSim)
+    sim._h = L.ref_create_opts(b"S", 0, 0, 1, 1, 1)
+    sim.n = 0
+    sim.set_state(spawn)
+    assign = np.empty(4096, np.uint32)
+    counters = np.empty(132, np.uint32)
+    cstep = C.c_uint32()
+    for s in range(1, STEPS + 1):
+        sim.step(1)
+        if s in (1, 17, 18):
+            L.ref_choice_state(sim._h, assign.ctypes.data, 4096, counters.ctypes.data, C.byref(cstep))
+            assert cstep.value == s
+            out["routed_assign%d" % s] = assign.copy()
+            out["routed_counters%d" % s] = counters.copy()
+        if s in (1, 18):
+            out["routed_state%d" % s] = sim.state()
+        if s in (50, STEPS):
+            out["routed_hash%d" % s] = np.array([fnv1a(sim.state())], np.uint64)
+    assert int(out["routed_hash250"][0]) == PIN_ROUTED, "%016x" % int(out["routed_hash250"][0])
+    sim = O.RefSim.__new__(O.RefSim)
+    sim._h = L.ref_create_opts(b"S", 0, 0, 1, 1, 0)
+    sim.n = 0
+    sim.set_state(spawn)
+    sim.step(STEPS)
+    out["level_hash250"] = np.array([fnv1a(sim.state())], np.uint64)
+    assert int(out["level_hash250"][0]) == PIN_ROUTED_LEVEL, "%016x" % int(out["level_hash250"][0])
+    path = os.path.join(HERE, "seated_S_choice.npz")
+    np.savez_compressed(path, **out)
+    print("wrote seated_S_choice.npz:", os.path.getsize(path), "bytes")
+
+
 def main():
     os.environ.setdefault("SWARM_NAV_CACHE", os.path.join("/tmp", "swarm_navcache"))
     O.build(ref=True)
     assert O.ref_available(), "the reference tree is needed: REF_DIR=<tree> make -C oracle ref"
     L = _bind(O.ref_lib())
+    if sys.argv[1:] == ["choice"]:
+        choice_records(L)
+        return
     out = {}
     assert _venue_records(L, b"S", out) == 40
 
@@ -192,6 +289,7 @@ def main():
     out["incline_hash250"] = np.array([fnv1a(out["incline_state250"])], np.uint64)
     np.savez_compressed(os.path.join(HERE, "seated_S.npz"), **out)
     print("wrote seated_S.npz:", os.path.getsize(os.path.join(HERE, "seated_S.npz")), "bytes")
+    choice_records(L)
     generated_venue(L, b"M", 16384)
     generated_venue(L, b"L", 65536)
 

@@ -3,9 +3,11 @@
 own sources) and its pinned state hashes (tools/golden_state.hpp:45, :62). The sorted pairs, the cell table and the
 contact bits are compared exactly; states within the step's stated tolerance (TOL) and then bit for bit.
 
-Three models of the reference: the dense forced scenario (every seat occupied, e_goal from a drive table: the contact
+Four models of the reference: the dense forced scenario (every seat occupied, e_goal from a drive table: the contact
 model alone), the nearest exit at the level speed (e_goal from the navigation field's anchors: navCell's NOFIT ring and
-surface rule, navGoal's wall rule), and the incline speed with the stair spacing."""
+surface rule, navGoal's wall rule), the incline speed with the stair spacing, and its default model -- the queue-aware
+exit choice on its own candidate table (tests/golden/seated_S_choice.npz) with the incline speed and stair spacing --
+against the pins "CPU counting venue S routed" (tools/golden_state.hpp:55, :69)."""
 import os
 import zlib
 
@@ -284,3 +286,115 @@ def test_generated_venue_runs_reproduce_the_reference(name):
             done = k
             assert fnv1a(sim.state()) == int(g[prefix + "hash%d" % k][0]), f"{name} {prefix}{k} steps"
         sim.close()
+
+
+# ---- the queue-aware exit choice on the reference's own table ----
+CHOICE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "seated_S_choice.npz")
+PIN_ROUTED = 0x434356ac8d65471d         # golden_state.hpp:55  CPU counting venue S routed
+PIN_ROUTED_LEVEL = 0x22ad15f59ee18632   # golden_state.hpp:69  CPU counting venue S routed, level spacing
+
+
+@pytest.fixture(scope="module")
+def choice(golden):
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from seated_choice import choice_index, decode_choice_entries
+    g = dict(np.load(CHOICE))
+    info = np.frombuffer(zlib.decompress(golden["nav_info_z"].tobytes()), np.uint32)
+    meta = g["choice_meta"]
+    E = int(meta[0])
+    return g, choice_index(info), decode_choice_entries(g), meta[3:3 + E].astype(np.float32), float(meta[1]), float(meta[2])
+
+
+def test_choice_fixture_decodes_to_a_consistent_table(choice):
+    """The table decoded from the fixture: every entry referenced once by the index, in grid order; every slot an exit
+    of the venue or empty, anchors inside the grid; the estimate's terms as sim_params.hpp folds them."""
+    g, index, entries, inv_cap, s_per_unit, quantum = choice
+    res, ne, steps = (int(x) for x in g["choice_grid"])
+    assert index.shape == (res * res,) and entries.shape == (ne, 36) and steps == 17
+    e = index & 0x7FFFFFFF
+    assert np.array_equal(e[e != 0], np.arange(1, ne + 1))
+    ex = (entries[:, :24] >> 25) & 63
+    assert ((ex < inv_cap.shape[0]) | (ex == 63)).all() and ((entries[:, :24] & 0x1FFFFFF) < res * res).all()
+    assert quantum == 2.0 ** -12 and s_per_unit > 0 and (inv_cap > 0).all()
+
+
+def test_choice_cache_file_reads_as_the_reference_table(built, tmp_path, monkeypatch):
+    """swarm_choice_cache_read on the cache file the unmodified reference writes for venue S (nav::saveChoice) gives
+    the reference's own index, entries and widths (their capacities: nav::setChoiceCapacities)."""
+    import ctypes as C
+    import glob
+    import swarm_gb300
+    from oracle import oracle as O
+    if not O.ref_available():
+        pytest.skip("the reference build (oracle/_ref) is not on this machine")
+    monkeypatch.setenv("SWARM_NAV_CACHE", str(tmp_path))
+    L = O.ref_lib()
+    L.ref_choice_table.restype = C.c_longlong
+    L.ref_choice_table.argtypes = [C.c_char_p, C.c_void_p, C.c_longlong, C.c_void_p, C.c_longlong, C.c_void_p, C.c_void_p]
+    meta = np.zeros(67, np.float32)
+    res = C.c_int()
+    ne = L.ref_choice_table(b"S", None, 0, None, 0, meta.ctypes.data, C.byref(res))
+    index = np.empty(res.value ** 2, np.uint32)
+    entries = np.empty((ne, 36), np.uint32)
+    L.ref_choice_table(b"S", index.ctypes.data, index.shape[0], entries.ctypes.data, ne, meta.ctypes.data, C.byref(res))
+    files = glob.glob(os.path.join(str(tmp_path), "nav_S_choice_*.bin"))
+    if not files:
+        pytest.skip("the reference process already held venue S's table (it builds or reads one per process)")
+    idx, ent, widths, grid = swarm_gb300.choice_cache_read(files[0])
+    assert grid[0] == res.value and np.array_equal(idx, index) and np.array_equal(ent, entries)
+    cap = (60.0 / (widths * 83.6)).astype(np.float32)
+    assert np.array_equal(cap, meta[3:3 + int(meta[0])])
+    bad = tmp_path / "bad.bin"
+    raw = bytearray(open(files[0], "rb").read())
+    raw[100] ^= 1
+    bad.write_bytes(bytes(raw))
+    with pytest.raises(swarm_gb300.SwarmError):
+        swarm_gb300.choice_cache_read(str(bad))
+
+
+def _routed(golden, nav_cells, choice, stair=True):
+    from swarm_gb300.venues import Venue
+    import swarm_gb300
+    g, index, entries, inv_cap, s_per_unit, quantum = choice
+    gr = golden["grid"]
+    inc = golden["incline"]
+    venue = Venue.seated(golden["layout"], int(gr[0]), gr[1], gr[2], gr[3], gr[4], nav_cells=nav_cells,
+                         nav_grid=golden["nav_grid"], incline_speed=True,
+                         stair_times=(inc[4], inc[5]) if stair else None, name="S")
+    sim = swarm_gb300.CrowdSim(swarm_gb300.params_reference(), venue, golden["nearest_spawn"].shape[0])
+    sim.set_seated_choice(index, entries, inv_cap, s_per_unit, quantum, int(g["choice_grid"][2]))
+    sim.set_state(golden["nearest_spawn"])
+    return sim
+
+
+@pytest.mark.gpu
+def test_routed_exit_choice_reproduces_the_reference(golden, nav_cells, choice):
+    """The reference's default model on venue S (queue-aware exit choice, incline speed, stair spacing EMPIRICAL) from
+    the seat spawn: the assignments and counters after the first choice, before and after the first evaluation (steps
+    17, 18), the states after 1 and 18 steps, the hash after 50, and after 250 steps the reference's pin."""
+    g = choice[0]
+    sim = _routed(golden, nav_cells, choice)
+    done = 0
+    for s in (1, 17, 18):
+        sim.step(s - done)
+        done = s
+        a, c = sim.exit_choice()
+        ref = g["routed_counters%d" % s]
+        assert np.array_equal(a, g["routed_assign%d" % s]), f"assignments after step {s}"
+        # GpuChoiceCounters: queue[128], switches, forced, evaluations, eligible
+        assert (c[0], c[1], c[2], c[3]) == (ref[130], ref[131], ref[128], ref[129]), f"counters after step {s}"
+        if s in (1, 18):
+            assert_state(sim.state(), g["routed_state%d" % s], f"{s} steps")
+    sim.step(32)
+    assert fnv1a(sim.state()) == int(g["routed_hash50"][0]), "50 steps"
+    sim.step(200)
+    assert fnv1a(sim.state()) == PIN_ROUTED == int(g["routed_hash250"][0]), "the pin after 250 steps"
+
+
+@pytest.mark.gpu
+def test_routed_exit_choice_with_level_spacing_reproduces_the_reference_pin(golden, nav_cells, choice):
+    """The same with the level spacing on the inclines (incline speed on, stair spacing off): the reference's pin."""
+    sim = _routed(golden, nav_cells, choice, stair=False)
+    sim.step(250)
+    assert fnv1a(sim.state()) == PIN_ROUTED_LEVEL
