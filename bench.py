@@ -21,7 +21,9 @@ cpu_baseline  the oracle port of the reference's CPU step (OpenMP, all host thre
 batched  the 256-instance batch as one packed state against the same instances launched one at a time.
 bowl   the 63 488-agent seated bowl: the plain step (as value) and its evacuation run to completion.
 reference_venue_L  the reference's own seated venue L (63 424 agents) with the reference's constants (K = 32), beside
-       the reference's published GPU step on that venue.
+       the reference's published GPU step on that venue (from the spawn and congested).
+reference_venue_S  venue S under the reference's default model (its queue-aware exit choice on its own table, the
+       incline speed and stair spacing), from the spawn and congested, beside the reference's published GPU step.
 adjoint  loss and gradient of 400 steps of the 16 384-agent hall (checkpoints every 20 steps, and the full tape)
        against the plain forward of the same steps.
 --impl reference  the reference's CPU step (the oracle port: the reference's own build needs its source tree, which
@@ -299,22 +301,65 @@ def bench_bowl(P, steps=50, warmup=5, cap=20000, chunk=100, evacuation=True):
             "nav_field": bench_nav_field(venue)}
 
 
+def _timed_steps(sim, stream, flush, steps):
+    """CUDA events per step on the handle's stream, the L2 flushed by a 256 MiB write before each step (outside the
+    events); returns (agent-steps: the agents active at the start of each step, total ms)."""
+    import torch
+    active, total = 0, 0.0
+    for k in range(steps):
+        active += int((sim.state()[:, 3] != 0).sum())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xFF)
+            e0.record(stream)
+            sim.step(1)
+            e1.record(stream)
+        stream.synchronize()
+        total += e0.elapsed_time(e1)
+    return active, total
+
+
+def _congest(sim, stream, chunk=10, cap=20000):
+    """Steps until at most half the agents that were active at the start remain (the reference's "congested" state,
+    checked every `chunk` steps); returns (steps taken, agents active)."""
+    import torch
+    start = int((sim.state()[:, 3] != 0).sum())
+    done = 0
+    while done < cap:
+        with torch.cuda.stream(stream):
+            sim.step(chunk)
+        done += chunk
+        left = int((sim.state()[:, 3] != 0).sum())
+        if 2 * left <= start:
+            return done, left
+    return done, left
+
+
+def _seated_golden(name):
+    import zlib
+    from swarm_gb300 import venues
+    g = dict(np.load(os.path.join(ROOT, "tests", "golden", "seated_%s.npz" % name)))
+    delta = np.frombuffer(zlib.decompress(g["nav_anchor_delta_z"].tobytes()), np.int32)
+    info = np.frombuffer(zlib.decompress(g["nav_info_z"].tobytes()), np.uint32)
+    cells = venues.nav_cells_from_anchors(np.cumsum(delta.astype(np.int64)), info, g["nav_grid"])
+    return g, cells, info
+
+
 def bench_venue_l(steps=30, warmup=5):
     """The reference's own largest venue in reference-parity mode: seated venue L (63 424 seats in N = 65 536; the
     reference's layout, navigation field and full seat spawn from tests/golden/seated_L.npz, written by the unmodified
     reference), the reference's constants (model units, K = 32: 31 sweeps and the final pass), nearest exit at the level
-    speed, and again with the incline speed and stair spacing. CUDA events per step on the handle's stream, the L2
+    speed, and again with the incline speed and stair spacing; both from the spawn and, for the first, again once half
+    the crowd has left (the reference's "congested" state). CUDA events per step on the handle's stream, the L2
     flushed by a 256 MiB write before each step. The reference publishes its own GPU step on this venue and spawn
-    (OpenGL on an AMD RX 7800 XT, default model): 1.861 ms a step, of which 0.2039 ms is its queue-aware exit choice
-    (results/benchmarks/thesis/perf_tables.md:17, :45) -- a pass not run here."""
+    (OpenGL on an AMD RX 7800 XT, its default model): 1.861 ms a step from the spawn, 3.928 ms congested, of which
+    0.2039 / 0.4564 ms is its queue-aware exit choice (results/benchmarks/thesis/perf_tables.md:17-18, :45-46) -- a
+    pass not run on L here (its 904 MB candidate table is not part of the fixtures; venue S runs it)."""
     import zlib
     import torch
     import swarm_gb300
     from swarm_gb300 import venues
-    g = dict(np.load(os.path.join(ROOT, "tests", "golden", "seated_L.npz")))
-    delta = np.frombuffer(zlib.decompress(g["nav_anchor_delta_z"].tobytes()), np.int32)
-    info = np.frombuffer(zlib.decompress(g["nav_info_z"].tobytes()), np.uint32)
-    cells = venues.nav_cells_from_anchors(np.cumsum(delta.astype(np.int64)), info, g["nav_grid"])
+    g, cells, _ = _seated_golden("L")
     spawn = np.frombuffer(zlib.decompress(g["spawn_z"].tobytes()), np.float32).reshape(-1, 8).copy()
     gr = g["grid"]
     P = swarm_gb300.params_reference()
@@ -323,7 +368,8 @@ def bench_venue_l(steps=30, warmup=5):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     out = {"workload": "reference venue L (63424 seated of 65536), reference constants (model units, K=32), full seat "
                        "spawn (seed 1337)", "agents": int(spawn.shape[0]), "bytes_per_agent_step": b_step,
-           "published_reference_gpu": {"ms_per_step": 1.861, "exit_choice_ms": 0.2039,
+           "published_reference_gpu": {"ms_per_step": 1.861, "exit_choice_ms": 0.2039, "congested_ms_per_step": 3.928,
+                                       "congested_exit_choice_ms": 0.4564,
                                        "hardware": "AMD RX 7800 XT, OpenGL 4.3 (published, not measured here)"}}
     for label, incline in (("nearest_exit_level_speed", False), ("incline_speed_stair_spacing", True)):
         inc = g["incline"]
@@ -337,22 +383,65 @@ def bench_venue_l(steps=30, warmup=5):
         with torch.cuda.stream(stream):
             sim.step(warmup)
         torch.cuda.synchronize()
-        active, total = 0, 0.0
-        for k in range(steps):
-            active += int((sim.state()[:, 3] != 0).sum())
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            with torch.cuda.stream(stream):
-                flush.fill_(k & 0xFF)
-                e0.record(stream)
-                sim.step(1)
-                e1.record(stream)
-            stream.synchronize()
-            total += e0.elapsed_time(e1)
-        sim.synchronize()
-        sim.close()
+        active, total = _timed_steps(sim, stream, flush, steps)
         value = active / (total * 1e-3)
         out[label] = {"value": value, "unit": UNIT, "ms_per_step": total / steps, "steps": steps, "warmup": warmup,
                       "fraction_of_hbm_roofline": value * b_step / (peaks()[0] * 1e9)}
+        if not incline:
+            taken, left = _congest(sim, stream)
+            active, total = _timed_steps(sim, stream, flush, steps)
+            value = active / (total * 1e-3)
+            out[label]["congested"] = {"value": value, "unit": UNIT, "ms_per_step": total / steps, "steps": steps,
+                                       "after_steps": warmup + steps + taken, "active_agents": left}
+        sim.synchronize()
+        sim.close()
+    return out
+
+
+def bench_venue_s(steps=30, warmup=5):
+    """The reference's venue S under its default model -- the queue-aware exit choice on the reference's own candidate
+    table (tests/golden/seated_S_choice.npz), the incline speed and the stair spacing (EMPIRICAL) --, the model whose
+    250-step state the tests pin to the reference's hash: the full seat spawn (3 728 agents in N = 4 096), the
+    reference's constants, from the spawn and once half the crowd has left. Each timed step is the choice pass's
+    kernels and the step, CUDA events, the L2 flushed before each. The reference publishes its GPU step on this venue
+    and model (AMD RX 7800 XT): 0.6775 ms from the spawn, 1.278 ms congested, of which 0.0925 / 0.1777 ms is the exit
+    choice (results/benchmarks/thesis/perf_tables.md:13-14, :41-42)."""
+    import torch
+    import swarm_gb300
+    from swarm_gb300 import venues
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    from seated_choice import choice_index, decode_choice_entries
+    g, cells, info = _seated_golden("S")
+    c = dict(np.load(os.path.join(ROOT, "tests", "golden", "seated_S_choice.npz")))
+    meta = c["choice_meta"]
+    gr, inc = g["grid"], g["incline"]
+    venue = venues.Venue.seated(g["layout"], int(gr[0]), gr[1], gr[2], gr[3], gr[4], nav_cells=cells,
+                                nav_grid=g["nav_grid"], incline_speed=True, stair_times=(inc[4], inc[5]), name="S")
+    spawn = g["nearest_spawn"]
+    stream = torch.cuda.Stream()
+    sim = swarm_gb300.CrowdSim(swarm_gb300.params_reference(), venue, spawn.shape[0])
+    sim.set_stream(stream.cuda_stream)
+    sim.set_seated_choice(choice_index(info), decode_choice_entries(c), meta[3:3 + int(meta[0])], float(meta[1]),
+                          float(meta[2]), int(c["choice_grid"][2]))
+    sim.set_state(spawn)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    with torch.cuda.stream(stream):
+        sim.step(warmup)
+    torch.cuda.synchronize()
+    out = {"workload": "reference venue S (3728 seated of 4096), reference default model (queue-aware exit choice, "
+                       "incline speed, stair spacing EMPIRICAL), reference constants (K=32), full seat spawn (seed 1337)",
+           "published_reference_gpu": {"ms_per_step": 0.6775, "exit_choice_ms": 0.0925, "congested_ms_per_step": 1.278,
+                                       "congested_exit_choice_ms": 0.1777,
+                                       "hardware": "AMD RX 7800 XT, OpenGL 4.3 (published, not measured here)"}}
+    active, total = _timed_steps(sim, stream, flush, steps)
+    out["spawn"] = {"value": active / (total * 1e-3), "unit": UNIT, "ms_per_step": total / steps, "steps": steps,
+                    "warmup": warmup}
+    taken, left = _congest(sim, stream)
+    active, total = _timed_steps(sim, stream, flush, steps)
+    out["congested"] = {"value": active / (total * 1e-3), "unit": UNIT, "ms_per_step": total / steps, "steps": steps,
+                        "after_steps": warmup + steps + taken, "active_agents": left}
+    sim.synchronize()
+    sim.close()
     return out
 
 
@@ -563,7 +652,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
     ap.add_argument("--no-bowl", action="store_true", help="skip the seated-bowl measurement")
     ap.add_argument("--adjoint-steps", type=int, default=400, help="steps of the adjoint measurement (400: the workload)")
-    ap.add_argument("--only", choices=["adjoint", "bowl", "bowl_step", "batched", "navfield", "venue_l"], default=None,
+    ap.add_argument("--only", choices=["adjoint", "bowl", "bowl_step", "batched", "navfield", "venue_l", "venue_s"], default=None,
                     help="run only this sub-measurement and print its object (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -578,6 +667,7 @@ def main():
         fn = {"adjoint": lambda: bench_adjoint(P, steps=args.adjoint_steps), "bowl": lambda: bench_bowl(P),
               "batched": lambda: bench_batched(P),
               "navfield": lambda: bench_nav_field(bowl_venue()), "venue_l": lambda: bench_venue_l(),
+              "venue_s": lambda: bench_venue_s(),
               "bowl_step": lambda: bench_bowl(P, steps=10, evacuation=False)}[args.only]
         print(json.dumps({args.only: fn()}))
         return 0
@@ -797,6 +887,10 @@ def main():
                 line["reference_venue_L"] = bench_venue_l()
             except Exception as e:  # reported, not fatal
                 line["reference_venue_L"] = {"error": str(e)[:300]}
+            try:
+                line["reference_venue_S"] = bench_venue_s()
+            except Exception as e:  # reported, not fatal
+                line["reference_venue_S"] = {"error": str(e)[:300]}
         if not args.no_adjoint and world == 1:
             try:
                 line["adjoint"] = bench_adjoint(P, steps=args.adjoint_steps)

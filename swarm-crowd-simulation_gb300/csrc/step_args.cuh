@@ -100,6 +100,7 @@ struct StepArgs {
     int32_t hashed;         // fused step: the keys and counts of this step's input were counted by the last final pass
     int32_t hashNext;       // fused step: count the next step's keys in the final pass (the launch's last step)
     int32_t steps;          // fused step: steps in this launch (0 or 1: one), a grid barrier between them
+    int32_t sweepLanes;     // fused step: lanes per slot in the Jacobi sweeps (1, 2, 4, 8; set by the launcher)
     int32_t fusedThreads;   // fused step: threads per block (0: n / SMs rounded up to a warp, 128..512; 1024 a batch)
     int32_t fusedBlocksPerSm;   // fused step: at most this many blocks per SM (0: as many as fit)
     int32_t scanTile;       // fused step: cells per scan tile (set by the launcher: blockDim x 8, or x 16 on sparse

@@ -528,39 +528,36 @@ __device__ __forceinline__ void sweepRows(const StepArgs& A, const VenueArgs& V,
     }
 }
 
-// One Jacobi sweep of an unparked slot s at b (cpu_crowd_sim.cpp:781-822 projectSlot); w of the result: displacement
-template <class Venue, class Nbr, bool kTape = false>
-__device__ __forceinline__ float4 projectCore(const StepArgs& A, const Venue& ven, float4 b, int s, float ri,
-                                             const uint32_t* rk0, const uint32_t* rk1, float4 plane, const Nbr& nb,
-                                             float4* corrOut = nullptr) {
+// One neighbour k of slot s at b in a sweep (cpu_crowd_sim.cpp:793-812): whether they touch, and k's push on s
+template <class Venue, class Nbr>
+__device__ __forceinline__ bool pairPush(const StepArgs& A, float4 b, int s, float ri, uint32_t k, const Nbr& nb, f2& c) {
     constexpr bool kUniform = Body<Venue>::kUniform;
     const SwarmParams& P = A.P;
-    f2 corr{0.0f, 0.0f};
-    int nContacts = 0;
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-        for (uint32_t k = rk0[j]; k < rk1[j]; k++) {
-            if (int(k) == s) continue;
-            const float4 op = nb.pos(k);
-            const float rj = kUniform ? 0.0f : nb.r(k);
-            const f3 offset = xyz(b) - xyz(op);
-            float dc, dc2;
-            if (kUniform) { dc = P.body_diam; dc2 = P.body_diam2; }
-            else { dc = ri + rj; dc2 = dc * dc; }
-            const float dxy2 = dot(xy(offset), xy(offset));
-            if (op.w >= 0.0f && fabsf(offset.z) < dc && dxy2 < dc2) {
-                const float dxy = sqrtf(dxy2);
-                const float shift = 0.5f * (dc - dxy);
-                f2 c;
-                if (dxy2 <= P.stacked_xy2) c = shift * pairDirection(A.sid[s], A.sid[k], P.hash_to_radians);
-                else c = shift * (xy(offset) / dxy);
-                corr = corr + c;
-                ++nContacts;
-            }
-        }
-    }
+    const float4 op = nb.pos(k);
+    const float rj = kUniform ? 0.0f : nb.r(k);
+    const f3 offset = xyz(b) - xyz(op);
+    float dc, dc2;
+    if (kUniform) { dc = P.body_diam; dc2 = P.body_diam2; }
+    else { dc = ri + rj; dc2 = dc * dc; }
+    const float dxy2 = dot(xy(offset), xy(offset));
+    if (!(op.w >= 0.0f && fabsf(offset.z) < dc && dxy2 < dc2)) return false;
+    const float dxy = sqrtf(dxy2);
+    const float shift = 0.5f * (dc - dxy);
+    if (dxy2 <= P.stacked_xy2) c = shift * pairDirection(A.sid[s], A.sid[k], P.hash_to_radians);
+    else c = shift * (xy(offset) / dxy);
+    return true;
+}
+
+// The sweep's end for slot s (cpu_crowd_sim.cpp:813-822): the pushes' average relaxed, capped, the fence and the wall
+// plane; w of the result: displacement
+template <class Venue, bool kTape = false>
+__device__ __forceinline__ float4 projectFinish(const StepArgs& A, const Venue& ven, float4 b, f2 corr, int nContacts,
+                                               float4 plane, float4* corrOut) {
+    const SwarmParams& P = A.P;
     corr = corr * (P.proj_relax / float(smax(nContacts, 1)));
-    if constexpr (kTape) *corrOut = make_float4(corr.x, corr.y, float(nContacts), 0.0f);
+    if constexpr (kTape) {
+        if (corrOut) *corrOut = make_float4(corr.x, corr.y, float(nContacts), 0.0f);
+    }
     const float len = length(corr);
     if (len > P.proj_max_shift) corr = corr * (P.proj_max_shift / len);
     f3 q = xyz(b);
@@ -572,6 +569,59 @@ __device__ __forceinline__ float4 projectCore(const StepArgs& A, const Venue& ve
     }
     const f2 d = xy(q) - xy(b);
     return make_float4(q.x, q.y, b.z, b.w + length(d));
+}
+
+// One Jacobi sweep of an unparked slot s at b (cpu_crowd_sim.cpp:781-822 projectSlot); w of the result: displacement
+template <class Venue, class Nbr, bool kTape = false>
+__device__ __forceinline__ float4 projectCore(const StepArgs& A, const Venue& ven, float4 b, int s, float ri,
+                                             const uint32_t* rk0, const uint32_t* rk1, float4 plane, const Nbr& nb,
+                                             float4* corrOut = nullptr) {
+    f2 corr{0.0f, 0.0f};
+    int nContacts = 0;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        for (uint32_t k = rk0[j]; k < rk1[j]; k++) {
+            if (int(k) == s) continue;
+            f2 c;
+            if (pairPush<Venue>(A, b, s, ri, k, nb, c)) {
+                corr = corr + c;
+                ++nContacts;
+            }
+        }
+    }
+    return projectFinish<Venue, kTape>(A, ven, b, corr, nContacts, plane, corrOut);
+}
+
+// The same sweep by a group of G lanes (G = 2, 4, 8; the group's lanes adjacent, `sub` = the lane's index in it): the
+// lanes take the slot's candidates in turn -- candidate i of the rows' visiting order (rows y, then slots) by lane
+// i mod G -- and every lane folds the group's pushes of a round in candidate order (shuffles), so each lane adds the
+// same pushes in the reference's order. The whole warp calls it together; go: the slot is unparked.
+template <class Venue, class Nbr>
+__device__ __forceinline__ void pairSumLanes(const StepArgs& A, float4 b, int s, float ri, const uint32_t* rk0,
+                                             const uint32_t* rk1, const Nbr& nb, bool go, int G, int sub, int groupBase,
+                                             f2& corr, int& nContacts) {
+    const uint32_t c0 = go ? rk1[0] - rk0[0] : 0u, c1 = go ? rk1[1] - rk0[1] : 0u, c2 = go ? rk1[2] - rk0[2] : 0u;
+    const uint32_t total = c0 + c1 + c2;
+    const uint32_t rounds = __reduce_max_sync(0xffffffffu, (total + uint32_t(G) - 1u) / uint32_t(G));
+    corr = f2{0.0f, 0.0f};
+    nContacts = 0;
+    for (uint32_t r = 0; r < rounds; ++r) {
+        const uint32_t i = r * uint32_t(G) + uint32_t(sub);
+        f2 c{0.0f, 0.0f};
+        int hit = 0;
+        if (i < total) {
+            const uint32_t k = i < c0 ? rk0[0] + i : i < c0 + c1 ? rk0[1] + (i - c0) : rk0[2] + (i - c0 - c1);
+            if (int(k) != s && pairPush<Venue>(A, b, s, ri, k, nb, c)) hit = 1;
+        }
+        for (int t = 0; t < G; ++t) {
+            const float cx = __shfl_sync(0xffffffffu, c.x, groupBase + t);
+            const float cy = __shfl_sync(0xffffffffu, c.y, groupBase + t);
+            if (__shfl_sync(0xffffffffu, hit, groupBase + t)) {
+                corr = corr + f2{cx, cy};
+                ++nContacts;
+            }
+        }
+    }
 }
 
 // One Jacobi sweep for slot s reading `in` from global memory
@@ -846,18 +896,47 @@ __global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREA
             float4* corr = kTape ? A.tapeCorr + size_t(it - 1) * size_t(n) : nullptr;
             // The sweeps read their neighbours straight from L2 (and L1, which catches a block's reuse): staging a
             // tile window in shared memory and its two block barriers cost more than they save
-            for (int s = tid; s < nActive; s += stride) {
-                float4 b = src[s];
-                if (b.w >= 0.0f) {
-                    const uint4 ra = A.rowsA[s];
-                    const uint2 rb = A.rowsB[s];
-                    const uint32_t rk0[3] = {ra.x, ra.z, rb.x}, rk1[3] = {ra.y, ra.w, rb.y};
-                    const float ri = kUniform ? A.P.body_radius : A.prm[s].x;
-                    const Venue ven{A.P, venueOfSlot<kB>(A, s)};
-                    b = projectCore<Venue, GlobalNbr, kTape>(A, ven, b, s, ri, rk0, rk1, A.plane[s], GlobalNbr{src, A.prm},
-                                                             kTape ? corr + s : nullptr);
+            if (!kB && A.sweepLanes > 1) {   // a group of lanes per slot (few agents for the GPU: the launcher's choice)
+                const int G = A.sweepLanes, lane = int(threadIdx.x & 31u), sub = lane & (G - 1);
+                const int per = 32 / G, warps = stride >> 5;
+                for (int first = (tid >> 5) * per; first < nActive; first += warps * per) {   // warp-uniform
+                    const int s = first + lane / G;
+                    const bool own = s < nActive;
+                    float4 b = own ? src[s] : make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+                    const bool go = own && b.w >= 0.0f;
+                    uint32_t rk0[3] = {0u, 0u, 0u}, rk1[3] = {0u, 0u, 0u};
+                    float ri = 0.0f;
+                    if (go) {
+                        const uint4 ra = A.rowsA[s];
+                        const uint2 rb = A.rowsB[s];
+                        rk0[0] = ra.x; rk0[1] = ra.z; rk0[2] = rb.x;
+                        rk1[0] = ra.y; rk1[1] = ra.w; rk1[2] = rb.y;
+                        ri = kUniform ? A.P.body_radius : A.prm[s].x;
+                    }
+                    f2 push;
+                    int contacts;
+                    pairSumLanes<Venue>(A, b, s, ri, rk0, rk1, GlobalNbr{src, A.prm}, go, G, sub, lane - sub, push, contacts);
+                    if (go) {
+                        const Venue ven{A.P, venueOfSlot<kB>(A, s)};
+                        b = projectFinish<Venue, kTape>(A, ven, b, push, contacts, A.plane[s],
+                                                        kTape && sub == 0 ? corr + s : nullptr);
+                    }
+                    if (own && sub == 0) dst[s] = b;
                 }
-                dst[s] = b;
+            } else {
+                for (int s = tid; s < nActive; s += stride) {
+                    float4 b = src[s];
+                    if (b.w >= 0.0f) {
+                        const uint4 ra = A.rowsA[s];
+                        const uint2 rb = A.rowsB[s];
+                        const uint32_t rk0[3] = {ra.x, ra.z, rb.x}, rk1[3] = {ra.y, ra.w, rb.y};
+                        const float ri = kUniform ? A.P.body_radius : A.prm[s].x;
+                        const Venue ven{A.P, venueOfSlot<kB>(A, s)};
+                        b = projectCore<Venue, GlobalNbr, kTape>(A, ven, b, s, ri, rk0, rk1, A.plane[s],
+                                                                 GlobalNbr{src, A.prm}, kTape ? corr + s : nullptr);
+                    }
+                    dst[s] = b;
+                }
             }
             in ^= 1;
             if (!gridBarrier(A, gridDim.x)) return;
@@ -974,12 +1053,33 @@ static int smCount() {
     return sms[dev];
 }
 
-static int fusedThreads(const StepArgs& A) {
+// The block size, and the sweeps' lanes per slot: a group of 8, 4 or 2 lanes per slot when that many threads still fit
+// one block per SM (few agents for the GPU: each slot's candidate walk split over its group), else one; a tuned block
+// size keeps one lane per slot
+static void fusedShape(const StepArgs& A, int& threads, int& lanes) {
     const int sms = smCount();
-    int threads = A.fusedThreads > 0 ? A.fusedThreads : ((A.n + sms - 1) / sms + 31) / 32 * 32;
     const int cap = A.venueTable ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREADS;
-    threads = threads < 128 ? 128 : (threads > cap ? cap : threads);
-    return (threads + 31) / 32 * 32;
+    lanes = 1;
+    if (A.fusedThreads <= 0 && !A.venueTable) {
+        for (int g = 8; g > 1; g >>= 1) {
+            const long long t = ((static_cast<long long>(A.n) * g + sms - 1) / sms + 31) / 32 * 32;
+            if (t <= cap) {
+                lanes = g;
+                threads = t < 128 ? 128 : int(t);
+                return;
+            }
+        }
+    }
+    threads = A.fusedThreads > 0 ? A.fusedThreads : ((A.n + sms - 1) / sms + 31) / 32 * 32;
+    const int floor = A.fusedThreads > 0 ? 32 : 128;   // a tuned block may be a single warp
+    threads = threads < floor ? floor : (threads > cap ? cap : threads);
+    threads = (threads + 31) / 32 * 32;
+}
+
+static int fusedThreads(const StepArgs& A) {
+    int threads, lanes;
+    fusedShape(A, threads, lanes);
+    return threads;
 }
 
 // 8 counts a thread, or 16 where that would take more tiles than there are SMs (sparse venues)
@@ -1002,7 +1102,9 @@ static cudaError_t fusedImpl(const StepArgs& A0, cudaStream_t st) {
     }
     const int sms = smCount();
     StepArgs A = A0;
-    const int threads = fusedThreads(A);
+    int threads, lanes;
+    fusedShape(A, threads, lanes);
+    A.sweepLanes = lanes;
     A.scanTile = fusedScanTile(A);
     // the occupancy of the last block size asked for, per device
     static thread_local int occThreads[MAX_DEVICES], occPerSm[MAX_DEVICES];
@@ -1021,7 +1123,7 @@ static cudaError_t fusedImpl(const StepArgs& A0, cudaStream_t st) {
     if (A.fusedBlocksPerSm > 0 && A.fusedBlocksPerSm < perSm) perSm = A.fusedBlocksPerSm;
     const int resident = perSm * sms;
     if (resident <= 0) return cudaErrorCooperativeLaunchTooLarge;
-    const int want = blocks(A.n, threads);
+    const int want = int((static_cast<long long>(A.n) * lanes + threads - 1) / threads);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(unsigned(want < resident ? want : resident));
     cfg.blockDim = dim3(unsigned(threads));
