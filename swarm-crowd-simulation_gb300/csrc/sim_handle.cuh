@@ -42,6 +42,8 @@ struct SwarmSim {
     float2* goal = nullptr;
     int* errFlag = nullptr;
     int* errHost = nullptr;     // pinned host word: errFlag copied in stream order (swarm_step_host reads it after one sync)
+    int* errHostDev = nullptr;  // its device view: the fused launch of a host-buffer call writes the flag there itself
+    bool sumsZero = false;      // the scan-tile sums are all zero (cleared, or left so by a fused launch that counted nothing)
     unsigned* barrier = nullptr;
     unsigned long long* stamps = nullptr;
     bool fused = true;          // the whole step as one persistent kernel when the grid fits on the GPU
@@ -118,8 +120,9 @@ struct SwarmSim {
     // The per-phase path hashes from zeroed counts: drop what a fused final pass counted ahead (and its scan-tile sums)
     bool clearCounts() {
         counted = false;
-        return cudaMemsetAsync(count, 0, (size_t(ncells) + 1) * 4, stream) == cudaSuccess &&
-               cudaMemsetAsync(tileSums, 0, (size_t(ncells) / 1024 + 2) * 4, stream) == cudaSuccess;
+        sumsZero = cudaMemsetAsync(count, 0, (size_t(ncells) + 1) * 4, stream) == cudaSuccess &&
+                   cudaMemsetAsync(tileSums, 0, (size_t(ncells) / 1024 + 2) * 4, stream) == cudaSuccess;
+        return sumsZero;
     }
     void dropGraphs() {
         for (auto& g : graph) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
@@ -135,6 +138,15 @@ struct SwarmSim {
             cudaStreamSynchronize(stream) != cudaSuccess)
             return fail(SWARM_E_CUDA, "step sync");
         return *errHost ? deviceError(*errHost) : SWARM_OK;
+    }
+    // The same after a fused launch that mirrors the flag into errHost itself (set to ERR_PENDING before it): one
+    // stream sync; a launch that ended early left the mirror pending, and the flag is then read from the device
+    int finishWithMirror() {
+        if (cudaStreamSynchronize(stream) != cudaSuccess) return fail(SWARM_E_CUDA, "step sync");
+        int flag = *static_cast<volatile int*>(errHost);
+        if (flag == swarm_gpu::ERR_PENDING && cudaMemcpy(&flag, errFlag, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+            return fail(SWARM_E_CUDA, "error flag");
+        return flag ? deviceError(flag) : SWARM_OK;
     }
     int enqueueStages(int in, int s0, int s1);
     int captureStages(int in, int s0, int s1, cudaGraphExec_t* out);

@@ -16,6 +16,8 @@ enum : uint8_t { C_EXIT = 1, C_FENCE_CCD = 2, C_FENCE = 4, C_FLOOR = 8, C_WALL =
 
 // Device-side error flags (bit set by a kernel, read by the host after the step)
 enum : int { ERR_TIMEOUT = 1, ERR_BOUNDS = 2 };
+// errMirror's value before a launch that should write it: no combination of the flags above
+constexpr int ERR_PENDING = 0x40000000;
 
 struct VenueArgs {
     int32_t kind;
@@ -64,6 +66,9 @@ struct StepArgs {
     // stateIn; after the final pass (one more grid barrier) the blocks copy stateOut to hostOut in order
     const float4* hostIn;
     float4* hostOut;
+    // a pinned host word (device view; null: none) the last block to finish the launch sets to the error flag, so
+    // that a host-buffer call reads the flag without a copy; a launch that ends early leaves it as it was
+    int* errMirror;
     // queue-aware exit choice (null: off): each agent's assigned exit, whose own distance field (exitFields + exit x
     // navNodes, on the nav grid) gives its e_goal
     const uint32_t* choiceAssign;

@@ -977,13 +977,17 @@ __global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREA
         if (!gridBarrier(A, gridDim.x)) return;
         for (size_t k = size_t(tid); k < 2 * size_t(n); k += size_t(stride)) A.hostOut[k] = sOut[k];
     }
-    if (A.stamps) {   // the end: the last block out records it
+    if (A.stamps || A.errMirror) {   // the end: the last block out records it, and the launch's error flag
         __syncthreads();
         if (threadIdx.x == 0) {
             __threadfence();
             cuda::atomic_ref<unsigned, cuda::thread_scope_device> done(A.barrier[2]);
             if (done.fetch_add(1u, cuda::memory_order_acq_rel) == gridDim.x - 1) {
-                A.stamps[4] = globalNs();
+                if (A.stamps) A.stamps[4] = globalNs();
+                if (A.errMirror) {
+                    const int flag = cuda::atomic_ref<int, cuda::thread_scope_device>(*A.err).load(cuda::memory_order_relaxed);
+                    cuda::atomic_ref<int, cuda::thread_scope_system>(*A.errMirror).store(flag, cuda::memory_order_release);
+                }
                 done.store(0u, cuda::memory_order_relaxed);
             }
         }

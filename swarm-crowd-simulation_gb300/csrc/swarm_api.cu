@@ -58,6 +58,7 @@ int SwarmSim::deviceError(int flag) {
     cudaMemset(barrier, 0, 16);   // a barrier that gave up leaves its counter behind
     cudaMemset(count, 0, (size_t(ncells) + 1) * 4);
     counted = false;
+    sumsZero = false;   // a launch that gave up may have left tile sums behind
     if (flag & 1) return fail(SWARM_E_TIMEOUT, "a device-side wait gave up (flag " + std::to_string(flag) + ")");
     return fail(SWARM_E_CUDA, "a device-side bounds check failed (flag " + std::to_string(flag) + ")");
 }
@@ -200,7 +201,8 @@ int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capac
               devAlloc(h, &h->proj1, N) && devAlloc(h, &h->vel1, N) && devAlloc(h, &h->plane, N) && devAlloc(h, &h->prm, N) &&
               devAlloc(h, &h->ctc, N) && devAlloc(h, &h->rowsA, N) && devAlloc(h, &h->rowsB, N) &&
               devAlloc(h, &h->goal, N) && devAlloc(h, &h->errFlag, 1) && devAlloc(h, &h->barrier, 4) && devAlloc(h, &h->stamps, 8) &&
-              cudaHostAlloc(reinterpret_cast<void**>(&h->errHost), sizeof(int), cudaHostAllocDefault) == cudaSuccess;
+              cudaHostAlloc(reinterpret_cast<void**>(&h->errHost), sizeof(int), cudaHostAllocMapped) == cudaSuccess &&
+              cudaHostGetDevicePointer(reinterpret_cast<void**>(&h->errHostDev), h->errHost, 0) == cudaSuccess;
     if (ok && V.kind == SWARM_VENUE_STADIUM) {
         const size_t nv = size_t(V.sdf_res) * size_t(V.sdf_res) * size_t(V.sdf_res);
         ok = devAlloc(h, &h->dSdf, nv) && cudaMemcpy(h->dSdf, V.sdf, nv * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
@@ -595,13 +597,17 @@ static int stepImpl(SwarmHandle h, int steps, bool countLast) {
             // the counts (and their scan-tile sums) carried from the last fused step, if its tile matches this one's
             const int tile = swarm_gpu::fusedScanTile(A);
             if (h->counted && tile != h->countedTile && !h->clearCounts()) return SWARM_E_CUDA;
-            if (!h->counted && !cudaOk(h, cudaMemsetAsync(h->tileSums, 0, (size_t(h->ncells) / 1024 + 2) * 4, h->stream), "tile sums"))
-                return SWARM_E_CUDA;
+            if (!h->counted && !h->sumsZero) {
+                if (!cudaOk(h, cudaMemsetAsync(h->tileSums, 0, (size_t(h->ncells) / 1024 + 2) * 4, h->stream), "tile sums"))
+                    return SWARM_E_CUDA;
+                h->sumsZero = true;
+            }
             A.hashed = h->counted ? 1 : 0;
             A.hashNext = (countLast || s + chunk < steps) ? 1 : 0;
             A.steps = chunk;
             A.hostIn = s == 0 ? h->hostIn : nullptr;
             A.hostOut = s + chunk == steps ? h->hostOut : nullptr;
+            A.errMirror = A.hostOut ? h->errHostDev : nullptr;
             if (A.hostIn && A.hashed) return h->fail(SWARM_E_STATE, "a host input needs the hash phase (counts left over)");
             // one step from counted keys, with counting, no host buffers and nothing timed: replayed from a graph
             // (one per state half) when graphs are on
@@ -624,29 +630,32 @@ static int stepImpl(SwarmHandle h, int steps, bool countLast) {
             }
             h->barrierExtra = 0;
             h->counted = A.hashNext != 0;
+            h->sumsZero = !h->counted;   // the launch clears the sums after its scans and adds none at its end
             h->countedTile = tile;
             if (h->timing && !cudaOk(h, cudaEventRecord(h->ev[4], h->stream), "event")) return SWARM_E_CUDA;
             h->launches += 1;
-        } else if (h->counted && !h->clearCounts()) {
-            return SWARM_E_CUDA;
-        } else if (h->useGraph && !h->timing) {
-            if (!h->graph[in] && h->captureStages(in, 0, 4, &h->graph[in]) != SWARM_OK) return SWARM_E_CUDA;
-            if (!cudaOk(h, cudaGraphLaunch(h->graph[in], h->stream), "graph launch")) return SWARM_E_CUDA;
-            h->launches += perStep;
         } else {
-            for (int st = 0; st < 4; ++st) {
-                if (h->timing && !cudaOk(h, cudaEventRecord(h->ev[st], h->stream), "event")) return SWARM_E_CUDA;
-                if (h->useGraph) {
-                    if (!h->stageGraph[in][st] && h->captureStages(in, st, st + 1, &h->stageGraph[in][st]) != SWARM_OK)
-                        return SWARM_E_CUDA;
-                    if (!cudaOk(h, cudaGraphLaunch(h->stageGraph[in][st], h->stream), "graph launch")) return SWARM_E_CUDA;
-                } else {
-                    const int rc = h->enqueueStages(in, st, st + 1);
-                    if (rc != SWARM_OK) return rc;
+            if (h->counted && !h->clearCounts()) return SWARM_E_CUDA;
+            h->sumsZero = false;   // the per-phase scan writes tile sums
+            if (h->useGraph && !h->timing) {
+                if (!h->graph[in] && h->captureStages(in, 0, 4, &h->graph[in]) != SWARM_OK) return SWARM_E_CUDA;
+                if (!cudaOk(h, cudaGraphLaunch(h->graph[in], h->stream), "graph launch")) return SWARM_E_CUDA;
+                h->launches += perStep;
+            } else {
+                for (int st = 0; st < 4; ++st) {
+                    if (h->timing && !cudaOk(h, cudaEventRecord(h->ev[st], h->stream), "event")) return SWARM_E_CUDA;
+                    if (h->useGraph) {
+                        if (!h->stageGraph[in][st] && h->captureStages(in, st, st + 1, &h->stageGraph[in][st]) != SWARM_OK)
+                            return SWARM_E_CUDA;
+                        if (!cudaOk(h, cudaGraphLaunch(h->stageGraph[in][st], h->stream), "graph launch")) return SWARM_E_CUDA;
+                    } else {
+                        const int rc = h->enqueueStages(in, st, st + 1);
+                        if (rc != SWARM_OK) return rc;
+                    }
                 }
+                if (h->timing && !cudaOk(h, cudaEventRecord(h->ev[4], h->stream), "event")) return SWARM_E_CUDA;
+                if (h->useGraph) h->launches += perStep;
             }
-            if (h->timing && !cudaOk(h, cudaEventRecord(h->ev[4], h->stream), "event")) return SWARM_E_CUDA;
-            if (h->useGraph) h->launches += perStep;
         }
         if (h->metricRes && h->enqueueMetrics(in) != SWARM_OK) return SWARM_E_CUDA;
         h->readIdx ^= chunk & 1;
@@ -797,12 +806,14 @@ int swarm_step_host(SwarmHandle h, const float* in_boids, float* out_boids, int 
     if (dIn && dOut) {
         h->hostIn = dIn;
         h->hostOut = dOut;
+        *static_cast<volatile int*>(h->errHost) = swarm_gpu::ERR_PENDING;   // the last launch's last block sets it
         const int rc = stepImpl(h, steps, false);
         h->hostIn = nullptr;
         h->hostOut = nullptr;
         if (rc != SWARM_OK) return rc;
-        // a barrier that gave up ends the launch before the output copy: the device flag says so
-        return h->finishWithFlag();
+        // a barrier that gave up ends the launch before the output copy: the flag says so (read from the device when the
+        // launch ended before it could write the mirror)
+        return h->finishWithMirror();
     }
     // the read half only: the final pass writes every agent of the other half
     if (!cudaOk(h, cudaMemcpyAsync(h->state[h->readIdx], in_boids, bytes, cudaMemcpyHostToDevice, h->stream), "upload")) return SWARM_E_CUDA;
