@@ -95,3 +95,22 @@ def test_step_host_in_place_and_continued_on_the_device(scene):
     sim.step(2)
     assert np.array_equal(_bits(sim.state()), _bits(ref))
     sim.close()
+
+
+def test_step_host_pinned_buffers_off_the_32_byte_grid(scene):
+    """Pinned buffers whose rows start 16 bytes off a 32-byte boundary (rows split across the host link's 32-byte
+    sectors): the same bits."""
+    import torch
+    import swarm_gb300
+    P, venue, b, r, v0 = scene
+    n = b.shape[0]
+    ref = _device_reference(P, venue, b, r, v0, 2)
+    sim = swarm_gb300.CrowdSim(P, venue, n)
+    sim.set_agent_params(r, v0)
+    h_in = torch.zeros(n * 8 + 4, dtype=torch.float32).pin_memory()
+    h_out = torch.zeros(n * 8 + 4, dtype=torch.float32).pin_memory()
+    assert h_in.data_ptr() % 32 == 0 and h_out.data_ptr() % 32 == 0
+    h_in[4:] = torch.from_numpy(b.reshape(-1))
+    sim.step_host(h_in.data_ptr() + 16, h_out.data_ptr() + 16, n, 2)
+    assert np.array_equal(_bits(h_out[4:].numpy().reshape(n, 8)), _bits(ref))
+    sim.close()
