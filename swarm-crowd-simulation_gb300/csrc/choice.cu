@@ -53,11 +53,33 @@ struct SeatedCands {
     }
 };
 
-__device__ __forceinline__ SeatedCands seatedCands(const VenueArgs& V, const ChoiceArgs& C, float4 p) {
-    const SeatedChoice sc{SeatedNav{SeatedGeom{V.seatDev}, StepUpConst{C.suSample, C.suTol, C.suMax}, 0.0f, 0.0f, 0.0f,
-                                    nullptr, V.navRes, V.navOrigin, V.navCell, V.navInv},
-                          C.chIndex, C.chEntries};
-    return SeatedCands{sc.entry(sc.cellOf(f2{p.x, p.y}))};
+__device__ __forceinline__ SeatedChoice seatedChoice(const VenueArgs& V, const ChoiceArgs& C) {
+    return SeatedChoice{SeatedNav{SeatedGeom{V.seatDev}, StepUpConst{C.suSample, C.suTol, C.suMax}, 0.0f, 0.0f, 0.0f,
+                                  nullptr, V.navRes, V.navOrigin, V.navCell, V.navInv},
+                        C.chIndex, C.chEntries};
+}
+
+// The agent's start position as the step's hash leaves it (a NaN position: (0, 0, 0, 1)): the reference's choice pass
+// runs after the hash
+__device__ __forceinline__ float4 choicePos(const ChoiceArgs& C, int i) {
+    const float4 p = C.state[2 * size_t(i)];
+    return isnan(p.x) ? make_float4(0.0f, 0.0f, 0.0f, 1.0f) : p;
+}
+
+// Each agent's choice cell (choiceCell, src/exit_choice.cpp:512-548) into chCell, by 8 lanes an agent (the surface
+// rule's step-up scans shared out): the stages and the step's e_goal read it instead of each finding it again
+constexpr int CHOICE_CELL_LANES = 8;
+__global__ void __launch_bounds__(256) k_choice_cell(ChoiceArgs C, VenueArgs V) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = t / CHOICE_CELL_LANES, sub = t % CHOICE_CELL_LANES;
+    const float4 p = i < C.n ? choicePos(C, i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const bool act = i < C.n && p.w != 0.0f;
+    const int cell = choiceCellLanes(seatedChoice(V, C), f2{p.x, p.y}, act, CHOICE_CELL_LANES, sub);
+    if (i < C.n && sub == 0) C.chCell[i] = act ? cell : -1;
+}
+
+__device__ __forceinline__ SeatedCands seatedCands(const VenueArgs& V, const ChoiceArgs& C, int i) {
+    return SeatedCands{seatedChoice(V, C).entry(C.chCell[i])};
 }
 
 // slotDist (exit_choice.hpp:172-175): q x quantum, exact in float (an empty slot: +infinity, never read here)
@@ -88,9 +110,8 @@ __device__ __forceinline__ int seatedBest(const ChoiceArgs& C, const SeatedCands
 // nav::evaluate for agent i (from its start-of-step position; an evacuated agent: none)
 __device__ __forceinline__ void seatedEvalAgent(const VenueArgs& V, const ChoiceArgs& C, int i) {
     C.pending[i] = make_uint2(SWARM_CHOICE_NONE, 0u);
-    const float4 p = C.state[2 * size_t(i)];
-    if (p.w == 0.0f) return;
-    const SeatedCands c = seatedCands(V, C, p);
+    if (choicePos(C, i).w == 0.0f) return;
+    const SeatedCands c = seatedCands(V, C, i);
     if (c.exit(0) == CHOICE_SLOT_EMPTY) return;
     const uint32_t cur = C.assign[i];
     const int curK = c.slotOf(cur);
@@ -113,9 +134,8 @@ __device__ __forceinline__ void seatedEvalAgent(const VenueArgs& V, const Choice
 // nav::apply for agent i, then its counts (choiceStep :743-760): its exit's queue (the block's shared counts), and the
 // key of its queue-ahead count at its own distance to that exit (all ones: none)
 __device__ __forceinline__ uint32_t seatedApplyAgent(const VenueArgs& V, const ChoiceArgs& C, int i, uint32_t* sQueue) {
-    const float4 p = C.state[2 * size_t(i)];
-    if (p.w == 0.0f) return 0xFFFFFFFFu;
-    const SeatedCands c = seatedCands(V, C, p);
+    if (choicePos(C, i).w == 0.0f) return 0xFFFFFFFFu;
+    const SeatedCands c = seatedCands(V, C, i);
     const uint32_t* aRead = C.ahead + size_t(C.step & 1u) * CHOICE_STRIDE * CHOICE_AHEAD_BINS;
     const uint32_t cur = C.assign[i];
     uint32_t ex = cur;
@@ -271,7 +291,7 @@ void SwarmSim::freeChoice() {
     dExitFields = nullptr; dChoiceExit = nullptr; dChoiceDist = nullptr; dChoiceInvCap = nullptr; dAssign = nullptr;
     dPending = nullptr; dChoiceHist = nullptr; dChoiceThr = nullptr; dChoiceQueue = nullptr; dChoiceAhead = nullptr;
     dChoiceCounters = nullptr;
-    dChIndex = nullptr; dChEntries = nullptr; chSPerUnit = 0.0f; chQuantum = 0.0f; choiceEvery = 0;
+    dChIndex = nullptr; dChEntries = nullptr; dChCell = nullptr; chSPerUnit = 0.0f; chQuantum = 0.0f; choiceEvery = 0;
 }
 
 std::vector<std::pair<void*, size_t>> SwarmSim::choiceLive() const {
@@ -296,7 +316,7 @@ ChoiceArgs choiceArgsOf(const SwarmSim& s, int in) {
     C.cExit = s.dChoiceExit; C.cDist = s.dChoiceDist; C.invCap = s.dChoiceInvCap;
     C.assign = s.dAssign; C.pending = s.dPending; C.hist = s.dChoiceHist; C.threshold = s.dChoiceThr;
     C.queue = s.dChoiceQueue; C.ahead = s.dChoiceAhead; C.counters = s.dChoiceCounters;
-    C.chIndex = s.dChIndex; C.chEntries = s.dChEntries; C.sPerUnit = s.chSPerUnit; C.quantum = s.chQuantum;
+    C.chIndex = s.dChIndex; C.chEntries = s.dChEntries; C.chCell = s.dChCell; C.sPerUnit = s.chSPerUnit; C.quantum = s.chQuantum;
     C.suSample = s.P.step_up_sample; C.suTol = s.P.step_up_tol; C.suMax = s.P.step_up_max_samples;
     return C;
 }
@@ -308,6 +328,11 @@ int SwarmSim::enqueueChoice(int in) {
     const swarm_gpu::VenueArgs V = args(in).V;
     const int blocks = (n + 255) / 256;
     swarm_gpu::k_choice_prefix<<<choiceExits, swarm_gpu::CHOICE_PREFIX_THREADS, 0, stream>>>(C, V);
+    if (C.chIndex) {
+        const long long lanes = static_cast<long long>(n) * swarm_gpu::CHOICE_CELL_LANES;
+        swarm_gpu::k_choice_cell<<<unsigned((lanes + 255) / 256), 256, 0, stream>>>(C, V);
+        ++launches;
+    }
     if (C.evalStep) {
         swarm_gpu::k_choice_eval<<<blocks, 256, 0, stream>>>(C, V);
         swarm_gpu::k_choice_thr<<<choiceExits, 32, 0, stream>>>(C, V);
@@ -402,6 +427,7 @@ extern "C" int swarm_set_seated_choice(SwarmHandle h, const SwarmSeatedChoiceSpe
         return true;
     };
     const bool ok = alloc(&h->dChIndex, cells * 4) && alloc(&h->dChEntries, ne * sizeof(SwarmNavChoiceCell)) &&
+                    alloc(&h->dChCell, N * 4) &&
                     alloc(&h->dChoiceInvCap, size_t(E) * 4) && alloc(&h->dAssign, N * 4) && alloc(&h->dPending, N * 8) &&
                     alloc(&h->dChoiceHist, size_t(E) * swarm_gpu::CHOICE_GAIN_BINS * 4) &&
                     alloc(&h->dChoiceThr, size_t(swarm_gpu::CHOICE_STRIDE) * 4) &&

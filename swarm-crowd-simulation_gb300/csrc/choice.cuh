@@ -36,6 +36,7 @@ struct ChoiceArgs {
     // constants of the choice cell's surface rule
     const uint32_t* chIndex;
     const uint32_t* chEntries;
+    int32_t* chCell;              // per agent: its choice cell this step (k_choice_cell)
     float sPerUnit, quantum;
     float suSample, suTol;
     int32_t suMax;

@@ -106,6 +106,7 @@ struct SwarmSim {
     // between evaluations (0: from dt, the grid venues' 3 s)
     uint32_t* dChIndex = nullptr;
     uint32_t* dChEntries = nullptr;
+    int32_t* dChCell = nullptr;             // per agent: its choice cell this step
     float chSPerUnit = 0.0f, chQuantum = 0.0f;
     int32_t choiceEvery = 0;
     std::vector<void*> choiceAllocs;

@@ -72,6 +72,7 @@ struct StepArgs {
     // queue-aware exit choice (null: off): each agent's assigned exit, whose own distance field (exitFields + exit x
     // navNodes, on the nav grid) gives its e_goal
     const uint32_t* choiceAssign;
+    const int32_t* choiceCell;   // a seated venue's table: each agent's choice cell at the step's start (the choice pass's)
     const float* exitFields;
     uint32_t navNodes;
     const float2* aparam;   // (radius, v0) per agent

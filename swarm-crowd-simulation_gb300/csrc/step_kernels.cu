@@ -314,8 +314,8 @@ __device__ __forceinline__ f2 goalOf(const StepArgs& A, const Venue& ven, f3 p, 
     }
     if constexpr (std::is_same<Venue, Seated>::value) {
         // the reference's table: its goal whatever the assignment (none yet: no candidate matches, e_goal 0 but the
-        // wall rule)
-        if (A.choiceAssign && ven.V.choiceIndex) return ven.choiceGoal(p, A.choiceAssign[id]);
+        // wall rule), in the choice cell the step's choice pass found for this position
+        if (A.choiceAssign && ven.V.choiceIndex) return ven.choiceGoalCell(p, A.choiceAssign[id], A.choiceCell[id]);
     }
     return ven.goal(p);
 }

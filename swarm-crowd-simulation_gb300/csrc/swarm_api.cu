@@ -103,6 +103,7 @@ StepArgs SwarmSim::args(int in) const {
     A.vel1 = vel1; A.plane = plane; A.ctc = ctc; A.rowsA = rowsA; A.rowsB = rowsB; A.goal = goal; A.err = errFlag; A.barrier = barrier; A.barrierExtra = barrierExtra;
     A.stamps = timing ? stamps : nullptr;
     A.choiceAssign = choiceExits ? dAssign : nullptr;
+    A.choiceCell = dChCell;
     A.exitFields = dExitFields;
     A.navNodes = uint32_t(size_t(V.nav_nx) * size_t(V.nav_ny));
     A.fusedThreads = tuning.threads;

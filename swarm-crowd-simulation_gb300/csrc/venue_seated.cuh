@@ -697,10 +697,16 @@ struct SeatedChoice {
     }
     // choiceCell (:512-548): the cell containing x; a NOFIT cell takes the FIT cell with candidates of its 3 x 3 ring
     // whose centre is nearest, else of the 5 x 5 ring's outer cells; then the surface rule over the 3 x 3 cells
+    SWARM_HD __forceinline__ bool fitPath(int j) const { return fit(j) && reachable(j); }
     SWARM_HD __noinline__ int cellOf(f2 x) const {
         const int res = nav.res;
         const f2 g{(x.x - nav.origin) * nav.inv, (x.y - nav.origin) * nav.inv};
         const int cx = sclamp(int(floorf(g.x)), 0, res - 1), cy = sclamp(int(floorf(g.y)), 0, res - 1);
+        const int i = ringPick(g, cx, cy);
+        return surfacePick(x, g, cx, cy, i);
+    }
+    SWARM_HD __forceinline__ int ringPick(f2 g, int cx, int cy) const {
+        const int res = nav.res;
         int i = cx + cy * res;
         if (!fit(i)) {
             float best = 1e9f;
@@ -717,29 +723,33 @@ struct SeatedChoice {
                         if (d2 < best) { best = d2; i = j; }
                     }
         }
-        if (!nav.reaches(x, nav.cellCentre(i))) {
-            float best = 1e9f;
-            int pick = i;
-            for (int dy = -1; dy <= 1; dy++)
-                for (int dx = -1; dx <= 1; dx++) {
-                    const int mx = cx + dx, my = cy + dy;
-                    if (mx < 0 || my < 0 || mx >= res || my >= res) continue;
-                    const int j = mx + my * res;
-                    if (j == i || !fit(j) || !reachable(j)) continue;
-                    const f2 q{g.x - (float(mx) + 0.5f), g.y - (float(my) + 0.5f)};
-                    const float d2 = q.x * q.x + q.y * q.y;
-                    if (d2 < best && nav.reaches(x, nav.cellCentre(j))) { best = d2; pick = j; }
-                }
-            i = pick;
-        }
         return i;
+    }
+    SWARM_HD __forceinline__ int surfacePick(f2 x, f2 g, int cx, int cy, int i) const {
+        const int res = nav.res;
+        if (nav.reaches(x, nav.cellCentre(i))) return i;
+        float best = 1e9f;
+        int pick = i;
+        for (int dy = -1; dy <= 1; dy++)
+            for (int dx = -1; dx <= 1; dx++) {
+                const int mx = cx + dx, my = cy + dy;
+                if (mx < 0 || my < 0 || mx >= res || my >= res) continue;
+                const int j = mx + my * res;
+                if (j == i || !fitPath(j)) continue;
+                const f2 q{g.x - (float(mx) + 0.5f), g.y - (float(my) + 0.5f)};
+                const float d2 = q.x * q.x + q.y * q.y;
+                if (d2 < best && nav.reaches(x, nav.cellCentre(j))) { best = d2; pick = j; }
+            }
+        return pick;
     }
     // choiceDirection / choiceGoal (:557-578): towards the anchor of the exit's own field in x's choice cell (its centre
     // in float, anchorCentre :550-555), 0 within the dead zone or when the exit is no candidate there; the component
     // into a wall or step face beside the agent removed
-    SWARM_HD __noinline__ f2 goal(f3 p, uint32_t exit) const {
+    SWARM_HD __noinline__ f2 goal(f3 p, uint32_t exit) const { return goalFromCell(p, exit, cellOf(xy(p))); }
+    // the same for an agent whose choice cell is known (the choice pass's, for the same position)
+    SWARM_HD __noinline__ f2 goalFromCell(f3 p, uint32_t exit, int cell_) const {
         const f2 x = xy(p);
-        const uint32_t* c = entry(cellOf(x));
+        const uint32_t* c = entry(cell_);
         f2 e{0.0f, 0.0f};
         if (c) {
             for (int k = 0; k < 24; ++k) {
@@ -764,6 +774,51 @@ struct SeatedChoice {
         return e;
     }
 };
+
+#ifdef __CUDACC__
+// choiceCell by a lane group (G lanes, sub the lane's index in it, the group's lanes adjacent; the whole warp calls it
+// together): the ring's pick and its surface check by the group's first lane; only when the agent may not walk straight
+// to the pick's centre, the rule's other reach checks -- each of the 3 x 3 cells (t = 3 (dy + 1) + dx + 1) it may visit
+// -- shared out over the lanes (check t by lane t mod G), their bits combined over the group, and the rule's choice
+// made from them in its own order: the cell cellOf gives. act: the lane's agent takes part (the others only join the
+// shuffles).
+__device__ __forceinline__ int choiceCellLanes(const SeatedChoice& sc, f2 x, bool act, int G, int sub) {
+    const SeatedNav& nav = sc.nav;
+    const int res = nav.res;
+    const int base = int(threadIdx.x & 31u) - sub;
+    const f2 g{(x.x - nav.origin) * nav.inv, (x.y - nav.origin) * nav.inv};
+    const int cx = sclamp(int(floorf(g.x)), 0, res - 1), cy = sclamp(int(floorf(g.y)), 0, res - 1);
+    const int i = act ? sc.ringPick(g, cx, cy) : cx + cy * res;
+    int direct = 1;
+    if (act && sub == 0) direct = nav.reaches(x, nav.cellCentre(i)) ? 1 : 0;
+    direct = __shfl_sync(0xffffffffu, direct, base);
+    const bool search = act && !direct;
+    uint32_t bits = 0u;
+    if (search) {
+        for (int t = sub; t < 9; t += G) {
+            const int mx = cx + t % 3 - 1, my = cy + t / 3 - 1;
+            if (mx < 0 || my < 0 || mx >= res || my >= res) continue;
+            const int j = mx + my * res;
+            if (j == i || !sc.fitPath(j)) continue;
+            if (nav.reaches(x, nav.cellCentre(j))) bits |= 1u << t;
+        }
+    }
+    for (int o = 1; o < G; o <<= 1) bits |= __shfl_xor_sync(0xffffffffu, bits, o);   // (aligned groups: partners inside)
+    if (!search) return i;
+    float best = 1e9f;
+    int pick = i;
+    for (int t = 0; t < 9; ++t) {
+        const int mx = cx + t % 3 - 1, my = cy + t / 3 - 1;
+        if (mx < 0 || my < 0 || mx >= res || my >= res) continue;
+        const int j = mx + my * res;
+        if (j == i || !sc.fitPath(j)) continue;
+        const f2 q{g.x - (float(mx) + 0.5f), g.y - (float(my) + 0.5f)};
+        const float d2 = q.x * q.x + q.y * q.y;
+        if (d2 < best && (bits >> t & 1u)) { best = d2; pick = j; }
+    }
+    return pick;
+}
+#endif
 
 struct Seated {
     const SwarmParams& P;
@@ -954,6 +1009,11 @@ struct Seated {
     }
     // e_goal under the queue-aware exit choice: the assigned exit's anchor in the agent's choice cell
     // (cpu_crowd_sim.cpp:214, nav::choiceGoal)
+    __device__ __forceinline__ f2 choiceGoalCell(f3 p, uint32_t exit, int cell) const {
+        return SeatedChoice{SeatedNav{geo(), stepUp(), P.goal_deadzone, P.feeler_reach, P.safe_eps, nullptr, V.navRes,
+                                      V.navOrigin, V.navCell, V.navInv},
+                            V.choiceIndex, V.choiceEntries}.goalFromCell(p, exit, cell);
+    }
     __device__ __forceinline__ f2 choiceGoal(f3 p, uint32_t exit) const {
         return SeatedChoice{SeatedNav{geo(), stepUp(), P.goal_deadzone, P.feeler_reach, P.safe_eps, nullptr, V.navRes,
                                       V.navOrigin, V.navCell, V.navInv},
