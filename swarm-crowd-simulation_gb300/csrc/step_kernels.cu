@@ -594,8 +594,8 @@ __device__ __forceinline__ float4 projectCore(const StepArgs& A, const Venue& ve
 
 // The same sweep by a group of G lanes (G = 2, 4, 8; the group's lanes adjacent, `sub` = the lane's index in it): the
 // lanes take the slot's candidates in turn -- candidate i of the rows' visiting order (rows y, then slots) by lane
-// i mod G -- and every lane folds the group's pushes of a round in candidate order (shuffles), so each lane adds the
-// same pushes in the reference's order. The whole warp calls it together; go: the slot is unparked.
+// i mod G -- and every lane folds the group's touching pushes of a round in candidate order (ballot, shuffles), so
+// each lane adds the same pushes in the reference's order. The whole warp calls it together; go: the slot is unparked.
 template <class Venue, class Nbr>
 __device__ __forceinline__ void pairSumLanes(const StepArgs& A, float4 b, int s, float ri, const uint32_t* rk0,
                                              const uint32_t* rk1, const Nbr& nb, bool go, int G, int sub, int groupBase,
@@ -613,13 +613,17 @@ __device__ __forceinline__ void pairSumLanes(const StepArgs& A, float4 b, int s,
             const uint32_t k = i < c0 ? rk0[0] + i : i < c0 + c1 ? rk0[1] + (i - c0) : rk0[2] + (i - c0 - c1);
             if (int(k) != s && pairPush<Venue>(A, b, s, ri, k, nb, c)) hit = 1;
         }
-        for (int t = 0; t < G; ++t) {
-            const float cx = __shfl_sync(0xffffffffu, c.x, groupBase + t);
-            const float cy = __shfl_sync(0xffffffffu, c.y, groupBase + t);
-            if (__shfl_sync(0xffffffffu, hit, groupBase + t)) {
-                corr = corr + f2{cx, cy};
-                ++nContacts;
-            }
+        // the group's touching candidates of the round, lowest lane (= candidate order) first; the loop is the same for
+        // every lane of the group, so its shuffles name the group's lanes alone
+        const unsigned gmask = (G == 32 ? 0xffffffffu : (1u << G) - 1u) << groupBase;
+        unsigned m = __ballot_sync(0xffffffffu, hit != 0) & gmask;
+        while (m) {
+            const int t = __ffs(m) - 1;
+            const float cx = __shfl_sync(gmask, c.x, t);
+            const float cy = __shfl_sync(gmask, c.y, t);
+            corr = corr + f2{cx, cy};
+            ++nContacts;
+            m &= m - 1u;
         }
     }
 }
