@@ -123,6 +123,104 @@ void fastMarchCpu(int nx, int ny, double h, std::vector<uint8_t> state, const fl
     for (size_t k = 0; k < M; ++k) out[k] = float(state[k] == 2 ? D[k] : maxFree + 10.0);
 }
 
+// Runs f(j) for j in [0, n) over the host's threads
+template <class F>
+void parallelRows(int n, F f) {
+    const int t = std::max(1, std::min(int(std::thread::hardware_concurrency()), 32));
+    std::vector<std::thread> pool;
+    for (int i = 0; i < t; ++i)
+        pool.emplace_back([&, i] { for (int j = i; j < n; j += t) f(j); });
+    for (auto& th : pool) th.join();
+}
+
+// The blocked band of a nav field: the wall nodes (kind 3: the walls and the clearance around them) within maxDist of a
+// node the solver reached get the value of the nearest reached node (Euclidean, over node centres) plus k x that
+// distance, instead of the solver's plain fill (largest reached value + 10 m). Beside a
+// wall's clearance band the field then rises gently into the band: its normalised negative gradient keeps the
+// route's direction with a push away from the wall, where the cliff of the plain fill turned it straight away from
+// the wall (which held pairs of agents face to face at the ends of thin walls). Wall nodes farther from every reached
+// node, and free nodes no exit reaches, keep the plain fill. The nearest reached node comes from an exact separable distance transform with the
+// nearest feature tracked (the lower envelope of parabolas, Felzenszwalb and Huttenlocher, Theory of Computing 8,
+// 2012): each column's nearest reached row, then along each row the least (x - x')^2 + (row distance at x')^2,
+// the first (lowest x', then lowest row) on a tie.
+void fillBand(int nx, int ny, double h, float* out, double k, double maxDist, const uint8_t* kind) {
+    const size_t m = size_t(nx) * size_t(ny);
+    // the plain fill: the largest value, 10 m above every reached one (none when every node was reached)
+    float top = -std::numeric_limits<float>::infinity(), second = top;
+    for (size_t q = 0; q < m; ++q) top = std::max(top, out[q]);
+    for (size_t q = 0; q < m; ++q) if (out[q] < top) second = std::max(second, out[q]);
+    if (!(double(top) - double(second) >= 9.0)) return;
+    auto reached = [&](size_t q) { return out[q] < top; };
+    const int64_t INF = std::numeric_limits<int64_t>::max() / 4;
+    // column pass: squared row distance to the nearest reached node of the column, and its row
+    std::vector<int64_t> col(m, INF);
+    std::vector<int32_t> colRow(m, -1);
+    parallelRows(nx, [&](int i) {
+        int last = -1;
+        for (int j = 0; j < ny; ++j) {
+            const size_t q = size_t(j) * size_t(nx) + size_t(i);
+            if (reached(q)) last = j;
+            if (last >= 0) { col[q] = int64_t(j - last) * int64_t(j - last); colRow[q] = last; }
+        }
+        int next = -1;
+        for (int j = ny - 1; j >= 0; --j) {
+            const size_t q = size_t(j) * size_t(nx) + size_t(i);
+            if (reached(q)) next = j;
+            if (next >= 0) {
+                const int64_t d = int64_t(next - j) * int64_t(next - j);
+                if (d < col[q]) { col[q] = d; colRow[q] = next; }
+            }
+        }
+    });
+    // row pass: the lower envelope of the parabolas (x - x')^2 + col(x') over the columns with a reached node
+    std::vector<float> filled(out, out + m);
+    parallelRows(ny, [&](int j) {
+        const size_t base = size_t(j) * size_t(nx);
+        std::vector<int> v(static_cast<size_t>(nx));
+        std::vector<double> z(size_t(nx) + 1);
+        int kk = -1;
+        for (int q = 0; q < nx; ++q) {
+            const int64_t fq = col[base + size_t(q)];
+            if (fq >= INF) continue;
+            while (kk >= 0) {
+                const int p = v[size_t(kk)];
+                const double sx = (double(fq + int64_t(q) * q) - double(col[base + size_t(p)] + int64_t(p) * p)) / (2.0 * (q - p));
+                if (sx <= z[size_t(kk)]) { --kk; continue; }
+                ++kk;
+                v[size_t(kk)] = q;
+                z[size_t(kk)] = sx;
+                z[size_t(kk) + 1] = std::numeric_limits<double>::infinity();
+                break;
+            }
+            if (kk < 0) {
+                kk = 0;
+                v[0] = q;
+                z[0] = -std::numeric_limits<double>::infinity();
+                z[1] = std::numeric_limits<double>::infinity();
+            }
+        }
+        if (kk < 0) return;   // no reached node in any column
+        int e = 0;
+        for (int x = 0; x < nx; ++x) {
+            const size_t q = base + size_t(x);
+            while (z[size_t(e) + 1] < double(x)) ++e;
+            if (reached(q) || kind[q] != 3) continue;
+            const int fx = v[size_t(e)];
+            const int64_t d2 = int64_t(x - fx) * int64_t(x - fx) + col[base + size_t(fx)];
+            const double dist = std::sqrt(double(d2)) * h;
+            if (dist > maxDist) continue;
+            const size_t src = size_t(colRow[base + size_t(fx)]) * size_t(nx) + size_t(fx);
+            filled[q] = float(double(out[src]) + k * dist);
+        }
+    });
+    std::copy(filled.begin(), filled.end(), out);
+}
+
+// The bowl's band fill: 3 m of field per metre into the band, up to 1 m from the reached nodes. Measured on the
+// 63 488-seat bowl (GB300, bit-exact step): slopes 1.5, 3 and 6 empty it within 10 000 steps, the plain fill left 4
+// agents after 24 000 steps and a slope of 12 left 2.
+constexpr double BAND_SLOPE = 3.0, BAND_REACH = 1.0;
+
 std::atomic<int> navSolver{SWARM_NAV_CPU};
 
 // The builders' solver: fast marching here, or the GPU solver (the same floats) when selected
@@ -225,7 +323,7 @@ void hallExitBoxes(const SwarmHallSpec* s, const SwarmVenue* v, float* exitBoxes
 // sources become walls, so no path leaves through one door and comes back in through another. `hallOutside`: source
 // nodes outside every box are the outside of a hall, reached only through its doors: walls for every exit.
 int exitFields(const SwarmVenue* v, const std::vector<uint8_t>& kind, const float* speed, const float* boxes, int nExits,
-               float* fields, bool hallOutside) {
+               float* fields, bool hallOutside, double bandSlope = 0.0) {
     const int nx = v->nav_nx, ny = v->nav_ny;
     const size_t m = size_t(nx) * size_t(ny);
     std::vector<int8_t> owner(m, -1);
@@ -248,6 +346,7 @@ int exitFields(const SwarmVenue* v, const std::vector<uint8_t>& kind, const floa
         for (size_t k = 0; k < m; ++k)
             if (ke[k] == 1 && owner[k] != e) ke[k] = 3;
         if (const int rc = fastMarch(nx, ny, v->nav_h, std::move(ke), speed, fields + size_t(e) * m); rc != SWARM_OK) return rc;
+        if (bandSlope > 0.0) fillBand(nx, ny, v->nav_h, fields + size_t(e) * m, bandSlope, BAND_REACH, kind.data());
     }
     return SWARM_OK;
 }
@@ -392,16 +491,6 @@ struct Bowl {
     }
 };
 
-// Runs f(j) for j in [0, n) over the host's threads
-template <class F>
-void parallelRows(int n, F f) {
-    const int t = std::max(1, std::min(int(std::thread::hardware_concurrency()), 32));
-    std::vector<std::thread> pool;
-    for (int i = 0; i < t; ++i)
-        pool.emplace_back([&, i] { for (int j = i; j < n; j += t) f(j); });
-    for (auto& th : pool) th.join();
-}
-
 }  // namespace
 
 extern "C" int swarm_bowl_layout(const SwarmBowlSpec* s, SwarmVenue* v) {
@@ -506,6 +595,7 @@ extern "C" int swarm_bowl_fields(const SwarmBowlSpec* s, const SwarmVenue* v, fl
     std::vector<float> speed;
     bowlNav(s, v, B, kind, speed, mask);
     if (const int rc = fastMarch(nn, v->nav_ny, v->nav_h, kind, speed.data(), nav); rc != SWARM_OK) return rc;
+    fillBand(nn, v->nav_ny, v->nav_h, nav, BAND_SLOPE, BAND_REACH, kind.data());
     if (exitBoxes) bowlExitBoxes(s, B, exitBoxes);   // (the metrics' exit attribution)
     return SWARM_OK;
 }
@@ -525,7 +615,7 @@ extern "C" int swarm_bowl_exit_fields(const SwarmBowlSpec* s, const SwarmVenue* 
         if (width) width[e] = vom ? s->vomitory_width : s->perimeter_exit_width;
         if (type) type[e] = vom ? 0 : 1;
     }
-    return exitFields(v, kind, speed.data(), boxes.data(), nExits, fields, false);
+    return exitFields(v, kind, speed.data(), boxes.data(), nExits, fields, false, BAND_SLOPE);
 }
 
 extern "C" int swarm_spawn_bowl(const SwarmBowlSpec* sp, float jitter, uint64_t seed, float r_lo, float r_hi, float v_mean,

@@ -57,15 +57,15 @@ def test_bowl_63488_vs_oracle(built):
 
 
 def test_bowl_63488_whole_evacuation_vs_oracle(built):
-    """The seated-bowl workload's whole run from the seats: bit for bit against the oracle at checkpoints every 1 000
-    steps until the crowd is out (or 14 000 steps), then the sorted pairs, the cell table and the contact bits."""
+    """The seated-bowl workload's whole run from the seats to its last agent out: bit for bit against the oracle at
+    checkpoints every 1 000 steps, the state at the step the crowd empties (found by the GPU run, checked on the
+    oracle), then the sorted pairs, the cell table and the contact bits."""
     import swarm_gb300
     from swarm_gb300 import venues
     venue, (b, r, v0) = venues.bowl_c2()
     sim, ora = _pair(swarm_gb300.params_si(), venue, b, r, v0)
-    n = b.shape[0]
     done = 0
-    while done < 14000:
+    while done < 16000:
         sim.step(1000)
         ora.step(1000)
         done += 1000
@@ -73,8 +73,7 @@ def test_bowl_63488_whole_evacuation_vs_oracle(built):
         assert np.array_equal(_bits(st), _bits(ora.state())), f"after {done} steps"
         if not (st[:, 3] != 0).any():
             break
-    left = int((st[:, 3] != 0).sum())
-    assert left <= n // 1000, f"{left} agents left after {done} steps"
+    assert not (st[:, 3] != 0).any(), f"{int((st[:, 3] != 0).sum())} agents left after {done} steps"
     assert np.array_equal(sim.grid()[0], ora.grid()[0]) and np.array_equal(sim.grid()[1], ora.grid()[1])
     assert np.array_equal(sim.cells(), ora.cells())
     assert np.array_equal(sim.contacts(), ora.contacts())
