@@ -302,7 +302,10 @@ int swarm_hall_fields(const SwarmHallSpec* spec, const SwarmVenue* venue, float*
  * from the cross-aisle up to a flat concourse of depth concourse behind the top row; a vomitory (an exit portal vomitory_width wide) lies across every gangway at row vomitory_row;
  * perimeter_exits gaps of perimeter_exit_width in the concourse's outer wall, evenly spaced, lead out. The floor
  * heightfield and the speed factors are on the wall grid; the nav field is the speed-weighted travel distance to the
- * nearest exit (one plan-view field: the levels never overlap in plan). All lengths in metres. */
+ * nearest exit (one plan-view field: the levels never overlap in plan). Its wall nodes (walls and their clearance)
+ * within 1 m of a reached node hold the nearest reached node's value + 3 per metre of distance, so that e_goal beside
+ * a wall keeps the route's direction with a push away from the wall; farther wall nodes and free nodes no exit
+ * reaches hold the largest reached value + 10 m. All lengths in metres. */
 typedef struct SwarmBowlSpec {
     int32_t sectors, rows, seats;       /* 32, 32, 62 */
     float seat_width, row_pitch, rise;  /* 0.5, 0.8, 0.4 */
@@ -369,7 +372,8 @@ typedef struct SwarmExitChoiceSpec {
 } SwarmExitChoiceSpec;
 /* Per-exit distance fields of the generated venues, solved as their nav_dist (same walls, speeds, solver) with one
  * exit's sources each (the other exits' sources blocked); fields: n_exits x nav_nx x nav_ny floats, width_m and type:
- * n_exits each (halls: n_doors doors of type 1; bowls: the sectors' vomitories, type 0, then the perimeter exits). */
+ * n_exits each (halls: n_doors doors of type 1; bowls: the sectors' vomitories, type 0, then the perimeter exits;
+ * a bowl's fields fill their wall band as its nav_dist does, each from its own reached nodes). */
 int swarm_hall_exit_fields(const SwarmHallSpec* spec, const SwarmVenue* venue, float* fields, float* width_m, uint8_t* type);
 int swarm_bowl_exit_fields(const SwarmBowlSpec* spec, const SwarmVenue* venue, float* fields, float* width_m, uint8_t* type);
 /* The candidate table on the venue's hash cells (grid_res_x x grid_res_y cells, `candidates` slots each): per cell the
