@@ -40,6 +40,12 @@ struct SwarmSim {
     uint4* rowsA = nullptr;
     uint2* rowsB = nullptr;
     float2* goal = nullptr;
+    // the fused step's contact lists (a single instance; null on a batch): CLIST_MAX slot indices per slot, entry j of
+    // slot s at j x n + s, the entries per slot, and the word that sends every slot back to its rows
+    uint32_t* clist = nullptr;
+    uint8_t* ccount = nullptr;
+    float* clistRef = nullptr;
+    int* listFlag = nullptr;
     int* errFlag = nullptr;
     int* errHost = nullptr;     // pinned host word: errFlag copied in stream order (swarm_step_host reads it after one sync)
     int* errHostDev = nullptr;  // its device view: the fused launch of a host-buffer call writes the flag there itself
@@ -118,6 +124,17 @@ struct SwarmSim {
 
     swarm_gpu::StepArgs args(int in) const;
     int fail(int code, const std::string& msg) { err = msg; return code; }
+    void dropContactLists() {
+        for (void* q : {static_cast<void*>(clist), static_cast<void*>(ccount), static_cast<void*>(clistRef),
+                        static_cast<void*>(listFlag)}) {
+            for (auto it = allocs.begin(); it != allocs.end(); ++it)
+                if (*it == q) { cudaFree(q); allocs.erase(it); break; }
+        }
+        clist = nullptr;
+        ccount = nullptr;
+        clistRef = nullptr;
+        listFlag = nullptr;
+    }
     // The per-phase path hashes from zeroed counts: drop what a fused final pass counted ahead (and its scan-tile sums)
     bool clearCounts() {
         counted = false;

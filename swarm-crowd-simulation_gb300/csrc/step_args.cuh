@@ -14,6 +14,12 @@ constexpr float WALL_NONE = 1e9f;
 // ContactBits (reference include/swarm/cpu_crowd_sim.hpp:52-61)
 enum : uint8_t { C_EXIT = 1, C_FENCE_CCD = 2, C_FENCE = 4, C_FLOOR = 8, C_WALL = 16, C_AGENT = 32, C_SWEEP = 64, C_STEP_UP = 128 };
 
+// The fused step's contact lists (StepArgs::clist): entries per slot, the count of a slot that keeps none, and the
+// fewest other slots in its 3 x 3 rows for which a slot keeps one
+constexpr int CLIST_MAX = 24;
+constexpr uint8_t CLIST_NONE = 0xFF;
+constexpr uint32_t CLIST_MIN_CANDIDATES = 16;
+
 // Device-side error flags (bit set by a kernel, read by the host after the step)
 enum : int { ERR_TIMEOUT = 1, ERR_BOUNDS = 2 };
 // errMirror's value before a launch that should write it: no combination of the flags above
@@ -107,6 +113,18 @@ struct StepArgs {
     int32_t hashNext;       // fused step: count the next step's keys in the final pass (the launch's last step)
     int32_t steps;          // fused step: steps in this launch (0 or 1: one), a grid barrier between them
     int32_t sweepLanes;     // fused step: lanes per slot in the Jacobi sweeps (1, 2, 4, 8; set by the launcher)
+    // fused step, one instance: contact lists (null: none). A sweep that builds them records, for each slot whose
+    // 3 x 3 rows hold more than CLIST_MIN_CANDIDATES others, the unparked slots nearer (xy) than its largest contact
+    // distance + listMargin, in visiting order (CLIST_NONE: none kept), and each slot's path length so far in clistRef;
+    // the later sweeps and the final pass walk the lists. A sweep in which a slot's path since the build passes half the
+    // margin sets its flag word, and the next sweep builds the lists again (a list can miss a contact only after two
+    // slots have moved a margin towards each other). The first sweep of a step always builds. Three flag words in turn:
+    // sweep k sets word k mod 3, sweep k + 1 reads it, sweep k + 2 clears it.
+    uint32_t* clist;
+    uint8_t* ccount;
+    float* clistRef;
+    int* listFlag;
+    float listMargin;
     int32_t fusedThreads;   // fused step: threads per block (0: n / SMs rounded up to a warp, 128..512; 1024 a batch)
     int32_t fusedBlocksPerSm;   // fused step: at most this many blocks per SM (0: as many as fit)
     int32_t scanTile;       // fused step: cells per scan tile (set by the launcher: blockDim x 8, or x 16 on sparse

@@ -529,12 +529,11 @@ __device__ __forceinline__ void sweepRows(const StepArgs& A, const VenueArgs& V,
 }
 
 // One neighbour k of slot s at b in a sweep (cpu_crowd_sim.cpp:793-812): whether they touch, and k's push on s
-template <class Venue, class Nbr>
-__device__ __forceinline__ bool pairPush(const StepArgs& A, float4 b, int s, float ri, uint32_t k, const Nbr& nb, f2& c) {
+// (op, rj: k's position and radius, loaded by the caller)
+template <class Venue>
+__device__ __forceinline__ bool pairPushAt(const StepArgs& A, float4 b, int s, float ri, uint32_t k, float4 op, float rj, f2& c) {
     constexpr bool kUniform = Body<Venue>::kUniform;
     const SwarmParams& P = A.P;
-    const float4 op = nb.pos(k);
-    const float rj = kUniform ? 0.0f : nb.r(k);
     const f3 offset = xyz(b) - xyz(op);
     float dc, dc2;
     if (kUniform) { dc = P.body_diam; dc2 = P.body_diam2; }
@@ -546,6 +545,19 @@ __device__ __forceinline__ bool pairPush(const StepArgs& A, float4 b, int s, flo
     if (dxy2 <= P.stacked_xy2) c = shift * pairDirection(A.sid[s], A.sid[k], P.hash_to_radians);
     else c = shift * (xy(offset) / dxy);
     return true;
+}
+template <class Venue, class Nbr>
+__device__ __forceinline__ bool pairPush(const StepArgs& A, float4 b, int s, float ri, uint32_t k, const Nbr& nb, f2& c) {
+    constexpr bool kUniform = Body<Venue>::kUniform;
+    return pairPushAt<Venue>(A, b, s, ri, k, nb.pos(k), kUniform ? 0.0f : nb.r(k), c);
+}
+
+// The contact lists' radius for slot s (its largest contact distance with any other + the margin), squared
+template <class Venue>
+__device__ __forceinline__ float listRadius2(const StepArgs& A, float ri) {
+    constexpr bool kUniform = Body<Venue>::kUniform;
+    const float rl = (kUniform ? A.P.body_diam : ri + A.P.r_pair_max) + A.listMargin;
+    return rl * rl;
 }
 
 // The sweep's end for slot s (cpu_crowd_sim.cpp:813-822): the pushes' average relaxed, capped, the fence and the wall
@@ -592,30 +604,125 @@ __device__ __forceinline__ float4 projectCore(const StepArgs& A, const Venue& ve
     return projectFinish<Venue, kTape>(A, ven, b, corr, nContacts, plane, corrOut);
 }
 
+// The first sweep of slot s with its contact list recorded (the fused step): projectCore's walk of the 3 x 3 rows,
+// keeping, in visiting order, every unparked other slot nearer (xy) than the list radius; CLIST_NONE when the rows hold
+// fewer than CLIST_MIN_CANDIDATES others or more than CLIST_MAX slots are near
+template <class Venue>
+__device__ __forceinline__ float4 projectBuild(const StepArgs& A, const Venue& ven, float4 b, int s, float ri,
+                                              const uint32_t* rk0, const uint32_t* rk1, float4 plane, const GlobalNbr& nb) {
+    constexpr bool kUniform = Body<Venue>::kUniform;
+    const uint32_t total = (rk1[0] - rk0[0]) + (rk1[1] - rk0[1]) + (rk1[2] - rk0[2]);
+    const bool keep = total > CLIST_MIN_CANDIDATES;   // (the rows hold slot s itself too)
+    const float r2 = listRadius2<Venue>(A, ri);
+    const size_t n = size_t(A.n);
+    f2 corr{0.0f, 0.0f};
+    int nContacts = 0;
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        for (uint32_t k = rk0[j]; k < rk1[j]; k++) {
+            if (int(k) == s) continue;
+            const float4 op = nb.pos(k);
+            const float rj = kUniform ? 0.0f : nb.r(k);
+            if (keep && op.w >= 0.0f) {
+                const float dx = b.x - op.x, dy = b.y - op.y;
+                if (dx * dx + dy * dy < r2) {
+                    if (cnt < uint32_t(CLIST_MAX)) A.clist[size_t(cnt) * n + size_t(s)] = k;
+                    ++cnt;
+                }
+            }
+            f2 c;
+            if (pairPushAt<Venue>(A, b, s, ri, k, op, rj, c)) {
+                corr = corr + c;
+                ++nContacts;
+            }
+        }
+    }
+    A.ccount[s] = keep && cnt <= uint32_t(CLIST_MAX) ? uint8_t(cnt) : CLIST_NONE;
+    A.clistRef[s] = b.w;
+    return projectFinish<Venue, false>(A, ven, b, corr, nContacts, plane, nullptr);
+}
+
+// A later sweep of slot s over its contact list of cnt slots (in the rows' visiting order: the same pushes in the
+// same order as the rows, whose other slots cannot touch s while the lists hold)
+template <class Venue>
+__device__ __forceinline__ float4 projectList(const StepArgs& A, const Venue& ven, float4 b, int s, float ri, uint32_t cnt,
+                                             float4 plane, const GlobalNbr& nb) {
+    const size_t n = size_t(A.n);
+    f2 corr{0.0f, 0.0f};
+    int nContacts = 0;
+    // the entries four at a time (their loads issued together, ahead of the neighbours' loads)
+    for (uint32_t i0 = 0; i0 < cnt; i0 += 4) {
+        uint32_t e[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) e[q] = i0 + uint32_t(q) < cnt ? A.clist[size_t(i0 + uint32_t(q)) * n + size_t(s)] : 0u;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (i0 + uint32_t(q) >= cnt) break;
+            f2 c;
+            if (pairPush<Venue>(A, b, s, ri, e[q], nb, c)) {
+                corr = corr + c;
+                ++nContacts;
+            }
+        }
+    }
+    return projectFinish<Venue, false>(A, ven, b, corr, nContacts, plane, nullptr);
+}
+
 // The same sweep by a group of G lanes (G = 2, 4, 8; the group's lanes adjacent, `sub` = the lane's index in it): the
 // lanes take the slot's candidates in turn -- candidate i of the rows' visiting order (rows y, then slots) by lane
 // i mod G -- and every lane folds the group's touching pushes of a round in candidate order (ballot, shuffles), so
 // each lane adds the same pushes in the reference's order. The whole warp calls it together; go: the slot is unparked.
-template <class Venue, class Nbr>
+// kMode 0: the slot's 3 x 3 rows; 1: the rows, recording the contact list as projectBuild does (in candidate order:
+// the group's recorded candidates of a round by lane); 2: its contact list of cnt slots (go: the list holds)
+template <class Venue, class Nbr, int kMode = 0>
 __device__ __forceinline__ void pairSumLanes(const StepArgs& A, float4 b, int s, float ri, const uint32_t* rk0,
                                              const uint32_t* rk1, const Nbr& nb, bool go, int G, int sub, int groupBase,
-                                             f2& corr, int& nContacts) {
-    const uint32_t c0 = go ? rk1[0] - rk0[0] : 0u, c1 = go ? rk1[1] - rk0[1] : 0u, c2 = go ? rk1[2] - rk0[2] : 0u;
-    const uint32_t total = c0 + c1 + c2;
+                                             f2& corr, int& nContacts, uint32_t cnt = 0) {
+    constexpr bool kUniform = Body<Venue>::kUniform;
+    uint32_t c0 = 0, c1 = 0, c2 = 0, total = 0;
+    if constexpr (kMode == 2) {
+        total = go ? cnt : 0u;
+    } else {
+        c0 = go ? rk1[0] - rk0[0] : 0u;
+        c1 = go ? rk1[1] - rk0[1] : 0u;
+        c2 = go ? rk1[2] - rk0[2] : 0u;
+        total = c0 + c1 + c2;
+    }
     const uint32_t rounds = __reduce_max_sync(0xffffffffu, (total + uint32_t(G) - 1u) / uint32_t(G));
+    const unsigned gmask = (G == 32 ? 0xffffffffu : (1u << G) - 1u) << groupBase;
+    const bool keep = kMode == 1 && total > CLIST_MIN_CANDIDATES;
+    const float r2 = kMode == 1 ? listRadius2<Venue>(A, ri) : 0.0f;
+    const size_t n = size_t(A.n);
+    uint32_t kept = 0;
     corr = f2{0.0f, 0.0f};
     nContacts = 0;
     for (uint32_t r = 0; r < rounds; ++r) {
         const uint32_t i = r * uint32_t(G) + uint32_t(sub);
         f2 c{0.0f, 0.0f};
-        int hit = 0;
+        int hit = 0, rec = 0;
+        uint32_t k = 0;
         if (i < total) {
-            const uint32_t k = i < c0 ? rk0[0] + i : i < c0 + c1 ? rk0[1] + (i - c0) : rk0[2] + (i - c0 - c1);
-            if (int(k) != s && pairPush<Venue>(A, b, s, ri, k, nb, c)) hit = 1;
+            if constexpr (kMode == 2) k = A.clist[size_t(i) * n + size_t(s)];
+            else k = i < c0 ? rk0[0] + i : i < c0 + c1 ? rk0[1] + (i - c0) : rk0[2] + (i - c0 - c1);
+            if (int(k) != s) {
+                const float4 op = nb.pos(k);
+                const float rj = kUniform ? 0.0f : nb.r(k);
+                if (kMode == 1 && keep && op.w >= 0.0f) {
+                    const float dx = b.x - op.x, dy = b.y - op.y;
+                    rec = dx * dx + dy * dy < r2 ? 1 : 0;
+                }
+                if (pairPushAt<Venue>(A, b, s, ri, k, op, rj, c)) hit = 1;
+            }
+        }
+        if constexpr (kMode == 1) {   // the group's recorded candidates of the round, in lane (= candidate) order
+            const unsigned rm = __ballot_sync(0xffffffffu, rec != 0) & gmask;
+            const uint32_t at = kept + uint32_t(__popc(rm & ((1u << (groupBase + sub)) - 1u)));
+            if (rec && at < uint32_t(CLIST_MAX)) A.clist[size_t(at) * n + size_t(s)] = k;
+            kept += uint32_t(__popc(rm));
         }
         // the group's touching candidates of the round, lowest lane (= candidate order) first; the loop is the same for
         // every lane of the group, so its shuffles name the group's lanes alone
-        const unsigned gmask = (G == 32 ? 0xffffffffu : (1u << G) - 1u) << groupBase;
         unsigned m = __ballot_sync(0xffffffffu, hit != 0) & gmask;
         while (m) {
             const int t = __ffs(m) - 1;
@@ -625,6 +732,10 @@ __device__ __forceinline__ void pairSumLanes(const StepArgs& A, float4 b, int s,
             ++nContacts;
             m &= m - 1u;
         }
+    }
+    if (kMode == 1 && go && sub == 0) {
+        A.ccount[s] = keep && kept <= uint32_t(CLIST_MAX) ? uint8_t(kept) : CLIST_NONE;
+        A.clistRef[s] = b.w;
     }
 }
 
@@ -867,6 +978,10 @@ __global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREA
         for (int s = tid; s < n; s += stride) rankGatherItem<kPerAgent, kB, Venue>(A, s, sIn);
         if (!gridBarrier(A, gridDim.x)) return;
         stamp(A, 1);
+        // the contact lists' flag of this step (read after the first sweep's barrier; the last step's final pass, which
+        // read it, ended three barriers ago)
+        if (!kB && !kTape && !std::is_same<Venue, GridVenue>::value && A.clist && blockIdx.x == 0 && threadIdx.x == 0)
+            for (int w = 0; w < 3; ++w) cuda::atomic_ref<int, cuda::thread_scope_device>(A.listFlag[w]).store(0, cuda::memory_order_relaxed);
         const int nActive = int(A.start[A.V.ncells]);
         // predict, tile by tile: the tile's perception window staged in shared memory (global reads when it is larger)
         const int allTilesP = (n + T - 1) / T;
@@ -893,11 +1008,26 @@ __global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREA
         if (!gridBarrier(A, gridDim.x)) return;
         stamp(A, 2);
         const int K = A.P.proj_iterations;
+        // the contact lists: the reference's venues (their K = 32 sweeps over dense rows), one instance, untaped (the
+        // first sweep records them, the later ones walk them while the flags are clear; predict cleared the flags); the
+        // grid venues' instances carry none of this code (their rows hold about 9 agents)
+        constexpr bool kListable = !kB && !kTape && !std::is_same<Venue, GridVenue>::value;
+        const bool lists = kListable && A.clist != nullptr;
+        const float listHold = 0.4995f * A.listMargin;   // (half the margin, less the float rounding of the path length)
         int in = 0;
         for (int it = 1; it < K; ++it) {
             const float4* src = kTape ? A.proj[0] + size_t(it - 1) * size_t(n) : A.proj[in];
             float4* dst = kTape ? A.proj[0] + size_t(it) * size_t(n) : A.proj[in ^ 1];
             float4* corr = kTape ? A.tapeCorr + size_t(it - 1) * size_t(n) : nullptr;
+            bool build = false, walk = false;
+            if (lists) {
+                const int f = it == 1 ? 1 : cuda::atomic_ref<int, cuda::thread_scope_device>(A.listFlag[(it - 1) % 3]).load(cuda::memory_order_relaxed);
+                build = f != 0;
+                walk = f == 0;
+                if (blockIdx.x == 0 && threadIdx.x == 0)
+                    cuda::atomic_ref<int, cuda::thread_scope_device>(A.listFlag[(it + 1) % 3]).store(0, cuda::memory_order_relaxed);
+            }
+            bool moved = false;   // a slot of this thread went beyond half the margin since its list was built
             // The sweeps read their neighbours straight from L2 (and L1, which catches a block's reuse): staging a
             // tile window in shared memory and its two block barriers cost more than they save
             if (!kB && A.sweepLanes > 1) {   // a group of lanes per slot (few agents for the GPU: the launcher's choice)
@@ -910,20 +1040,42 @@ __global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREA
                     const bool go = own && b.w >= 0.0f;
                     uint32_t rk0[3] = {0u, 0u, 0u}, rk1[3] = {0u, 0u, 0u};
                     float ri = 0.0f;
+                    uint32_t cnt = CLIST_NONE;
                     if (go) {
-                        const uint4 ra = A.rowsA[s];
-                        const uint2 rb = A.rowsB[s];
-                        rk0[0] = ra.x; rk0[1] = ra.z; rk0[2] = rb.x;
-                        rk1[0] = ra.y; rk1[1] = ra.w; rk1[2] = rb.y;
+                        if (walk) cnt = A.ccount[s];
+                        if (cnt == CLIST_NONE) {
+                            const uint4 ra = A.rowsA[s];
+                            const uint2 rb = A.rowsB[s];
+                            rk0[0] = ra.x; rk0[1] = ra.z; rk0[2] = rb.x;
+                            rk1[0] = ra.y; rk1[1] = ra.w; rk1[2] = rb.y;
+                        }
                         ri = kUniform ? A.P.body_radius : A.prm[s].x;
                     }
                     f2 push;
                     int contacts;
-                    pairSumLanes<Venue>(A, b, s, ri, rk0, rk1, GlobalNbr{src, A.prm}, go, G, sub, lane - sub, push, contacts);
+                    // (warp-uniform choice: every lane of the warp takes the same path)
+                    if (kListable && build) {
+                        pairSumLanes<Venue, GlobalNbr, 1>(A, b, s, ri, rk0, rk1, GlobalNbr{src, A.prm}, go, G, sub, lane - sub, push, contacts);
+                    } else if (kListable && walk && __any_sync(0xffffffffu, go && cnt != CLIST_NONE)) {
+                        // the group's slot walks its list, or its rows (rk) when it keeps none: two passes, each lane
+                        // group taking part in the pass of its own kind
+                        f2 pl; int cl;
+                        pairSumLanes<Venue, GlobalNbr, 2>(A, b, s, ri, rk0, rk1, GlobalNbr{src, A.prm}, go && cnt != CLIST_NONE, G, sub,
+                                                          lane - sub, pl, cl, cnt);
+                        f2 pr; int cr;
+                        pairSumLanes<Venue, GlobalNbr, 0>(A, b, s, ri, rk0, rk1, GlobalNbr{src, A.prm}, go && cnt == CLIST_NONE, G, sub,
+                                                          lane - sub, pr, cr);
+                        push = cnt != CLIST_NONE ? pl : pr;
+                        contacts = cnt != CLIST_NONE ? cl : cr;
+                    } else {
+                        pairSumLanes<Venue>(A, b, s, ri, rk0, rk1, GlobalNbr{src, A.prm}, go, G, sub, lane - sub, push, contacts);
+                    }
                     if (go) {
                         const Venue ven{A.P, venueOfSlot<kB>(A, s)};
+                        const float ref = lists ? (build ? b.w : A.clistRef[s]) : 0.0f;
                         b = projectFinish<Venue, kTape>(A, ven, b, push, contacts, A.plane[s],
                                                         kTape && sub == 0 ? corr + s : nullptr);
+                        moved |= lists && b.w - ref > listHold;
                     }
                     if (own && sub == 0) dst[s] = b;
                 }
@@ -931,17 +1083,28 @@ __global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREA
                 for (int s = tid; s < nActive; s += stride) {
                     float4 b = src[s];
                     if (b.w >= 0.0f) {
-                        const uint4 ra = A.rowsA[s];
-                        const uint2 rb = A.rowsB[s];
-                        const uint32_t rk0[3] = {ra.x, ra.z, rb.x}, rk1[3] = {ra.y, ra.w, rb.y};
                         const float ri = kUniform ? A.P.body_radius : A.prm[s].x;
                         const Venue ven{A.P, venueOfSlot<kB>(A, s)};
-                        b = projectCore<Venue, GlobalNbr, kTape>(A, ven, b, s, ri, rk0, rk1, A.plane[s],
-                                                                 GlobalNbr{src, A.prm}, kTape ? corr + s : nullptr);
+                        const uint32_t cnt = walk ? A.ccount[s] : CLIST_NONE;
+                        const float ref = lists ? (build ? b.w : A.clistRef[s]) : 0.0f;
+                        if (kListable && cnt != CLIST_NONE) {
+                            b = projectList<Venue>(A, ven, b, s, ri, cnt, A.plane[s], GlobalNbr{src, A.prm});
+                        } else {
+                            const uint4 ra = A.rowsA[s];
+                            const uint2 rb = A.rowsB[s];
+                            const uint32_t rk0[3] = {ra.x, ra.z, rb.x}, rk1[3] = {ra.y, ra.w, rb.y};
+                            if (kListable && build)
+                                b = projectBuild<Venue>(A, ven, b, s, ri, rk0, rk1, A.plane[s], GlobalNbr{src, A.prm});
+                            else
+                                b = projectCore<Venue, GlobalNbr, kTape>(A, ven, b, s, ri, rk0, rk1, A.plane[s],
+                                                                         GlobalNbr{src, A.prm}, kTape ? corr + s : nullptr);
+                        }
+                        moved |= lists && b.w - ref > listHold;
                     }
                     dst[s] = b;
                 }
             }
+            if (moved) cuda::atomic_ref<int, cuda::thread_scope_device>(A.listFlag[it % 3]).store(1, cuda::memory_order_relaxed);
             in ^= 1;
             if (!gridBarrier(A, gridDim.x)) return;
         }
@@ -949,6 +1112,8 @@ __global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREA
         // The final pass reads its neighbours from L2 too (warp-aligned slots: the next step's count is warp-collective)
         {
             const float4* src = kTape ? A.proj[0] + size_t(K > 0 ? K - 1 : 0) * size_t(n) : A.proj[in];
+            const bool walk = lists && K > 1 &&
+                              cuda::atomic_ref<int, cuda::thread_scope_device>(A.listFlag[(K - 1) % 3]).load(cuda::memory_order_relaxed) == 0;
             for (int base = tid - int(threadIdx.x & 31u); base < n; base += stride) {
                 const int s = base + int(threadIdx.x & 31u);
                 const bool own = s < nActive;
@@ -958,12 +1123,17 @@ __global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREA
                     const VenueArgs& V = venueOfSlot<kB>(A, s);
                     const Venue ven{A.P, V};
                     if (A.projectInFinal && b.w >= 0.0f) {
-                        const uint4 ra = A.rowsA[s];
-                        const uint2 rb = A.rowsB[s];
-                        const uint32_t rk0[3] = {ra.x, ra.z, rb.x}, rk1[3] = {ra.y, ra.w, rb.y};
                         const float ri = kUniform ? A.P.body_radius : A.prm[s].x;
-                        b = projectCore<Venue, GlobalNbr, kTape>(A, ven, b, s, ri, rk0, rk1, A.plane[s], GlobalNbr{src, A.prm},
-                                                                 kTape && K > 0 ? A.tapeCorr + size_t(K - 1) * size_t(n) + s : nullptr);
+                        const uint32_t cnt = walk ? A.ccount[s] : CLIST_NONE;
+                        if (kListable && cnt != CLIST_NONE) {
+                            b = projectList<Venue>(A, ven, b, s, ri, cnt, A.plane[s], GlobalNbr{src, A.prm});
+                        } else {
+                            const uint4 ra = A.rowsA[s];
+                            const uint2 rb = A.rowsB[s];
+                            const uint32_t rk0[3] = {ra.x, ra.z, rb.x}, rk1[3] = {ra.y, ra.w, rb.y};
+                            b = projectCore<Venue, GlobalNbr, kTape>(A, ven, b, s, ri, rk0, rk1, A.plane[s], GlobalNbr{src, A.prm},
+                                                                     kTape && K > 0 ? A.tapeCorr + size_t(K - 1) * size_t(n) + s : nullptr);
+                        }
                     }
                     if (kTape) A.tapeQK[s] = b;
                     nextKey = finalActive(A, V, ven, s, b, sOut);

@@ -100,6 +100,14 @@ StepArgs SwarmSim::args(int in) const {
     A.key = key; A.rank = rank; A.count = count; A.start = start; A.cells = cells; A.tileSums = tileSums;
     A.sidTmp = sidTmp; A.sid = sid; A.skey = skey;
     A.pos0 = pos0; A.vel0 = vel0; A.prm = prm; A.proj[0] = proj0; A.proj[1] = proj1;
+    // the contact lists where the crowd is dense for its hash cells: 9 cells of rows then hold 16 or more agents on
+    // average (the reference's seated venues and terrace); sparser crowds (the benchmark halls and the bowl, about 9)
+    // gain nothing from them and would pay their loads in every sweep
+    const bool dense = clist && 9.0 * double(n) >= 16.0 * double(ncells);
+    A.clist = dense ? clist : nullptr;
+    A.ccount = ccount; A.clistRef = clistRef; A.listFlag = listFlag;
+    // half the largest contact distance of a pair (model units: the uniform body's)
+    A.listMargin = 0.5f * (V.kind == SWARM_VENUE_GRID ? 2.0f * P.r_pair_max : P.body_diam);
     A.vel1 = vel1; A.plane = plane; A.ctc = ctc; A.rowsA = rowsA; A.rowsB = rowsB; A.goal = goal; A.err = errFlag; A.barrier = barrier; A.barrierExtra = barrierExtra;
     A.stamps = timing ? stamps : nullptr;
     A.choiceAssign = choiceExits ? dAssign : nullptr;
@@ -201,7 +209,9 @@ int swarm_create(const SwarmParams* params, const SwarmVenue* venue, int n_capac
               devAlloc(h, &h->skey, N) && devAlloc(h, &h->pos0, N) && devAlloc(h, &h->vel0, N) && devAlloc(h, &h->proj0, N) &&
               devAlloc(h, &h->proj1, N) && devAlloc(h, &h->vel1, N) && devAlloc(h, &h->plane, N) && devAlloc(h, &h->prm, N) &&
               devAlloc(h, &h->ctc, N) && devAlloc(h, &h->rowsA, N) && devAlloc(h, &h->rowsB, N) &&
-              devAlloc(h, &h->goal, N) && devAlloc(h, &h->errFlag, 1) && devAlloc(h, &h->barrier, 4) && devAlloc(h, &h->stamps, 8) &&
+              devAlloc(h, &h->goal, N) && devAlloc(h, &h->errFlag, 1) &&
+              devAlloc(h, &h->clist, N * swarm_gpu::CLIST_MAX) && devAlloc(h, &h->ccount, N) && devAlloc(h, &h->clistRef, N) &&
+              devAlloc(h, &h->listFlag, 4) && devAlloc(h, &h->barrier, 4) && devAlloc(h, &h->stamps, 8) &&
               cudaHostAlloc(reinterpret_cast<void**>(&h->errHost), sizeof(int), cudaHostAllocMapped) == cudaSuccess &&
               cudaHostGetDevicePointer(reinterpret_cast<void**>(&h->errHostDev), h->errHost, 0) == cudaSuccess;
     if (ok && V.kind == SWARM_VENUE_STADIUM) {
@@ -285,6 +295,7 @@ int swarm_batch_create(const SwarmParams* params, const SwarmVenue* venues, cons
     SwarmHandle h = nullptr;
     const int rc = swarm_create(params, &all, int(total), &h);
     if (rc != SWARM_OK) return rc;
+    h->dropContactLists();   // (a batch's fused step walks its rows)
     // every instance's fields in two device buffers, and its venue record
     float *dWall = nullptr, *dNav = nullptr;
     if (!devAlloc(h, &dWall, nWall) || !devAlloc(h, &dNav, nNav) || !devAlloc(h, &h->dVenueTable, size_t(m)) ||

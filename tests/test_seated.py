@@ -288,6 +288,30 @@ def test_generated_venue_runs_reproduce_the_reference(name):
         sim.close()
 
 
+@pytest.mark.gpu
+def test_contact_lists_keep_the_bits_into_the_congested_run():
+    """Venue L from its full seat spawn for 2 250 steps (past the half-empty, congested state, where sweeps move agents
+    far enough to rebuild the fused step's contact lists): the fused step, which walks its contact lists in the
+    sweeps, and the per-phase kernels, which walk the whole 3 x 3 rows, give the same bits every 250 steps; then the
+    cell table and the contact bits."""
+    import swarm_gb300
+    g, cells, spawn = _generated("L")
+    a = swarm_gb300.CrowdSim(swarm_gb300.params_reference(), _venue(g, cells), spawn.shape[0])
+    b = swarm_gb300.CrowdSim(swarm_gb300.params_reference(), _venue(g, cells), spawn.shape[0])
+    a.set_state(spawn)
+    b.set_state(spawn)
+    b.set_fused(False)
+    for k in range(9):
+        a.step(250)
+        b.step(250)
+        assert np.array_equal(_bits(a.state()), _bits(b.state())), f"after {250 * (k + 1)} steps"
+    assert 2 * int((a.state()[:, 3] != 0).sum()) < int((spawn[:, 3] != 0).sum()), "the run reached the congested state"
+    assert np.array_equal(a.cells(), b.cells())
+    assert np.array_equal(a.contacts(), b.contacts())
+    a.close()
+    b.close()
+
+
 # ---- the queue-aware exit choice on the reference's own table ----
 CHOICE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "seated_S_choice.npz")
 PIN_ROUTED = 0x434356ac8d65471d         # golden_state.hpp:55  CPU counting venue S routed
