@@ -103,6 +103,34 @@ def test_bowl_fields_and_seats(bowl_small):
     assert A["exit_mask"].sum() > 0
 
 
+def test_bowl_nav_band_fill(bowl_small):
+    """The bowl's nav field beside its walls: every wall node (wall SDF within the clearance) within 1 m of a node the
+    solver reached holds the value of a nearest reached node (Euclidean, over node centres) + 3 per metre of that
+    distance; wall nodes farther away keep the plain fill (the largest reached value + 10 m)."""
+    ndimage = pytest.importorskip("scipy.ndimage")
+    spec, venue, _ = bowl_small
+    v = venue.struct
+    nav = venue.arrays["nav"].reshape(v.nav_ny, v.nav_nx).astype(np.float64)
+    wall = venue.arrays["wall"].reshape(v.wall_ny, v.wall_nx)[::2, ::2]   # nav node (i, j) is wall node (2i, 2j)
+    top = nav.max()
+    kind3 = wall <= spec.clearance
+    reached = ~kind3 & (nav < top)
+    dist, (iy, ix) = ndimage.distance_transform_edt(~reached, return_indices=True)
+    band = kind3 & (dist * v.nav_h <= 1.0)
+    assert band.sum() > 10000
+    assert (nav[kind3 & (dist * v.nav_h > 1.0 + 1e-6)] == top).all()
+    ys, xs = np.nonzero(band)
+    rng = np.random.default_rng(0)
+    for k in rng.choice(ys.size, 3000, replace=False):
+        y, x = int(ys[k]), int(xs[k])
+        d = dist[y, x]
+        r = int(np.ceil(d))
+        wy, wx = np.mgrid[max(y - r, 0):min(y + r, v.nav_ny - 1) + 1, max(x - r, 0):min(x + r, v.nav_nx - 1) + 1]
+        tie = reached[wy, wx] & (np.abs(np.hypot(wy - y, wx - x) - d) < 1e-9)
+        want = (nav[wy, wx][tie] + 3.0 * (d * float(v.nav_h))).astype(np.float32)
+        assert tie.any() and np.float32(nav[y, x]) in want, (y, x, d)
+
+
 def test_small_bowl_evacuates_on_the_oracle(bowl_small):
     """The whole crowd finds the gangways, the stairs and an exit (the oracle, 768 agents)."""
     import swarm_gb300
