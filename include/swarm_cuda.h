@@ -440,8 +440,8 @@ int swarm_spawn_lattice(int nx, int ny, int n, float spacing, float cx, float cy
  * the caller's device arrays. Its working memory is a fixed array compiled into this library (about 1.8 MB per GPU
  * that loads it, held until exit): at most 65536 agents and 131072 cells; larger sizes or a misaligned state return
  * SWARM_E_INVALID. It calls no allocator. The first call on a device looks up the array's address with that device
- * current and keeps it; after a cudaDeviceReset the address is gone, so do not call it on that device again in the
- * same process. Returns when its work on `stream` is done: SWARM_E_CUDA if a launch failed or the kernels met a slot
+ * current and keeps it (make that first call before any stream capture); after a cudaDeviceReset the address is
+ * gone, so do not call it on that device again in the same process. Returns when its work on `stream` is done: SWARM_E_CUDA if a launch failed or the kernels met a slot
  * out of range. All calls share the array: calls that overlap on the GPU (from several host threads) race and can
  * give such an error, so order them. */
 int swarm_sort_grid_noalloc(const float* d_boids, int n, int grid_res_x, int grid_res_y, float domain_min_x,
