@@ -82,15 +82,15 @@ def test_launch_configurations_give_the_same_bits_and_autotune_restores_state(bu
 
 @pytest.mark.gpu
 def test_full_batch_256_instances_equal_solo_runs_and_oracle(built):
-    """The batched workload at full size (256 halls, N log-uniform in [1 024, 65 536], 3.78 M agents), 20 steps:
-    every instance bit-identical to its solo CUDA run, and 8 instances (the 4 smallest, the 4 largest) to the
-    oracle."""
+    """The batched workload at full size and length (256 halls, N log-uniform in [1 024, 65 536], 3.78 M agents,
+    1 000 steps): every instance bit-identical to its solo CUDA run, and 8 instances (the 4 smallest, the 4 largest) to
+    the oracle."""
     import swarm_gb300
     from swarm_gb300 import venues
     vens, boids, r, v0, counts = venues.build_batch(256, 0)
     assert len(vens) == 256 and counts.min() >= 1024 and counts.max() <= 65536
     P = swarm_gb300.params_si()
-    steps = 20
+    steps = 1000
     batch = swarm_gb300.BatchSim(P, vens, counts)
     batch.set_state(boids)
     batch.set_agent_params(r, v0)
