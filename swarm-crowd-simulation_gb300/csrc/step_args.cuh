@@ -114,7 +114,7 @@ struct StepArgs {
     int32_t steps;          // fused step: steps in this launch (0 or 1: one), a grid barrier between them
     int32_t sweepLanes;     // fused step: lanes per slot in the Jacobi sweeps (1, 2, 4, 8; set by the launcher)
     // fused step, one instance: contact lists (null: none). A sweep that builds them records, for each slot whose
-    // 3 x 3 rows hold more than CLIST_MIN_CANDIDATES others, the unparked slots nearer (xy) than its largest contact
+    // 3 x 3 rows hold at least CLIST_MIN_CANDIDATES others, the unparked slots nearer (xy) than its largest contact
     // distance + listMargin, in visiting order (CLIST_NONE: none kept), and each slot's path length so far in clistRef;
     // the later sweeps and the final pass walk the lists. A sweep in which a slot's path since the build passes half the
     // margin sets its flag word, and the next sweep builds the lists again (a list can miss a contact only after two
