@@ -360,6 +360,50 @@ struct PredWindow {
     __device__ __forceinline__ float r(uint32_t k) const { return r_[k - lo]; }
 };
 
+// The rest of predict once the neighbours are summed: desired speed, direction, obstacle avoidance, kinematics,
+// the static contacts and the wall plane (cpu_crowd_sim.cpp:727-777)
+template <class Venue, class Nbr>
+__device__ __forceinline__ void predictFinish(const StepArgs& A, const Venue& ven, int s, float4 p, float4 v, f2 eGoal, f2 sep,
+                                              float sAhead, float ri, const Nbr& nb) {
+    constexpr bool kUniform = Body<Venue>::kUniform;
+    const SwarmParams& P = A.P;
+    uint32_t contact = 0;
+    float vDes;
+    if constexpr (std::is_same<Venue, Seated>::value) {
+        vDes = ven.desiredSpeed(xy(p), eGoal, sAhead);   // the incline speed and stair spacing when on
+    } else if (kUniform) {
+        vDes = sclamp((sAhead - P.body_diam) * P.headway_rate, 0.0f, P.v_max) * length(eGoal);
+    } else {
+        const float vFree = A.prm[s].y * ven.speedFactor(xyz(p));
+        vDes = sclamp(sAhead * P.headway_rate, 0.0f, vFree) * length(eGoal);
+    }
+    const f2 eDir = safeNormalize(eGoal + sep, P.safe_eps);
+
+    // obstacle avoidance at torso height
+    const f2 aObs = nb.obstacle(uint32_t(s), ven, p);
+
+    // kinematics
+    const f2 vEq = eDir * vDes + aObs * P.tau_relax;
+    f3 nv = xyz(v);
+    setXY(nv, vEq + (xy(nv) - vEq) * P.relax_step);
+    const float along = dot(xy(nv), eGoal);
+    if (along > vDes) setXY(nv, xy(nv) - eGoal * (along - vDes));
+    nv.z -= P.gravity_dt;
+    nv.z = smin(nv.z, 0.0f);
+    if (length(xy(nv)) > P.v_max) setXY(nv, safeNormalize(xy(nv), P.safe_eps) * P.v_max);
+    f3 np = xyz(p) + nv * P.dt;
+
+    f3 wall;
+    const bool grounded = ven.resolveStatic(xyz(p), np, nv, false, wall, contact, ri);
+    if (wall.x == 0.0f && wall.y == 0.0f) wall = ven.wallPlaneProbe(np, ri);
+    A.proj[0][s] = make_float4(np.x, np.y, np.z, 0.0f);
+    A.vel1[s] = make_float4(nv.x, nv.y, nv.z, 0.0f);
+    const f2 wn{wall.x, wall.y};
+    A.plane[s] = make_float4(wn.x, wn.y, dot(xy(np), wn) - wall.z,
+                             (nonzero(wn) ? PLANE_WALL : 0.0f) + (grounded ? PLANE_GROUNDED : 0.0f));
+    A.ctc[s] = uint8_t(contact);
+}
+
 template <class Venue, bool kB, bool kTape = false, class Nbr = PredGlobal>
 __device__ __forceinline__ void predictCore(const StepArgs& A, int s, const Nbr& nb) {
     constexpr bool kUniform = Body<Venue>::kUniform;
@@ -369,7 +413,6 @@ __device__ __forceinline__ void predictCore(const StepArgs& A, int s, const Nbr&
     const VenueArgs& V = venueOfSlot<kB>(A, s);
     const Venue ven{A.P, V};
     const uint32_t self = A.sid[s], cid = A.skey[s] - V.cellOffset;
-    uint32_t contact = 0;
     const float4 p = A.pos0[s], v = A.vel0[s];
     if (ven.exits(p)) {
         A.proj[0][s] = make_float4(P.park_coord, P.park_coord, P.park_coord, -1.0f);
@@ -458,40 +501,134 @@ __device__ __forceinline__ void predictCore(const StepArgs& A, int s, const Nbr&
         }
     }
     if constexpr (kTape) A.tapePred[s] = make_float4(sep.x, sep.y, sAhead, __int_as_float(jstar));
-    float vDes;
-    if constexpr (std::is_same<Venue, Seated>::value) {
-        vDes = ven.desiredSpeed(xy(p), eGoal, sAhead);   // the incline speed and stair spacing when on
-    } else if (kUniform) {
-        vDes = sclamp((sAhead - P.body_diam) * P.headway_rate, 0.0f, P.v_max) * length(eGoal);
-    } else {
-        const float vFree = A.prm[s].y * ven.speedFactor(xyz(p));
-        vDes = sclamp(sAhead * P.headway_rate, 0.0f, vFree) * length(eGoal);
+    predictFinish<Venue>(A, ven, s, p, v, eGoal, sep, sAhead, ri, nb);
+}
+
+// predictCore by a group of G lanes per slot (G = 2, 4, 8, adjacent lanes; `sub` = the lane's index in its group):
+// every lane of the group evaluates the slot's own terms, the lanes take the neighbour candidates in turn --
+// candidate i of the rows' visiting order (rows y, then slots) by lane i mod G -- and in each round every lane adds
+// the group's nonzero separation terms in candidate order (ballot, shuffles), so each lane sums exactly the
+// reference's nonzero terms in the reference's order (a +0 or -0 term never changes a sum that starts at +0). The
+// nearest agent ahead is the least key over the candidates that qualify (the sequential update takes key < sAhead
+// under a condition that does not depend on sAhead): a minimum, reduced over the group. Lane 0 of the group writes.
+// The whole warp calls it together (own: the lane has a slot below n); one instance, untaped.
+template <class Venue, class Nbr>
+__device__ __forceinline__ void predictLanes(const StepArgs& A, int s, bool own, const Nbr& nb, int G, int sub, int groupBase) {
+    constexpr bool kUniform = Body<Venue>::kUniform;
+    const SwarmParams& P = A.P;
+    const VenueArgs& V = A.V;
+    const Venue ven{A.P, V};
+    const int nActive = int(A.start[V.ncells]);
+    const bool live = own && s < nActive;
+    uint32_t self = 0;
+    float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f), v = p;
+    bool go = false;
+    if (live) {
+        self = A.sid[s];
+        p = A.pos0[s];
+        v = A.vel0[s];
+        go = !ven.exits(p);
     }
-    const f2 eDir = safeNormalize(eGoal + sep, P.safe_eps);
-
-    // obstacle avoidance at torso height
-    const f2 aObs = nb.obstacle(uint32_t(s), ven, p);
-
-    // kinematics
-    const f2 vEq = eDir * vDes + aObs * P.tau_relax;
-    f3 nv = xyz(v);
-    setXY(nv, vEq + (xy(nv) - vEq) * P.relax_step);
-    const float along = dot(xy(nv), eGoal);
-    if (along > vDes) setXY(nv, xy(nv) - eGoal * (along - vDes));
-    nv.z -= P.gravity_dt;
-    nv.z = smin(nv.z, 0.0f);
-    if (length(xy(nv)) > P.v_max) setXY(nv, safeNormalize(xy(nv), P.safe_eps) * P.v_max);
-    f3 np = xyz(p) + nv * P.dt;
-
-    f3 wall;
-    const bool grounded = ven.resolveStatic(xyz(p), np, nv, false, wall, contact, ri);
-    if (wall.x == 0.0f && wall.y == 0.0f) wall = ven.wallPlaneProbe(np, ri);
-    A.proj[0][s] = make_float4(np.x, np.y, np.z, 0.0f);
-    A.vel1[s] = make_float4(nv.x, nv.y, nv.z, 0.0f);
-    const f2 wn{wall.x, wall.y};
-    A.plane[s] = make_float4(wn.x, wn.y, dot(xy(np), wn) - wall.z,
-                             (nonzero(wn) ? PLANE_WALL : 0.0f) + (grounded ? PLANE_GROUNDED : 0.0f));
-    A.ctc[s] = uint8_t(contact);
+    constexpr int MAXR = 2 * 4 + 1;   // PERC_RING <= 4
+    uint32_t rk0[MAXR], rk1[MAXR];
+    f2 eGoal{0.0f, 0.0f};
+    float ri = 0.0f, reach2 = 0.0f;
+#pragma unroll
+    for (int j = 0; j < MAXR; ++j) rk0[j] = rk1[j] = 0;
+    if (go) {   // predictCore's own terms and rows
+        const uint32_t cid = A.skey[s] - V.cellOffset;
+        eGoal = nb.goal(uint32_t(s), ven, xyz(p), self);
+        ri = kUniform ? P.body_radius : A.prm[s].x;
+        const int resX = V.resX, resY = V.resY;
+        const int cx = int(cid % uint32_t(resX)), cy = int(cid / uint32_t(resX));
+        const int R = P.perc_ring;
+        const float csx = V.dspanX / float(resX), csy = V.dspanY / float(resY);
+        const float margin = 0.01f * smax(csx, csy);
+        const float vFreeSelf = kUniform ? P.v_max : A.prm[s].y * ven.speedFactor(xyz(p));
+        const float dcMax = kUniform ? P.body_diam : ri + P.r_pair_max;
+        float headway;
+        if constexpr (std::is_same<Venue, Seated>::value) headway = vFreeSelf * ven.maxHeadwayTime();
+        else headway = vFreeSelf / P.headway_rate;
+        const float reach = smax(dcMax + headway, kUniform ? P.r_sep : dcMax + P.sep_margin) * 1.01f + margin;
+        const float rPerc = smin(sqrtf(P.r_perc2) + margin, reach);
+        reach2 = reach * reach;
+#pragma unroll
+        for (int j = 0; j < MAXR; ++j) {
+            const int y = j - R;
+            const int ny = cy + y;
+            if (y > R || ny < 0 || ny >= resY) continue;
+            const float ylo = V.dminY + float(ny) * csy - margin, yhi = V.dminY + float(ny + 1) * csy + margin;
+            const float dy = fmaxf(0.0f, fmaxf(ylo - p.y, p.y - yhi));
+            if (dy >= rPerc) continue;
+            const float w = sqrtf(rPerc * rPerc - dy * dy) + margin;
+            const int xlo = max(max(cx - R, 0), int(floorf((p.x - w - V.dminX) / csx)));
+            const int xhi = min(min(cx + R, resX - 1), int(floorf((p.x + w - V.dminX) / csx)));
+            if (xlo > xhi) continue;
+            rk0[j] = A.start[V.cellOffset + xlo + ny * resX];
+            rk1[j] = A.start[V.cellOffset + xhi + 1 + ny * resX];
+        }
+    }
+    uint32_t total = 0;
+#pragma unroll
+    for (int j = 0; j < MAXR; ++j) total += rk1[j] - rk0[j];
+    const uint32_t rounds = __reduce_max_sync(0xffffffffu, (total + uint32_t(G) - 1u) / uint32_t(G));
+    const unsigned gmask = (G == 32 ? 0xffffffffu : (1u << G) - 1u) << groupBase;
+    f2 sep{0.0f, 0.0f};
+    float sAhead = 1e9f;
+    for (uint32_t rd = 0; rd < rounds; ++rd) {
+        const uint32_t i = rd * uint32_t(G) + uint32_t(sub);
+        f2 c{0.0f, 0.0f};
+        if (i < total) {
+            uint32_t k = 0, acc = 0;   // candidate i's slot: the row whose run holds it
+#pragma unroll
+            for (int j = 0; j < MAXR; ++j) {
+                const uint32_t len = rk1[j] - rk0[j];
+                if (i >= acc && i < acc + len) k = rk0[j] + (i - acc);
+                acc += len;
+            }
+            if (int(k) != s) {
+                const float4 op = nb.pos(k);
+                const f3 offset = xyz(p) - xyz(op);
+                const float dxy2 = dot(xy(offset), xy(offset));
+                if (dxy2 < reach2 && dxy2 < P.r_perc2) {
+                    const uint32_t other = nb.sid(k);
+                    const float rj = kUniform ? 0.0f : nb.r(k);
+                    float dc, rs, rs2;
+                    if (kUniform) { dc = P.body_diam; rs = P.r_sep; rs2 = P.r_sep2; }
+                    else { dc = ri + rj; rs = dc + P.sep_margin; rs2 = rs * rs; }
+                    c = separationForce(P, offset, self, other, rs, rs2);
+                    const float ahead = -dot(xy(offset), eGoal);
+                    const float lateral = fabsf(offset.x * eGoal.y - offset.y * eGoal.x);
+                    const float dxy = sqrtf(dxy2);
+                    const float key = kUniform ? dxy : dxy - dc;
+                    if (ahead > 0.0f && lateral < dc && key < sAhead) {
+                        const f2 eOther = nb.goal(k, ven, xyz(op), other);
+                        const float aheadOther = dot(xy(offset), eOther);
+                        const bool mutual = aheadOther > 0.0f && fabsf(offset.x * eOther.y - offset.y * eOther.x) < dc;
+                        if (!mutual || ahead > aheadOther || (ahead == aheadOther && self > other)) sAhead = key;
+                    }
+                }
+            }
+        }
+        // the group's nonzero separation terms of the round, lowest lane (= candidate order) first
+        unsigned m = __ballot_sync(0xffffffffu, c.x != 0.0f || c.y != 0.0f) & gmask;
+        while (m) {
+            const int t = __ffs(m) - 1;
+            const float cx = __shfl_sync(gmask, c.x, t);
+            const float cy = __shfl_sync(gmask, c.y, t);
+            sep = sep + f2{cx, cy};
+            m &= m - 1u;
+        }
+    }
+    for (int o = 1; o < G; o <<= 1) sAhead = fminf(sAhead, __shfl_xor_sync(0xffffffffu, sAhead, o));
+    if (!live || sub != 0) return;
+    if (!go) {   // it reached an exit: parked this step
+        A.proj[0][s] = make_float4(P.park_coord, P.park_coord, P.park_coord, -1.0f);
+        A.vel1[s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        A.ctc[s] = C_EXIT;
+        return;
+    }
+    predictFinish<Venue>(A, ven, s, p, v, eGoal, sep, sAhead, ri, nb);
 }
 
 template <class Venue, bool kB, bool kTape = false>
@@ -921,7 +1058,9 @@ __device__ __forceinline__ uint2 predWindow(const StepArgs& A, int t, int T, int
 
 // kTape (the adjoint's recompute): sweep k reads q[k - 1] and writes q[k], q[k] = proj[0] + k n, with its relaxed
 // corrections at tapeCorr + (k - 1) n; the final pass records the last sweep's result in tapeQK; predict its record
-template <class Venue, bool kPerAgent, bool kB, bool kTape = false>
+// kLanes: the instance for few agents on the reference's venues -- predict takes the sweeps' lane groups too (the
+// other instances carry none of that code)
+template <class Venue, bool kPerAgent, bool kB, bool kTape = false, bool kLanes = false>
 __global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREADS, 1) k_step_fused(StepArgs A) {
     constexpr bool kUniform = Body<Venue>::kUniform;
     __shared__ uint32_t warpSums[32];
@@ -983,11 +1122,15 @@ __global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREA
         if (!kB && !kTape && !std::is_same<Venue, GridVenue>::value && A.clist && blockIdx.x == 0 && threadIdx.x == 0)
             for (int w = 0; w < 3; ++w) cuda::atomic_ref<int, cuda::thread_scope_device>(A.listFlag[w]).store(0, cuda::memory_order_relaxed);
         const int nActive = int(A.start[A.V.ncells]);
-        // predict, tile by tile: the tile's perception window staged in shared memory (global reads when it is larger)
-        const int allTilesP = (n + T - 1) / T;
+        // predict, tile by tile: the tile's perception window staged in shared memory (global reads when it is larger);
+        // in the lanes instance, with the sweeps' lane groups (few agents for the GPU), a group of lanes per slot here
+        // too: tiles of T / G slots
+        const int GP = kLanes ? A.sweepLanes : 1;
+        const int TP = T / GP;
+        const int allTilesP = (n + TP - 1) / TP;
         for (int t = blockIdx.x; t < allTilesP; t += gridDim.x) {
-            const int s = t * T + int(threadIdx.x);
-            const uint2 win = predWindow<kB>(A, t, T, nActive);
+            const int s = t * TP + int(threadIdx.x) / GP;
+            const uint2 win = predWindow<kB>(A, t, TP, nActive);
             const bool useWin = win.y > win.x && win.y - win.x <= uint32_t(WIN_CAP);
             if (useWin) {
                 for (uint32_t k = win.x + threadIdx.x; k < win.y; k += blockDim.x) {
@@ -998,6 +1141,16 @@ __global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREA
                 }
             }
             __syncthreads();
+            if constexpr (kLanes) {
+                if (GP > 1) {   // the whole warp together (its lanes' groups)
+                    const int lane = int(threadIdx.x & 31u), sub = lane & (GP - 1);
+                    if (useWin) predictLanes<Venue>(A, s, s < n, PredWindow{smPos, smR, smSid, smGoal, A.P, win.x}, GP, sub, lane - sub);
+                    else predictLanes<Venue>(A, s, s < n, PredGlobal{A}, GP, sub, lane - sub);
+                    if (sub == 0 && s < nActive) prepareSweepItem<kB>(A, s);
+                    __syncthreads();   // the window is reused by the next tile
+                    continue;
+                }
+            }
             if (s < n) {
                 if (useWin) predictCore<Venue, kB, kTape>(A, s, PredWindow{smPos, smR, smSid, smGoal, A.P, win.x});
                 else predictCore<Venue, kB, kTape>(A, s, PredGlobal{A});
@@ -1267,13 +1420,13 @@ int fusedScanTile(const StepArgs& A) {
     return tiles8 > smCount() ? T * 2 * SCAN_ITEMS : T * SCAN_ITEMS;
 }
 
-template <class Venue, bool kPerAgent, bool kB, bool kTape = false>
+template <class Venue, bool kPerAgent, bool kB, bool kTape = false, bool kLanes = false>
 static cudaError_t fusedImpl(const StepArgs& A0, cudaStream_t st) {
     // the dynamic shared memory limit is a per-device attribute of the kernel: set once per device, kept only when set
     static thread_local bool smemSet[MAX_DEVICES] = {};
     const int dev = currentDevice();
     if (!smemSet[dev]) {
-        const cudaError_t e = cudaFuncSetAttribute(k_step_fused<Venue, kPerAgent, kB, kTape>,
+        const cudaError_t e = cudaFuncSetAttribute(k_step_fused<Venue, kPerAgent, kB, kTape, kLanes>,
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, FUSED_SMEM);
         if (e != cudaSuccess) return e;
         smemSet[dev] = true;
@@ -1292,7 +1445,7 @@ static cudaError_t fusedImpl(const StepArgs& A0, cudaStream_t st) {
         occInit = true;
     }
     if (occThreads[dev] != threads) {
-        const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occPerSm[dev], k_step_fused<Venue, kPerAgent, kB, kTape>,
+        const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occPerSm[dev], k_step_fused<Venue, kPerAgent, kB, kTape, kLanes>,
                                                                             threads, FUSED_SMEM);
         if (e != cudaSuccess) return e;
         occThreads[dev] = threads;
@@ -1312,12 +1465,17 @@ static cudaError_t fusedImpl(const StepArgs& A0, cudaStream_t st) {
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_step_fused<Venue, kPerAgent, kB, kTape>, A);
+    return cudaLaunchKernelEx(&cfg, k_step_fused<Venue, kPerAgent, kB, kTape, kLanes>, A);
 }
 
 cudaError_t launch_step_fused(const StepArgs& A, cudaStream_t st) {
-    if (A.V.kind == SWARM_VENUE_STADIUM) return fusedImpl<Stadium, false, false>(A, st);
-    if (A.V.kind == SWARM_VENUE_SEATED) return fusedImpl<Seated, false, false>(A, st);
+    if (A.V.kind != SWARM_VENUE_GRID) {   // the reference's venues: the lanes instance when the sweeps take lane groups
+        int threads, lanes;
+        fusedShape(A, threads, lanes);
+        if (A.V.kind == SWARM_VENUE_STADIUM)
+            return lanes > 1 ? fusedImpl<Stadium, false, false, false, true>(A, st) : fusedImpl<Stadium, false, false>(A, st);
+        return lanes > 1 ? fusedImpl<Seated, false, false, false, true>(A, st) : fusedImpl<Seated, false, false>(A, st);
+    }
     if (A.venueTable) return fusedImpl<GridVenue, true, true>(A, st);
     return fusedImpl<GridVenue, true, false>(A, st);
 }
