@@ -24,6 +24,8 @@ reference_venue_L  the reference's own seated venue L (63 424 agents) with the r
        the reference's published GPU step on that venue (from the spawn and congested).
 reference_venue_S  venue S under the reference's default model (its queue-aware exit choice on its own table, the
        incline speed and stair spacing), from the spawn and congested, beside the reference's published GPU step.
+reference_terrace  the reference's baked terrace (4 096 agents, K = 32) from the spawn and congested, beside the
+       reference's published GPU step on it.
 adjoint  loss and gradient of 400 steps of the 16 384-agent hall (checkpoints every 20 steps, and the full tape)
        against the plain forward of the same steps.
 --impl reference  the reference's CPU step (the oracle port: the reference's own build needs its source tree, which
@@ -445,6 +447,45 @@ def bench_venue_s(steps=30, warmup=5):
     return out
 
 
+def bench_terrace(steps=30, warmup=5):
+    """The reference's own terrace in reference-parity mode: its baked venue (stadium.sdf, the pitch fence, the egress
+    router; tests/golden/stadium_sdf.zlib), 4 096 agents from the reference's bleacher spawn as its CPU build draws it on
+    this platform (tests/golden/terrace_ref.npz; the reference's published run drew its spawn with another standard
+    library), the reference's constants (model units, K = 32), from the spawn and once half the crowd has left. CUDA
+    events per step on the handle's stream, the L2 flushed before each step. The reference publishes its GPU step on
+    this venue at N = 4 096 from the spawn (OpenGL on an AMD RX 7800 XT): 0.7239 ms
+    (results/benchmarks/thesis/perf_tables.md:28)."""
+    import zlib
+    import torch
+    import swarm_gb300
+    from swarm_gb300.venues import Venue
+    golden = os.path.join(ROOT, "tests", "golden")
+    sdf = np.frombuffer(zlib.decompress(open(os.path.join(golden, "stadium_sdf.zlib"), "rb").read()), np.float32).copy()
+    spawn = np.load(os.path.join(golden, "terrace_ref.npz"))["spawn"]
+    stream = torch.cuda.Stream()
+    sim = swarm_gb300.CrowdSim(swarm_gb300.params_reference(), Venue.stadium(sdf), spawn.shape[0])
+    sim.set_stream(stream.cuda_stream)
+    sim.set_state(spawn)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    with torch.cuda.stream(stream):
+        sim.step(warmup)
+    torch.cuda.synchronize()
+    out = {"workload": "reference terrace (stadium.sdf), 4096 agents from the reference's bleacher spawn, reference "
+                       "constants (model units, K=32)",
+           "published_reference_gpu": {"ms_per_step": 0.7239,
+                                       "hardware": "AMD RX 7800 XT, OpenGL 4.3 (published, not measured here)"}}
+    active, total = _timed_steps(sim, stream, flush, steps)
+    out["spawn"] = {"value": active / (total * 1e-3), "unit": UNIT, "ms_per_step": total / steps, "steps": steps,
+                    "warmup": warmup}
+    taken, left = _congest(sim, stream)
+    active, total = _timed_steps(sim, stream, flush, steps)
+    out["congested"] = {"value": active / (total * 1e-3), "unit": UNIT, "ms_per_step": total / steps, "steps": steps,
+                        "after_steps": warmup + steps + taken, "active_agents": left}
+    sim.synchronize()
+    sim.close()
+    return out
+
+
 def bowl_venue():
     """The seated bowl's venue alone (its nav grid is the solver's workload)."""
     from swarm_gb300 import venues
@@ -652,7 +693,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
     ap.add_argument("--no-bowl", action="store_true", help="skip the seated-bowl measurement")
     ap.add_argument("--adjoint-steps", type=int, default=400, help="steps of the adjoint measurement (400: the workload)")
-    ap.add_argument("--only", choices=["adjoint", "bowl", "bowl_step", "batched", "navfield", "venue_l", "venue_s"], default=None,
+    ap.add_argument("--only", choices=["adjoint", "bowl", "bowl_step", "batched", "navfield", "venue_l", "venue_s", "terrace"], default=None,
                     help="run only this sub-measurement and print its object (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -667,7 +708,7 @@ def main():
         fn = {"adjoint": lambda: bench_adjoint(P, steps=args.adjoint_steps), "bowl": lambda: bench_bowl(P),
               "batched": lambda: bench_batched(P),
               "navfield": lambda: bench_nav_field(bowl_venue()), "venue_l": lambda: bench_venue_l(),
-              "venue_s": lambda: bench_venue_s(),
+              "venue_s": lambda: bench_venue_s(), "terrace": lambda: bench_terrace(),
               "bowl_step": lambda: bench_bowl(P, steps=10, evacuation=False)}[args.only]
         print(json.dumps({args.only: fn()}))
         return 0
@@ -891,6 +932,10 @@ def main():
                 line["reference_venue_S"] = bench_venue_s()
             except Exception as e:  # reported, not fatal
                 line["reference_venue_S"] = {"error": str(e)[:300]}
+            try:
+                line["reference_terrace"] = bench_terrace()
+            except Exception as e:  # reported, not fatal
+                line["reference_terrace"] = {"error": str(e)[:300]}
         if not args.no_adjoint and world == 1:
             try:
                 line["adjoint"] = bench_adjoint(P, steps=args.adjoint_steps)
