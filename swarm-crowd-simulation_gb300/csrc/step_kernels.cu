@@ -1095,7 +1095,7 @@ __global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREA
             sIn = sOut;
             sOut = t;
         }
-        // The scan runs in tiles of A.scanTile cells (8 counts a thread, or 16 on sparse venues). Whoever counted the
+        // The scan runs in tiles of A.scanTile cells (4 or 8 counts a thread, or 16 on sparse venues). Whoever counted the
         // keys -- the previous fused step's final pass, or the hash here -- also summed them per tile, so the scan starts
         // at its apply phase (the tile sums were zero before that counting: cleared below, or by the host).
         if (step == 0 && !A.hashed) {
@@ -1103,10 +1103,11 @@ __global__ void __launch_bounds__(kB ? FUSED_MAX_THREADS_BATCH : FUSED_MAX_THREA
                 hashItem<kB, true>(A, base + int(threadIdx.x & 31u), sIn, A.hostIn);
             if (!gridBarrier(A, gridDim.x)) return;
         }
-        const bool wide = A.scanTile > T * SCAN_ITEMS;
+        const bool wide = A.scanTile > T * SCAN_ITEMS, narrow = A.scanTile < T * SCAN_ITEMS;
         const int tiles = (A.V.ncells + 1 + A.scanTile - 1) / A.scanTile;
         for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
             if (wide) scanApplyTile<2 * SCAN_ITEMS>(A, t, warpSums, &prefix);
+            else if (narrow) scanApplyTile<SCAN_ITEMS / 2>(A, t, warpSums, &prefix);
             else scanApplyTile<SCAN_ITEMS>(A, t, warpSums, &prefix);
         }
         // barrierExtra: the timeout test's block that never arrives
@@ -1413,9 +1414,13 @@ static int fusedThreads(const StepArgs& A) {
     return threads;
 }
 
-// 8 counts a thread, or 16 where that would take more tiles than there are SMs (sparse venues)
+// 4 counts a thread where the tiles of 4 still number no more than the SMs (more blocks share the apply phase; a tile
+// of at least 1 024 cells, as the tile sums' buffer assumes), else 8, or 16 where 8 would take more tiles than there
+// are SMs (sparse venues)
 int fusedScanTile(const StepArgs& A) {
     const int T = fusedThreads(A);
+    const int tiles4 = (A.V.ncells + 1 + T * (SCAN_ITEMS / 2) - 1) / (T * (SCAN_ITEMS / 2));
+    if (T * (SCAN_ITEMS / 2) >= 1024 && tiles4 <= smCount()) return T * (SCAN_ITEMS / 2);
     const int tiles8 = (A.V.ncells + 1 + T * SCAN_ITEMS - 1) / (T * SCAN_ITEMS);
     return tiles8 > smCount() ? T * 2 * SCAN_ITEMS : T * SCAN_ITEMS;
 }
