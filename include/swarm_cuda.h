@@ -242,7 +242,8 @@ int swarm_set_graph(SwarmHandle h, int enabled);
  * sweeps, final), replayed from CUDA graphs when swarm_set_graph is on. Both give the same bits. */
 int swarm_set_fused(SwarmHandle h, int enabled);
 /* The launch configuration: the fused persistent kernel (fused = 1) with `threads` per block (0: the state size over
- * the SMs, rounded up to a warp, 128..512, or 128..1024 for a batch) and at most `blocks_per_sm` blocks per SM (0: as many as fit; fewer blocks
+ * the SMs, rounded up to a warp, 128..512, or 128..1024 for a batch; else 64..512, 64..1024 for a batch, rounded up to
+ * a warp; below 64 is SWARM_E_INVALID) and at most `blocks_per_sm` blocks per SM (0: as many as fit; fewer blocks
  * mean more agents per thread), or one kernel per phase (fused = 0: one Jacobi sweep per launch). steps_per_launch
  * (fused only): the steps of one swarm_step call that one persistent launch runs, with one more grid barrier between
  * steps (0: all of them; 1: a launch per step); steps with the exit choice, the metrics or stage timing on take a

@@ -1403,7 +1403,7 @@ static void fusedShape(const StepArgs& A, int& threads, int& lanes) {
         }
     }
     threads = A.fusedThreads > 0 ? A.fusedThreads : ((A.n + sms - 1) / sms + 31) / 32 * 32;
-    const int floor = A.fusedThreads > 0 ? 32 : 128;   // a tuned block may be a single warp
+    const int floor = A.fusedThreads > 0 ? 64 : 128;   // a tuned block may be two warps (a scan tile of 16 x 64 cells)
     threads = threads < floor ? floor : (threads > cap ? cap : threads);
     threads = (threads + 31) / 32 * 32;
 }
@@ -1414,15 +1414,20 @@ static int fusedThreads(const StepArgs& A) {
     return threads;
 }
 
-// 4 counts a thread where the tiles of 4 still number no more than the SMs (more blocks share the apply phase; a tile
-// of at least 1 024 cells, as the tile sums' buffer assumes), else 8, or 16 where 8 would take more tiles than there
-// are SMs (sparse venues)
+// Counts a thread in the scan's apply phase: 4, 8 or 16, whichever gives the fewest counts on the busiest block (tiles
+// per block, rounded up, x counts a thread: the phase's critical path), the larger on a tie; 4 only for a tile of at
+// least 1 024 cells (as the tile sums' buffer assumes)
 int fusedScanTile(const StepArgs& A) {
     const int T = fusedThreads(A);
-    const int tiles4 = (A.V.ncells + 1 + T * (SCAN_ITEMS / 2) - 1) / (T * (SCAN_ITEMS / 2));
-    if (T * (SCAN_ITEMS / 2) >= 1024 && tiles4 <= smCount()) return T * (SCAN_ITEMS / 2);
-    const int tiles8 = (A.V.ncells + 1 + T * SCAN_ITEMS - 1) / (T * SCAN_ITEMS);
-    return tiles8 > smCount() ? T * 2 * SCAN_ITEMS : T * SCAN_ITEMS;
+    const int sms = smCount();
+    int best = 0, bestCost = 0;
+    for (int items = 2 * SCAN_ITEMS; items >= SCAN_ITEMS / 2; items /= 2) {
+        if (T * items < 1024) continue;
+        const int tiles = (A.V.ncells + 1 + T * items - 1) / (T * items);
+        const int cost = (tiles + sms - 1) / sms * items;
+        if (best == 0 || cost < bestCost) { best = items; bestCost = cost; }
+    }
+    return T * best;
 }
 
 template <class Venue, bool kPerAgent, bool kB, bool kTape = false, bool kLanes = false>

@@ -497,6 +497,8 @@ int swarm_set_tuning(SwarmHandle h, const SwarmTuning* t) {
     if (!h || !t || t->threads < 0 || t->blocks_per_sm < 0 || t->steps_per_launch < 0) return SWARM_E_INVALID;
     if (t->threads > (h->instances ? 1024 : 512))
         return h->fail(SWARM_E_INVALID, "threads above " + std::to_string(h->instances ? 1024 : 512) + " per block");
+    // (the fused step's scan tiles hold at least 1 024 cells: 16 counts a thread of at least 64 threads)
+    if (t->threads > 0 && t->threads < 64) return h->fail(SWARM_E_INVALID, "threads below 64 per block");
     h->tuning = *t;
     h->fused = t->fused != 0;
     h->dropGraphs();

@@ -73,6 +73,8 @@ def test_launch_configurations_give_the_same_bits_and_autotune_restores_state(bu
     sim = swarm_gb300.CrowdSim(P, venue, boids.shape[0])
     sim.set_state(boids)
     sim.set_agent_params(r, v0)
+    with pytest.raises(swarm_gb300.SwarmError):   # below 64 threads a block: refused (the scan tiles' size)
+        sim.set_tuning(True, 32, 0)
     best = sim.autotune(steps=2)
     assert best["ms_per_step"] > 0
     assert np.array_equal(_bits(sim.state()), _bits(boids))   # the trials' state is restored
