@@ -36,8 +36,9 @@ steps 1, 17 and 18 (the first evaluation), the states after 1 and 18 steps, the 
 and tests/golden/seated_M.npz, seated_L.npz: the generated venues M (15 832 seats, N = 16 384) and L (63 424 seats,
 N = 65 536) -- several straight gangways, doors per gangway head, corner doors, merged corner gangways -- with the
 layout, grid, compact navigation table as above, the full seat spawn spawnSeatedCrowd(venue, N, 1.0, 1337) (zlib), and
-the FNV-1a hashes of the reference's states after 1, 10 and 50 steps under {nearest exit, level speed} and after 10
-steps under {nearest exit, incline speed, stair spacing EMPIRICAL}.
+the FNV-1a hashes of the reference's states after 1, 10, 50 and 250 steps under {nearest exit, level speed} and after
+10 and 250 steps under {nearest exit, incline speed, stair spacing EMPIRICAL}. Written alone by
+`python tests/golden/make_seated_golden.py generated`.
 """
 import ctypes as C
 import lzma
@@ -143,7 +144,7 @@ def generated_venue(L, name, n):
     assert L.ref_spawn_seated(name, n, 1.0, 1337, spawn.ctypes.data) == 0
     out["spawn_z"] = np.frombuffer(zlib.compress(spawn.tobytes(), 9), np.uint8)
     out["n"] = np.array([n, int((spawn[:, 3] != 0).sum())], np.int64)
-    for prefix, incline, stair, keep in (("nearest_", 0, 0, (1, 10, 50)), ("incline_", 1, 1, (10,))):
+    for prefix, incline, stair, keep in (("nearest_", 0, 0, (1, 10, 50, 250)), ("incline_", 1, 1, (10, 250))):
         sim = _sim(L, name, incline, stair)
         sim.set_state(spawn)
         done = 0
@@ -242,6 +243,10 @@ def main():
     L = _bind(O.ref_lib())
     if sys.argv[1:] == ["choice"]:
         choice_records(L)
+        return
+    if sys.argv[1:] == ["generated"]:
+        generated_venue(L, b"M", 16384)
+        generated_venue(L, b"L", 65536)
         return
     out = {}
     assert _venue_records(L, b"S", out) == 40

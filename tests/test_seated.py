@@ -272,12 +272,12 @@ def test_geometry_of_the_generated_venues_equals_the_reference(tmp_path, name):
 @pytest.mark.parametrize("name", ["M", "L"])
 def test_generated_venue_runs_reproduce_the_reference(name):
     """Venues M (15 832 seated, N = 16 384) and L (63 424 seated, N = 65 536) from their full seat spawns: the states
-    after 1, 10 and 50 steps at the nearest exit and level speed, and after 10 steps with the incline speed and stair
-    spacing, hash to the reference's own states (FNV-1a of the raw state)."""
+    after 1, 10, 50 and 250 steps at the nearest exit and level speed, and after 10 and 250 steps with the incline
+    speed and stair spacing, hash to the reference's own states (FNV-1a of the raw state)."""
     import swarm_gb300
     g, cells, spawn = _generated(name)
     assert spawn.shape[0] == int(g["n"][0]) and int((spawn[:, 3] != 0).sum()) == int(g["n"][1])
-    for prefix, incline, keep in (("nearest_", False, (1, 10, 50)), ("incline_", True, (10,))):
+    for prefix, incline, keep in (("nearest_", False, (1, 10, 50, 250)), ("incline_", True, (10, 250))):
         sim = swarm_gb300.CrowdSim(swarm_gb300.params_reference(), _venue(g, cells, incline), spawn.shape[0])
         sim.set_state(spawn)
         done = 0
