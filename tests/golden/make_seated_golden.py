@@ -39,6 +39,10 @@ layout, grid, compact navigation table as above, the full seat spawn spawnSeated
 the FNV-1a hashes of the reference's states after 1, 10, 50 and 250 steps under {nearest exit, level speed} and after
 10 and 250 steps under {nearest exit, incline speed, stair spacing EMPIRICAL}. Written alone by
 `python tests/golden/make_seated_golden.py generated`.
+
+tests/golden/seated_S_evac.npz: the active count after every step of venue S's full seat spawn run by the reference's
+CPU step to its last agent out, routed (its default model) and at the nearest exit and level speed. Written alone by
+`python tests/golden/make_seated_golden.py evacuation`.
 """
 import ctypes as C
 import lzma
@@ -157,6 +161,31 @@ def generated_venue(L, name, n):
     print("wrote", os.path.basename(path), os.path.getsize(path), "bytes")
 
 
+def evacuation_records(L):
+    """seated_S_evac.npz: the reference's CPU step on venue S from the full seat spawn run to its last agent out, under
+    its default model (queue-aware exit choice, incline speed, stair spacing EMPIRICAL) and at the nearest exit and
+    level speed: the active count after every step (the routed run empties at step 1361, as the reference's own
+    validation output records for its CPU counting sort)."""
+    g = np.load(os.path.join(HERE, "seated_S.npz"))
+    spawn = g["nearest_spawn"]
+    out = {}
+    for prefix, opts in (("routed_", (0, 0, 1, 1, 1)), ("nearest_", (0, 0, 0, 0, 0))):
+        sim = O.RefSim.__new__(O.RefSim)
+        sim._h = L.ref_create_opts(b"S", *opts)
+        sim.n = 0
+        sim.set_state(spawn)
+        active = []
+        while not active or (active[-1] > 0 and len(active) < 5000):
+            sim.step(1)
+            active.append(int((sim.state()[:, 3] != 0).sum()))
+        assert active[-1] == 0
+        out[prefix + "active"] = np.array(active, np.int32)
+    assert out["routed_active"].shape[0] == 1361, out["routed_active"].shape
+    path = os.path.join(HERE, "seated_S_evac.npz")
+    np.savez_compressed(path, **out)
+    print("wrote seated_S_evac.npz:", os.path.getsize(path), "bytes")
+
+
 def _lz(a):
     return np.frombuffer(lzma.compress(np.ascontiguousarray(a).tobytes(), preset=9 | lzma.PRESET_EXTREME), np.uint8)
 
@@ -244,6 +273,9 @@ def main():
     if sys.argv[1:] == ["choice"]:
         choice_records(L)
         return
+    if sys.argv[1:] == ["evacuation"]:
+        evacuation_records(L)
+        return
     if sys.argv[1:] == ["generated"]:
         generated_venue(L, b"M", 16384)
         generated_venue(L, b"L", 65536)
@@ -297,6 +329,7 @@ def main():
     choice_records(L)
     generated_venue(L, b"M", 16384)
     generated_venue(L, b"L", 65536)
+    evacuation_records(L)
 
 
 if __name__ == "__main__":
