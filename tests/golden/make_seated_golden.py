@@ -42,7 +42,8 @@ the FNV-1a hashes of the reference's states after 1, 10, 50 and 250 steps under 
 
 tests/golden/seated_S_evac.npz: the active count after every step of venue S's full seat spawn run by the reference's
 CPU step to its last agent out, routed (its default model) and at the nearest exit and level speed. Written alone by
-`python tests/golden/make_seated_golden.py evacuation`.
+`python tests/golden/make_seated_golden.py evacuation`; tests/golden/seated_M_evac.npz, seated_L_evac.npz: the same for
+M and L at the nearest exit and level speed (`python tests/golden/make_seated_golden.py generated_evacuation M L`).
 """
 import ctypes as C
 import lzma
@@ -186,6 +187,23 @@ def evacuation_records(L):
     print("wrote seated_S_evac.npz:", os.path.getsize(path), "bytes")
 
 
+def generated_evacuation(L, name):
+    """seated_<name>_evac.npz: the reference's CPU step on a generated venue (M or L) from its full seat spawn (the
+    fixture's) run to its last agent out at the nearest exit and level speed: the active count after every step."""
+    g = np.load(os.path.join(HERE, "seated_%s.npz" % name.decode()))
+    spawn = np.frombuffer(zlib.decompress(g["spawn_z"].tobytes()), np.float32).reshape(-1, 8).copy()
+    sim = _sim(L, name)
+    sim.set_state(spawn)
+    active = []
+    while not active or (active[-1] > 0 and len(active) < 40000):
+        sim.step(1)
+        active.append(int((sim.state()[:, 3] != 0).sum()))
+    assert active[-1] == 0
+    path = os.path.join(HERE, "seated_%s_evac.npz" % name.decode())
+    np.savez_compressed(path, nearest_active=np.array(active, np.int32))
+    print("wrote", os.path.basename(path), os.path.getsize(path), "bytes,", len(active), "steps")
+
+
 def _lz(a):
     return np.frombuffer(lzma.compress(np.ascontiguousarray(a).tobytes(), preset=9 | lzma.PRESET_EXTREME), np.uint8)
 
@@ -276,6 +294,10 @@ def main():
     if sys.argv[1:] == ["evacuation"]:
         evacuation_records(L)
         return
+    if sys.argv[1:2] == ["generated_evacuation"]:
+        for name in sys.argv[2:] or ["M", "L"]:
+            generated_evacuation(L, name.encode())
+        return
     if sys.argv[1:] == ["generated"]:
         generated_venue(L, b"M", 16384)
         generated_venue(L, b"L", 65536)
@@ -330,6 +352,8 @@ def main():
     generated_venue(L, b"M", 16384)
     generated_venue(L, b"L", 65536)
     evacuation_records(L)
+    generated_evacuation(L, b"M")
+    generated_evacuation(L, b"L")
 
 
 if __name__ == "__main__":
