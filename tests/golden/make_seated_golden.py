@@ -164,13 +164,15 @@ def generated_venue(L, name, n):
 
 def evacuation_records(L):
     """seated_S_evac.npz: the reference's CPU step on venue S from the full seat spawn run to its last agent out, under
-    its default model (queue-aware exit choice, incline speed, stair spacing EMPIRICAL) and at the nearest exit and
-    level speed: the active count after every step (the routed run empties at step 1361, as the reference's own
-    validation output records for its CPU counting sort)."""
+    its default model (queue-aware exit choice, incline speed, stair spacing EMPIRICAL), the same with the level
+    spacing, at the nearest exit and level speed, and at the nearest exit with the incline speed and stair spacing:
+    the active count after every step (the routed run empties at step 1361, as the reference's own validation output
+    records for its CPU counting sort)."""
     g = np.load(os.path.join(HERE, "seated_S.npz"))
     spawn = g["nearest_spawn"]
     out = {}
-    for prefix, opts in (("routed_", (0, 0, 1, 1, 1)), ("nearest_", (0, 0, 0, 0, 0))):
+    for prefix, opts in (("routed_", (0, 0, 1, 1, 1)), ("nearest_", (0, 0, 0, 0, 0)), ("routed_level_", (0, 0, 1, 1, 0)),
+                         ("incline_", (0, 0, 0, 1, 1))):
         sim = O.RefSim.__new__(O.RefSim)
         sim._h = L.ref_create_opts(b"S", *opts)
         sim.n = 0

@@ -442,19 +442,20 @@ def test_routed_exit_choice_with_level_spacing_reproduces_the_reference_pin(gold
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("model", ["routed", "nearest"])
+@pytest.mark.parametrize("model", ["routed", "routed_level", "nearest", "incline"])
 def test_whole_evacuation_matches_the_reference(golden, nav_cells, choice, model):
     """Venue S's full seat spawn run to its last agent out through swarm_run_evacuation, under the reference's default
-    model (queue-aware exit choice on its own table, incline speed, stair spacing) and at the nearest exit and level
-    speed: the active count after every step is the reference's own CPU run (tests/golden/seated_S_evac.npz), so the
-    crowd empties at the same step (routed: step 1 361, the step the reference's validation output records for its
-    CPU counting sort)."""
+    model (queue-aware exit choice on its own table, incline speed, stair spacing), the same with the level spacing,
+    at the nearest exit and level speed, and at the nearest exit with the incline speed and stair spacing: the active
+    count after every step is the reference's own CPU run (tests/golden/seated_S_evac.npz), so the crowd empties at
+    the same step (routed: step 1 361, the step the reference's validation output records for its CPU counting
+    sort)."""
     ref = np.load(os.path.join(os.path.dirname(CHOICE), "seated_S_evac.npz"))[model + "_active"]
-    if model == "routed":
-        sim = _routed(golden, nav_cells, choice)
-        assert ref.shape[0] == 1361
+    if model.startswith("routed"):
+        sim = _routed(golden, nav_cells, choice, stair=model == "routed")
+        assert model != "routed" or ref.shape[0] == 1361
     else:
-        sim = _sim(golden, golden["nearest_spawn"], nav_cells)
+        sim = _sim(golden, golden["nearest_spawn"], nav_cells, incline=model == "incline")
     stats, active = sim.run_evacuation(ref.shape[0] + 500)
     assert stats["remaining"] == 0 and stats["steps"] == ref.shape[0] == stats["t100_step"]
     assert np.array_equal(active, ref)
