@@ -43,7 +43,8 @@ the FNV-1a hashes of the reference's states after 1, 10, 50 and 250 steps under 
 tests/golden/seated_S_evac.npz: the active count after every step of venue S's full seat spawn run by the reference's
 CPU step to its last agent out, routed (its default model) and at the nearest exit and level speed. Written alone by
 `python tests/golden/make_seated_golden.py evacuation`; tests/golden/seated_M_evac.npz, seated_L_evac.npz: the same for
-M and L at the nearest exit and level speed (`python tests/golden/make_seated_golden.py generated_evacuation M L`).
+M and L at the nearest exit, at the level speed and with the incline speed and stair spacing
+(`python tests/golden/make_seated_golden.py generated_evacuation M L`).
 """
 import ctypes as C
 import lzma
@@ -191,19 +192,23 @@ def evacuation_records(L):
 
 def generated_evacuation(L, name):
     """seated_<name>_evac.npz: the reference's CPU step on a generated venue (M or L) from its full seat spawn (the
-    fixture's) run to its last agent out at the nearest exit and level speed: the active count after every step."""
+    fixture's) run to its last agent out at the nearest exit, at the level speed and with the incline speed and stair
+    spacing: the active count after every step."""
     g = np.load(os.path.join(HERE, "seated_%s.npz" % name.decode()))
     spawn = np.frombuffer(zlib.decompress(g["spawn_z"].tobytes()), np.float32).reshape(-1, 8).copy()
-    sim = _sim(L, name)
-    sim.set_state(spawn)
-    active = []
-    while not active or (active[-1] > 0 and len(active) < 40000):
-        sim.step(1)
-        active.append(int((sim.state()[:, 3] != 0).sum()))
-    assert active[-1] == 0
+    out = {}
+    for prefix, incline in (("nearest_", 0), ("incline_", 1)):
+        sim = _sim(L, name, incline, incline)
+        sim.set_state(spawn)
+        active = []
+        while not active or (active[-1] > 0 and len(active) < 40000):
+            sim.step(1)
+            active.append(int((sim.state()[:, 3] != 0).sum()))
+        assert active[-1] == 0
+        out[prefix + "active"] = np.array(active, np.int32)
     path = os.path.join(HERE, "seated_%s_evac.npz" % name.decode())
-    np.savez_compressed(path, nearest_active=np.array(active, np.int32))
-    print("wrote", os.path.basename(path), os.path.getsize(path), "bytes,", len(active), "steps")
+    np.savez_compressed(path, **out)
+    print("wrote", os.path.basename(path), os.path.getsize(path), "bytes,", {k: v.shape[0] for k, v in out.items()}, "steps")
 
 
 def _lz(a):

@@ -314,14 +314,15 @@ def test_contact_lists_keep_the_bits_into_the_congested_run():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["M", "L"])
-def test_generated_venue_whole_evacuation_matches_the_reference(name):
-    """Venues M and L from their full seat spawns run to the last agent out at the nearest exit and level speed
-    through swarm_run_evacuation: the active count after every step is the reference's own CPU run
-    (tests/golden/seated_<name>_evac.npz), so each empties at the same step."""
+@pytest.mark.parametrize("model", ["nearest", "incline"])
+def test_generated_venue_whole_evacuation_matches_the_reference(name, model):
+    """Venues M and L from their full seat spawns run to the last agent out at the nearest exit, at the level speed and
+    with the incline speed and stair spacing, through swarm_run_evacuation: the active count after every step is the
+    reference's own CPU run (tests/golden/seated_<name>_evac.npz), so each empties at the same step."""
     import swarm_gb300
     g, cells, spawn = _generated(name)
-    ref = np.load(os.path.join(os.path.dirname(GOLDEN), "seated_%s_evac.npz" % name))["nearest_active"]
-    sim = swarm_gb300.CrowdSim(swarm_gb300.params_reference(), _venue(g, cells), spawn.shape[0])
+    ref = np.load(os.path.join(os.path.dirname(GOLDEN), "seated_%s_evac.npz" % name))[model + "_active"]
+    sim = swarm_gb300.CrowdSim(swarm_gb300.params_reference(), _venue(g, cells, model == "incline"), spawn.shape[0])
     sim.set_state(spawn)
     stats, active = sim.run_evacuation(ref.shape[0] + 1000)
     assert stats["remaining"] == 0 and stats["steps"] == ref.shape[0] == stats["t100_step"]
